@@ -1,0 +1,295 @@
+"""Benchmark of the MicroFC hot path on GB300.
+
+Workload: 2-D air shock (Mach 1.47) on a water droplet, 1024 x 512 cells,
+2 fluids (7 equations), WENO5-JS + HLLC + TVD-RK3, plain FP64.  One "step" is
+one full time step (3 fused RK-stage launches).  Metric: cell-updates/s =
+interior cells x steps / seconds.
+
+* value   -- device-resident state, CUDA-event time of each step on the
+             library's stream; L2 is flushed (256 MiB write) between steps.
+* e2e     -- the same through the public API with host buffers: every step
+             uploads the state from pinned host memory, advances one step and
+             downloads the state (all inside the timed region).
+* roofline     -- HBM roofline of the stage kernel (algorithmic 448 B per
+                  cell-update) against the measured copy bandwidth.
+* fp64_roofline -- the bound that actually limits this FP64 path: algorithmic
+                  flops per cell-update (counted by the oracle) x rate vs the
+                  FP64 peak.
+* cpu_baseline -- the oracle (C++ restatement of the reference's CPU code,
+                  OpenMP over the host cores) on a 1024 x 64 strip.
+
+``--impl reference`` times that CPU implementation alone and prints the
+reference arm's line.  Under torchrun (N > 1) every rank runs an independent
+replica (the path has no exchange on a one-GPU-per-box deployment); value is
+the sum over ranks with the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+NX, NY = 1024, 512
+BYTES_PER_CELL_UPDATE = 448  # 8 * S doubles, S = 7 (fused RK3 compulsory traffic)
+WORKLOAD = "2D shock-droplet 1024x512, 2 fluids, WENO5-JS + HLLC + TVD-RK3, plain FP64"
+METRIC = "cell-updates/s (2D shock-droplet 1024x512, plain FP64)"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _profile_value(name: str, key: str):
+    """A figure from a committed ncu summary under profiles/ (``key: value``)."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.strip().startswith(key + ":"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([s.strip() for s in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[2 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_baseline(steps: int = 2, ny: int = 64):
+    """The oracle on a 1024 x ny strip of the workload, all host cores."""
+    import oracle
+    from microfc_gb300 import cases, preprocess
+    full = cases.shock_droplet_2d(nx=NX, ny=NY)
+    case = cases.shock_droplet_2d(nx=NX, ny=ny, dt=full.dt)
+    x_cb, y_cb, _, q = preprocess.generate(case)
+    o = oracle.Oracle(case, x_cb, y_cb, threads=os.cpu_count() or 1)
+    o.set_state(q)
+    o.tvd_rk(case.dt)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.tvd_rk(case.dt)
+    t = time.perf_counter() - t0
+    cores = oracle.lib().mfo_get_threads()
+    return {"value": case.cells * steps / t, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} full RK3 time steps of the workload's physics on a {NX}x{ny} strip "
+                      f"(C++ restatement of the reference's CPU code, OpenMP over {cores} threads)"}
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    import oracle
+    from microfc_gb300 import cases, preprocess
+    ny = 64
+    full = cases.shock_droplet_2d(nx=NX, ny=NY)
+    case = cases.shock_droplet_2d(nx=NX, ny=ny, dt=full.dt)
+    x_cb, y_cb, _, q = preprocess.generate(case)
+    o = oracle.Oracle(case, x_cb, y_cb, threads=os.cpu_count() or 1)
+    o.set_state(q)
+    for _ in range(args.warmup):
+        o.tvd_rk(case.dt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.tvd_rk(case.dt)
+    t = time.perf_counter() - t0
+    v = case.cells * args.steps / t
+    cores = oracle.lib().mfo_get_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps * (NY / ny),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": f"{NX}x{ny} strip per step", "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} RK3 steps on a {NX}x{ny} strip of the workload; the reference "
+                                   "(Fortran) cannot be built here, so its C++ restatement (the oracle) runs"},
+        "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    from microfc_gb300 import Simulation, cases, preprocess
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    case = cases.shock_droplet_2d(nx=NX, ny=NY, precision=args.precision)
+    x_cb, y_cb, _, q0 = preprocess.generate(case)
+    sim = Simulation(case, x_cb, y_cb, q_cons=q0, device=local)
+    stream = torch.cuda.ExternalStream(sim.stream, device=torch.device("cuda", local))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            dist.barrier()
+
+    # ---- device-resident timing -------------------------------------------------
+    for _ in range(args.warmup):
+        sim.tvd_rk(0, case.dt)
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    l0 = sim.launches
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for i in range(args.steps):
+                flush.fill_(float(i))  # evict the state from L2 between timed steps
+                ev[i][0].record(stream)
+                sim.tvd_rk(0, case.dt)
+                ev[i][1].record(stream)
+        barrier()
+    launches = sim.launches - l0
+    ms = [a.elapsed_time(b) for a, b in ev]
+    t_total = sum(ms) / 1e3
+    if ws > 1:
+        tt = torch.tensor([t_total], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt.item())
+    cells = case.cells
+    value = ws * cells * args.steps / t_total
+    ms_step = 1e3 * t_total / args.steps
+    if sim.status() != 0:
+        raise RuntimeError("device flagged a non-finite state during the benchmark")
+
+    # ---- end to end through the public API with host buffers --------------------
+    host = torch.empty(case.shape, dtype=torch.float64, pin_memory=True).numpy()
+    host[...] = q0
+    e2e_steps = max(3, min(args.steps, 10))
+    sim.upload(host)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.upload(host)
+        sim.tvd_rk(0, case.dt)
+        sim.download(host)
+    t_e2e = time.perf_counter() - t0
+    if ws > 1:
+        tt = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e = ws * cells * e2e_steps / t_e2e
+    state_bytes = int(np.prod(case.shape)) * 8
+
+    # ---- rooflines ---------------------------------------------------------------------
+    hbm, peak_kind = _peaks()
+    per_launch_s = t_total / launches
+    achieved = BYTES_PER_CELL_UPDATE * cells / 3 / per_launch_s / 1e9
+    traffic = _profile_value("stage_kernel_fp64_droplet_1024x512.md", "dram_bytes_per_launch")
+    flops = _profile_value("stage_kernel_fp64_droplet_1024x512.md", "algorithmic_flops_per_cell_update")
+    fp64_peak = _profile_value("stage_kernel_fp64_droplet_1024x512.md", "fp64_peak_tflops")
+    fp64_peak_kind = "measured (DFMA loop, profiles/)" if fp64_peak else "nominal"
+    fp64_peak = fp64_peak or 1.25
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64 state / f32 WENO+HLLC",
+        "data": "synthetic (reference-style case inputs, generated in-process)",
+        "config": {"workload": WORKLOAD if args.precision == "fp64" else WORKLOAD.replace("plain FP64", "split"),
+                   "cells": cells, "equations": case.sys_size, "dt": case.dt,
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": state_bytes,
+                "d2h_bytes_per_step": state_bytes, "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
+                     if peak_kind == "measured" else "fallback"},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if flops:
+        ach = flops * value / ws / 1e12
+        line["fp64_roofline"] = {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+                                 "frac": ach / fp64_peak, "peak_kind": fp64_peak_kind,
+                                 "flops_per_cell_update": flops}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    sim.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

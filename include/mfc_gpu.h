@@ -1,0 +1,149 @@
+/*
+ * mfc_gpu.h -- C ABI of the GB300-native MicroFC hot path.
+ *
+ * Drop-in boundary for MicroFC's right-hand side and TVD Runge-Kutta step of
+ * the 5-equation diffuse-interface model (cons -> prim with the stiffened-gas
+ * mixture EOS, WENO reconstruction, HLLC with the alpha*div(u) source, flux
+ * divergence, RK update).  Every entry point is plain C: POD structs, raw
+ * pointers and sizes, an int status (0 = success), and no C++ exception ever
+ * crosses it.  A Fortran host binds it with ISO_C_BINDING; the Python host in
+ * microfc_gb300/ binds it with ctypes.
+ *
+ * Reference interfaces replaced (paths inside the MicroFC project):
+ *   mfc_gpu_init            s_initialize_{rhs,weno,riemann_solvers,time_steppers}_module
+ *                           (src/simulation/m_rhs.fpp:123, m_weno.fpp:103,
+ *                            m_riemann_solvers.fpp:357, m_time_steppers.fpp:53)
+ *                           and the input namelist (m_start_up.fpp:73-83)
+ *   mfc_gpu_upload/download the "!$acc update device/host(q_cons_ts(1))" transfers
+ *                           (src/simulation/p_main.fpp:191-193, 295-296)
+ *   mfc_gpu_compute_rhs     s_compute_rhs (src/simulation/m_rhs.fpp:405-679)
+ *   mfc_gpu_tvd_rk          s_1st/2nd/3rd_order_tvd_rk (m_time_steppers.fpp:129, 197, 271)
+ *   mfc_gpu_run             the time-stepping loop of p_main (p_main.fpp:196-318)
+ *   mfc_gpu_status          the NaN scan of p_main.fpp:295-305 (as a device flag)
+ *   mfc_gpu_finalize        s_finalize_*_module
+ *
+ * State layout handed across the ABI: one scalar field per equation, exactly
+ * the reference's q_cons_vf(i)%sf, x fastest.  The device keeps all RK
+ * registers resident in HBM as one SoA block [register][equation][z][y][x]
+ * (rows padded to 256 bytes); ghost cells are never stored -- boundary
+ * conditions are applied by index mapping inside the kernels.
+ */
+#ifndef MFC_GPU_H
+#define MFC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MFC_GPU_ABI_VERSION 1
+#define MFC_MAX_FLUIDS 4
+
+/* Status codes (non-zero means the host should abort, as s_mpi_abort does). */
+#define MFC_OK 0
+#define MFC_ERR_INVALID 1   /* bad argument / unsupported configuration   */
+#define MFC_ERR_CUDA 2      /* CUDA runtime error                          */
+#define MFC_ERR_NOMEM 3     /* device allocation failed                    */
+#define MFC_ERR_STATE 4     /* NaN / non-physical state flagged by a kernel */
+
+/* Bits of the device status word returned by mfc_gpu_status. */
+#define MFC_FLAG_NAN 0x1u          /* NaN or Inf written to a conserved field */
+#define MFC_FLAG_NEG_PRESSURE 0x2u /* non-positive (p + pi_inf-mix/gamma-mix) */
+#define MFC_FLAG_TIMEOUT 0x4u      /* a bounded device wait gave up           */
+
+/* Precision of the reconstruction/Riemann arithmetic. */
+#define MFC_PREC_FP64 0  /* plain FP64 everywhere (parity path)                       */
+#define MFC_PREC_SPLIT 1 /* FP32 WENO/HLLC; FP64 state, RK update, pressure recovery   */
+
+/*
+ * Case parameters: the solver-relevant subset of the reference's &user_inputs
+ * namelist (src/simulation/m_start_up.fpp:73-83) plus the z extent p (the
+ * reference is 2-D only) and the GPU-specific precision/device choices.
+ *
+ * Cell boundaries are the reference's x_cb(-1:m), y_cb(-1:n), z_cb(-1:p)
+ * (m+2, n+2, p+2 values) as read from x_cb.dat / y_cb.dat
+ * (m_start_up.fpp:326-367); ghost widths and the grid-dependent WENO
+ * coefficients are derived from them on the host exactly as
+ * s_populate_grid_variables_buffers and s_compute_weno_coefficients do.
+ */
+typedef struct mfc_params {
+  int32_t m, n, p;          /* interior cells minus one per direction (n = p = 0 in 1-D) */
+  int32_t num_fluids;       /* 1 .. MFC_MAX_FLUIDS                                        */
+  int32_t weno_order;       /* 1, 3 or 5                                                  */
+  double weno_eps;          /* (0, 1e-6]                                                  */
+  int32_t time_stepper;     /* 1, 2 or 3 (TVD RK order)                                   */
+  int32_t bc_x_beg, bc_x_end, bc_y_beg, bc_y_end, bc_z_beg, bc_z_end; /* -1 .. -12         */
+  double gammas[MFC_MAX_FLUIDS];  /* fluid_pp(i)%gamma  = 1/(gamma_i - 1)                 */
+  double pi_infs[MFC_MAX_FLUIDS]; /* fluid_pp(i)%pi_inf = gamma_i*pi_inf_i/(gamma_i - 1)  */
+  const double* x_cb;       /* host, m+2 values                                           */
+  const double* y_cb;       /* host, n+2 values, or NULL when n == 0                      */
+  const double* z_cb;       /* host, p+2 values, or NULL when p == 0                      */
+  int32_t precision;        /* MFC_PREC_FP64 or MFC_PREC_SPLIT                            */
+  int32_t device;           /* CUDA device ordinal (the reference binds local_rank % ndev) */
+} mfc_params;
+
+typedef struct mfc_gpu_ctx mfc_gpu_ctx;
+
+/* Library ABI version; lets a host check it loaded a matching build. */
+int mfc_gpu_abi_version(void);
+
+/* Last error message of the calling thread (never NULL). */
+const char* mfc_gpu_last_error(void);
+
+/* Allocates the device state (3 RK registers + rhs + grid tables) and
+ * uploads the grid.  Replaces s_initialize_*_module. */
+int mfc_gpu_init(const mfc_params* params, mfc_gpu_ctx** ctx_out);
+
+/* Number of equations (sys_size = 2*num_fluids + num_dims + 1). */
+int mfc_gpu_sys_size(const mfc_gpu_ctx* ctx);
+
+/* Copy equation `var` (0-based) of register 0 (q_cons_ts(1)) from/to a host
+ * array.  host_sf points at element (0,0,0) of the interior; ld_y is the
+ * distance in elements between consecutive y rows and ld_z between z planes.
+ * A Fortran host passes c_loc(sf(0,0)) with ld_y = m + 2*buff_size + 1.
+ * Synchronous with respect to the context's stream. */
+int mfc_gpu_upload(mfc_gpu_ctx* ctx, int var, const double* host_sf, int64_t ld_y, int64_t ld_z);
+int mfc_gpu_download(mfc_gpu_ctx* ctx, int var, double* host_sf, int64_t ld_y, int64_t ld_z);
+
+/* Whole-state copies of register 0, [S][p+1][n+1][m+1] contiguous. */
+int mfc_gpu_upload_state(mfc_gpu_ctx* ctx, const double* host_q);
+int mfc_gpu_download_state(mfc_gpu_ctx* ctx, double* host_q);
+
+/* Drop-in for s_compute_rhs(q_cons_ts(1), q_prim_vf, rhs_vf, t_step): computes
+ * the RHS of register 0 into host arrays rhs_out and prim_out (either may be
+ * NULL), both [S][p+1][n+1][m+1].  Uses the unfused sweep kernels; intended
+ * for verification and for hosts that run their own time integrator. */
+int mfc_gpu_compute_rhs(mfc_gpu_ctx* ctx, double* rhs_out, double* prim_out);
+
+/* Drop-in for s_{1,2,3}_order_tvd_rk(t_step, time_avg): one full time step of
+ * register 0 with time step dt, as fused stage kernels (one launch per RK
+ * stage).  When last_step != 0 the call does nothing, mirroring the early
+ * return at t_step == t_step_stop (m_rhs.fpp:452).  Asynchronous. */
+int mfc_gpu_tvd_rk(mfc_gpu_ctx* ctx, double dt, int last_step);
+
+/* The time loop of p_main (p_main.fpp:196-318) from t_step_start to
+ * t_step_stop, including the trim of dt at the last step of the CPU build.
+ * *dt_inout carries dt in and the final (possibly trimmed) dt out.
+ * Synchronous; returns MFC_ERR_STATE if a kernel flagged a NaN. */
+int mfc_gpu_run(mfc_gpu_ctx* ctx, int t_step_start, int t_step_stop, double* dt_inout);
+
+/* Waits for the context's stream and returns the accumulated device status
+ * bits (MFC_FLAG_*) in *flags; clears them when clear != 0. */
+int mfc_gpu_status(mfc_gpu_ctx* ctx, uint32_t* flags, int clear);
+
+/* The CUDA stream (cudaStream_t) the context launches on, for event timing. */
+void* mfc_gpu_stream(mfc_gpu_ctx* ctx);
+
+/* Number of kernel launches the context has issued since init. */
+int64_t mfc_gpu_launch_count(const mfc_gpu_ctx* ctx);
+
+/* Frees all device memory of the context. */
+int mfc_gpu_finalize(mfc_gpu_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MFC_GPU_H */

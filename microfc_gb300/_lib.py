@@ -1,0 +1,97 @@
+"""ctypes binding of ``libmfc_gpu.so`` (the C ABI in include/mfc_gpu.h).
+
+The library is built in-tree by :mod:`microfc_gb300.build`.  There is no CPU
+fallback: if the library cannot be built or loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+MFC_MAX_FLUIDS = 4
+MFC_OK, MFC_ERR_INVALID, MFC_ERR_CUDA, MFC_ERR_NOMEM, MFC_ERR_STATE = 0, 1, 2, 3, 4
+MFC_FLAG_NAN, MFC_FLAG_NEG_PRESSURE, MFC_FLAG_TIMEOUT = 0x1, 0x2, 0x4
+MFC_PREC_FP64, MFC_PREC_SPLIT = 0, 1
+
+# every symbol include/mfc_gpu.h declares (checked by the tests)
+EXPORTS = (
+    "mfc_gpu_abi_version", "mfc_gpu_last_error", "mfc_gpu_init", "mfc_gpu_sys_size",
+    "mfc_gpu_upload", "mfc_gpu_download", "mfc_gpu_upload_state", "mfc_gpu_download_state",
+    "mfc_gpu_compute_rhs", "mfc_gpu_tvd_rk", "mfc_gpu_run", "mfc_gpu_status", "mfc_gpu_stream",
+    "mfc_gpu_launch_count", "mfc_gpu_finalize",
+)
+
+
+class MfcParams(ctypes.Structure):
+    _fields_ = [
+        ("m", ctypes.c_int32), ("n", ctypes.c_int32), ("p", ctypes.c_int32),
+        ("num_fluids", ctypes.c_int32),
+        ("weno_order", ctypes.c_int32),
+        ("weno_eps", ctypes.c_double),
+        ("time_stepper", ctypes.c_int32),
+        ("bc_x_beg", ctypes.c_int32), ("bc_x_end", ctypes.c_int32),
+        ("bc_y_beg", ctypes.c_int32), ("bc_y_end", ctypes.c_int32),
+        ("bc_z_beg", ctypes.c_int32), ("bc_z_end", ctypes.c_int32),
+        ("gammas", ctypes.c_double * MFC_MAX_FLUIDS),
+        ("pi_infs", ctypes.c_double * MFC_MAX_FLUIDS),
+        ("x_cb", ctypes.POINTER(ctypes.c_double)),
+        ("y_cb", ctypes.POINTER(ctypes.c_double)),
+        ("z_cb", ctypes.POINTER(ctypes.c_double)),
+        ("precision", ctypes.c_int32),
+        ("device", ctypes.c_int32),
+    ]
+
+
+class MfcError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[mfc_gpu error {code}] {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    from . import build
+    return build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) the in-tree CUDA library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    from . import build
+    if build_if_missing and not build.up_to_date():
+        build.build()
+    if not os.path.exists(build.LIB):
+        raise MfcError(MFC_ERR_CUDA, f"{build.LIB} is missing: build it with python -m microfc_gb300.build")
+    L = ctypes.CDLL(build.LIB)
+    dp = ctypes.POINTER(ctypes.c_double)
+    vp = ctypes.c_void_p
+    i64 = ctypes.c_int64
+    L.mfc_gpu_abi_version.restype = ctypes.c_int
+    L.mfc_gpu_last_error.restype = ctypes.c_char_p
+    L.mfc_gpu_init.argtypes = [ctypes.POINTER(MfcParams), ctypes.POINTER(vp)]
+    L.mfc_gpu_sys_size.argtypes = [vp]
+    L.mfc_gpu_upload.argtypes = [vp, ctypes.c_int, dp, i64, i64]
+    L.mfc_gpu_download.argtypes = [vp, ctypes.c_int, dp, i64, i64]
+    L.mfc_gpu_upload_state.argtypes = [vp, dp]
+    L.mfc_gpu_download_state.argtypes = [vp, dp]
+    L.mfc_gpu_compute_rhs.argtypes = [vp, dp, dp]
+    L.mfc_gpu_tvd_rk.argtypes = [vp, ctypes.c_double, ctypes.c_int]
+    L.mfc_gpu_run.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp]
+    L.mfc_gpu_status.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32), ctypes.c_int]
+    L.mfc_gpu_stream.argtypes = [vp]
+    L.mfc_gpu_stream.restype = vp
+    L.mfc_gpu_launch_count.argtypes = [vp]
+    L.mfc_gpu_launch_count.restype = i64
+    L.mfc_gpu_finalize.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def check(rc: int) -> None:
+    if rc != MFC_OK:
+        msg = load().mfc_gpu_last_error().decode(errors="replace")
+        raise MfcError(rc, msg)

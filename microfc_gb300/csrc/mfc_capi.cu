@@ -1,0 +1,508 @@
+// C ABI of the GB300 MicroFC hot path (declared in include/mfc_gpu.h).
+//
+// Host side: validates the case like s_check_input_file
+// (src/simulation/m_start_up.fpp:117-290), builds the grid ghost layers
+// (m_start_up.fpp:517-655) and the grid-dependent WENO coefficients
+// (src/simulation/m_weno.fpp:168-363) once, uploads them, and drives the
+// fused stage kernels for the TVD RK schemes of m_time_steppers.fpp and the
+// time loop of p_main.fpp.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/mfc_gpu.h"
+#include "mfc_launch.h"
+
+namespace {
+
+thread_local std::string g_err = "";
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define MFC_CUDA(call)                                                                            \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess) return fail(MFC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+std::once_flag g_reg_once;
+std::vector<mfc::StageEntry> g_reg;
+
+void build_registry() {
+  std::call_once(g_reg_once, [] {
+    mfc::register_stage_1d(g_reg);
+    mfc::register_stage_2d_fp64(g_reg);
+    mfc::register_stage_2d_fp32(g_reg);
+  });
+}
+
+// ---------------------------------------------------------------------------
+// Grid ghost layers and WENO coefficients (host, FP64).
+struct AxisHost {
+  int s = 0, b = 0;             // s = last interior index (m), b = buff_size
+  std::vector<double> cb, d;    // cb(-1-b : s+b), d(-b : s+b)
+  double& CB(int i) { return cb[(size_t)(i + 1 + b)]; }
+  double& D(int i) { return d[(size_t)(i + b)]; }
+};
+
+// s_populate_grid_variables_buffers, m_start_up.fpp:517-655 (widths and
+// boundaries only; cell centres are not used by the hot path).
+void grid_ghosts(AxisHost& a, int bcb, int bce) {
+  const int s = a.s, b = a.b;
+  for (int i = 0; i <= s; ++i) a.D(i) = a.CB(i) - a.CB(i - 1);
+  for (int i = 1; i <= b; ++i) a.D(-i) = bcb <= -3 ? a.D(0) : bcb == -2 ? a.D(i - 1) : a.D(s - (i - 1));
+  for (int i = 1; i <= b; ++i) a.CB(-1 - i) = a.CB(-i) - a.D(-i);
+  for (int i = 1; i <= b; ++i) a.D(s + i) = bce <= -3 ? a.D(s) : bce == -2 ? a.D(s - (i - 1)) : a.D(i - 1);
+  for (int i = 1; i <= b; ++i) a.CB(s + i) = a.CB(s + (i - 1)) + a.D(s + i);
+}
+
+// One cell's record: polyL[3][2], polyR[3][2], dL[3], dR[3], beta[3][3]
+// (record layout of mfc::kPL .. mfc::kBeta).  Formulas of
+// s_compute_weno_coefficients, m_weno.fpp:193-346, for cell i+1 from the
+// boundaries s_cb(i-2 .. i+3).
+void weno_record(AxisHost& a, int i, int wo, double* r) {
+  auto S = [&](int k) { return a.CB(k); };
+  auto sq = [](double x) { return x * x; };
+  double* pL = r + mfc::kPL;
+  double* pR = r + mfc::kPR;
+  double* dL = r + mfc::kDL;
+  double* dR = r + mfc::kDR;
+  double* be = r + mfc::kBeta;
+  std::fill(r, r + mfc::kNumCoef, 0.0);
+  if (wo == 3) {
+    pR[0] = (S(i) - S(i + 1)) / (S(i) - S(i + 2));
+    pR[2] = (S(i) - S(i + 1)) / (S(i - 1) - S(i + 1));
+    pL[0] = -pR[0];
+    pL[2] = -pR[2];
+    dR[0] = (S(i - 1) - S(i + 1)) / (S(i - 1) - S(i + 2));
+    dL[0] = (S(i - 1) - S(i)) / (S(i - 1) - S(i + 2));
+    dR[1] = 1.0 - dR[0];
+    dL[1] = 1.0 - dL[0];
+    be[0] = 4.0 * sq(S(i) - S(i + 1)) / sq(S(i) - S(i + 2));
+    be[3] = 4.0 * sq(S(i) - S(i + 1)) / sq(S(i - 1) - S(i + 1));
+    return;
+  }
+  // polynomial coefficients [k][j] -> index 2k+j
+  pR[0] = ((S(i) - S(i + 1)) * (S(i + 1) - S(i + 2))) / ((S(i) - S(i + 3)) * (S(i + 3) - S(i + 1)));
+  pR[2] = ((S(i - 1) - S(i + 1)) * (S(i + 1) - S(i))) / ((S(i - 1) - S(i + 2)) * (S(i + 2) - S(i)));
+  pR[3] = ((S(i) - S(i + 1)) * (S(i + 1) - S(i + 2))) / ((S(i - 1) - S(i + 1)) * (S(i - 1) - S(i + 2)));
+  pR[5] = ((S(i) - S(i + 1)) * (S(i + 1) - S(i - 1))) / ((S(i - 2) - S(i)) * (S(i - 2) - S(i + 1)));
+  pL[0] = ((S(i + 1) - S(i)) * (S(i) - S(i + 2))) / ((S(i) - S(i + 3)) * (S(i + 3) - S(i + 1)));
+  pL[2] = ((S(i) - S(i - 1)) * (S(i) - S(i + 1))) / ((S(i - 1) - S(i + 2)) * (S(i) - S(i + 2)));
+  pL[3] = ((S(i + 1) - S(i)) * (S(i) - S(i + 2))) / ((S(i - 1) - S(i + 1)) * (S(i - 1) - S(i + 2)));
+  pL[5] = ((S(i - 1) - S(i)) * (S(i) - S(i + 1))) / ((S(i - 2) - S(i)) * (S(i - 2) - S(i + 1)));
+  pR[1] = ((S(i) - S(i + 2)) + (S(i + 1) - S(i + 3))) / ((S(i) - S(i + 2)) * (S(i) - S(i + 3))) * ((S(i) - S(i + 1)));
+  pR[4] = ((S(i - 2) - S(i + 1)) + (S(i - 1) - S(i + 1))) / ((S(i - 1) - S(i + 1)) * (S(i + 1) - S(i - 2))) *
+          ((S(i + 1) - S(i)));
+  pL[1] = ((S(i) - S(i + 2)) + (S(i) - S(i + 3))) / ((S(i) - S(i + 2)) * (S(i) - S(i + 3))) * ((S(i + 1) - S(i)));
+  pL[4] = ((S(i - 2) - S(i)) + (S(i - 1) - S(i + 1))) / ((S(i - 2) - S(i + 1)) * (S(i + 1) - S(i - 1))) *
+          ((S(i) - S(i + 1)));
+  dR[0] = ((S(i - 2) - S(i + 1)) * (S(i + 1) - S(i - 1))) / ((S(i - 2) - S(i + 3)) * (S(i + 3) - S(i - 1)));
+  dR[2] = ((S(i + 1) - S(i + 2)) * (S(i + 1) - S(i + 3))) / ((S(i - 2) - S(i + 2)) * (S(i - 2) - S(i + 3)));
+  dL[0] = ((S(i - 2) - S(i)) * (S(i) - S(i - 1))) / ((S(i - 2) - S(i + 3)) * (S(i + 3) - S(i - 1)));
+  dL[2] = ((S(i) - S(i + 2)) * (S(i) - S(i + 3))) / ((S(i - 2) - S(i + 2)) * (S(i - 2) - S(i + 3)));
+  dR[1] = 1.0 - dR[0] - dR[2];
+  dL[1] = 1.0 - dL[0] - dL[2];
+  const double h = S(i) - S(i + 1);
+  be[0] = 4.0 * sq(h) *
+          (10.0 * sq(S(i + 1) - S(i)) + (S(i + 1) - S(i)) * (S(i + 2) - S(i + 1)) + sq(S(i + 2) - S(i + 1))) /
+          (sq(S(i) - S(i + 3)) * sq(S(i + 1) - S(i + 3)));
+  be[1] = 4.0 * sq(h) *
+          (19.0 * sq(S(i + 1) - S(i)) - (S(i + 1) - S(i)) * (S(i + 3) - S(i + 1)) +
+           2.0 * (S(i + 2) - S(i)) * ((S(i + 2) - S(i)) + (S(i + 3) - S(i + 1)))) /
+          ((S(i) - S(i + 2)) * sq(S(i) - S(i + 3)) * (S(i + 3) - S(i + 1)));
+  be[2] = 4.0 * sq(h) *
+          (10.0 * sq(S(i + 1) - S(i)) + (S(i + 1) - S(i)) * ((S(i + 2) - S(i)) + (S(i + 3) - S(i + 1))) +
+           sq((S(i + 2) - S(i)) + (S(i + 3) - S(i + 1)))) /
+          (sq(S(i) - S(i + 2)) * sq(S(i) - S(i + 3)));
+  be[3] = 4.0 * sq(h) *
+          (10.0 * sq(S(i + 1) - S(i)) + sq(S(i) - S(i - 1)) + (S(i) - S(i - 1)) * (S(i + 1) - S(i))) /
+          (sq(S(i - 1) - S(i + 2)) * sq(S(i) - S(i + 2)));
+  be[4] = 4.0 * sq(h) *
+          ((S(i) - S(i + 1)) * ((S(i) - S(i - 1)) + 20.0 * (S(i + 1) - S(i))) +
+           (2.0 * (S(i) - S(i - 1)) + (S(i + 1) - S(i))) * (S(i + 2) - S(i))) /
+          ((S(i + 1) - S(i - 1)) * sq(S(i - 1) - S(i + 2)) * (S(i + 2) - S(i)));
+  be[5] = 4.0 * sq(h) *
+          (10.0 * sq(S(i + 1) - S(i)) + (S(i + 1) - S(i)) * (S(i + 2) - S(i + 1)) + sq(S(i + 2) - S(i + 1))) /
+          (sq(S(i - 1) - S(i + 1)) * sq(S(i - 1) - S(i + 2)));
+  be[6] = 4.0 * sq(h) *
+          (12.0 * sq(S(i + 1) - S(i)) + sq((S(i) - S(i - 2)) + (S(i) - S(i - 1))) +
+           3.0 * ((S(i) - S(i - 2)) + (S(i) - S(i - 1))) * (S(i + 1) - S(i))) /
+          (sq(S(i - 2) - S(i + 1)) * sq(S(i - 1) - S(i + 1)));
+  be[7] = 4.0 * sq(h) *
+          (19.0 * sq(S(i + 1) - S(i)) + ((S(i) - S(i - 2)) * (S(i) - S(i + 1))) +
+           2.0 * (S(i + 1) - S(i - 1)) * ((S(i) - S(i - 2)) + (S(i + 1) - S(i - 1)))) /
+          ((S(i - 2) - S(i)) * sq(S(i - 2) - S(i + 1)) * (S(i + 1) - S(i - 1)));
+  be[8] = 4.0 * sq(h) *
+          (10.0 * sq(S(i + 1) - S(i)) + sq(S(i) - S(i - 1)) + (S(i) - S(i - 1)) * (S(i + 1) - S(i))) /
+          (sq(S(i - 2) - S(i)) * sq(S(i - 2) - S(i + 1)));
+}
+
+}  // namespace
+
+struct mfc_gpu_ctx {
+  mfc_params prm{};
+  int nd = 1, S = 0, b = 0;
+  int n[3] = {1, 1, 1};
+  int64_t pitch = 0, sy = 0, sz = 0, sv = 0, reg_elems = 0;
+  double* state = nullptr;      // 3 registers
+  double* reg[3] = {nullptr, nullptr, nullptr};
+  double* rhs = nullptr;
+  double* tables = nullptr;     // inv_d and coefficient tables
+  uint32_t* status = nullptr;
+  cudaStream_t stream = nullptr;
+  mfc::DevParams dev{};
+  const mfc::StageEntry* stage = nullptr;
+  int64_t launches = 0;
+};
+
+namespace {
+
+int validate(const mfc_params* p) {
+  if (!p) return fail(MFC_ERR_INVALID, "params is NULL");
+  if (p->m <= 0) return fail(MFC_ERR_INVALID, "Unsupported value of m");
+  if (p->n < 0 || p->p < 0) return fail(MFC_ERR_INVALID, "Unsupported value of n or p");
+  if (p->p > 0 && p->n == 0) return fail(MFC_ERR_INVALID, "p > 0 requires n > 0");
+  if (p->p > 0) return fail(MFC_ERR_INVALID, "3-D cases are not built into this library yet");
+  if (p->num_fluids < 1 || p->num_fluids > 2) return fail(MFC_ERR_INVALID, "Unsupported value of num_fluids (1 or 2)");
+  if (p->weno_order != 1 && p->weno_order != 3 && p->weno_order != 5)
+    return fail(MFC_ERR_INVALID, "Unsupported value of weno_order");
+  const int stcls = 5 * p->weno_order;  // num_stcls_min*weno_order, m_start_up.fpp:182-189
+  if (p->m + 1 < stcls) return fail(MFC_ERR_INVALID, "Unsupported combination of values of m and weno_order");
+  if (p->n > 0 && p->n + 1 < stcls) return fail(MFC_ERR_INVALID, "Unsupported combination of values of n and weno_order");
+  if (!(p->weno_eps > 0.0) || p->weno_eps > 1e-6) return fail(MFC_ERR_INVALID, "Unsupported value of weno_eps");
+  if (p->time_stepper < 1 || p->time_stepper > 3) return fail(MFC_ERR_INVALID, "Unsupported value of time_stepper");
+  const int bcs[6] = {p->bc_x_beg, p->bc_x_end, p->bc_y_beg, p->bc_y_end, p->bc_z_beg, p->bc_z_end};
+  const int ndim = 1 + (p->n > 0) + (p->p > 0);
+  for (int d = 0; d < ndim; ++d) {
+    for (int e = 0; e < 2; ++e) {
+      const int bc = bcs[2 * d + e];
+      if (bc < -12 || bc > -1)
+        return fail(MFC_ERR_INVALID, "Unsupported boundary condition (processor boundaries need a halo exchange)");
+    }
+    if ((bcs[2 * d] == -1) != (bcs[2 * d + 1] == -1))
+      return fail(MFC_ERR_INVALID, "Periodic boundaries must be set at both ends");
+  }
+  for (int f = 0; f < p->num_fluids; ++f) {
+    if (!(p->gammas[f] > 0.0)) return fail(MFC_ERR_INVALID, "Unsupported value of fluid_pp%gamma");
+    if (p->pi_infs[f] < 0.0) return fail(MFC_ERR_INVALID, "Unsupported value of fluid_pp%pi_inf");
+  }
+  if (!p->x_cb) return fail(MFC_ERR_INVALID, "x_cb is NULL");
+  if (p->n > 0 && !p->y_cb) return fail(MFC_ERR_INVALID, "y_cb is NULL");
+  if (p->precision != MFC_PREC_FP64 && p->precision != MFC_PREC_SPLIT)
+    return fail(MFC_ERR_INVALID, "Unsupported precision");
+  return MFC_OK;
+}
+
+int launch_stage(mfc_gpu_ctx* c, const double* qin, const double* qbase, double* qout, double dt, int kind) {
+  cudaError_t e = c->stage->launch(c->dev, qin, qbase, qout, dt, kind, c->stream);
+  if (e != cudaSuccess) return fail(MFC_ERR_CUDA, std::string("stage launch: ") + cudaGetErrorString(e));
+  c->launches += 1;
+  return MFC_OK;
+}
+
+// cons -> prim of the interior cells (for mfc_gpu_compute_rhs's prim output).
+template <int ND, int NF>
+__global__ void prim_kernel(const mfc::DevParams P, const double* __restrict__ q, double* __restrict__ out) {
+  using Q = mfc::Eqs<ND, NF>;
+  const int64_t cells = (int64_t)P.n[0] * P.n[1] * P.n[2];
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < cells; c += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(c % P.n[0]);
+    const int y = (int)((c / P.n[0]) % P.n[1]);
+    const int z = (int)(c / ((int64_t)P.n[0] * P.n[1]));
+    const int64_t o = z * P.sz + y * P.sy + x;
+    double v[Q::S];
+#pragma unroll
+    for (int k = 0; k < Q::S; ++k) v[k] = q[o + k * P.sv];
+    mfc::cons_to_prim<ND, NF>(v, P);
+#pragma unroll
+    for (int k = 0; k < Q::S; ++k) out[o + k * P.sv] = v[k];
+  }
+}
+
+int copy_var(mfc_gpu_ctx* c, double* dev_reg, int var, const double* host, double* host_out, int64_t ld_y,
+             int64_t ld_z) {
+  if (var < 0 || var >= c->S) return fail(MFC_ERR_INVALID, "variable index out of range");
+  if (ld_y < c->n[0] || (c->n[2] > 1 && ld_z < ld_y * c->n[1]))
+    return fail(MFC_ERR_INVALID, "leading dimension smaller than the interior extent");
+  for (int z = 0; z < c->n[2]; ++z) {
+    double* d = dev_reg + var * c->sv + z * c->sz;
+    if (host) {
+      MFC_CUDA(cudaMemcpy2DAsync(d, (size_t)c->sy * 8, host + z * ld_z, (size_t)ld_y * 8, (size_t)c->n[0] * 8,
+                                 (size_t)c->n[1], cudaMemcpyHostToDevice, c->stream));
+    } else {
+      MFC_CUDA(cudaMemcpy2DAsync(host_out + z * ld_z, (size_t)ld_y * 8, d, (size_t)c->sy * 8, (size_t)c->n[0] * 8,
+                                 (size_t)c->n[1], cudaMemcpyDeviceToHost, c->stream));
+    }
+  }
+  return MFC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mfc_gpu_abi_version(void) { return MFC_GPU_ABI_VERSION; }
+
+const char* mfc_gpu_last_error(void) { return g_err.c_str(); }
+
+int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
+  if (!out) return fail(MFC_ERR_INVALID, "ctx_out is NULL");
+  *out = nullptr;
+  int rc = validate(p);
+  if (rc) return rc;
+  build_registry();
+  MFC_CUDA(cudaSetDevice(p->device));
+
+  auto* c = new mfc_gpu_ctx();
+  c->prm = *p;
+  c->nd = 1 + (p->n > 0) + (p->p > 0);
+  c->S = 2 * p->num_fluids + c->nd + 1;
+  const int polyn = (p->weno_order - 1) / 2;
+  c->b = polyn + 2;
+  c->n[0] = p->m + 1;
+  c->n[1] = p->n + 1;
+  c->n[2] = p->p + 1;
+  c->pitch = (c->n[0] + 31) / 32 * 32;  // 256-byte rows
+  c->sy = c->pitch;
+  c->sz = c->sy * c->n[1];
+  c->sv = c->sz * c->n[2];
+  c->reg_elems = c->sv * c->S;
+
+  for (const auto& e : g_reg) {
+    if (e.nd == c->nd && e.nf == p->num_fluids && e.wo == p->weno_order && e.prec == p->precision) {
+      c->stage = &e;
+      break;
+    }
+  }
+  if (!c->stage) {
+    delete c;
+    return fail(MFC_ERR_INVALID, "no kernel compiled for this dimensionality / fluid count / WENO order / precision");
+  }
+
+  auto cleanup = [&](int code) {
+    mfc_gpu_finalize(c);
+    return code;
+  };
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return cleanup(fail(MFC_ERR_CUDA, cudaGetErrorString(e)));
+  if ((e = cudaMalloc(&c->state, sizeof(double) * c->reg_elems * 3)) != cudaSuccess)
+    return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
+  if ((e = cudaMalloc(&c->rhs, sizeof(double) * c->reg_elems)) != cudaSuccess)
+    return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
+  if ((e = cudaMalloc(&c->status, sizeof(uint32_t))) != cudaSuccess)
+    return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
+  cudaMemsetAsync(c->state, 0, sizeof(double) * c->reg_elems * 3, c->stream);
+  cudaMemsetAsync(c->status, 0, sizeof(uint32_t), c->stream);
+  for (int r = 0; r < 3; ++r) c->reg[r] = c->state + r * c->reg_elems;
+
+  // grid tables: per direction inv_d[n] then kNumCoef * (n + 2*pad) coefficients
+  const double* cbs[3] = {p->x_cb, p->y_cb, p->z_cb};
+  const int bcb[3] = {p->bc_x_beg, p->bc_y_beg, p->bc_z_beg};
+  const int bce[3] = {p->bc_x_end, p->bc_y_end, p->bc_z_end};
+  std::vector<double> host;
+  size_t off_inv[3] = {0, 0, 0}, off_coef[3] = {0, 0, 0};
+  int cstride[3] = {0, 0, 0};
+  for (int d = 0; d < c->nd; ++d) {
+    AxisHost a;
+    a.s = c->n[d] - 1;
+    a.b = c->b;
+    a.cb.assign((size_t)(a.s + 2 * a.b + 2), 0.0);
+    a.d.assign((size_t)(a.s + 2 * a.b + 1), 0.0);
+    for (int i = -1; i <= a.s; ++i) a.CB(i) = cbs[d][i + 1];
+    grid_ghosts(a, bcb[d], bce[d]);
+    for (int i = 0; i <= a.s; ++i)
+      if (!(a.D(i) > 0.0)) return cleanup(fail(MFC_ERR_INVALID, "cell boundaries must increase"));
+    off_inv[d] = host.size();
+    for (int i = 0; i <= a.s; ++i) host.push_back(1.0 / a.D(i));  // the reference's 1d0/dx(k)
+    const int pad = mfc::kCoefPad;
+    cstride[d] = c->n[d] + 2 * pad;
+    off_coef[d] = host.size();
+    host.resize(host.size() + (size_t)mfc::kNumCoef * cstride[d], 0.0);
+    if (p->weno_order > 1) {
+      // the reference defines coefficients for cells -b+polyn .. s+b-polyn
+      const int lo = -c->b + polyn, hi = a.s + c->b - polyn;
+      double rec[mfc::kNumCoef];
+      for (int cell = -pad; cell <= a.s + pad; ++cell) {
+        const int src = std::min(std::max(cell, lo), hi);
+        weno_record(a, src - 1, p->weno_order, rec);
+        for (int k = 0; k < mfc::kNumCoef; ++k) host[off_coef[d] + (size_t)k * cstride[d] + (cell + pad)] = rec[k];
+      }
+    }
+  }
+  if ((e = cudaMalloc(&c->tables, sizeof(double) * host.size())) != cudaSuccess)
+    return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
+  if ((e = cudaMemcpy(c->tables, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cleanup(fail(MFC_ERR_CUDA, cudaGetErrorString(e)));
+
+  mfc::DevParams& D = c->dev;
+  for (int d = 0; d < 3; ++d) {
+    D.n[d] = c->n[d];
+    D.bc_beg[d] = bcb[d];
+    D.bc_end[d] = bce[d];
+    D.inv_d[d] = d < c->nd ? c->tables + off_inv[d] : nullptr;
+    D.coef[d] = d < c->nd ? c->tables + off_coef[d] : nullptr;
+    D.cstride[d] = cstride[d];
+  }
+  D.sy = c->sy;
+  D.sz = c->sz;
+  D.sv = c->sv;
+  for (int f = 0; f < mfc::kMaxFluids; ++f) {
+    D.gammas[f] = f < p->num_fluids ? p->gammas[f] : 0.0;
+    D.pi_infs[f] = f < p->num_fluids ? p->pi_infs[f] : 0.0;
+  }
+  D.weno_eps = p->weno_eps;
+  D.coff = mfc::kCoefPad;
+  D.status = c->status;
+
+  if ((e = c->stage->prepare()) != cudaSuccess) return cleanup(fail(MFC_ERR_CUDA, cudaGetErrorString(e)));
+  if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cleanup(fail(MFC_ERR_CUDA, cudaGetErrorString(e)));
+  *out = c;
+  return MFC_OK;
+}
+
+int mfc_gpu_sys_size(const mfc_gpu_ctx* c) { return c ? c->S : 0; }
+
+int mfc_gpu_upload(mfc_gpu_ctx* c, int var, const double* host_sf, int64_t ld_y, int64_t ld_z) {
+  if (!c || !host_sf) return fail(MFC_ERR_INVALID, "NULL argument");
+  int rc = copy_var(c, c->reg[0], var, host_sf, nullptr, ld_y, ld_z);
+  if (rc) return rc;
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  return MFC_OK;
+}
+
+int mfc_gpu_download(mfc_gpu_ctx* c, int var, double* host_sf, int64_t ld_y, int64_t ld_z) {
+  if (!c || !host_sf) return fail(MFC_ERR_INVALID, "NULL argument");
+  int rc = copy_var(c, c->reg[0], var, nullptr, host_sf, ld_y, ld_z);
+  if (rc) return rc;
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  return MFC_OK;
+}
+
+int mfc_gpu_upload_state(mfc_gpu_ctx* c, const double* host_q) {
+  if (!c || !host_q) return fail(MFC_ERR_INVALID, "NULL argument");
+  const int64_t cells = (int64_t)c->n[0] * c->n[1] * c->n[2];
+  for (int v = 0; v < c->S; ++v) {
+    int rc = copy_var(c, c->reg[0], v, host_q + v * cells, nullptr, c->n[0], (int64_t)c->n[0] * c->n[1]);
+    if (rc) return rc;
+  }
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  return MFC_OK;
+}
+
+int mfc_gpu_download_state(mfc_gpu_ctx* c, double* host_q) {
+  if (!c || !host_q) return fail(MFC_ERR_INVALID, "NULL argument");
+  const int64_t cells = (int64_t)c->n[0] * c->n[1] * c->n[2];
+  for (int v = 0; v < c->S; ++v) {
+    int rc = copy_var(c, c->reg[0], v, nullptr, host_q + v * cells, c->n[0], (int64_t)c->n[0] * c->n[1]);
+    if (rc) return rc;
+  }
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  return MFC_OK;
+}
+
+int mfc_gpu_compute_rhs(mfc_gpu_ctx* c, double* rhs_out, double* prim_out) {
+  if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  int rc = launch_stage(c, c->reg[0], c->reg[0], c->rhs, 0.0, mfc::kRhsOnly);
+  if (rc) return rc;
+  const int64_t cells = (int64_t)c->n[0] * c->n[1] * c->n[2];
+  if (rhs_out) {
+    for (int v = 0; v < c->S; ++v)
+      if ((rc = copy_var(c, c->rhs, v, nullptr, rhs_out + v * cells, c->n[0], (int64_t)c->n[0] * c->n[1]))) return rc;
+  }
+  if (prim_out) {
+    double* tmp = c->reg[2];  // scratch register; not live between time steps
+    const int nf = c->prm.num_fluids;
+    const unsigned blocks = (unsigned)std::min<int64_t>((cells + 255) / 256, 4096);
+    if (c->nd == 1 && nf == 1) prim_kernel<1, 1><<<blocks, 256, 0, c->stream>>>(c->dev, c->reg[0], tmp);
+    else if (c->nd == 1 && nf == 2) prim_kernel<1, 2><<<blocks, 256, 0, c->stream>>>(c->dev, c->reg[0], tmp);
+    else if (c->nd == 2 && nf == 1) prim_kernel<2, 1><<<blocks, 256, 0, c->stream>>>(c->dev, c->reg[0], tmp);
+    else prim_kernel<2, 2><<<blocks, 256, 0, c->stream>>>(c->dev, c->reg[0], tmp);
+    MFC_CUDA(cudaGetLastError());
+    c->launches += 1;
+    for (int v = 0; v < c->S; ++v)
+      if ((rc = copy_var(c, tmp, v, nullptr, prim_out + v * cells, c->n[0], (int64_t)c->n[0] * c->n[1]))) return rc;
+  }
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  return MFC_OK;
+}
+
+int mfc_gpu_tvd_rk(mfc_gpu_ctx* c, double dt, int last_step) {
+  if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  if (last_step) return MFC_OK;  // s_compute_rhs returns before any update at t_step_stop
+  int rc;
+  double** R = c->reg;
+  switch (c->prm.time_stepper) {
+    case 1:
+      if ((rc = launch_stage(c, R[0], R[0], R[1], dt, mfc::kRkEuler))) return rc;
+      std::swap(R[0], R[1]);
+      return MFC_OK;
+    case 2:
+      if ((rc = launch_stage(c, R[0], R[0], R[1], dt, mfc::kRkEuler))) return rc;
+      return launch_stage(c, R[1], R[0], R[0], dt, mfc::kRk2Final);
+    default:
+      if ((rc = launch_stage(c, R[0], R[0], R[1], dt, mfc::kRkEuler))) return rc;
+      if ((rc = launch_stage(c, R[1], R[0], R[2], dt, mfc::kRk3Mid))) return rc;
+      return launch_stage(c, R[2], R[0], R[0], dt, mfc::kRk3Final);
+  }
+}
+
+int mfc_gpu_run(mfc_gpu_ctx* c, int t_step_start, int t_step_stop, double* dt_inout) {
+  if (!c || !dt_inout) return fail(MFC_ERR_INVALID, "NULL argument");
+  if (t_step_start < 0 || t_step_stop <= t_step_start)
+    return fail(MFC_ERR_INVALID, "Unsupported combination of values of t_step_start and t_step_stop");
+  double dt = *dt_inout;
+  int t_step = t_step_start;
+  double mytime = t_step == 0 ? 0.0 : t_step * dt;
+  const double finaltime = t_step_stop * dt;
+  for (;;) {
+    mytime = mytime + dt;
+    int rc = mfc_gpu_tvd_rk(c, dt, t_step == t_step_stop);
+    if (rc) return rc;
+    if (t_step == t_step_stop) break;
+    if ((mytime + dt) >= finaltime) dt = finaltime - mytime;
+    t_step = t_step + 1;
+  }
+  *dt_inout = dt;
+  uint32_t flags = 0;
+  int rc = mfc_gpu_status(c, &flags, 0);
+  if (rc) return rc;
+  if (flags & MFC_FLAG_NAN) return fail(MFC_ERR_STATE, "NaN or Inf in the conservative state");
+  return MFC_OK;
+}
+
+int mfc_gpu_status(mfc_gpu_ctx* c, uint32_t* flags, int clear) {
+  if (!c || !flags) return fail(MFC_ERR_INVALID, "NULL argument");
+  MFC_CUDA(cudaMemcpyAsync(flags, c->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  if (clear) MFC_CUDA(cudaMemsetAsync(c->status, 0, sizeof(uint32_t), c->stream));
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  return MFC_OK;
+}
+
+void* mfc_gpu_stream(mfc_gpu_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int64_t mfc_gpu_launch_count(const mfc_gpu_ctx* c) { return c ? c->launches : 0; }
+
+int mfc_gpu_finalize(mfc_gpu_ctx* c) {
+  if (!c) return MFC_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaFree(c->state);
+  cudaFree(c->rhs);
+  cudaFree(c->tables);
+  cudaFree(c->status);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return MFC_OK;
+}
+
+}  // extern "C"

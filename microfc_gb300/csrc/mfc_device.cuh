@@ -1,0 +1,248 @@
+// Device-side building blocks of the GB300 MicroFC hot path: the parameter
+// block every kernel receives by value, boundary-condition index mapping,
+// the stiffened-gas cons -> prim conversion, WENO1/3/5 and HLLC.
+//
+// The arithmetic follows the reference's operation order (file:line cited at
+// each function) so that the FP64 path matches the CPU reference to round-off
+// (nvcc contracts a*b+c into FMA, the only deviation).  RT is the type of the
+// reconstruction/Riemann arithmetic: double for the plain path, float for the
+// split-precision path.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mfc {
+
+constexpr int kMaxFluids = 4;
+constexpr int kNumCoef = 27;  // per cell: polyL[3][2], polyR[3][2], dL[3], dR[3], beta[3][3]
+// offsets inside one coefficient record
+constexpr int kPL = 0, kPR = 6, kDL = 12, kDR = 15, kBeta = 18;
+
+struct DevParams {
+  int n[3];             // interior cells per direction (m+1, n+1, p+1); 1 when unused
+  int64_t sy, sz, sv;   // element strides: y row, z plane, equation
+  int bc_beg[3], bc_end[3];
+  double gammas[kMaxFluids], pi_infs[kMaxFluids];
+  double weno_eps;
+  const double* inv_d[3];  // 1/dx(i) for i = 0 .. n-1 (per direction)
+  const double* coef[3];   // WENO coefficients, SoA: coef[k * cstride + (i + coff)],
+                           // cells i = -kCoefPad .. n-1+kCoefPad, coff = kCoefPad
+  int coff, cstride[3];
+  uint32_t* status;
+};
+
+// Equation index layout, m_global_parameters.fpp:302-310 (0-based).
+template <int ND, int NF>
+struct Eqs {
+  static constexpr int S = 2 * NF + ND + 1;
+  static constexpr int MOM = NF;
+  static constexpr int E = NF + ND;
+  static constexpr int ADV = NF + ND + 1;
+};
+
+// Ghost-cell mapping of m_rhs.fpp:686-908: a cell index c outside [0, n) is
+// replaced by the interior cell whose value the ghost holds; *flip is set
+// when the normal momentum changes sign (symmetry, bc -2).  bc <= -3 is
+// ghost-cell extrapolation, -2 symmetry, -1 periodic.  The final clamp only
+// matters for cells of partial edge tiles that lie beyond the ghost layers;
+// their values never reach a stored result.
+__device__ __forceinline__ int map_cell(int c, int n, int bcb, int bce, bool* flip) {
+  if (c < 0) {
+    *flip = (bcb == -2);
+    c = (bcb == -1) ? c + n : (bcb == -2) ? -c - 1 : 0;
+  } else if (c >= n) {
+    *flip = (bce == -2);
+    c = (bce == -1) ? c - n : (bce == -2) ? 2 * n - 1 - c : n - 1;
+  }
+  return c < 0 ? 0 : (c >= n ? n - 1 : c);
+}
+
+// Coefficient tables cover cells -kCoefPad .. n-1+kCoefPad; cells of partial
+// edge tiles beyond that range reuse the last record (their results are
+// never stored).
+constexpr int kCoefPad = 4;
+__device__ __forceinline__ int clamp_coef_index(int c, int n) {
+  return c < -kCoefPad ? -kCoefPad : (c > n - 1 + kCoefPad ? n - 1 + kCoefPad : c);
+}
+
+__device__ __forceinline__ bool not_finite(double x) {
+  const uint32_t hi = (uint32_t)(__double_as_longlong(x) >> 32);
+  return (hi & 0x7ff00000u) == 0x7ff00000u;
+}
+
+// cons -> prim of one cell, m_variables_conversion.fpp:326-373 and
+// s_compute_pressure :98-106.  q holds the S conservative values on entry and
+// the primitive ones on exit (partial densities and volume fractions are the
+// same in both sets).  Always FP64: the pressure recovery from total energy
+// cancels digits in the stiffened-gas EOS.
+template <int ND, int NF>
+__device__ __forceinline__ void cons_to_prim(double (&q)[Eqs<ND, NF>::S], const DevParams& P) {
+  using Q = Eqs<ND, NF>;
+  double rho = 0.0, gam = 0.0, pinf = 0.0, dyn = 0.0;
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    rho = rho + q[f];
+    gam = gam + q[Q::ADV + f] * P.gammas[f];
+    pinf = pinf + q[Q::ADV + f] * P.pi_infs[f];
+  }
+  rho = fmax(rho, 1e-16);
+#pragma unroll
+  for (int d = 0; d < ND; ++d) {
+    const double mom = q[Q::MOM + d];
+    const double vel = mom / rho;
+    q[Q::MOM + d] = vel;
+    dyn = dyn + 0.5 * mom * vel;
+  }
+  q[Q::E] = (q[Q::E] - dyn - pinf) / gam;
+}
+
+// WENO reconstruction of one cell from its stencil, m_weno.fpp:391-536.
+// c: the cell's kNumCoef coefficients; v[k] = value at offset k - 2.
+// Returns the left-face (x_{j-1/2}) and right-face (x_{j+1/2}) values.
+template <int WO, class RT>
+__device__ __forceinline__ void weno_cell(const RT* __restrict__ c, const RT (&v)[5], RT eps, RT& vL, RT& vR) {
+  if constexpr (WO == 1) {
+    vL = v[2];
+    vR = v[2];
+  } else if constexpr (WO == 3) {
+    const RT d0 = v[3] - v[2];
+    const RT dm1 = v[2] - v[1];
+    const RT b0 = c[kBeta + 0] * d0 * d0 + eps;
+    const RT b1 = c[kBeta + 3] * dm1 * dm1 + eps;
+    RT p0 = v[2] + c[kPL + 0] * d0;
+    RT p1 = v[2] + c[kPL + 2] * dm1;
+    RT a0 = c[kDL + 0] / (b0 * b0), a1 = c[kDL + 1] / (b1 * b1);
+    RT s = a0 + a1;
+    vL = (a0 / s) * p0 + (a1 / s) * p1;
+    p0 = v[2] + c[kPR + 0] * d0;
+    p1 = v[2] + c[kPR + 2] * dm1;
+    a0 = c[kDR + 0] / (b0 * b0);
+    a1 = c[kDR + 1] / (b1 * b1);
+    s = a0 + a1;
+    vR = (a0 / s) * p0 + (a1 / s) * p1;
+  } else {
+    const RT d1 = v[4] - v[3];
+    const RT d0 = v[3] - v[2];
+    const RT dm1 = v[2] - v[1];
+    const RT dm2 = v[1] - v[0];
+    const RT b0 = c[kBeta + 0] * d1 * d1 + c[kBeta + 1] * d1 * d0 + c[kBeta + 2] * d0 * d0 + eps;
+    const RT b1 = c[kBeta + 3] * d0 * d0 + c[kBeta + 4] * d0 * dm1 + c[kBeta + 5] * dm1 * dm1 + eps;
+    const RT b2 = c[kBeta + 6] * dm1 * dm1 + c[kBeta + 7] * dm1 * dm2 + c[kBeta + 8] * dm2 * dm2 + eps;
+    const RT bb0 = b0 * b0, bb1 = b1 * b1, bb2 = b2 * b2;
+    {
+      const RT p0 = v[2] + c[kPL + 0] * d1 + c[kPL + 1] * d0;
+      const RT p1 = v[2] + c[kPL + 2] * d0 + c[kPL + 3] * dm1;
+      const RT p2 = v[2] + c[kPL + 4] * dm1 + c[kPL + 5] * dm2;
+      const RT a0 = c[kDL + 0] / bb0, a1 = c[kDL + 1] / bb1, a2 = c[kDL + 2] / bb2;
+      const RT s = a0 + a1 + a2;
+      vL = (a0 / s) * p0 + (a1 / s) * p1 + (a2 / s) * p2;
+    }
+    {
+      const RT p0 = v[2] + c[kPR + 0] * d1 + c[kPR + 1] * d0;
+      const RT p1 = v[2] + c[kPR + 2] * d0 + c[kPR + 3] * dm1;
+      const RT p2 = v[2] + c[kPR + 4] * dm1 + c[kPR + 5] * dm2;
+      const RT a0 = c[kDR + 0] / bb0, a1 = c[kDR + 1] / bb1, a2 = c[kDR + 2] / bb2;
+      const RT s = a0 + a1 + a2;
+      vR = (a0 / s) * p0 + (a1 / s) * p1 + (a2 / s) * p2;
+    }
+  }
+}
+
+// HLLC flux across one face, m_riemann_solvers.fpp:132-327, for sweep
+// direction DIR.  qL/qR are the primitive states left and right of the face
+// (the reference's vR(j) and vL(j+1), after its argument swap at
+// m_rhs.fpp:545-556).  F receives the S fluxes, ustar the interface velocity
+// (vel_src(dir_idx(1)) -> flux_src(advxb)).
+//
+// xi_M and xi_P of the reference are exactly 1/0 or 0/1 (0.5 +- sign(0.5,
+// s_S)), so the flux is the upwind side's term alone; evaluating only that
+// side gives the same values and halves the arithmetic.
+template <int ND, int NF, int DIR, class RT>
+__device__ __forceinline__ void hllc_face(const RT (&qL)[Eqs<ND, NF>::S], const RT (&qR)[Eqs<ND, NF>::S],
+                                          const RT (&gam_i)[NF], const RT (&pi_i)[NF], RT (&F)[Eqs<ND, NF>::S],
+                                          RT& ustar) {
+  using Q = Eqs<ND, NF>;
+  RT rmsL = RT(0), rmsR = RT(0);
+#pragma unroll
+  for (int d = 0; d < ND; ++d) {
+    rmsL = rmsL + qL[Q::MOM + d] * qL[Q::MOM + d];
+    rmsR = rmsR + qR[Q::MOM + d] * qR[Q::MOM + d];
+  }
+  const RT pL = qL[Q::E], pR = qR[Q::E];
+  RT rhoL = RT(0), gamL = RT(0), piL = RT(0), rhoR = RT(0), gamR = RT(0), piR = RT(0);
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    rhoL = rhoL + qL[f];
+    gamL = gamL + qL[Q::ADV + f] * gam_i[f];
+    piL = piL + qL[Q::ADV + f] * pi_i[f];
+    rhoR = rhoR + qR[f];
+    gamR = gamR + qR[Q::ADV + f] * gam_i[f];
+    piR = piR + qR[Q::ADV + f] * pi_i[f];
+  }
+  const RT EL = gamL * pL + piL + RT(0.5) * rhoL * rmsL;
+  const RT ER = gamR * pR + piR + RT(0.5) * rhoR * rmsR;
+  const RT HL = (EL + pL) / rhoL;
+  const RT HR = (ER + pR) / rhoR;
+  const RT cL = sqrt((HL - RT(0.5) * rmsL) / gamL);
+  const RT cR = sqrt((HR - RT(0.5) * rmsR) / gamR);
+  const RT uL = qL[Q::MOM + DIR], uR = qR[Q::MOM + DIR];
+  const RT sL = fmin(uL - cL, uR - cR);
+  const RT sR = fmax(uR + cR, uL + cL);
+  const RT sS = (pR - pL + rhoL * uL * (sL - uL) - rhoR * uR * (sR - uR)) / (rhoL * (sL - uL) - rhoR * (sR - uR));
+  if (!signbit(sS)) {  // xi_M = 1, xi_P = 0
+    const RT sM = fmin(RT(0), sL);
+    const RT xi = (sL - uL) / (sL - sS);
+    const RT w = uL + sM * (xi - RT(1));
+#pragma unroll
+    for (int f = 0; f < NF; ++f) F[f] = qL[f] * w;
+#pragma unroll
+    for (int d = 0; d < ND; ++d) {
+      const RT vd = qL[Q::MOM + d];
+      if (d == DIR) F[Q::MOM + d] = rhoL * (uL * vd + sM * (xi * sS - vd)) + pL;
+      else F[Q::MOM + d] = rhoL * (uL * vd + sM * (xi * vd - vd));
+    }
+    F[Q::E] = uL * (EL + pL) + sM * (xi * (EL + (sS - uL) * (rhoL * sS + pL / (sL - uL))) - EL);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) F[Q::ADV + f] = qL[Q::ADV + f] * w;
+    ustar = w;
+  } else {  // xi_M = 0, xi_P = 1
+    const RT sP = fmax(RT(0), sR);
+    const RT xi = (sR - uR) / (sR - sS);
+    const RT w = uR + sP * (xi - RT(1));
+#pragma unroll
+    for (int f = 0; f < NF; ++f) F[f] = qR[f] * w;
+#pragma unroll
+    for (int d = 0; d < ND; ++d) {
+      const RT vd = qR[Q::MOM + d];
+      if (d == DIR) F[Q::MOM + d] = rhoR * (uR * vd + sP * (xi * sS - vd)) + pR;
+      else F[Q::MOM + d] = rhoR * (uR * vd + sP * (xi * vd - vd));
+    }
+    F[Q::E] = uR * (ER + pR) + sP * (xi * (ER + (sS - uR) * (rhoR * sS + pR / (sR - uR))) - ER);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) F[Q::ADV + f] = qR[Q::ADV + f] * w;
+    ustar = w;
+  }
+}
+
+// RK stage combinations, m_time_steppers.fpp:163-348, in the reference's
+// operation order.  base = q_cons_ts(1), in = the stage's input register.
+enum RkKind : int {
+  kRkEuler = 0,   // base + dt*rhs          (RK1; stage 1 of RK2/RK3)
+  kRk2Final = 1,  // (base + in + dt*rhs)/2
+  kRk3Mid = 2,    // (3*base + in + dt*rhs)/4
+  kRk3Final = 3,  // (base + 2*in + 2*dt*rhs)/3
+  kRhsOnly = 4,   // store rhs itself (s_compute_rhs)
+};
+
+__device__ __forceinline__ double rk_combine(int kind, double base, double in, double dt, double r) {
+  switch (kind) {
+    case kRkEuler: return base + dt * r;
+    case kRk2Final: return (base + in + dt * r) / 2.0;
+    case kRk3Mid: return (3.0 * base + in + dt * r) / 4.0;
+    case kRk3Final: return (base + 2.0 * in + 2.0 * dt * r) / 3.0;
+    default: return r;
+  }
+}
+
+}  // namespace mfc

@@ -1,0 +1,268 @@
+// The fused RK-stage kernel: one launch computes, for a TX x TY tile of
+// cells, everything MicroFC's s_compute_rhs does (m_rhs.fpp:405-679) and the
+// RK stage update that follows it (m_time_steppers.fpp:298-348):
+//
+//   phase 1  load the tile plus an H-cell halo of the conservative state from
+//            HBM (coalesced along x), apply the ghost-cell boundary conditions
+//            by index mapping and convert to primitive variables in FP64
+//   phase 2  x-direction WENO of every variable of every cell that borders a
+//            face of the tile
+//   phase 3  x-direction HLLC on the TX+1 faces of each row
+//   phase 4  x flux divergence + alpha*div(u) into registers, and y WENO
+//   phase 5  y-direction HLLC
+//   phase 6  y flux divergence, RK combination, store (coalesced)
+//
+// Interface states and fluxes live only in shared memory; per stage HBM sees
+// one read of the stage input (plus halo re-reads, which hit L2) and of the
+// RK base register, and one write of the stage output.
+#pragma once
+
+#include "mfc_device.cuh"
+
+namespace mfc {
+
+template <int ND, int NF, int WO, class RT, int TX, int TY>
+struct StageShape {
+  using Q = Eqs<ND, NF>;
+  static constexpr int S = Q::S;
+  static constexpr int H = (WO + 1) / 2;  // halo depth
+  static constexpr int TYE = (ND > 1) ? TY : 1;
+  static constexpr int LX = TX + 2 * H;
+  static constexpr int LY = (ND > 1) ? TY + 2 * H : 1;
+  static constexpr int NQ = S * LY * LX;  // primitive tile
+  // WENO outputs (left and right face values), x and y layouts share space
+  static constexpr int NWX = S * TYE * (TX + 2);
+  static constexpr int NWY = (ND > 1) ? S * (TY + 2) * TX : 0;
+  static constexpr int NW = NWX > NWY ? NWX : NWY;
+  // fluxes + interface velocity
+  static constexpr int NFX = (S + 1) * TYE * (TX + 1);
+  static constexpr int NFY = (ND > 1) ? (S + 1) * (TY + 1) * TX : 0;
+  static constexpr int NFL = NFX > NFY ? NFX : NFY;
+  static constexpr size_t kSmemBytes = sizeof(RT) * (size_t(NQ) + 2 * size_t(NW) + size_t(NFL));
+};
+
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const double* __restrict__ qin,
+                                                   const double* __restrict__ qbase, double* __restrict__ qout,
+                                                   const double dt, const int kind) {
+  using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
+  using Q = Eqs<ND, NF>;
+  constexpr int S = Sh::S, H = Sh::H, LX = Sh::LX, LY = Sh::LY, TYE = Sh::TYE;
+  constexpr int CPT = (TX * TYE + NT - 1) / NT;  // interior cells per thread
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  RT* sq = reinterpret_cast<RT*>(smem_raw);  // [S][LY][LX] primitive
+  RT* wl = sq + Sh::NQ;                       // left-face values
+  RT* wr = wl + Sh::NW;                       // right-face values
+  RT* fl = wr + Sh::NW;                       // fluxes [S+1][...]
+
+  const int tid = threadIdx.x;
+  const int x0 = blockIdx.x * TX;
+  const int y0 = (ND > 1) ? blockIdx.y * TY : 0;
+  const int nx = P.n[0], ny = P.n[1];
+
+  RT gam_i[NF], pi_i[NF];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    gam_i[f] = RT(P.gammas[f]);
+    pi_i[f] = RT(P.pi_infs[f]);
+  }
+  const RT eps = RT(P.weno_eps);
+
+  // ---- phase 1: load + BCs + cons -> prim --------------------------------
+  for (int c = tid; c < LX * LY; c += NT) {
+    const int lx = c % LX, ly = c / LX;
+    const bool hx = lx < H || lx >= H + TX;
+    const bool hy = (ND > 1) && (ly < H || ly >= H + TY);
+    if (hx && hy) continue;  // corners are never read
+    bool fx = false, fy = false;
+    const int gx = map_cell(x0 - H + lx, nx, P.bc_beg[0], P.bc_end[0], &fx);
+    const int gy = (ND > 1) ? map_cell(y0 - H + ly, ny, P.bc_beg[1], P.bc_end[1], &fy) : 0;
+    const double* src = qin + gy * P.sy + gx;
+    double q[S];
+#pragma unroll
+    for (int v = 0; v < S; ++v) q[v] = __ldg(src + v * P.sv);
+    if (fx) q[Q::MOM] = -q[Q::MOM];
+    if (ND > 1 && fy) q[Q::MOM + 1] = -q[Q::MOM + 1];
+    cons_to_prim<ND, NF>(q, P);
+#pragma unroll
+    for (int v = 0; v < S; ++v) sq[(v * LY + ly) * LX + lx] = RT(q[v]);
+  }
+  __syncthreads();
+
+  // ---- phase 2: x WENO over cells x0-1 .. x0+TX of the interior rows -------
+  {
+    constexpr int NCX = TX + 2;
+    const double* cf = P.coef[0];
+    const int cs = P.cstride[0];
+    for (int it = tid; it < S * TYE * NCX; it += NT) {
+      const int cx = it % NCX;
+      const int r = it / NCX;
+      const int ty = r % TYE, v = r / TYE;
+      const int ly = (ND > 1) ? ty + H : 0;
+      const int lx = cx + H - 1;
+      const RT* row = sq + (v * LY + ly) * LX;
+      RT st[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const int o = k - 2;
+        st[k] = (o >= -(WO / 2) && o <= WO / 2) ? row[lx + o] : RT(0);
+      }
+      RT c[kNumCoef];
+      if constexpr (WO > 1) {
+        const int gi = clamp_coef_index(x0 - 1 + cx, nx) + P.coff;
+#pragma unroll
+        for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
+      }
+      RT vl, vr;
+      weno_cell<WO, RT>(c, st, eps, vl, vr);
+      wl[(v * TYE + ty) * NCX + cx] = vl;
+      wr[(v * TYE + ty) * NCX + cx] = vr;
+    }
+  }
+  __syncthreads();
+
+  // ---- phase 3: x HLLC on faces x0-1/2 .. x0+TX-1/2 ------------------------
+  {
+    constexpr int NCX = TX + 2, NFXr = TX + 1;
+    for (int it = tid; it < TYE * NFXr; it += NT) {
+      const int f = it % NFXr, ty = it / NFXr;
+      const int gface = x0 - 1 + f;  // face gface+1/2
+      RT qL[S], qR[S], F[S], us;
+      const bool lfr = (gface == -1 && P.bc_beg[0] == -4);      // qL(-1) = qR(0)
+      const bool rfl = (gface == nx - 1 && P.bc_end[0] == -4);  // qR(m+1) = qL(m)
+#pragma unroll
+      for (int v = 0; v < S; ++v) {
+        const RT a = wr[(v * TYE + ty) * NCX + f];
+        const RT b = wl[(v * TYE + ty) * NCX + f + 1];
+        qL[v] = lfr ? b : a;
+        qR[v] = rfl ? a : b;
+      }
+      hllc_face<ND, NF, 0, RT>(qL, qR, gam_i, pi_i, F, us);
+#pragma unroll
+      for (int v = 0; v < S; ++v) fl[(v * TYE + ty) * NFXr + f] = F[v];
+      fl[(S * TYE + ty) * NFXr + f] = us;
+    }
+  }
+  __syncthreads();
+
+  // ---- phase 4: x flux divergence (registers) + y WENO ----------------------
+  double rhs[CPT][S];
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    const int e = tid + k * NT;
+    if (e >= TX * TYE) break;
+    const int tx = e % TX, ty = e / TX;
+    const int gx = x0 + tx;
+    constexpr int NFXr = TX + 1;
+    const double inv = __ldg(P.inv_d[0] + (gx < nx ? gx : nx - 1));
+#pragma unroll
+    for (int v = 0; v < S; ++v)
+      rhs[k][v] = inv * (double(fl[(v * TYE + ty) * NFXr + tx]) - double(fl[(v * TYE + ty) * NFXr + tx + 1]));
+    const double du = double(fl[(S * TYE + ty) * NFXr + tx + 1]) - double(fl[(S * TYE + ty) * NFXr + tx]);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      const double a = double(sq[((Q::ADV + f) * LY + (ND > 1 ? ty + H : 0)) * LX + tx + H]);
+      rhs[k][Q::ADV + f] = rhs[k][Q::ADV + f] + inv * a * du;
+    }
+  }
+  if constexpr (ND > 1) {
+    constexpr int NCY = TY + 2;
+    const double* cf = P.coef[1];
+    const int cs = P.cstride[1];
+    for (int it = tid; it < S * NCY * TX; it += NT) {
+      const int tx = it % TX;
+      const int r = it / TX;
+      const int cy = r % NCY, v = r / NCY;
+      const int ly = cy + H - 1, lx = tx + H;
+      const RT* col = sq + v * LY * LX + lx;
+      RT st[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const int o = k - 2;
+        st[k] = (o >= -(WO / 2) && o <= WO / 2) ? col[(ly + o) * LX] : RT(0);
+      }
+      RT c[kNumCoef];
+      if constexpr (WO > 1) {
+        const int gi = clamp_coef_index(y0 - 1 + cy, ny) + P.coff;
+#pragma unroll
+        for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
+      }
+      RT vl, vr;
+      weno_cell<WO, RT>(c, st, eps, vl, vr);
+      wl[(v * NCY + cy) * TX + tx] = vl;
+      wr[(v * NCY + cy) * TX + tx] = vr;
+    }
+    __syncthreads();
+
+    // ---- phase 5: y HLLC on faces y0-1/2 .. y0+TY-1/2 ----------------------
+    constexpr int NFYr = TY + 1;
+    for (int it = tid; it < NFYr * TX; it += NT) {
+      const int tx = it % TX, f = it / TX;
+      const int gface = y0 - 1 + f;
+      RT qL[S], qR[S], F[S], us;
+      const bool lfr = (gface == -1 && P.bc_beg[1] == -4);
+      const bool rfl = (gface == ny - 1 && P.bc_end[1] == -4);
+#pragma unroll
+      for (int v = 0; v < S; ++v) {
+        const RT a = wr[(v * NCY + f) * TX + tx];
+        const RT b = wl[(v * NCY + f + 1) * TX + tx];
+        qL[v] = lfr ? b : a;
+        qR[v] = rfl ? a : b;
+      }
+      hllc_face<ND, NF, 1, RT>(qL, qR, gam_i, pi_i, F, us);
+#pragma unroll
+      for (int v = 0; v < S; ++v) fl[(v * NFYr + f) * TX + tx] = F[v];
+      fl[(S * NFYr + f) * TX + tx] = us;
+    }
+    __syncthreads();
+
+    // ---- phase 6a: y flux divergence ------------------------------------------
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+      const int e = tid + k * NT;
+      if (e >= TX * TY) break;
+      const int tx = e % TX, ty = e / TX;
+      const int gy = y0 + ty;
+      const double inv = __ldg(P.inv_d[1] + (gy < ny ? gy : ny - 1));
+#pragma unroll
+      for (int v = 0; v < S; ++v)
+        rhs[k][v] = rhs[k][v] + inv * (double(fl[(v * NFYr + ty) * TX + tx]) - double(fl[(v * NFYr + ty + 1) * TX + tx]));
+      const double du = double(fl[(S * NFYr + ty + 1) * TX + tx]) - double(fl[(S * NFYr + ty) * TX + tx]);
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        const double a = double(sq[((Q::ADV + f) * LY + ty + H) * LX + tx + H]);
+        rhs[k][Q::ADV + f] = rhs[k][Q::ADV + f] + inv * a * du;
+      }
+    }
+  }
+
+  // ---- phase 6b: RK combination and store ------------------------------------
+  bool bad = false;
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    const int e = tid + k * NT;
+    if (e >= TX * TYE) break;
+    const int tx = e % TX, ty = e / TX;
+    const int gx = x0 + tx, gy = y0 + ty;
+    if (gx >= nx || (ND > 1 && gy >= ny)) continue;
+    const int64_t o = gy * P.sy + gx;
+#pragma unroll
+    for (int v = 0; v < S; ++v) {
+      double r = rhs[k][v];
+      double out;
+      if (kind == kRhsOnly) {
+        out = r;
+      } else {
+        const double b = __ldg(qbase + o + v * P.sv);
+        const double in = (kind == kRkEuler) ? b : __ldg(qin + o + v * P.sv);
+        out = rk_combine(kind, b, in, dt, r);
+      }
+      bad |= not_finite(out);
+      qout[o + v * P.sv] = out;
+    }
+  }
+  if (bad && P.status) atomicOr(P.status, 1u);
+}
+
+}  // namespace mfc

@@ -1,0 +1,17 @@
+// Instantiations of the fused stage kernel for 2-D cases, split precision:
+// FP32 WENO and HLLC, FP64 state, pressure recovery and RK update.
+#include "mfc_launch.h"
+
+namespace mfc {
+
+void register_stage_2d_fp32(std::vector<StageEntry>& r) {
+  r.push_back(stage_entry<2, 2, 5, float, 32, 16, 256>());
+  r.push_back(stage_entry<2, 2, 5, float, 32, 32, 512>());
+  r.push_back(stage_entry<2, 1, 5, float, 32, 16, 256>());
+  r.push_back(stage_entry<2, 2, 3, float, 32, 16, 256>());
+  r.push_back(stage_entry<2, 2, 1, float, 32, 16, 256>());
+  r.push_back(stage_entry<2, 1, 3, float, 32, 16, 256>());
+  r.push_back(stage_entry<2, 1, 1, float, 32, 16, 256>());
+}
+
+}  // namespace mfc

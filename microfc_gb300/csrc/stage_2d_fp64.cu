@@ -1,0 +1,21 @@
+// Instantiations of the fused stage kernel for 2-D cases, FP64 arithmetic.
+// Tile variants (TX x TY cells, NT threads) are chosen by the autotuner; the
+// first entry per configuration is the default.
+#include "mfc_launch.h"
+
+namespace mfc {
+
+void register_stage_2d_fp64(std::vector<StageEntry>& r) {
+#define MFC_2D(NF, WO)                                           \
+  r.push_back(stage_entry<2, NF, WO, double, 16, 16, 256>());   \
+  r.push_back(stage_entry<2, NF, WO, double, 32, 16, 512>());
+  MFC_2D(2, 5)
+  MFC_2D(1, 5)
+#undef MFC_2D
+  r.push_back(stage_entry<2, 2, 3, double, 16, 16, 256>());
+  r.push_back(stage_entry<2, 2, 1, double, 16, 16, 256>());
+  r.push_back(stage_entry<2, 1, 3, double, 16, 16, 256>());
+  r.push_back(stage_entry<2, 1, 1, double, 16, 16, 256>());
+}
+
+}  // namespace mfc

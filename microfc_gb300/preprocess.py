@@ -1,0 +1,140 @@
+"""Grid and initial condition: the reference's pre_process, vectorised.
+
+* uniform grid: src/pre_process/m_grid.f90:54-70
+* patches: line segment (1), circle (2), rectangle (3) from
+  src/pre_process/m_create_patches.fpp:47-313; sphere (8) and cuboid (9) are
+  their 3-D analogues (the reference is 2-D only)
+* smoothed-patch blending: src/pre_process/m_assign_patches.fpp:54-165
+* prim -> cons: src/common/m_variables_conversion.fpp:385-443
+
+Returns the cell boundaries x_cb(-1:m), y_cb(-1:n), z_cb(-1:p) and the
+conservative state [S, p+1, n+1, m+1] that the simulation reads from
+p_all/p0/0/*.dat.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .case import Case
+
+
+def uniform_grid(m: int, beg: float, end: float):
+    dx = (end - beg) / float(m + 1)
+    i = np.arange(m + 1, dtype=np.float64)
+    cc = beg + 5e-1 * dx * (2.0 * i + 1.0)
+    cb = np.empty(m + 2)
+    cb[:-1] = beg + dx * i
+    cb[-1] = end
+    return cb, cc, dx
+
+
+def generate(case: Case):
+    """Initial condition of a case; returns (x_cb, y_cb, z_cb, q_cons)."""
+    m, n, p = case.m, case.n, case.p
+    nf, nd, S = case.num_fluids, case.num_dims, case.sys_size
+    mb, E, ab = case.mom_idx, case.E_idx, case.adv_idx
+    x_cb, xcc, dx = uniform_grid(m, *case.x_domain)
+    y_cb, ycc, dy = uniform_grid(n, *case.y_domain) if n > 0 else (None, np.zeros(1), 0.0)
+    z_cb, zcc, dz = uniform_grid(p, *case.z_domain) if p > 0 else (None, np.zeros(1), 0.0)
+    Z, Y, X = np.meshgrid(zcc, ycc, xcc, indexing="ij")
+    shape = (p + 1, n + 1, m + 1)
+    prim = np.zeros((S,) + shape)
+    pid = np.zeros(shape, dtype=np.int64)
+
+    for ip, pt in enumerate(case.patches):
+        alter = np.isin(pid, (0,) + tuple(pt.alter_patch))
+        eta = np.ones(shape)
+        xc, yc, zc = pt.centroid
+        lx, ly, lz = pt.length
+        g = pt.geometry
+        smooth_id = pt.smooth_patch_id if pt.smooth_patch_id else ip + 1
+        if g == 1:
+            hit = ((xc - 0.5 * lx) <= X) & ((xc + 0.5 * lx) >= X) & alter
+        elif g in (3, 9):
+            hit = (((xc - 0.5 * lx) <= X) & ((xc + 0.5 * lx) >= X) &
+                   ((yc - 0.5 * ly) <= Y) & ((yc + 0.5 * ly) >= Y) & alter)
+            if g == 9:
+                hit &= ((zc - 0.5 * lz) <= Z) & ((zc + 0.5 * lz) >= Z)
+        elif g in (2, 8):
+            r2 = (X - xc) * (X - xc) + (Y - yc) * (Y - yc)
+            h = min(dx, dy)
+            if g == 8:
+                r2 = r2 + (Z - zc) * (Z - zc)
+                h = min(h, dz)
+            if pt.smoothen:
+                eta = np.tanh(pt.smooth_coeff / h * (np.sqrt(r2) - pt.radius)) * (-0.5) + 0.5
+            hit = ((r2 <= pt.radius * pt.radius) & alter) | (pid == smooth_id)
+        else:
+            raise ValueError(f"unsupported patch geometry {g}")
+        if not hit.any():
+            continue
+        e = eta[hit]
+        orig = prim[:, hit].copy()
+        for f in range(nf):
+            prim[f][hit] = e * pt.alpha_rho[f] + (1.0 - e) * orig[f]
+            prim[ab + f][hit] = e * pt.alpha[f] + (1.0 - e) * orig[ab + f]
+        for d in range(nd):
+            prim[mb + d][hit] = e * pt.vel[d] + (1.0 - e) * orig[mb + d]
+        prim[E][hit] = e * pt.pres + (1.0 - e) * orig[E]
+        owner = pid[hit]
+        owner[(1.0 - e) < 1e-16] = ip + 1
+        pid[hit] = owner
+
+    # prim -> cons, m_variables_conversion.fpp:406-443
+    q = np.empty_like(prim)
+    rho = np.zeros(shape)
+    gam = np.zeros(shape)
+    pinf = np.zeros(shape)
+    for f in range(nf):
+        rho = rho + prim[f]
+        gam = gam + prim[ab + f] * case.gammas[f]
+        pinf = pinf + prim[ab + f] * case.pi_infs[f]
+    q[:nf] = prim[:nf]
+    dyn = np.zeros(shape)
+    for d in range(nd):
+        q[mb + d] = rho * prim[mb + d]
+        dyn = dyn + q[mb + d] * prim[mb + d] / 2.0
+    q[E] = gam * prim[E] + dyn + pinf
+    q[ab:ab + nf] = prim[ab:ab + nf]
+    return x_cb, y_cb, z_cb, q
+
+
+def to_primitive(case: Case, q: np.ndarray) -> np.ndarray:
+    """cons -> prim (m_variables_conversion.fpp:326-373) of a whole state, FP64."""
+    nf, nd = case.num_fluids, case.num_dims
+    mb, E, ab = case.mom_idx, case.E_idx, case.adv_idx
+    prim = q.copy()
+    rho = np.zeros(q.shape[1:])
+    gam = np.zeros(q.shape[1:])
+    pinf = np.zeros(q.shape[1:])
+    for f in range(nf):
+        rho = rho + q[f]
+        gam = gam + q[ab + f] * case.gammas[f]
+        pinf = pinf + q[ab + f] * case.pi_infs[f]
+    rho = np.maximum(rho, 1e-16)
+    dyn = np.zeros(q.shape[1:])
+    for d in range(nd):
+        prim[mb + d] = q[mb + d] / rho
+        dyn = dyn + 0.5 * q[mb + d] * prim[mb + d]
+    prim[E] = (q[E] - dyn - pinf) / gam
+    return prim
+
+
+def max_wave_dt(case: Case, q: np.ndarray, cfl: float, x_cb, y_cb=None, z_cb=None) -> float:
+    """dt = cfl * min over cells of min_d dx_d/(|u_d| + c), with the mixture
+    sound speed of the reference's ICFL monitor (m_data_output.fpp:215-221)."""
+    prim = to_primitive(case, q)
+    nf, nd = case.num_fluids, case.num_dims
+    mb, E, ab = case.mom_idx, case.E_idx, case.adv_idx
+    rho = sum(prim[f] for f in range(nf))
+    gam = sum(prim[ab + f] * case.gammas[f] for f in range(nf))
+    pinf = sum(prim[ab + f] * case.pi_infs[f] for f in range(nf))
+    c = np.sqrt(((gam + 1.0) * prim[E] + pinf) / (gam * rho))
+    cbs = (x_cb, y_cb, z_cb)
+    best = np.inf
+    for d in range(nd):
+        w = np.diff(np.asarray(cbs[d]))
+        shp = [1, 1, 1]
+        shp[2 - d] = -1
+        best = min(best, float(np.min(w.reshape(shp) / (np.abs(prim[mb + d]) + c))))
+    return cfl * best

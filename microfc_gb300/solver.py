@@ -1,0 +1,145 @@
+"""Python host of the GB300 hot path, mirroring the reference's simulation
+interfaces.
+
+=====================================  =========================================
+reference (src/simulation/...)         here
+=====================================  =========================================
+s_initialize_*_module                  ``Simulation(case, ...)`` -> mfc_gpu_init
+!$acc update device(q_cons_ts(1))      ``Simulation.upload``    -> mfc_gpu_upload_state
+!$acc update host(q_cons_ts(1))        ``Simulation.download``  -> mfc_gpu_download_state
+s_compute_rhs (m_rhs.fpp:405)          ``Simulation.s_compute_rhs``
+s_1st/2nd/3rd_order_tvd_rk             ``Simulation.s_1st_order_tvd_rk`` ...
+p_main time loop (p_main.fpp:196-318)  ``Simulation.run``       -> mfc_gpu_run
+s_finalize_*_module                    ``Simulation.close``     -> mfc_gpu_finalize
+=====================================  =========================================
+
+Every call goes through the C ABI of ``libmfc_gpu.so``; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from . import preprocess
+from .case import Case
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Simulation:
+    """Device-resident state of one case (q_cons_ts, rhs, grid, WENO tables)."""
+
+    def __init__(self, case: Case, x_cb=None, y_cb=None, z_cb=None, q_cons=None, device: int = 0,
+                 check: bool = True):
+        if check:
+            case.check()
+        self.case = case
+        if x_cb is None or q_cons is None:
+            gx, gy, gz, gq = preprocess.generate(case)
+            x_cb = gx if x_cb is None else x_cb
+            y_cb = gy if y_cb is None else y_cb
+            z_cb = gz if z_cb is None else z_cb
+            q_cons = gq if q_cons is None else q_cons
+        self.L = _lib.load()
+        self._cb = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (x_cb, y_cb, z_cb)]
+        P = _lib.MfcParams()
+        P.m, P.n, P.p = case.m, case.n, case.p
+        P.num_fluids = case.num_fluids
+        P.weno_order = case.weno_order
+        P.weno_eps = case.weno_eps
+        P.time_stepper = case.time_stepper
+        P.bc_x_beg, P.bc_x_end = case.bc_x
+        P.bc_y_beg, P.bc_y_end = case.bc_y
+        P.bc_z_beg, P.bc_z_end = case.bc_z
+        for i in range(case.num_fluids):
+            P.gammas[i] = case.gammas[i]
+            P.pi_infs[i] = case.pi_infs[i]
+        P.x_cb = _dp(self._cb[0])
+        P.y_cb = _dp(self._cb[1]) if self._cb[1] is not None else None
+        P.z_cb = _dp(self._cb[2]) if self._cb[2] is not None else None
+        P.precision = _lib.MFC_PREC_SPLIT if case.precision == "split" else _lib.MFC_PREC_FP64
+        P.device = device
+        self._params = P
+        h = ctypes.c_void_p()
+        _lib.check(self.L.mfc_gpu_init(ctypes.byref(P), ctypes.byref(h)))
+        self._h = h
+        self.S = self.L.mfc_gpu_sys_size(h)
+        self.dt = case.dt
+        self.upload(q_cons)
+
+    # -- life cycle -----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.L.mfc_gpu_finalize(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state transfer -------------------------------------------------------
+    def upload(self, q: np.ndarray) -> None:
+        a = np.ascontiguousarray(q, dtype=np.float64).reshape(self.case.shape)
+        _lib.check(self.L.mfc_gpu_upload_state(self._h, _dp(a)))
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        a = out if out is not None else np.empty(self.case.shape, dtype=np.float64)
+        _lib.check(self.L.mfc_gpu_download_state(self._h, _dp(a)))
+        return a
+
+    def upload_var(self, var: int, sf: np.ndarray, ld_y: int, ld_z: int = 0) -> None:
+        """Copy one equation from a host array laid out like q_cons_vf(var)%sf."""
+        _lib.check(self.L.mfc_gpu_upload(self._h, int(var), _dp(sf), int(ld_y), int(ld_z)))
+
+    def download_var(self, var: int, sf: np.ndarray, ld_y: int, ld_z: int = 0) -> None:
+        _lib.check(self.L.mfc_gpu_download(self._h, int(var), _dp(sf), int(ld_y), int(ld_z)))
+
+    # -- the hot path -----------------------------------------------------------
+    def s_compute_rhs(self):
+        """RHS and primitive variables of the current state (both [S,p+1,n+1,m+1])."""
+        rhs = np.empty(self.case.shape)
+        prim = np.empty(self.case.shape)
+        _lib.check(self.L.mfc_gpu_compute_rhs(self._h, _dp(rhs), _dp(prim)))
+        return rhs, prim
+
+    def tvd_rk(self, t_step: int, dt: float | None = None) -> None:
+        """One call of the configured s_*_order_tvd_rk (asynchronous)."""
+        last = int(t_step == self.case.t_step_stop)
+        _lib.check(self.L.mfc_gpu_tvd_rk(self._h, float(self.dt if dt is None else dt), last))
+
+    s_1st_order_tvd_rk = s_2nd_order_tvd_rk = s_3rd_order_tvd_rk = tvd_rk
+
+    def run(self, t_step_start: int | None = None, t_step_stop: int | None = None) -> float:
+        """The p_main time loop; returns the (possibly trimmed) final dt."""
+        a = self.case.t_step_start if t_step_start is None else t_step_start
+        b = self.case.t_step_stop if t_step_stop is None else t_step_stop
+        dt = ctypes.c_double(self.case.dt)
+        _lib.check(self.L.mfc_gpu_run(self._h, int(a), int(b), ctypes.byref(dt)))
+        self.dt = dt.value
+        return dt.value
+
+    def status(self, clear: bool = False) -> int:
+        f = ctypes.c_uint32(0)
+        _lib.check(self.L.mfc_gpu_status(self._h, ctypes.byref(f), int(clear)))
+        return f.value
+
+    @property
+    def stream(self) -> int:
+        """The cudaStream_t the context launches on (as an integer handle)."""
+        return self.L.mfc_gpu_stream(self._h) or 0
+
+    @property
+    def launches(self) -> int:
+        return self.L.mfc_gpu_launch_count(self._h)

@@ -1,0 +1,137 @@
+// C ABI of the MicroFC oracle (test infrastructure only; see mfc_oracle.hpp).
+//
+// Loaded with ctypes by tests/, by __graft_entry__.smoke() and by the CPU
+// baseline leg of bench.py.  All arrays are x-fastest over the interior
+// cells (m+1)*(n+1)*(p+1) unless stated otherwise.
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "mfc_oracle.hpp"
+#include "mfc_oracle_ic.hpp"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using namespace mfc_oracle;
+
+extern "C" {
+
+// Mirrors the solver-relevant part of the reference's &user_inputs namelist
+// (src/simulation/m_start_up.fpp:73-83), plus the z extent p.
+struct mfo_params {
+  int m, n, p;
+  int num_fluids;
+  int weno_order;
+  double weno_eps;
+  int time_stepper;
+  int bc_x_beg, bc_x_end, bc_y_beg, bc_y_end, bc_z_beg, bc_z_end;
+  double gammas[kMaxFluids];
+  double pi_infs[kMaxFluids];
+};
+
+static Params to_params(const mfo_params* q) {
+  Params P;
+  P.m = q->m; P.n = q->n; P.p = q->p;
+  P.num_fluids = q->num_fluids;
+  P.weno_order = q->weno_order;
+  P.weno_eps = q->weno_eps;
+  P.time_stepper = q->time_stepper;
+  P.bc_x_beg = q->bc_x_beg; P.bc_x_end = q->bc_x_end;
+  P.bc_y_beg = q->bc_y_beg; P.bc_y_end = q->bc_y_end;
+  P.bc_z_beg = q->bc_z_beg; P.bc_z_end = q->bc_z_end;
+  for (int i = 0; i < kMaxFluids; ++i) { P.gammas[i] = q->gammas[i]; P.pi_infs[i] = q->pi_infs[i]; }
+  return P;
+}
+
+void* mfo_create(const mfo_params* q, const double* x_cb, const double* y_cb, const double* z_cb) {
+  auto* s = new (std::nothrow) Solver<double>();
+  if (!s) return nullptr;
+  s->init(to_params(q), x_cb, y_cb, z_cb);
+  return s;
+}
+
+void mfo_destroy(void* h) { delete static_cast<Solver<double>*>(h); }
+
+int mfo_sys_size(void* h) { return static_cast<Solver<double>*>(h)->S; }
+
+// reg: 0 = q_cons_ts(1), 1 = q_cons_ts(2)
+void mfo_set_state(void* h, int reg, const double* interior) {
+  auto* s = static_cast<Solver<double>*>(h);
+  const Params& P = s->P;
+  long c = 0;
+  for (int v = 0; v < s->S; ++v)
+    for (int k = 0; k <= P.p; ++k)
+      for (int j = 0; j <= P.n; ++j)
+        for (int i = 0; i <= P.m; ++i) s->q_cons_ts[reg][v](i, j, k) = interior[c++];
+}
+
+void mfo_get_state(void* h, int reg, double* interior) {
+  auto* s = static_cast<Solver<double>*>(h);
+  const Params& P = s->P;
+  long c = 0;
+  for (int v = 0; v < s->S; ++v)
+    for (int k = 0; k <= P.p; ++k)
+      for (int j = 0; j <= P.n; ++j)
+        for (int i = 0; i <= P.m; ++i) interior[c++] = s->q_cons_ts[reg][v](i, j, k);
+}
+
+// s_compute_rhs on register reg; writes rhs (S x cells) and the primitive
+// variables of the interior cells (S x cells).
+void mfo_compute_rhs(void* h, int reg, double* rhs_out, double* prim_out) {
+  auto* s = static_cast<Solver<double>*>(h);
+  const Params& P = s->P;
+  s->compute_rhs(reg, false);
+  long c = 0;
+  for (int v = 0; v < s->S; ++v)
+    for (int k = 0; k <= P.p; ++k)
+      for (int j = 0; j <= P.n; ++j)
+        for (int i = 0; i <= P.m; ++i, ++c) {
+          if (rhs_out) rhs_out[c] = s->rhs[v](i, j, k);
+          if (prim_out) prim_out[c] = s->qp[v](i, j, k);
+        }
+}
+
+// One call of s_{1,2,3}_order_tvd_rk with the given dt.
+void mfo_tvd_rk(void* h, double dt, int last_step) {
+  auto* s = static_cast<Solver<double>*>(h);
+  s->dt = dt;
+  s->tvd_rk(last_step != 0);
+}
+
+// The p_main.fpp time loop; returns the trimmed dt of the last step.
+double mfo_run(void* h, int t_step_start, int t_step_stop, double dt) {
+  return static_cast<Solver<double>*>(h)->run(t_step_start, t_step_stop, dt);
+}
+
+void mfo_set_threads(int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+}
+
+int mfo_get_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// pre_process restatement: uniform grid and patches -> conservative state.
+int mfo_generate_ic(const mfo_params* q, const mfo_patch* patches, int num_patches, double x_beg, double x_end,
+                    double y_beg, double y_end, double z_beg, double z_end, double* x_cb, double* y_cb, double* z_cb,
+                    double* cons_out) {
+  return generate_ic(to_params(q), patches, num_patches, x_beg, x_end, y_beg, y_end, z_beg, z_end, x_cb, y_cb,
+                     z_cb, cons_out);
+}
+
+// Operation counts of one full time step of the oracle, per interior cell.
+// Defined in mfc_oracle_flops.cpp (built without OpenMP).
+int mfo_count_ops(const mfo_params* q, const double* x_cb, const double* y_cb, const double* z_cb,
+                  const double* state, double dt, double* counts_out);
+}

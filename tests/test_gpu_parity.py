@@ -1,0 +1,135 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle.
+
+The bar, from the plain FP64 contract: relative L1 <= 1e-10 in every
+conserved field after the stated number of steps.  The split-precision path
+is checked against the FP64 oracle at <= 1e-3 in density and volume fraction.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l1
+from microfc_gb300 import Simulation, cases, preprocess
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-10
+TOL_SPLIT = 1e-3
+
+
+def _oracle_run(oracle_lib, case, x_cb, y_cb, q, steps):
+    o = oracle_lib.Oracle(case, x_cb, y_cb)
+    o.set_state(q)
+    dt = o.run(0, steps, case.dt)
+    return o.get_state(), dt
+
+
+def _gpu_run(case, x_cb, y_cb, q, steps):
+    with Simulation(case, x_cb, y_cb, q_cons=q) as sim:
+        dt = sim.run(0, steps)
+        assert sim.status() == 0
+        return sim.download(), dt
+
+
+def _check(case, got, ref, tol):
+    err = rel_l1(got, ref)
+    assert np.all(np.isfinite(got))
+    assert err.max() <= tol, f"{case.name}: per-field rel L1 {err}"
+    return err
+
+
+@pytest.mark.parametrize("weno_order", [5, 3, 1])
+@pytest.mark.parametrize("time_stepper", [3, 2, 1])
+def test_sod_1d_matches_oracle(oracle_lib, weno_order, time_stepper):
+    case = cases.sod_1d(m=399, steps=100, dt=1e-4).replace(weno_order=weno_order, time_stepper=time_stepper)
+    x_cb, _, _, q = preprocess.generate(case)
+    ref, dref = _oracle_run(oracle_lib, case, x_cb, None, q, 100)
+    got, dgot = _gpu_run(case, x_cb, None, q, 100)
+    assert dgot == dref
+    _check(case, got, ref, TOL_FP64)
+
+
+def test_sod_1d_config_size_100_steps(oracle_lib):
+    case = cases.sod_1d()  # 1000 cells, dt 5e-5
+    x_cb, _, _, q = preprocess.generate(case)
+    ref, _ = _oracle_run(oracle_lib, case, x_cb, None, q, 100)
+    got, _ = _gpu_run(case, x_cb, None, q, 100)
+    _check(case, got, ref, TOL_FP64)
+
+
+@pytest.mark.parametrize("nx,ny", [(64, 32), (100, 60)])
+def test_droplet_2d_small_matches_oracle(oracle_lib, nx, ny):
+    case = cases.shock_droplet_2d(nx=nx, ny=ny, steps=50)
+    x_cb, y_cb, _, q = preprocess.generate(case)
+    ref, _ = _oracle_run(oracle_lib, case, x_cb, y_cb, q, 50)
+    got, _ = _gpu_run(case, x_cb, y_cb, q, 50)
+    _check(case, got, ref, TOL_FP64)
+
+
+@pytest.mark.parametrize("bc", [(-1, -1), (-2, -2), (-4, -4), (-2, -3)])
+def test_droplet_2d_boundary_conditions(oracle_lib, bc):
+    case = cases.shock_droplet_2d(nx=48, ny=32, steps=30).replace(bc_x=bc, bc_y=bc)
+    x_cb, y_cb, _, q = preprocess.generate(case)
+    ref, _ = _oracle_run(oracle_lib, case, x_cb, y_cb, q, 30)
+    got, _ = _gpu_run(case, x_cb, y_cb, q, 30)
+    _check(case, got, ref, TOL_FP64)
+
+
+def test_compute_rhs_matches_oracle(oracle_lib):
+    case = cases.shock_droplet_2d(nx=64, ny=48, steps=10)
+    x_cb, y_cb, _, q = preprocess.generate(case)
+    o = oracle_lib.Oracle(case, x_cb, y_cb)
+    o.set_state(q)
+    o.run(0, 5, case.dt)  # develop some structure first
+    q5 = o.get_state()
+    rref, pref = o.compute_rhs(0)
+    with Simulation(case, x_cb, y_cb, q_cons=q5) as sim:
+        rhs, prim = sim.s_compute_rhs()
+    assert rel_l1(prim, pref).max() <= 1e-13
+    # the rhs is a difference of fluxes; compare against its own magnitude
+    assert rel_l1(rhs, rref).max() <= 1e-9
+
+
+@pytest.mark.slow
+def test_droplet_2d_full_size_100_steps(oracle_lib):
+    """The headline configuration (1024x512) after 100 steps."""
+    case = cases.shock_droplet_2d()
+    x_cb, y_cb, _, q = preprocess.generate(case)
+    ref, _ = _oracle_run(oracle_lib, case, x_cb, y_cb, q, 100)
+    got, _ = _gpu_run(case, x_cb, y_cb, q, 100)
+    err = _check(case, got, ref, TOL_FP64)
+    print("per-field rel L1 after 100 steps:", err)
+
+
+def test_split_precision_error_bounded(oracle_lib):
+    case = cases.shock_droplet_2d(nx=256, ny=128, steps=100)
+    x_cb, y_cb, _, q = preprocess.generate(case)
+    ref, _ = _oracle_run(oracle_lib, case, x_cb, y_cb, q, 100)
+    got, _ = _gpu_run(case.replace(precision="split"), x_cb, y_cb, q, 100)
+    err = rel_l1(got, ref)
+    nf = case.num_fluids
+    dens_alpha = list(range(nf)) + [case.adv_idx + f for f in range(nf)]
+    assert np.all(np.isfinite(got))
+    assert err[dens_alpha].max() <= TOL_SPLIT, err
+    print("split precision per-field rel L1:", err)
+
+
+def test_status_flags_nan_and_clear():
+    """A NaN planted in the uploaded state is flagged by the stage kernel and
+    reported as an error by the run loop (the reference aborts on NaN)."""
+    from microfc_gb300._lib import MfcError, MFC_FLAG_NAN
+    case = cases.sod_1d(m=99, steps=2, dt=1e-4)
+    x_cb, _, _, q = preprocess.generate(case)
+    q[0, 0, 0, 50] = np.nan
+    with Simulation(case, x_cb, q_cons=q) as sim:
+        with pytest.raises(MfcError):
+            sim.run(0, 2)
+        assert sim.status(clear=True) & MFC_FLAG_NAN
+        assert sim.status() == 0
+
+
+def test_launch_count_is_stages_times_steps():
+    case = cases.sod_1d(m=99, steps=7, dt=1e-4)
+    x_cb, _, _, q = preprocess.generate(case)
+    with Simulation(case, x_cb, q_cons=q) as sim:
+        sim.run(0, 7)
+        assert sim.launches == 3 * 7
