@@ -12,9 +12,9 @@ interior cells x steps / seconds.
              downloads the state (all inside the timed region).
 * roofline     -- HBM roofline of the stage kernel (algorithmic 448 B per
                   cell-update) against the measured copy bandwidth.
-* fp64_roofline -- the bound that actually limits this FP64 path: algorithmic
+* compute_roofline -- the bound that actually limits this path: algorithmic
                   flops per cell-update (counted by the oracle) x rate vs the
-                  FP64 peak.
+                  FP64 (or, split precision, FP32) FMA peak measured in-process.
 * cpu_baseline -- the oracle (C++ restatement of the reference's CPU code,
                   OpenMP over the host cores) on a 1024 x 64 strip.
 
@@ -104,7 +104,7 @@ class ClockSampler:
         sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
         mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[2 + i]})
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.samples)}
 
@@ -178,6 +178,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nx", type=int, default=NX, help="cells in x (profiling runs; the benchmark is 1024)")
+    ap.add_argument("--ny", type=int, default=NY, help="cells in y (profiling runs; the benchmark is 512)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -187,14 +189,15 @@ def main():
     import numpy as np
     import torch
     import torch.distributed as dist
-    from microfc_gb300 import Simulation, cases, preprocess
+    from microfc_gb300 import Simulation, _lib, cases, preprocess
 
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     if ws > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    case = cases.shock_droplet_2d(nx=NX, ny=NY, precision=args.precision)
+    fp64_peak, fp32_peak = _lib.measure_peaks(local)
+    case = cases.shock_droplet_2d(nx=args.nx, ny=args.ny, precision=args.precision)
     x_cb, y_cb, _, q0 = preprocess.generate(case)
     sim = Simulation(case, x_cb, y_cb, q_cons=q0, device=local)
     stream = torch.cuda.ExternalStream(sim.stream, device=torch.device("cuda", local))
@@ -256,10 +259,7 @@ def main():
     per_launch_s = t_total / launches
     achieved = BYTES_PER_CELL_UPDATE * cells / 3 / per_launch_s / 1e9
     traffic = _profile_value("stage_kernel_fp64_droplet_1024x512.md", "dram_bytes_per_launch")
-    flops = _profile_value("stage_kernel_fp64_droplet_1024x512.md", "algorithmic_flops_per_cell_update")
-    fp64_peak = _profile_value("stage_kernel_fp64_droplet_1024x512.md", "fp64_peak_tflops")
-    fp64_peak_kind = "measured (DFMA loop, profiles/)" if fp64_peak else "nominal"
-    fp64_peak = fp64_peak or 1.25
+    flops = _profile_value("flop_count_droplet_1024x512.md", "algorithmic_flops_per_cell_update")
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -277,10 +277,13 @@ def main():
         "clocks": clk.summary(),
     }
     if flops:
+        peak = fp64_peak if args.precision == "fp64" else fp32_peak
         ach = flops * value / ws / 1e12
-        line["fp64_roofline"] = {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
-                                 "frac": ach / fp64_peak, "peak_kind": fp64_peak_kind,
-                                 "flops_per_cell_update": flops}
+        line["compute_roofline"] = {
+            "bound": "fp64" if args.precision == "fp64" else "fp32", "achieved": ach, "peak": peak,
+            "unit": "TFLOP/s", "frac": ach / peak, "flops_per_cell_update": flops,
+            "peak_kind": "measured in-process (FMA chains, mfc_gpu_measure_peaks)",
+            "peaks_measured": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak}}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     sim.close()

@@ -142,6 +142,11 @@ int64_t mfc_gpu_launch_count(const mfc_gpu_ctx* ctx);
 /* Frees all device memory of the context. */
 int mfc_gpu_finalize(mfc_gpu_ctx* ctx);
 
+/* Diagnostic with no reference counterpart: measures the device's FP64 and
+ * FP32 fused-multiply-add throughput (TFLOP/s, 2 flops per FMA), the
+ * denominators of the compute roofline reported by the benchmark. */
+int mfc_gpu_measure_peaks(int device, double* fp64_tflops, double* fp32_tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,7 +18,7 @@ EXPORTS = (
     "mfc_gpu_abi_version", "mfc_gpu_last_error", "mfc_gpu_init", "mfc_gpu_sys_size",
     "mfc_gpu_upload", "mfc_gpu_download", "mfc_gpu_upload_state", "mfc_gpu_download_state",
     "mfc_gpu_compute_rhs", "mfc_gpu_tvd_rk", "mfc_gpu_run", "mfc_gpu_status", "mfc_gpu_stream",
-    "mfc_gpu_launch_count", "mfc_gpu_finalize",
+    "mfc_gpu_launch_count", "mfc_gpu_finalize", "mfc_gpu_measure_peaks",
 )
 
 
@@ -87,8 +87,16 @@ def load(build_if_missing: bool = True):
     L.mfc_gpu_launch_count.argtypes = [vp]
     L.mfc_gpu_launch_count.restype = i64
     L.mfc_gpu_finalize.argtypes = [vp]
+    L.mfc_gpu_measure_peaks.argtypes = [ctypes.c_int, dp, dp]
     _lib = L
     return L
+
+
+def measure_peaks(device: int = 0):
+    """(fp64, fp32) FMA throughput of the device in TFLOP/s."""
+    a, b = ctypes.c_double(0), ctypes.c_double(0)
+    check(load().mfc_gpu_measure_peaks(int(device), ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
 
 
 def check(rc: int) -> None:

@@ -17,8 +17,17 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmfc_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-I", os.path.join(HERE, "..", "include")]
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]
+
+
+def unit_flags(src: str) -> list[str]:
+    """Per-unit flags.  The plain FP64 path is bit-faithful to the CPU
+    reference's operation order, so its device code is compiled without FMA
+    contraction (-fmad=false); host code never contracts (-ffp-contract=off,
+    which matters on aarch64 hosts where GCC contracts by default).  The
+    split-precision units keep contraction."""
+    return [] if src.endswith("_fp32.cu") else ["-fmad=false"]
 
 
 def _nvcc() -> str:
@@ -33,7 +42,7 @@ def sources() -> list[str]:
 
 
 def _deps() -> list[str]:
-    out = []
+    out = [os.path.abspath(__file__)]
     for d in (CSRC, os.path.join(HERE, "..", "include")):
         out += [os.path.join(d, f) for f in os.listdir(d) if f.endswith((".cu", ".cuh", ".h"))]
     return out
@@ -55,7 +64,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
 
     def compile_one(src: str) -> str:
         obj = os.path.join(BUILD, os.path.basename(src).replace(".cu", ".o"))
-        cmd = [nvcc, *ARCH, *flags, "-c", src, "-o", obj]
+        cmd = [nvcc, *ARCH, *flags, *unit_flags(src), "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -39,7 +39,8 @@ std::vector<mfc::StageEntry> g_reg;
 
 void build_registry() {
   std::call_once(g_reg_once, [] {
-    mfc::register_stage_1d(g_reg);
+    mfc::register_stage_1d_fp64(g_reg);
+    mfc::register_stage_1d_fp32(g_reg);
     mfc::register_stage_2d_fp64(g_reg);
     mfc::register_stage_2d_fp32(g_reg);
   });

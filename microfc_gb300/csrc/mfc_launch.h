@@ -45,7 +45,8 @@ StageEntry stage_entry() {
 }
 
 // Defined in the instantiation translation units.
-void register_stage_1d(std::vector<StageEntry>& r);
+void register_stage_1d_fp64(std::vector<StageEntry>& r);
+void register_stage_1d_fp32(std::vector<StageEntry>& r);
 void register_stage_2d_fp64(std::vector<StageEntry>& r);
 void register_stage_2d_fp32(std::vector<StageEntry>& r);
 
