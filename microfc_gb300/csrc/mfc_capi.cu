@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/mfc_gpu.h"
+#include "mfc_grid.h"
 #include "mfc_launch.h"
 
 namespace {
@@ -46,109 +47,16 @@ void build_registry() {
   });
 }
 
-// ---------------------------------------------------------------------------
-// Grid ghost layers and WENO coefficients (host, FP64).
-struct AxisHost {
-  int s = 0, b = 0;             // s = last interior index (m), b = buff_size
-  std::vector<double> cb, d;    // cb(-1-b : s+b), d(-b : s+b)
-  double& CB(int i) { return cb[(size_t)(i + 1 + b)]; }
-  double& D(int i) { return d[(size_t)(i + b)]; }
-};
-
-// s_populate_grid_variables_buffers, m_start_up.fpp:517-655 (widths and
-// boundaries only; cell centres are not used by the hot path).
-void grid_ghosts(AxisHost& a, int bcb, int bce) {
-  const int s = a.s, b = a.b;
-  for (int i = 0; i <= s; ++i) a.D(i) = a.CB(i) - a.CB(i - 1);
-  for (int i = 1; i <= b; ++i) a.D(-i) = bcb <= -3 ? a.D(0) : bcb == -2 ? a.D(i - 1) : a.D(s - (i - 1));
-  for (int i = 1; i <= b; ++i) a.CB(-1 - i) = a.CB(-i) - a.D(-i);
-  for (int i = 1; i <= b; ++i) a.D(s + i) = bce <= -3 ? a.D(s) : bce == -2 ? a.D(s - (i - 1)) : a.D(i - 1);
-  for (int i = 1; i <= b; ++i) a.CB(s + i) = a.CB(s + (i - 1)) + a.D(s + i);
-}
-
-// One cell's record: polyL[3][2], polyR[3][2], dL[3], dR[3], beta[3][3]
-// (record layout of mfc::kPL .. mfc::kBeta).  Formulas of
-// s_compute_weno_coefficients, m_weno.fpp:193-346, for cell i+1 from the
-// boundaries s_cb(i-2 .. i+3).
-void weno_record(AxisHost& a, int i, int wo, double* r) {
-  auto S = [&](int k) { return a.CB(k); };
-  auto sq = [](double x) { return x * x; };
-  double* pL = r + mfc::kPL;
-  double* pR = r + mfc::kPR;
-  double* dL = r + mfc::kDL;
-  double* dR = r + mfc::kDR;
-  double* be = r + mfc::kBeta;
-  std::fill(r, r + mfc::kNumCoef, 0.0);
-  if (wo == 3) {
-    pR[0] = (S(i) - S(i + 1)) / (S(i) - S(i + 2));
-    pR[2] = (S(i) - S(i + 1)) / (S(i - 1) - S(i + 1));
-    pL[0] = -pR[0];
-    pL[2] = -pR[2];
-    dR[0] = (S(i - 1) - S(i + 1)) / (S(i - 1) - S(i + 2));
-    dL[0] = (S(i - 1) - S(i)) / (S(i - 1) - S(i + 2));
-    dR[1] = 1.0 - dR[0];
-    dL[1] = 1.0 - dL[0];
-    be[0] = 4.0 * sq(S(i) - S(i + 1)) / sq(S(i) - S(i + 2));
-    be[3] = 4.0 * sq(S(i) - S(i + 1)) / sq(S(i - 1) - S(i + 1));
-    return;
-  }
-  // polynomial coefficients [k][j] -> index 2k+j
-  pR[0] = ((S(i) - S(i + 1)) * (S(i + 1) - S(i + 2))) / ((S(i) - S(i + 3)) * (S(i + 3) - S(i + 1)));
-  pR[2] = ((S(i - 1) - S(i + 1)) * (S(i + 1) - S(i))) / ((S(i - 1) - S(i + 2)) * (S(i + 2) - S(i)));
-  pR[3] = ((S(i) - S(i + 1)) * (S(i + 1) - S(i + 2))) / ((S(i - 1) - S(i + 1)) * (S(i - 1) - S(i + 2)));
-  pR[5] = ((S(i) - S(i + 1)) * (S(i + 1) - S(i - 1))) / ((S(i - 2) - S(i)) * (S(i - 2) - S(i + 1)));
-  pL[0] = ((S(i + 1) - S(i)) * (S(i) - S(i + 2))) / ((S(i) - S(i + 3)) * (S(i + 3) - S(i + 1)));
-  pL[2] = ((S(i) - S(i - 1)) * (S(i) - S(i + 1))) / ((S(i - 1) - S(i + 2)) * (S(i) - S(i + 2)));
-  pL[3] = ((S(i + 1) - S(i)) * (S(i) - S(i + 2))) / ((S(i - 1) - S(i + 1)) * (S(i - 1) - S(i + 2)));
-  pL[5] = ((S(i - 1) - S(i)) * (S(i) - S(i + 1))) / ((S(i - 2) - S(i)) * (S(i - 2) - S(i + 1)));
-  pR[1] = ((S(i) - S(i + 2)) + (S(i + 1) - S(i + 3))) / ((S(i) - S(i + 2)) * (S(i) - S(i + 3))) * ((S(i) - S(i + 1)));
-  pR[4] = ((S(i - 2) - S(i + 1)) + (S(i - 1) - S(i + 1))) / ((S(i - 1) - S(i + 1)) * (S(i + 1) - S(i - 2))) *
-          ((S(i + 1) - S(i)));
-  pL[1] = ((S(i) - S(i + 2)) + (S(i) - S(i + 3))) / ((S(i) - S(i + 2)) * (S(i) - S(i + 3))) * ((S(i + 1) - S(i)));
-  pL[4] = ((S(i - 2) - S(i)) + (S(i - 1) - S(i + 1))) / ((S(i - 2) - S(i + 1)) * (S(i + 1) - S(i - 1))) *
-          ((S(i) - S(i + 1)));
-  dR[0] = ((S(i - 2) - S(i + 1)) * (S(i + 1) - S(i - 1))) / ((S(i - 2) - S(i + 3)) * (S(i + 3) - S(i - 1)));
-  dR[2] = ((S(i + 1) - S(i + 2)) * (S(i + 1) - S(i + 3))) / ((S(i - 2) - S(i + 2)) * (S(i - 2) - S(i + 3)));
-  dL[0] = ((S(i - 2) - S(i)) * (S(i) - S(i - 1))) / ((S(i - 2) - S(i + 3)) * (S(i + 3) - S(i - 1)));
-  dL[2] = ((S(i) - S(i + 2)) * (S(i) - S(i + 3))) / ((S(i - 2) - S(i + 2)) * (S(i - 2) - S(i + 3)));
-  dR[1] = 1.0 - dR[0] - dR[2];
-  dL[1] = 1.0 - dL[0] - dL[2];
-  const double h = S(i) - S(i + 1);
-  be[0] = 4.0 * sq(h) *
-          (10.0 * sq(S(i + 1) - S(i)) + (S(i + 1) - S(i)) * (S(i + 2) - S(i + 1)) + sq(S(i + 2) - S(i + 1))) /
-          (sq(S(i) - S(i + 3)) * sq(S(i + 1) - S(i + 3)));
-  be[1] = 4.0 * sq(h) *
-          (19.0 * sq(S(i + 1) - S(i)) - (S(i + 1) - S(i)) * (S(i + 3) - S(i + 1)) +
-           2.0 * (S(i + 2) - S(i)) * ((S(i + 2) - S(i)) + (S(i + 3) - S(i + 1)))) /
-          ((S(i) - S(i + 2)) * sq(S(i) - S(i + 3)) * (S(i + 3) - S(i + 1)));
-  be[2] = 4.0 * sq(h) *
-          (10.0 * sq(S(i + 1) - S(i)) + (S(i + 1) - S(i)) * ((S(i + 2) - S(i)) + (S(i + 3) - S(i + 1))) +
-           sq((S(i + 2) - S(i)) + (S(i + 3) - S(i + 1)))) /
-          (sq(S(i) - S(i + 2)) * sq(S(i) - S(i + 3)));
-  be[3] = 4.0 * sq(h) *
-          (10.0 * sq(S(i + 1) - S(i)) + sq(S(i) - S(i - 1)) + (S(i) - S(i - 1)) * (S(i + 1) - S(i))) /
-          (sq(S(i - 1) - S(i + 2)) * sq(S(i) - S(i + 2)));
-  be[4] = 4.0 * sq(h) *
-          ((S(i) - S(i + 1)) * ((S(i) - S(i - 1)) + 20.0 * (S(i + 1) - S(i))) +
-           (2.0 * (S(i) - S(i - 1)) + (S(i + 1) - S(i))) * (S(i + 2) - S(i))) /
-          ((S(i + 1) - S(i - 1)) * sq(S(i - 1) - S(i + 2)) * (S(i + 2) - S(i)));
-  be[5] = 4.0 * sq(h) *
-          (10.0 * sq(S(i + 1) - S(i)) + (S(i + 1) - S(i)) * (S(i + 2) - S(i + 1)) + sq(S(i + 2) - S(i + 1))) /
-          (sq(S(i - 1) - S(i + 1)) * sq(S(i - 1) - S(i + 2)));
-  be[6] = 4.0 * sq(h) *
-          (12.0 * sq(S(i + 1) - S(i)) + sq((S(i) - S(i - 2)) + (S(i) - S(i - 1))) +
-           3.0 * ((S(i) - S(i - 2)) + (S(i) - S(i - 1))) * (S(i + 1) - S(i))) /
-          (sq(S(i - 2) - S(i + 1)) * sq(S(i - 1) - S(i + 1)));
-  be[7] = 4.0 * sq(h) *
-          (19.0 * sq(S(i + 1) - S(i)) + ((S(i) - S(i - 2)) * (S(i) - S(i + 1))) +
-           2.0 * (S(i + 1) - S(i - 1)) * ((S(i) - S(i - 2)) + (S(i + 1) - S(i - 1)))) /
-          ((S(i - 2) - S(i)) * sq(S(i - 2) - S(i + 1)) * (S(i + 1) - S(i - 1)));
-  be[8] = 4.0 * sq(h) *
-          (10.0 * sq(S(i + 1) - S(i)) + sq(S(i) - S(i - 1)) + (S(i) - S(i - 1)) * (S(i + 1) - S(i))) /
-          (sq(S(i - 2) - S(i)) * sq(S(i - 2) - S(i + 1)));
-}
-
 }  // namespace
+
+namespace mfc {
+const StageEntry* find_stage(int nd, int nf, int wo, int prec) {
+  build_registry();
+  for (const auto& e : g_reg)
+    if (e.nd == nd && e.nf == nf && e.wo == wo && e.prec == prec) return &e;
+  return nullptr;
+}
+}  // namespace mfc
 
 struct mfc_gpu_ctx {
   mfc_params prm{};
@@ -169,39 +77,8 @@ struct mfc_gpu_ctx {
 namespace {
 
 int validate(const mfc_params* p) {
-  if (!p) return fail(MFC_ERR_INVALID, "params is NULL");
-  if (p->m <= 0) return fail(MFC_ERR_INVALID, "Unsupported value of m");
-  if (p->n < 0 || p->p < 0) return fail(MFC_ERR_INVALID, "Unsupported value of n or p");
-  if (p->p > 0 && p->n == 0) return fail(MFC_ERR_INVALID, "p > 0 requires n > 0");
-  if (p->p > 0) return fail(MFC_ERR_INVALID, "3-D cases are not built into this library yet");
-  if (p->num_fluids < 1 || p->num_fluids > 2) return fail(MFC_ERR_INVALID, "Unsupported value of num_fluids (1 or 2)");
-  if (p->weno_order != 1 && p->weno_order != 3 && p->weno_order != 5)
-    return fail(MFC_ERR_INVALID, "Unsupported value of weno_order");
-  const int stcls = 5 * p->weno_order;  // num_stcls_min*weno_order, m_start_up.fpp:182-189
-  if (p->m + 1 < stcls) return fail(MFC_ERR_INVALID, "Unsupported combination of values of m and weno_order");
-  if (p->n > 0 && p->n + 1 < stcls) return fail(MFC_ERR_INVALID, "Unsupported combination of values of n and weno_order");
-  if (!(p->weno_eps > 0.0) || p->weno_eps > 1e-6) return fail(MFC_ERR_INVALID, "Unsupported value of weno_eps");
-  if (p->time_stepper < 1 || p->time_stepper > 3) return fail(MFC_ERR_INVALID, "Unsupported value of time_stepper");
-  const int bcs[6] = {p->bc_x_beg, p->bc_x_end, p->bc_y_beg, p->bc_y_end, p->bc_z_beg, p->bc_z_end};
-  const int ndim = 1 + (p->n > 0) + (p->p > 0);
-  for (int d = 0; d < ndim; ++d) {
-    for (int e = 0; e < 2; ++e) {
-      const int bc = bcs[2 * d + e];
-      if (bc < -12 || bc > -1)
-        return fail(MFC_ERR_INVALID, "Unsupported boundary condition (processor boundaries need a halo exchange)");
-    }
-    if ((bcs[2 * d] == -1) != (bcs[2 * d + 1] == -1))
-      return fail(MFC_ERR_INVALID, "Periodic boundaries must be set at both ends");
-  }
-  for (int f = 0; f < p->num_fluids; ++f) {
-    if (!(p->gammas[f] > 0.0)) return fail(MFC_ERR_INVALID, "Unsupported value of fluid_pp%gamma");
-    if (p->pi_infs[f] < 0.0) return fail(MFC_ERR_INVALID, "Unsupported value of fluid_pp%pi_inf");
-  }
-  if (!p->x_cb) return fail(MFC_ERR_INVALID, "x_cb is NULL");
-  if (p->n > 0 && !p->y_cb) return fail(MFC_ERR_INVALID, "y_cb is NULL");
-  if (p->precision != MFC_PREC_FP64 && p->precision != MFC_PREC_SPLIT)
-    return fail(MFC_ERR_INVALID, "Unsupported precision");
-  return MFC_OK;
+  const std::string why = mfc::validate_params(p);
+  return why.empty() ? MFC_OK : fail(MFC_ERR_INVALID, why);
 }
 
 int launch_stage(mfc_gpu_ctx* c, const double* qin, const double* qbase, double* qout, double dt, int kind) {
@@ -279,12 +156,7 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
   c->sv = c->sz * c->n[2];
   c->reg_elems = c->sv * c->S;
 
-  for (const auto& e : g_reg) {
-    if (e.nd == c->nd && e.nf == p->num_fluids && e.wo == p->weno_order && e.prec == p->precision) {
-      c->stage = &e;
-      break;
-    }
-  }
+  c->stage = mfc::find_stage(c->nd, p->num_fluids, p->weno_order, p->precision);
   if (!c->stage) {
     delete c;
     return fail(MFC_ERR_INVALID, "no kernel compiled for this dimensionality / fluid count / WENO order / precision");
@@ -308,39 +180,12 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
   for (int r = 0; r < 3; ++r) c->reg[r] = c->state + r * c->reg_elems;
 
   // grid tables: per direction inv_d[n] then kNumCoef * (n + 2*pad) coefficients
-  const double* cbs[3] = {p->x_cb, p->y_cb, p->z_cb};
   const int bcb[3] = {p->bc_x_beg, p->bc_y_beg, p->bc_z_beg};
   const int bce[3] = {p->bc_x_end, p->bc_y_end, p->bc_z_end};
-  std::vector<double> host;
-  size_t off_inv[3] = {0, 0, 0}, off_coef[3] = {0, 0, 0};
-  int cstride[3] = {0, 0, 0};
-  for (int d = 0; d < c->nd; ++d) {
-    AxisHost a;
-    a.s = c->n[d] - 1;
-    a.b = c->b;
-    a.cb.assign((size_t)(a.s + 2 * a.b + 2), 0.0);
-    a.d.assign((size_t)(a.s + 2 * a.b + 1), 0.0);
-    for (int i = -1; i <= a.s; ++i) a.CB(i) = cbs[d][i + 1];
-    grid_ghosts(a, bcb[d], bce[d]);
-    for (int i = 0; i <= a.s; ++i)
-      if (!(a.D(i) > 0.0)) return cleanup(fail(MFC_ERR_INVALID, "cell boundaries must increase"));
-    off_inv[d] = host.size();
-    for (int i = 0; i <= a.s; ++i) host.push_back(1.0 / a.D(i));  // the reference's 1d0/dx(k)
-    const int pad = mfc::kCoefPad;
-    cstride[d] = c->n[d] + 2 * pad;
-    off_coef[d] = host.size();
-    host.resize(host.size() + (size_t)mfc::kNumCoef * cstride[d], 0.0);
-    if (p->weno_order > 1) {
-      // the reference defines coefficients for cells -b+polyn .. s+b-polyn
-      const int lo = -c->b + polyn, hi = a.s + c->b - polyn;
-      double rec[mfc::kNumCoef];
-      for (int cell = -pad; cell <= a.s + pad; ++cell) {
-        const int src = std::min(std::max(cell, lo), hi);
-        weno_record(a, src - 1, p->weno_order, rec);
-        for (int k = 0; k < mfc::kNumCoef; ++k) host[off_coef[d] + (size_t)k * cstride[d] + (cell + pad)] = rec[k];
-      }
-    }
-  }
+  mfc::GridTables gt;
+  const std::string why = mfc::build_grid_tables(p, c->nd, c->n, c->b, gt);
+  if (!why.empty()) return cleanup(fail(MFC_ERR_INVALID, why));
+  const std::vector<double>& host = gt.host;
   if ((e = cudaMalloc(&c->tables, sizeof(double) * host.size())) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if ((e = cudaMemcpy(c->tables, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
@@ -351,9 +196,9 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
     D.n[d] = c->n[d];
     D.bc_beg[d] = bcb[d];
     D.bc_end[d] = bce[d];
-    D.inv_d[d] = d < c->nd ? c->tables + off_inv[d] : nullptr;
-    D.coef[d] = d < c->nd ? c->tables + off_coef[d] : nullptr;
-    D.cstride[d] = cstride[d];
+    D.inv_d[d] = d < c->nd ? c->tables + gt.off_inv[d] : nullptr;
+    D.coef[d] = d < c->nd ? c->tables + gt.off_coef[d] : nullptr;
+    D.cstride[d] = gt.cstride[d];
   }
   D.sy = c->sy;
   D.sz = c->sz;

@@ -44,6 +44,9 @@ StageEntry stage_entry() {
                     &stage_prepare<ND, NF, WO, RT, TX, TY, NT>, &stage_launch<ND, NF, WO, RT, TX, TY, NT>};
 }
 
+// The default (first registered) launcher of a configuration, or nullptr.
+const StageEntry* find_stage(int nd, int nf, int wo, int prec);
+
 // Defined in the instantiation translation units.
 void register_stage_1d_fp64(std::vector<StageEntry>& r);
 void register_stage_1d_fp32(std::vector<StageEntry>& r);
