@@ -142,6 +142,24 @@ int64_t mfc_gpu_launch_count(const mfc_gpu_ctx* ctx);
 /* Frees all device memory of the context. */
 int mfc_gpu_finalize(mfc_gpu_ctx* ctx);
 
+/* No counterpart in the reference.  One time step like mfc_gpu_tvd_rk, for
+ * callers that cannot allocate device memory (their device memory belongs to
+ * another allocator -- a framework's caching pool, or an OpenACC runtime that
+ * owns the state arrays -- or they must avoid the device-wide synchronisation
+ * of cudaMalloc/cudaFree).  It allocates nothing: the intermediate RK
+ * register, grid tables and status word live in a fixed file-scope device
+ * array of about 58 MiB that each GPU loading the library holds until exit.
+ * q_in (state at t^n) and q_out (state at t^{n+1}) are distinct device
+ * arrays [S][p+1][n+1][ld_y], x fastest.  Limits: S*(n+1)*(p+1)*ld_y <=
+ * 7*2^20 doubles and at most 4096 cells per direction; larger cases return
+ * MFC_ERR_INVALID.  Synchronous with respect to `stream` (a cudaStream_t,
+ * NULL = legacy default stream); returns MFC_ERR_STATE if a NaN was written.
+ * All calls share the array: calls that overlap on the GPU race.  The first
+ * call on a device looks up the array's address with that device current;
+ * make it before any stream capture. */
+int mfc_gpu_tvd_rk_noalloc(const mfc_params* params, const double* q_in, double* q_out, int64_t ld_y, double dt,
+                           void* stream);
+
 /* Diagnostic with no reference counterpart: measures the device's FP64 and
  * FP32 fused-multiply-add throughput (TFLOP/s, 2 flops per FMA), the
  * denominators of the compute roofline reported by the benchmark. */

@@ -18,7 +18,7 @@ EXPORTS = (
     "mfc_gpu_abi_version", "mfc_gpu_last_error", "mfc_gpu_init", "mfc_gpu_sys_size",
     "mfc_gpu_upload", "mfc_gpu_download", "mfc_gpu_upload_state", "mfc_gpu_download_state",
     "mfc_gpu_compute_rhs", "mfc_gpu_tvd_rk", "mfc_gpu_run", "mfc_gpu_status", "mfc_gpu_stream",
-    "mfc_gpu_launch_count", "mfc_gpu_finalize", "mfc_gpu_measure_peaks",
+    "mfc_gpu_launch_count", "mfc_gpu_finalize", "mfc_gpu_measure_peaks", "mfc_gpu_tvd_rk_noalloc",
 )
 
 
@@ -88,6 +88,7 @@ def load(build_if_missing: bool = True):
     L.mfc_gpu_launch_count.restype = i64
     L.mfc_gpu_finalize.argtypes = [vp]
     L.mfc_gpu_measure_peaks.argtypes = [ctypes.c_int, dp, dp]
+    L.mfc_gpu_tvd_rk_noalloc.argtypes = [ctypes.POINTER(MfcParams), vp, vp, i64, ctypes.c_double, vp]
     _lib = L
     return L
 

@@ -56,6 +56,8 @@ const StageEntry* find_stage(int nd, int nf, int wo, int prec) {
     if (e.nd == nd && e.nf == nf && e.wo == wo && e.prec == prec) return &e;
   return nullptr;
 }
+
+int report_error(int code, const std::string& msg) { return fail(code, msg); }
 }  // namespace mfc
 
 struct mfc_gpu_ctx {

@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
 #include <vector>
 
 #include "mfc_device.cuh"
@@ -46,6 +47,9 @@ StageEntry stage_entry() {
 
 // The default (first registered) launcher of a configuration, or nullptr.
 const StageEntry* find_stage(int nd, int nf, int wo, int prec);
+
+// Records msg as the calling thread's mfc_gpu_last_error() and returns code.
+int report_error(int code, const std::string& msg);
 
 // Defined in the instantiation translation units.
 void register_stage_1d_fp64(std::vector<StageEntry>& r);
