@@ -142,6 +142,33 @@ int64_t mfc_gpu_launch_count(const mfc_gpu_ctx* ctx);
 /* Frees all device memory of the context. */
 int mfc_gpu_finalize(mfc_gpu_ctx* ctx);
 
+/* No counterpart in the reference (which tunes nothing).  Autotuner: times a
+ * few first-stage launches of every compiled tile variant of the context's
+ * configuration (the state is not advanced), keeps the fastest and returns
+ * its index and per-launch time in milliseconds. */
+int mfc_gpu_tune(mfc_gpu_ctx* ctx, int reps, int* variant_out, double* ms_out);
+
+/* ---- Ensemble mode (no reference counterpart; the reference runs one case
+ * per process).  Up to 96 independent 2-D cases that share num_fluids,
+ * weno_order, precision, time_stepper (2 or 3) and device, each with its own
+ * grid, boundary conditions, fluids and dt, advanced by one persistent
+ * launch per RK stage over a work list of (case, tile) pairs. */
+typedef struct mfc_gpu_ensemble mfc_gpu_ensemble;
+
+int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_cases, mfc_gpu_ensemble** out);
+/* Case state copies, [S][n+1][m+1] contiguous (register 0). */
+int mfc_gpu_ensemble_upload(mfc_gpu_ensemble* ens, int case_index, const double* host_q);
+int mfc_gpu_ensemble_download(mfc_gpu_ensemble* ens, int case_index, double* host_q);
+/* Autotuner over the compiled ensemble tile variants (see mfc_gpu_tune). */
+int mfc_gpu_ensemble_tune(mfc_gpu_ensemble* ens, int reps, int* variant_out, double* ms_out);
+/* Steps t_step_start .. t_step_stop-1 of every case; each case's last step
+ * uses its dt after the p_main trim.  use_graph != 0 replays the stage
+ * launches of a step from a CUDA graph.  Synchronous; MFC_ERR_STATE on NaN. */
+int mfc_gpu_ensemble_run(mfc_gpu_ensemble* ens, int t_step_start, int t_step_stop, int use_graph);
+void* mfc_gpu_ensemble_stream(mfc_gpu_ensemble* ens);
+int64_t mfc_gpu_ensemble_launch_count(const mfc_gpu_ensemble* ens);
+int mfc_gpu_ensemble_finalize(mfc_gpu_ensemble* ens);
+
 /* No counterpart in the reference.  One time step like mfc_gpu_tvd_rk, for
  * callers that cannot allocate device memory (their device memory belongs to
  * another allocator -- a framework's caching pool, or an OpenACC runtime that

@@ -19,6 +19,9 @@ EXPORTS = (
     "mfc_gpu_upload", "mfc_gpu_download", "mfc_gpu_upload_state", "mfc_gpu_download_state",
     "mfc_gpu_compute_rhs", "mfc_gpu_tvd_rk", "mfc_gpu_run", "mfc_gpu_status", "mfc_gpu_stream",
     "mfc_gpu_launch_count", "mfc_gpu_finalize", "mfc_gpu_measure_peaks", "mfc_gpu_tvd_rk_noalloc",
+    "mfc_gpu_tune", "mfc_gpu_ensemble_init", "mfc_gpu_ensemble_upload", "mfc_gpu_ensemble_download",
+    "mfc_gpu_ensemble_tune", "mfc_gpu_ensemble_run", "mfc_gpu_ensemble_stream", "mfc_gpu_ensemble_launch_count",
+    "mfc_gpu_ensemble_finalize",
 )
 
 
@@ -89,6 +92,18 @@ def load(build_if_missing: bool = True):
     L.mfc_gpu_finalize.argtypes = [vp]
     L.mfc_gpu_measure_peaks.argtypes = [ctypes.c_int, dp, dp]
     L.mfc_gpu_tvd_rk_noalloc.argtypes = [ctypes.POINTER(MfcParams), vp, vp, i64, ctypes.c_double, vp]
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.mfc_gpu_tune.argtypes = [vp, ctypes.c_int, ip, dp]
+    L.mfc_gpu_ensemble_init.argtypes = [ctypes.POINTER(MfcParams), dp, ctypes.c_int, ctypes.POINTER(vp)]
+    L.mfc_gpu_ensemble_upload.argtypes = [vp, ctypes.c_int, dp]
+    L.mfc_gpu_ensemble_download.argtypes = [vp, ctypes.c_int, dp]
+    L.mfc_gpu_ensemble_tune.argtypes = [vp, ctypes.c_int, ip, dp]
+    L.mfc_gpu_ensemble_run.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.mfc_gpu_ensemble_stream.argtypes = [vp]
+    L.mfc_gpu_ensemble_stream.restype = vp
+    L.mfc_gpu_ensemble_launch_count.argtypes = [vp]
+    L.mfc_gpu_ensemble_launch_count.restype = i64
+    L.mfc_gpu_ensemble_finalize.argtypes = [vp]
     _lib = L
     return L
 

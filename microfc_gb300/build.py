@@ -26,8 +26,12 @@ def unit_flags(src: str) -> list[str]:
     reference's operation order, so its device code is compiled without FMA
     contraction (-fmad=false); host code never contracts (-ffp-contract=off,
     which matters on aarch64 hosts where GCC contracts by default).  The
-    split-precision units keep contraction."""
-    return [] if src.endswith("_fp32.cu") else ["-fmad=false"]
+    split-precision units keep contraction and use the approximate FP32
+    division and square root (their FP32 results are checked against the
+    FP64 oracle at a stated tolerance, not bit for bit)."""
+    if src.endswith("_fp32.cu"):
+        return ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
+    return ["-fmad=false"]
 
 
 def _nvcc() -> str:

@@ -1,0 +1,14 @@
+// Instantiations of the ensemble stage kernel, split precision.
+#include "mfc_ensemble.cuh"
+
+namespace mfc {
+
+void register_ensemble_fp32(std::vector<EnsembleEntry>& r) {
+  r.push_back(ensemble_entry<2, 5, float, 32, 16, 256>());
+  r.push_back(ensemble_entry<2, 5, float, 16, 16, 256>());
+  r.push_back(ensemble_entry<2, 5, float, 32, 8, 256>());
+  r.push_back(ensemble_entry<2, 5, float, 32, 32, 512>());
+  r.push_back(ensemble_entry<2, 5, float, 64, 8, 256>());
+}
+
+}  // namespace mfc

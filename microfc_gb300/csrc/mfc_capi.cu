@@ -44,6 +44,8 @@ void build_registry() {
     mfc::register_stage_1d_fp32(g_reg);
     mfc::register_stage_2d_fp64(g_reg);
     mfc::register_stage_2d_fp32(g_reg);
+    mfc::register_stage_3d_fp64(g_reg);
+    mfc::register_stage_3d_fp32(g_reg);
   });
 }
 
@@ -68,6 +70,7 @@ struct mfc_gpu_ctx {
   double* state = nullptr;      // 3 registers
   double* reg[3] = {nullptr, nullptr, nullptr};
   double* rhs = nullptr;
+  double* work = nullptr;       // 3-D: partial RHS between the directional sweeps
   double* tables = nullptr;     // inv_d and coefficient tables
   uint32_t* status = nullptr;
   cudaStream_t stream = nullptr;
@@ -86,7 +89,7 @@ int validate(const mfc_params* p) {
 int launch_stage(mfc_gpu_ctx* c, const double* qin, const double* qbase, double* qout, double dt, int kind) {
   cudaError_t e = c->stage->launch(c->dev, qin, qbase, qout, dt, kind, c->stream);
   if (e != cudaSuccess) return fail(MFC_ERR_CUDA, std::string("stage launch: ") + cudaGetErrorString(e));
-  c->launches += 1;
+  c->launches += c->stage->kernels;
   return MFC_OK;
 }
 
@@ -175,6 +178,8 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if ((e = cudaMalloc(&c->rhs, sizeof(double) * c->reg_elems)) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
+  if (c->nd == 3 && (e = cudaMalloc(&c->work, sizeof(double) * c->reg_elems)) != cudaSuccess)
+    return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if ((e = cudaMalloc(&c->status, sizeof(uint32_t))) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   cudaMemsetAsync(c->state, 0, sizeof(double) * c->reg_elems * 3, c->stream);
@@ -212,6 +217,7 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
   D.weno_eps = p->weno_eps;
   D.coff = mfc::kCoefPad;
   D.status = c->status;
+  D.work = c->work;
 
   if ((e = c->stage->prepare()) != cudaSuccess) return cleanup(fail(MFC_ERR_CUDA, cudaGetErrorString(e)));
   if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cleanup(fail(MFC_ERR_CUDA, cudaGetErrorString(e)));
@@ -275,7 +281,9 @@ int mfc_gpu_compute_rhs(mfc_gpu_ctx* c, double* rhs_out, double* prim_out) {
     if (c->nd == 1 && nf == 1) prim_kernel<1, 1><<<blocks, 256, 0, c->stream>>>(c->dev, c->reg[0], tmp);
     else if (c->nd == 1 && nf == 2) prim_kernel<1, 2><<<blocks, 256, 0, c->stream>>>(c->dev, c->reg[0], tmp);
     else if (c->nd == 2 && nf == 1) prim_kernel<2, 1><<<blocks, 256, 0, c->stream>>>(c->dev, c->reg[0], tmp);
-    else prim_kernel<2, 2><<<blocks, 256, 0, c->stream>>>(c->dev, c->reg[0], tmp);
+    else if (c->nd == 2) prim_kernel<2, 2><<<blocks, 256, 0, c->stream>>>(c->dev, c->reg[0], tmp);
+    else if (nf == 1) prim_kernel<3, 1><<<blocks, 256, 0, c->stream>>>(c->dev, c->reg[0], tmp);
+    else prim_kernel<3, 2><<<blocks, 256, 0, c->stream>>>(c->dev, c->reg[0], tmp);
     MFC_CUDA(cudaGetLastError());
     c->launches += 1;
     for (int v = 0; v < c->S; ++v)
@@ -329,6 +337,49 @@ int mfc_gpu_run(mfc_gpu_ctx* c, int t_step_start, int t_step_stop, double* dt_in
   return MFC_OK;
 }
 
+int mfc_gpu_tune(mfc_gpu_ctx* c, int reps, int* variant_out, double* ms_out) {
+  if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  if (reps < 1) reps = 5;
+  uint32_t saved = 0;  // the timing launches must not leave flags behind
+  MFC_CUDA(cudaMemcpyAsync(&saved, c->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  const mfc::StageEntry* best = nullptr;
+  int idx = -1, best_idx = -1;
+  float best_ms = 0.f;
+  cudaEvent_t a, b;
+  MFC_CUDA(cudaEventCreate(&a));
+  MFC_CUDA(cudaEventCreate(&b));
+  for (const auto& e : g_reg) {
+    if (e.nd != c->nd || e.nf != c->prm.num_fluids || e.wo != c->prm.weno_order || e.prec != c->prm.precision)
+      continue;
+    ++idx;
+    if (e.prepare() != cudaSuccess) continue;
+    // first-stage launches read register 0 and write register 1 only
+    if (e.launch(c->dev, c->reg[0], c->reg[0], c->reg[1], 0.0, mfc::kRkEuler, c->stream) != cudaSuccess) continue;
+    cudaEventRecord(a, c->stream);
+    for (int r = 0; r < reps; ++r) e.launch(c->dev, c->reg[0], c->reg[0], c->reg[1], 0.0, mfc::kRkEuler, c->stream);
+    cudaEventRecord(b, c->stream);
+    if (cudaEventSynchronize(b) != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    ms /= reps;
+    if (!best || ms < best_ms) {
+      best = &e;
+      best_ms = ms;
+      best_idx = idx;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  MFC_CUDA(cudaMemcpyAsync(c->status, &saved, sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  if (!best) return fail(MFC_ERR_CUDA, "no tile variant could be timed");
+  c->stage = best;
+  if (variant_out) *variant_out = best_idx;
+  if (ms_out) *ms_out = best_ms;
+  return MFC_OK;
+}
+
 int mfc_gpu_status(mfc_gpu_ctx* c, uint32_t* flags, int clear) {
   if (!c || !flags) return fail(MFC_ERR_INVALID, "NULL argument");
   MFC_CUDA(cudaMemcpyAsync(flags, c->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
@@ -348,6 +399,7 @@ int mfc_gpu_finalize(mfc_gpu_ctx* c) {
   cudaFree(c->rhs);
   cudaFree(c->tables);
   cudaFree(c->status);
+  cudaFree(c->work);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return MFC_OK;

@@ -2,11 +2,11 @@
 // block every kernel receives by value, boundary-condition index mapping,
 // the stiffened-gas cons -> prim conversion, WENO1/3/5 and HLLC.
 //
-// The arithmetic follows the reference's operation order (file:line cited at
-// each function) so that the FP64 path matches the CPU reference to round-off
-// (nvcc contracts a*b+c into FMA, the only deviation).  RT is the type of the
-// reconstruction/Riemann arithmetic: double for the plain path, float for the
-// split-precision path.
+// The FP64 arithmetic follows the reference's operation order (file:line
+// cited at each function); compiled without FMA contraction it reproduces
+// the CPU reference bit for bit.  RT is the type of the reconstruction and
+// Riemann arithmetic: double for the plain path, float for the
+// split-precision path, which also uses the *_split / *_fast variants below.
 #pragma once
 
 #include <cstdint>
@@ -30,6 +30,7 @@ struct DevParams {
                            // cells i = -kCoefPad .. n-1+kCoefPad, coff = kCoefPad
   int coff, cstride[3];
   uint32_t* status;
+  void* work;  // 3-D: partial RHS between the directional sweeps ([S][z][y][x], RT)
 };
 
 // Equation index layout, m_global_parameters.fpp:302-310 (0-based).
@@ -66,6 +67,39 @@ __device__ __forceinline__ int clamp_coef_index(int c, int n) {
   return c < -kCoefPad ? -kCoefPad : (c > n - 1 + kCoefPad ? n - 1 + kCoefPad : c);
 }
 
+// FP64 <-> FP32 conversions for the split path done with integer operations
+// on the IEEE-754 bit fields, so that they do not occupy GB300's narrow FP64
+// pipe (which executes the hardware conversion instructions).  double ->
+// float truncates the significand (error < 1 ulp of float), flushes results
+// below the smallest normal float to signed zero and maps everything above
+// the float range (and NaN) to infinity; float -> double is exact for
+// normal numbers and zero (denormal floats are flushed to zero, as the split
+// units run with -ftz=true).
+__device__ __forceinline__ float d2f_bits(double x) {
+  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+  const uint32_t sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  const uint32_t mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const uint32_t r = e <= 0 ? sign : (e >= 255 ? (sign | 0x7f800000u) : (sign | ((uint32_t)e << 23) | mant));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ double f2d_bits(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t sign = b & 0x80000000u, e = (b >> 23) & 0xffu, mant = b & 0x7fffffu;
+  const uint32_t hi = e == 0 ? sign : (sign | ((e + (1023u - 127u)) << 20) | (mant >> 3));
+  const uint32_t lo = e == 0 ? 0u : (mant << 29);
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// Approximate FP32 reciprocal (PTX rcp.approx.ftz.f32); the split path
+// refines it where more accuracy is needed.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 __device__ __forceinline__ bool not_finite(double x) {
   const uint32_t hi = (uint32_t)(__double_as_longlong(x) >> 32);
   return (hi & 0x7ff00000u) == 0x7ff00000u;
@@ -95,6 +129,77 @@ __device__ __forceinline__ void cons_to_prim(double (&q)[Eqs<ND, NF>::S], const 
     dyn = dyn + 0.5 * mom * vel;
   }
   q[Q::E] = (q[Q::E] - dyn - pinf) / gam;
+}
+
+// cons -> prim for the split-precision path.  What needs FP64 stays FP64:
+// the mixture sums and the recovered internal energy dE = E - rho|u|^2/2 -
+// pi_inf, where the stiffened-gas EOS cancels ~4 digits for water.  The
+// dynamic pressure uses 1/rho from an FP32 reciprocal refined by one FP64
+// Newton step (relative error ~1e-14).  The well-conditioned remainder
+// (velocity = m/rho, p = dE/gamma) is evaluated in FP32 for the FP32
+// reconstruction that consumes it.
+template <int ND, int NF>
+__device__ __forceinline__ void cons_to_prim_split(const double (&q)[Eqs<ND, NF>::S], const DevParams& P,
+                                                   float (&out)[Eqs<ND, NF>::S]) {
+  using Q = Eqs<ND, NF>;
+  double rho = 0.0, gam = 0.0, pinf = 0.0;
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    rho = rho + q[f];
+    gam = fma(q[Q::ADV + f], P.gammas[f], gam);
+    pinf = fma(q[Q::ADV + f], P.pi_infs[f], pinf);
+  }
+  rho = fmax(rho, 1e-16);
+  const float r0 = rcp_approx(d2f_bits(rho));
+  const double r0d = f2d_bits(r0);
+  const double irho = fma(r0d, fma(-rho, r0d, 1.0), r0d);
+  double m2 = 0.0;
+#pragma unroll
+  for (int d = 0; d < ND; ++d) m2 = fma(q[Q::MOM + d], q[Q::MOM + d], m2);
+  const double dE = q[Q::E] - (0.5 * irho) * m2 - pinf;
+  const float irf = d2f_bits(irho);
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    out[f] = d2f_bits(q[f]);
+    out[Q::ADV + f] = d2f_bits(q[Q::ADV + f]);
+  }
+#pragma unroll
+  for (int d = 0; d < ND; ++d) out[Q::MOM + d] = d2f_bits(q[Q::MOM + d]) * irf;
+  out[Q::E] = __fdividef(d2f_bits(dE), d2f_bits(gam));
+}
+
+// WENO5 for the split-precision path: the same stencils, smoothness
+// indicators and weights as weno_cell, with the divisions regrouped -- one
+// reciprocal of beta_k^2 shared by the left and right weights and one
+// reciprocal of sum(alpha_k) per face value.  The weights are still
+// normalised before they multiply the candidate values, so nothing grows
+// beyond the operands' range.  Mathematically identical; rounding differs.
+__device__ __forceinline__ void weno5_cell_fast(const float* __restrict__ c, const float (&v)[5], float eps, float& vL,
+                                                float& vR) {
+  const float d1 = v[4] - v[3];
+  const float d0 = v[3] - v[2];
+  const float dm1 = v[2] - v[1];
+  const float dm2 = v[1] - v[0];
+  const float b0 = fmaf(d1, fmaf(c[kBeta + 0], d1, c[kBeta + 1] * d0), fmaf(c[kBeta + 2] * d0, d0, eps));
+  const float b1 = fmaf(d0, fmaf(c[kBeta + 3], d0, c[kBeta + 4] * dm1), fmaf(c[kBeta + 5] * dm1, dm1, eps));
+  const float b2 = fmaf(dm1, fmaf(c[kBeta + 6], dm1, c[kBeta + 7] * dm2), fmaf(c[kBeta + 8] * dm2, dm2, eps));
+  const float r0 = rcp_approx(b0 * b0), r1 = rcp_approx(b1 * b1), r2 = rcp_approx(b2 * b2);
+  {
+    const float p0 = fmaf(c[kPL + 1], d0, fmaf(c[kPL + 0], d1, v[2]));
+    const float p1 = fmaf(c[kPL + 3], dm1, fmaf(c[kPL + 2], d0, v[2]));
+    const float p2 = fmaf(c[kPL + 5], dm2, fmaf(c[kPL + 4], dm1, v[2]));
+    const float a0 = c[kDL + 0] * r0, a1 = c[kDL + 1] * r1, a2 = c[kDL + 2] * r2;
+    const float is = rcp_approx(a0 + a1 + a2);
+    vL = fmaf(a2 * is, p2, fmaf(a1 * is, p1, (a0 * is) * p0));
+  }
+  {
+    const float p0 = fmaf(c[kPR + 1], d0, fmaf(c[kPR + 0], d1, v[2]));
+    const float p1 = fmaf(c[kPR + 3], dm1, fmaf(c[kPR + 2], d0, v[2]));
+    const float p2 = fmaf(c[kPR + 5], dm2, fmaf(c[kPR + 4], dm1, v[2]));
+    const float a0 = c[kDR + 0] * r0, a1 = c[kDR + 1] * r1, a2 = c[kDR + 2] * r2;
+    const float is = rcp_approx(a0 + a1 + a2);
+    vR = fmaf(a2 * is, p2, fmaf(a1 * is, p1, (a0 * is) * p0));
+  }
 }
 
 // WENO reconstruction of one cell from its stencil, m_weno.fpp:391-536.
@@ -241,6 +346,18 @@ __device__ __forceinline__ double rk_combine(int kind, double base, double in, d
     case kRk2Final: return (base + in + dt * r) / 2.0;
     case kRk3Mid: return (3.0 * base + in + dt * r) / 4.0;
     case kRk3Final: return (base + 2.0 * in + 2.0 * dt * r) / 3.0;
+    default: return r;
+  }
+}
+
+// The same combinations for the split-precision path: FP64 state and
+// accumulation, fused, with the division by 3 replaced by a multiplication.
+__device__ __forceinline__ double rk_combine_split(int kind, double base, double in, double dt, double r) {
+  switch (kind) {
+    case kRkEuler: return fma(dt, r, base);
+    case kRk2Final: return 0.5 * fma(dt, r, base + in);
+    case kRk3Mid: return 0.25 * fma(dt, r, fma(3.0, base, in));
+    case kRk3Final: return (1.0 / 3.0) * fma(2.0 * dt, r, fma(2.0, in, base));
     default: return r;
   }
 }

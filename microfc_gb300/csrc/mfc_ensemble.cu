@@ -1,0 +1,364 @@
+// C ABI of the ensemble mode (include/mfc_gpu.h, mfc_gpu_ensemble_*): many
+// independent 2-D cases of uneven grid size advanced by one persistent
+// launch per RK stage, optionally replayed from a CUDA graph, with the tile
+// shape chosen by a project-written autotuner.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/mfc_gpu.h"
+#include "mfc_ensemble.cuh"
+#include "mfc_grid.h"
+#include "mfc_launch.h"
+
+namespace {
+
+std::once_flag g_once;
+std::vector<mfc::EnsembleEntry> g_ens;
+
+void build_ens_registry() {
+  std::call_once(g_once, [] {
+    mfc::register_ensemble_fp64(g_ens);
+    mfc::register_ensemble_fp32(g_ens);
+  });
+}
+
+// dt of the last full step after the p_main trim (p_main.fpp:214, 287).
+double trimmed_last_dt(double dt, int t_start, int t_stop) {
+  int t = t_start;
+  double mytime = t == 0 ? 0.0 : t * dt;
+  const double finaltime = t_stop * dt;
+  double cur = dt;
+  for (;;) {
+    mytime = mytime + cur;
+    if (t == t_stop - 1) return cur;
+    if ((mytime + cur) >= finaltime) cur = finaltime - mytime;
+    t = t + 1;
+  }
+}
+
+}  // namespace
+
+struct mfc_gpu_ensemble {
+  int num = 0, nf = 0, wo = 0, prec = 0, ts = 3, device = 0;
+  std::vector<mfc::EnsCase> cases;  // host copy with device pointers
+  std::vector<int> nx, ny;
+  std::vector<double> dt;
+  double* state = nullptr;
+  double* tables = nullptr;
+  uint32_t* status = nullptr;
+  cudaStream_t stream = nullptr;
+  const mfc::EnsembleEntry* entry = nullptr;
+  int grid = 0, total_tiles = 0;
+  int64_t launches = 0;
+  mfc::EnsParams* ep = nullptr;  // host staging of the kernel parameters
+};
+
+namespace {
+
+int configure(mfc_gpu_ensemble* e, const mfc::EnsembleEntry* en) {
+  cudaError_t err = cudaFuncSetAttribute(en->func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)en->smem);
+  if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+  int bps = 0, sms = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, en->func, en->nt, en->smem);
+  if (err == cudaSuccess) err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device);
+  if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+  if (bps < 1) return mfc::report_error(MFC_ERR_INVALID, "ensemble tile variant does not fit on an SM");
+  int base = 0;
+  for (int i = 0; i < e->num; ++i) {
+    const int tx = (e->nx[i] + en->tx - 1) / en->tx, ty = (e->ny[i] + en->ty - 1) / en->ty;
+    e->cases[i].tiles_x = tx;
+    e->cases[i].tile_base = base;
+    base += tx * ty;
+  }
+  e->total_tiles = base;
+  e->grid = std::min(base, bps * sms);
+  e->entry = en;
+  return MFC_OK;
+}
+
+int launch_stage(mfc_gpu_ensemble* e, int stage, int last) {
+  mfc::EnsParams& E = *e->ep;
+  E.num_cases = e->num;
+  E.total_tiles = e->total_tiles;
+  E.stage = stage;
+  E.time_stepper = e->ts;
+  E.last_step = last;
+  for (int i = 0; i < e->num; ++i) E.c[i] = e->cases[i];
+  cudaError_t err = e->entry->launch(E, e->grid, e->stream);
+  if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+  e->launches += 1;
+  return MFC_OK;
+}
+
+int launch_step(mfc_gpu_ensemble* e, int last) {
+  const int stages = e->ts == 2 ? 2 : 3;
+  for (int s = 0; s < stages; ++s) {
+    int rc = launch_stage(e, s, last);
+    if (rc) return rc;
+  }
+  return MFC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_cases, mfc_gpu_ensemble** out) {
+  if (!out || !cases || !dts) return mfc::report_error(MFC_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (num_cases < 1 || num_cases > mfc::kMaxEnsemble)
+    return mfc::report_error(MFC_ERR_INVALID, "an ensemble holds 1 to 96 cases");
+  const mfc_params& c0 = cases[0];
+  for (int i = 0; i < num_cases; ++i) {
+    const mfc_params& p = cases[i];
+    const std::string why = mfc::validate_params(&p);
+    if (!why.empty()) return mfc::report_error(MFC_ERR_INVALID, "case " + std::to_string(i) + ": " + why);
+    if (p.n == 0 || p.p != 0) return mfc::report_error(MFC_ERR_INVALID, "ensemble cases must be 2-D");
+    if (p.num_fluids != c0.num_fluids || p.weno_order != c0.weno_order || p.precision != c0.precision ||
+        p.time_stepper != c0.time_stepper || p.device != c0.device)
+      return mfc::report_error(MFC_ERR_INVALID,
+                               "ensemble cases must share num_fluids, weno_order, precision, time_stepper, device");
+    if (!(dts[i] > 0.0)) return mfc::report_error(MFC_ERR_INVALID, "Unsupported value of dt");
+  }
+  if (c0.time_stepper == 1)
+    return mfc::report_error(MFC_ERR_INVALID, "the ensemble mode runs the 2nd and 3rd order TVD RK schemes");
+  build_ens_registry();
+  const mfc::EnsembleEntry* en = nullptr;
+  for (const auto& x : g_ens)
+    if (x.nf == c0.num_fluids && x.wo == c0.weno_order && x.prec == c0.precision) { en = &x; break; }
+  if (!en) return mfc::report_error(MFC_ERR_INVALID, "no ensemble kernel compiled for this configuration");
+  cudaError_t err = cudaSetDevice(c0.device);
+  if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+
+  auto* e = new mfc_gpu_ensemble();
+  e->num = num_cases;
+  e->nf = c0.num_fluids;
+  e->wo = c0.weno_order;
+  e->prec = c0.precision;
+  e->ts = c0.time_stepper;
+  e->device = c0.device;
+  e->cases.resize(num_cases);
+  e->nx.resize(num_cases);
+  e->ny.resize(num_cases);
+  e->dt.assign(dts, dts + num_cases);
+  e->ep = new mfc::EnsParams();
+  auto cleanup = [&](int code) {
+    mfc_gpu_ensemble_finalize(e);
+    return code;
+  };
+
+  // sizes, grid tables
+  std::vector<int64_t> reg_off(num_cases), tab_off(num_cases);
+  std::vector<mfc::GridTables> gts(num_cases);
+  int64_t state_elems = 0, table_elems = 0;
+  const int b = (c0.weno_order - 1) / 2 + 2;
+  for (int i = 0; i < num_cases; ++i) {
+    const mfc_params& p = cases[i];
+    const int n[3] = {p.m + 1, p.n + 1, 1};
+    e->nx[i] = n[0];
+    e->ny[i] = n[1];
+    const std::string why = mfc::build_grid_tables(&p, 2, n, b, gts[i]);
+    if (!why.empty()) return cleanup(mfc::report_error(MFC_ERR_INVALID, "case " + std::to_string(i) + ": " + why));
+    const int64_t pitch = (n[0] + 31) / 32 * 32;
+    mfc::DevParams& D = e->cases[i].P;
+    std::memset(&D, 0, sizeof(D));
+    D.n[0] = n[0];
+    D.n[1] = n[1];
+    D.n[2] = 1;
+    D.sy = pitch;
+    D.sz = pitch * n[1];
+    D.sv = D.sz;
+    const int bcb[3] = {p.bc_x_beg, p.bc_y_beg, p.bc_z_beg};
+    const int bce[3] = {p.bc_x_end, p.bc_y_end, p.bc_z_end};
+    for (int d = 0; d < 3; ++d) {
+      D.bc_beg[d] = bcb[d];
+      D.bc_end[d] = bce[d];
+      D.cstride[d] = gts[i].cstride[d];
+    }
+    for (int f = 0; f < mfc::kMaxFluids; ++f) {
+      D.gammas[f] = f < p.num_fluids ? p.gammas[f] : 0.0;
+      D.pi_infs[f] = f < p.num_fluids ? p.pi_infs[f] : 0.0;
+    }
+    D.weno_eps = p.weno_eps;
+    D.coff = mfc::kCoefPad;
+    const int S = 2 * p.num_fluids + 3;
+    reg_off[i] = state_elems;
+    state_elems += 3 * D.sv * S;
+    tab_off[i] = table_elems;
+    table_elems += (int64_t)gts[i].host.size();
+  }
+  if ((err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (err = cudaMalloc(&e->state, sizeof(double) * state_elems)) != cudaSuccess ||
+      (err = cudaMalloc(&e->tables, sizeof(double) * table_elems)) != cudaSuccess ||
+      (err = cudaMalloc(&e->status, sizeof(uint32_t))) != cudaSuccess)
+    return cleanup(mfc::report_error(MFC_ERR_NOMEM, cudaGetErrorString(err)));
+  cudaMemsetAsync(e->state, 0, sizeof(double) * state_elems, e->stream);
+  cudaMemsetAsync(e->status, 0, sizeof(uint32_t), e->stream);
+  for (int i = 0; i < num_cases; ++i) {
+    mfc::EnsCase& C = e->cases[i];
+    const int S = 2 * cases[i].num_fluids + 3;
+    for (int r = 0; r < 3; ++r) C.reg[r] = e->state + reg_off[i] + r * C.P.sv * S;
+    double* tb = e->tables + tab_off[i];
+    if ((err = cudaMemcpyAsync(tb, gts[i].host.data(), sizeof(double) * gts[i].host.size(), cudaMemcpyHostToDevice,
+                               e->stream)) != cudaSuccess)
+      return cleanup(mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err)));
+    for (int d = 0; d < 2; ++d) {
+      C.P.inv_d[d] = tb + gts[i].off_inv[d];
+      C.P.coef[d] = tb + gts[i].off_coef[d];
+    }
+    C.P.status = e->status;
+    C.dt = e->dt[i];
+    C.dt_last = e->dt[i];
+  }
+  int rc = configure(e, en);
+  if (rc) return cleanup(rc);
+  if ((err = cudaStreamSynchronize(e->stream)) != cudaSuccess)
+    return cleanup(mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err)));
+  *out = e;
+  return MFC_OK;
+}
+
+int mfc_gpu_ensemble_upload(mfc_gpu_ensemble* e, int i, const double* host_q) {
+  if (!e || !host_q || i < 0 || i >= e->num) return mfc::report_error(MFC_ERR_INVALID, "bad ensemble upload");
+  const mfc::EnsCase& C = e->cases[i];
+  const int S = 2 * e->nf + 3;
+  for (int v = 0; v < S; ++v) {
+    cudaError_t err = cudaMemcpy2DAsync(C.reg[0] + v * C.P.sv, (size_t)C.P.sy * 8,
+                                        host_q + (int64_t)v * e->nx[i] * e->ny[i], (size_t)e->nx[i] * 8,
+                                        (size_t)e->nx[i] * 8, (size_t)e->ny[i], cudaMemcpyHostToDevice, e->stream);
+    if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+  }
+  cudaError_t err = cudaStreamSynchronize(e->stream);
+  return err == cudaSuccess ? MFC_OK : mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+}
+
+int mfc_gpu_ensemble_download(mfc_gpu_ensemble* e, int i, double* host_q) {
+  if (!e || !host_q || i < 0 || i >= e->num) return mfc::report_error(MFC_ERR_INVALID, "bad ensemble download");
+  const mfc::EnsCase& C = e->cases[i];
+  const int S = 2 * e->nf + 3;
+  for (int v = 0; v < S; ++v) {
+    cudaError_t err = cudaMemcpy2DAsync(host_q + (int64_t)v * e->nx[i] * e->ny[i], (size_t)e->nx[i] * 8,
+                                        C.reg[0] + v * C.P.sv, (size_t)C.P.sy * 8, (size_t)e->nx[i] * 8,
+                                        (size_t)e->ny[i], cudaMemcpyDeviceToHost, e->stream);
+    if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+  }
+  cudaError_t err = cudaStreamSynchronize(e->stream);
+  return err == cudaSuccess ? MFC_OK : mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+}
+
+// The project's autotuner for the ensemble: times `reps` launches of the
+// first RK stage (which reads register 0 and writes register 1, leaving the
+// state untouched) for every compiled tile variant of this configuration,
+// keeps the fastest and reports its index (registry order) and time.
+int mfc_gpu_ensemble_tune(mfc_gpu_ensemble* e, int reps, int* variant_out, double* ms_out) {
+  if (!e) return mfc::report_error(MFC_ERR_INVALID, "NULL ensemble");
+  if (reps < 1) reps = 5;
+  uint32_t saved = 0;  // the timing launches must not leave flags behind
+  cudaError_t serr = cudaMemcpyAsync(&saved, e->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream);
+  if (serr == cudaSuccess) serr = cudaStreamSynchronize(e->stream);
+  if (serr != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(serr));
+  const mfc::EnsembleEntry* best = nullptr;
+  int best_idx = -1, idx = -1;
+  float best_ms = 0.f;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  for (const auto& x : g_ens) {
+    if (x.nf != e->nf || x.wo != e->wo || x.prec != e->prec) continue;
+    ++idx;
+    if (configure(e, &x) != MFC_OK) continue;
+    if (launch_stage(e, 0, 0) != MFC_OK) continue;  // warm-up
+    cudaEventRecord(a, e->stream);
+    for (int r = 0; r < reps; ++r) launch_stage(e, 0, 0);
+    cudaEventRecord(b, e->stream);
+    if (cudaEventSynchronize(b) != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    ms /= reps;
+    if (!best || ms < best_ms) {
+      best = &x;
+      best_ms = ms;
+      best_idx = idx;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaMemcpyAsync(e->status, &saved, sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream);
+  if (!best) return mfc::report_error(MFC_ERR_CUDA, "no ensemble tile variant could be timed");
+  int rc = configure(e, best);
+  if (rc) return rc;
+  if (variant_out) *variant_out = best_idx;
+  if (ms_out) *ms_out = best_ms;
+  cudaError_t err = cudaStreamSynchronize(e->stream);
+  return err == cudaSuccess ? MFC_OK : mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+}
+
+// Time steps t_step_start .. t_step_stop-1 for every case (each with its own
+// dt; the last step uses that case's dt after the p_main trim).  With
+// use_graph the stage launches of one step are captured once in a CUDA graph
+// (and once more for the last step) and replayed.  Synchronous.
+int mfc_gpu_ensemble_run(mfc_gpu_ensemble* e, int t_step_start, int t_step_stop, int use_graph) {
+  if (!e) return mfc::report_error(MFC_ERR_INVALID, "NULL ensemble");
+  if (t_step_start < 0 || t_step_stop <= t_step_start)
+    return mfc::report_error(MFC_ERR_INVALID, "Unsupported combination of values of t_step_start and t_step_stop");
+  for (int i = 0; i < e->num; ++i) e->cases[i].dt_last = trimmed_last_dt(e->dt[i], t_step_start, t_step_stop);
+  const int steps = t_step_stop - t_step_start;
+  int rc = MFC_OK;
+  if (!use_graph) {
+    for (int s = 0; s < steps && !rc; ++s) rc = launch_step(e, s == steps - 1);
+  } else {
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    for (int last = 0; last < 2 && !rc; ++last) {
+      cudaGraph_t g = nullptr;
+      cudaError_t err = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+      if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+      const int64_t before = e->launches;
+      rc = launch_step(e, last);
+      e->launches = before;  // counted when replayed
+      err = cudaStreamEndCapture(e->stream, &g);
+      if (!rc && err != cudaSuccess) rc = mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+      if (!rc && (err = cudaGraphInstantiate(&exec[last], g, 0)) != cudaSuccess)
+        rc = mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+      if (g) cudaGraphDestroy(g);
+    }
+    const int per_step = e->ts == 2 ? 2 : 3;
+    for (int s = 0; s < steps && !rc; ++s) {
+      cudaError_t err = cudaGraphLaunch(exec[s == steps - 1 ? 1 : 0], e->stream);
+      if (err != cudaSuccess) rc = mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+      e->launches += per_step;
+    }
+    cudaStreamSynchronize(e->stream);
+    for (auto& x : exec)
+      if (x) cudaGraphExecDestroy(x);
+  }
+  if (rc) return rc;
+  uint32_t flags = 0;
+  cudaError_t err = cudaMemcpyAsync(&flags, e->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
+  if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+  if (flags & MFC_FLAG_NAN) return mfc::report_error(MFC_ERR_STATE, "NaN or Inf in an ensemble case");
+  return MFC_OK;
+}
+
+void* mfc_gpu_ensemble_stream(mfc_gpu_ensemble* e) { return e ? (void*)e->stream : nullptr; }
+
+int64_t mfc_gpu_ensemble_launch_count(const mfc_gpu_ensemble* e) { return e ? e->launches : 0; }
+
+int mfc_gpu_ensemble_finalize(mfc_gpu_ensemble* e) {
+  if (!e) return MFC_OK;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  cudaFree(e->state);
+  cudaFree(e->tables);
+  cudaFree(e->status);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e->ep;
+  delete e;
+  return MFC_OK;
+}
+
+}  // extern "C"

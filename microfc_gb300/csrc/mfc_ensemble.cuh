@@ -1,0 +1,89 @@
+// Ensemble of independent 2-D cases advanced together: one persistent launch
+// per RK stage walks a work list of (case, tile) pairs, so 64 small cases of
+// uneven size fill the GPU like one large one.  Each tile runs exactly the
+// single-case stage_tile, so every case gets the same bits it would get
+// alone.  The per-case parameter blocks travel in the kernel's parameter
+// space (__grid_constant__), which keeps their fields in the constant bank.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "mfc_device.cuh"
+#include "mfc_stage.cuh"
+
+namespace mfc {
+
+constexpr int kMaxEnsemble = 96;
+
+struct EnsCase {
+  DevParams P;
+  double* reg[3];         // RK registers; reg[0] holds q_cons_ts(1)
+  double dt, dt_last;     // the case's dt and its (possibly trimmed) last-step dt
+  int tiles_x, tile_base; // tiles per row, first tile in the work list
+};
+
+struct EnsParams {
+  int num_cases, total_tiles, stage, time_stepper, last_step;
+  EnsCase c[kMaxEnsemble];
+};
+static_assert(sizeof(EnsParams) <= 32764, "ensemble parameters must fit the kernel parameter space");
+
+template <int NF, int WO, class RT, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT) ensemble_stage_kernel(const __grid_constant__ EnsParams E) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  for (int t = blockIdx.x; t < E.total_tiles; t += gridDim.x) {
+    int lo = 0, hi = E.num_cases - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (E.c[mid].tile_base <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const EnsCase& C = E.c[lo];
+    const int lt = t - C.tile_base;
+    const int x0 = (lt % C.tiles_x) * TX, y0 = (lt / C.tiles_x) * TY;
+    const double* in;
+    double* out;
+    int kind;
+    if (E.stage == 0) {
+      in = C.reg[0], out = C.reg[1], kind = kRkEuler;
+    } else if (E.time_stepper == 2) {
+      in = C.reg[1], out = C.reg[0], kind = kRk2Final;
+    } else if (E.stage == 1) {
+      in = C.reg[1], out = C.reg[2], kind = kRk3Mid;
+    } else {
+      in = C.reg[2], out = C.reg[0], kind = kRk3Final;
+    }
+    stage_tile<2, NF, WO, RT, TX, TY, NT>(C.P, in, C.reg[0], out, E.last_step ? C.dt_last : C.dt, kind, x0, y0,
+                                          smem_raw);
+    __syncthreads();  // the next tile reuses the shared memory
+  }
+}
+
+struct EnsembleEntry {
+  int nf, wo, prec, tx, ty, nt;
+  size_t smem;
+  const void* func;
+  cudaError_t (*launch)(const EnsParams& E, int grid, cudaStream_t st);
+};
+
+template <int NF, int WO, class RT, int TX, int TY, int NT>
+cudaError_t ensemble_launch(const EnsParams& E, int grid, cudaStream_t st) {
+  using Sh = StageShape<2, NF, WO, RT, TX, TY>;
+  ensemble_stage_kernel<NF, WO, RT, TX, TY, NT><<<grid, NT, Sh::kSmemBytes, st>>>(E);
+  return cudaGetLastError();
+}
+
+template <int NF, int WO, class RT, int TX, int TY, int NT>
+EnsembleEntry ensemble_entry() {
+  using Sh = StageShape<2, NF, WO, RT, TX, TY>;
+  return EnsembleEntry{NF, WO, sizeof(RT) == 8 ? 0 : 1, TX, TY, NT, Sh::kSmemBytes,
+                       reinterpret_cast<const void*>(&ensemble_stage_kernel<NF, WO, RT, TX, TY, NT>),
+                       &ensemble_launch<NF, WO, RT, TX, TY, NT>};
+}
+
+void register_ensemble_fp64(std::vector<EnsembleEntry>& r);
+void register_ensemble_fp32(std::vector<EnsembleEntry>& r);
+
+}  // namespace mfc

@@ -166,7 +166,6 @@ inline std::string validate_params(const mfc_params* p) {
   if (p->m <= 0) return "Unsupported value of m";
   if (p->n < 0 || p->p < 0) return "Unsupported value of n or p";
   if (p->p > 0 && p->n == 0) return "p > 0 requires n > 0";
-  if (p->p > 0) return "3-D cases are not built into this library yet";
   if (p->num_fluids < 1 || p->num_fluids > 2) return "Unsupported value of num_fluids (1 or 2)";
   if (p->weno_order != 1 && p->weno_order != 3 && p->weno_order != 5) return "Unsupported value of weno_order";
   const int stcls = 5 * p->weno_order;  // num_stcls_min*weno_order, m_start_up.fpp:182-189
@@ -189,6 +188,8 @@ inline std::string validate_params(const mfc_params* p) {
   }
   if (!p->x_cb) return "x_cb is NULL";
   if (p->n > 0 && !p->y_cb) return "y_cb is NULL";
+  if (p->p > 0 && !p->z_cb) return "z_cb is NULL";
+  if (p->p > 0 && p->p + 1 < stcls) return "Unsupported combination of values of p and weno_order";
   if (p->precision != MFC_PREC_FP64 && p->precision != MFC_PREC_SPLIT) return "Unsupported precision";
   return "";
 }

@@ -8,8 +8,11 @@
 #include <string>
 #include <vector>
 
+#include <type_traits>
+
 #include "mfc_device.cuh"
 #include "mfc_stage.cuh"
+#include "mfc_sweep.cuh"
 
 namespace mfc {
 
@@ -17,6 +20,7 @@ struct StageEntry {
   int nd, nf, wo, prec;  // prec: 0 = FP64, 1 = split (FP32 WENO/HLLC)
   int tx, ty, nt;
   size_t smem;
+  int kernels;  // kernel launches per RK stage (1 in 1-D/2-D, 3 sweeps in 3-D)
   cudaError_t (*prepare)();
   cudaError_t (*launch)(const DevParams& P, const double* qin, const double* qbase, double* qout, double dt,
                         int kind, cudaStream_t st);
@@ -41,9 +45,49 @@ cudaError_t stage_launch(const DevParams& P, const double* qin, const double* qb
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT>
 StageEntry stage_entry() {
   using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
-  return StageEntry{ND, NF, WO, sizeof(RT) == 8 ? 0 : 1, TX, TY, NT, Sh::kSmemBytes,
+  return StageEntry{ND, NF, WO, sizeof(RT) == 8 ? 0 : 1, TX, TY, NT, Sh::kSmemBytes, 1,
                     &stage_prepare<ND, NF, WO, RT, TX, TY, NT>, &stage_launch<ND, NF, WO, RT, TX, TY, NT>};
 }
+
+// 3-D: three directional sweeps per stage (mfc_sweep.cuh).  The x sweep uses
+// TA0 x TB0 x TC0 tiles (x along the sweep); the y and z sweeps use
+// TA1 x TB1 x 1 tiles with x across the pencils.
+template <int NF, int WO, class RT, int TA0, int TB0, int TC0, int TA1, int TB1, int NT>
+struct Sweep3D {
+  template <int DIR>
+  using K = std::conditional_t<DIR == 0, SweepShape<NF, WO, RT, 0, TA0, TB0, TC0>,
+                               SweepShape<NF, WO, RT, DIR, TA1, TB1, 1>>;
+
+  template <int DIR>
+  static cudaError_t prep() {
+    if constexpr (DIR == 0)
+      return cudaFuncSetAttribute(sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K<0>::kSmemBytes);
+    else
+      return cudaFuncSetAttribute(sweep_kernel<NF, WO, RT, DIR, TA1, TB1, 1, NT>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K<DIR>::kSmemBytes);
+  }
+  static cudaError_t prepare() {
+    cudaError_t e = prep<0>();
+    if (e == cudaSuccess) e = prep<1>();
+    if (e == cudaSuccess) e = prep<2>();
+    return e;
+  }
+  static cudaError_t launch(const DevParams& P, const double* qin, const double* qbase, double* qout, double dt,
+                            int kind, cudaStream_t st) {
+    const unsigned nx = P.n[0], ny = P.n[1], nz = P.n[2];
+    const dim3 g0((nx + TA0 - 1) / TA0, (ny + TB0 - 1) / TB0, (nz + TC0 - 1) / TC0);
+    const dim3 g1((nx + TB1 - 1) / TB1, (ny + TA1 - 1) / TA1, nz);
+    const dim3 g2((nx + TB1 - 1) / TB1, (nz + TA1 - 1) / TA1, ny);
+    sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT><<<g0, NT, K<0>::kSmemBytes, st>>>(P, qin, qbase, qout, dt, kind);
+    sweep_kernel<NF, WO, RT, 1, TA1, TB1, 1, NT><<<g1, NT, K<1>::kSmemBytes, st>>>(P, qin, qbase, qout, dt, kind);
+    sweep_kernel<NF, WO, RT, 2, TA1, TB1, 1, NT><<<g2, NT, K<2>::kSmemBytes, st>>>(P, qin, qbase, qout, dt, kind);
+    return cudaGetLastError();
+  }
+  static StageEntry entry() {
+    return StageEntry{3, NF, WO, sizeof(RT) == 8 ? 0 : 1, TA0, TB1, NT, K<1>::kSmemBytes, 3, &prepare, &launch};
+  }
+};
 
 // The default (first registered) launcher of a configuration, or nullptr.
 const StageEntry* find_stage(int nd, int nf, int wo, int prec);
@@ -56,5 +100,7 @@ void register_stage_1d_fp64(std::vector<StageEntry>& r);
 void register_stage_1d_fp32(std::vector<StageEntry>& r);
 void register_stage_2d_fp64(std::vector<StageEntry>& r);
 void register_stage_2d_fp32(std::vector<StageEntry>& r);
+void register_stage_3d_fp64(std::vector<StageEntry>& r);
+void register_stage_3d_fp32(std::vector<StageEntry>& r);
 
 }  // namespace mfc

@@ -80,6 +80,9 @@ extern "C" int mfc_gpu_tvd_rk_noalloc(const mfc_params* p, const double* q_in, d
                                       double dt, void* stream) {
   const std::string why = mfc::validate_params(p);
   if (!why.empty()) return mfc::report_error(MFC_ERR_INVALID, why);
+  if (p->p > 0)
+    return mfc::report_error(MFC_ERR_INVALID, "mfc_gpu_tvd_rk_noalloc handles 1-D and 2-D cases; 3-D cases need "
+                                              "the RHS work buffer that mfc_gpu_init allocates");
   if (!q_in || !q_out) return mfc::report_error(MFC_ERR_INVALID, "q_in and q_out must be device arrays");
   if (q_in == q_out) return mfc::report_error(MFC_ERR_INVALID, "q_in and q_out must be different arrays");
   const int nd = 1 + (p->n > 0) + (p->p > 0);

@@ -21,6 +21,16 @@
 
 namespace mfc {
 
+// Precision changes of the accumulation type: identity for FP64, the
+// integer bit-field conversions for the split path's FP32.
+template <class T>
+__device__ __forceinline__ T narrow(double x) {
+  if constexpr (sizeof(T) == 4) return d2f_bits(x);
+  else return x;
+}
+__device__ __forceinline__ double widen(double x) { return x; }
+__device__ __forceinline__ double widen(float x) { return f2d_bits(x); }
+
 template <int ND, int NF, int WO, class RT, int TX, int TY>
 struct StageShape {
   using Q = Eqs<ND, NF>;
@@ -38,27 +48,38 @@ struct StageShape {
   static constexpr int NFX = (S + 1) * TYE * (TX + 1);
   static constexpr int NFY = (ND > 1) ? (S + 1) * (TY + 1) * TX : 0;
   static constexpr int NFL = NFX > NFY ? NFX : NFY;
-  static constexpr size_t kSmemBytes = sizeof(RT) * (size_t(NQ) + 2 * size_t(NW) + size_t(NFL));
+  // split precision: the tile's WENO coefficients, converted to FP32 once
+  static constexpr int NCX = TX + 2, NCY = (ND > 1) ? TY + 2 : 0;
+  static constexpr int NCOEF = (sizeof(RT) == 4 && WO == 5) ? kNumCoef * (NCX + NCY) : 0;
+  static constexpr size_t kSmemBytes = sizeof(RT) * (size_t(NQ) + 2 * size_t(NW) + size_t(NFL) + size_t(NCOEF));
 };
 
+// One tile of one RK stage; the tile's first cell is (x0, y0).  Used by the
+// single-case kernel (one tile per block) and by the ensemble kernel (many
+// tiles of many cases per persistent block).  smem_raw must hold
+// StageShape::kSmemBytes.
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT>
-__global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const double* __restrict__ qin,
-                                                   const double* __restrict__ qbase, double* __restrict__ qout,
-                                                   const double dt, const int kind) {
+__device__ __forceinline__ void stage_tile(const DevParams& P, const double* __restrict__ qin,
+                                           const double* __restrict__ qbase, double* __restrict__ qout,
+                                           const double dt, const int kind, const int x0, const int y0,
+                                           unsigned char* smem_raw) {
   using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
   using Q = Eqs<ND, NF>;
   constexpr int S = Sh::S, H = Sh::H, LX = Sh::LX, LY = Sh::LY, TYE = Sh::TYE;
   constexpr int CPT = (TX * TYE + NT - 1) / NT;  // interior cells per thread
+  // split precision: FP32 reconstruction, Riemann solve and flux divergence;
+  // the plain path keeps everything in FP64 in the reference's order
+  constexpr bool kSplit = sizeof(RT) == 4;
+  using AT = RT;  // type of the flux-divergence accumulation
 
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   RT* sq = reinterpret_cast<RT*>(smem_raw);  // [S][LY][LX] primitive
   RT* wl = sq + Sh::NQ;                       // left-face values
   RT* wr = wl + Sh::NW;                       // right-face values
   RT* fl = wr + Sh::NW;                       // fluxes [S+1][...]
+  RT* scx = fl + Sh::NFL;                     // split: FP32 x coefficients [kNumCoef][TX+2]
+  RT* scy = scx + kNumCoef * Sh::NCX;         // split: FP32 y coefficients [kNumCoef][TY+2]
 
   const int tid = threadIdx.x;
-  const int x0 = blockIdx.x * TX;
-  const int y0 = (ND > 1) ? blockIdx.y * TY : 0;
   const int nx = P.n[0], ny = P.n[1];
 
   RT gam_i[NF], pi_i[NF];
@@ -84,9 +105,28 @@ __global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const doub
     for (int v = 0; v < S; ++v) q[v] = __ldg(src + v * P.sv);
     if (fx) q[Q::MOM] = -q[Q::MOM];
     if (ND > 1 && fy) q[Q::MOM + 1] = -q[Q::MOM + 1];
-    cons_to_prim<ND, NF>(q, P);
+    if constexpr (kSplit) {
+      float pr[S];
+      cons_to_prim_split<ND, NF>(q, P, pr);
 #pragma unroll
-    for (int v = 0; v < S; ++v) sq[(v * LY + ly) * LX + lx] = RT(q[v]);
+      for (int v = 0; v < S; ++v) sq[(v * LY + ly) * LX + lx] = pr[v];
+    } else {
+      cons_to_prim<ND, NF>(q, P);
+#pragma unroll
+      for (int v = 0; v < S; ++v) sq[(v * LY + ly) * LX + lx] = RT(q[v]);
+    }
+  }
+  if constexpr (Sh::NCOEF > 0) {
+    for (int it = tid; it < kNumCoef * Sh::NCX; it += NT) {
+      const int cx = it % Sh::NCX, k = it / Sh::NCX;
+      scx[it] = d2f_bits(__ldg(P.coef[0] + k * P.cstride[0] + clamp_coef_index(x0 - 1 + cx, nx) + P.coff));
+    }
+    if constexpr (ND > 1) {
+      for (int it = tid; it < kNumCoef * Sh::NCY; it += NT) {
+        const int cy = it % Sh::NCY, k = it / Sh::NCY;
+        scy[it] = d2f_bits(__ldg(P.coef[1] + k * P.cstride[1] + clamp_coef_index(y0 - 1 + cy, ny) + P.coff));
+      }
+    }
   }
   __syncthreads();
 
@@ -109,13 +149,17 @@ __global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const doub
         st[k] = (o >= -(WO / 2) && o <= WO / 2) ? row[lx + o] : RT(0);
       }
       RT c[kNumCoef];
-      if constexpr (WO > 1) {
+      if constexpr (Sh::NCOEF > 0) {
+#pragma unroll
+        for (int k = 0; k < kNumCoef; ++k) c[k] = scx[k * NCX + cx];
+      } else if constexpr (WO > 1) {
         const int gi = clamp_coef_index(x0 - 1 + cx, nx) + P.coff;
 #pragma unroll
         for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
       }
       RT vl, vr;
-      weno_cell<WO, RT>(c, st, eps, vl, vr);
+      if constexpr (kSplit && WO == 5) weno5_cell_fast(c, st, eps, vl, vr);
+      else weno_cell<WO, RT>(c, st, eps, vl, vr);
       wl[(v * TYE + ty) * NCX + cx] = vl;
       wr[(v * TYE + ty) * NCX + cx] = vr;
     }
@@ -147,7 +191,7 @@ __global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const doub
   __syncthreads();
 
   // ---- phase 4: x flux divergence (registers) + y WENO ----------------------
-  double rhs[CPT][S];
+  AT rhs[CPT][S];
 #pragma unroll
   for (int k = 0; k < CPT; ++k) {
     const int e = tid + k * NT;
@@ -155,14 +199,14 @@ __global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const doub
     const int tx = e % TX, ty = e / TX;
     const int gx = x0 + tx;
     constexpr int NFXr = TX + 1;
-    const double inv = __ldg(P.inv_d[0] + (gx < nx ? gx : nx - 1));
+    const AT inv = narrow<AT>(__ldg(P.inv_d[0] + (gx < nx ? gx : nx - 1)));
 #pragma unroll
     for (int v = 0; v < S; ++v)
-      rhs[k][v] = inv * (double(fl[(v * TYE + ty) * NFXr + tx]) - double(fl[(v * TYE + ty) * NFXr + tx + 1]));
-    const double du = double(fl[(S * TYE + ty) * NFXr + tx + 1]) - double(fl[(S * TYE + ty) * NFXr + tx]);
+      rhs[k][v] = inv * (AT(fl[(v * TYE + ty) * NFXr + tx]) - AT(fl[(v * TYE + ty) * NFXr + tx + 1]));
+    const AT du = AT(fl[(S * TYE + ty) * NFXr + tx + 1]) - AT(fl[(S * TYE + ty) * NFXr + tx]);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
-      const double a = double(sq[((Q::ADV + f) * LY + (ND > 1 ? ty + H : 0)) * LX + tx + H]);
+      const AT a = AT(sq[((Q::ADV + f) * LY + (ND > 1 ? ty + H : 0)) * LX + tx + H]);
       rhs[k][Q::ADV + f] = rhs[k][Q::ADV + f] + inv * a * du;
     }
   }
@@ -183,13 +227,17 @@ __global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const doub
         st[k] = (o >= -(WO / 2) && o <= WO / 2) ? col[(ly + o) * LX] : RT(0);
       }
       RT c[kNumCoef];
-      if constexpr (WO > 1) {
+      if constexpr (Sh::NCOEF > 0) {
+#pragma unroll
+        for (int k = 0; k < kNumCoef; ++k) c[k] = scy[k * NCY + cy];
+      } else if constexpr (WO > 1) {
         const int gi = clamp_coef_index(y0 - 1 + cy, ny) + P.coff;
 #pragma unroll
         for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
       }
       RT vl, vr;
-      weno_cell<WO, RT>(c, st, eps, vl, vr);
+      if constexpr (kSplit && WO == 5) weno5_cell_fast(c, st, eps, vl, vr);
+      else weno_cell<WO, RT>(c, st, eps, vl, vr);
       wl[(v * NCY + cy) * TX + tx] = vl;
       wr[(v * NCY + cy) * TX + tx] = vr;
     }
@@ -224,14 +272,14 @@ __global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const doub
       if (e >= TX * TY) break;
       const int tx = e % TX, ty = e / TX;
       const int gy = y0 + ty;
-      const double inv = __ldg(P.inv_d[1] + (gy < ny ? gy : ny - 1));
+      const AT inv = narrow<AT>(__ldg(P.inv_d[1] + (gy < ny ? gy : ny - 1)));
 #pragma unroll
       for (int v = 0; v < S; ++v)
-        rhs[k][v] = rhs[k][v] + inv * (double(fl[(v * NFYr + ty) * TX + tx]) - double(fl[(v * NFYr + ty + 1) * TX + tx]));
-      const double du = double(fl[(S * NFYr + ty + 1) * TX + tx]) - double(fl[(S * NFYr + ty) * TX + tx]);
+        rhs[k][v] = rhs[k][v] + inv * (AT(fl[(v * NFYr + ty) * TX + tx]) - AT(fl[(v * NFYr + ty + 1) * TX + tx]));
+      const AT du = AT(fl[(S * NFYr + ty + 1) * TX + tx]) - AT(fl[(S * NFYr + ty) * TX + tx]);
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
-        const double a = double(sq[((Q::ADV + f) * LY + ty + H) * LX + tx + H]);
+        const AT a = AT(sq[((Q::ADV + f) * LY + ty + H) * LX + tx + H]);
         rhs[k][Q::ADV + f] = rhs[k][Q::ADV + f] + inv * a * du;
       }
     }
@@ -249,20 +297,30 @@ __global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const doub
     const int64_t o = gy * P.sy + gx;
 #pragma unroll
     for (int v = 0; v < S; ++v) {
-      double r = rhs[k][v];
+      const double r = widen(rhs[k][v]);
       double out;
       if (kind == kRhsOnly) {
         out = r;
       } else {
         const double b = __ldg(qbase + o + v * P.sv);
         const double in = (kind == kRkEuler) ? b : __ldg(qin + o + v * P.sv);
-        out = rk_combine(kind, b, in, dt, r);
+        if constexpr (kSplit) out = rk_combine_split(kind, b, in, dt, r);
+        else out = rk_combine(kind, b, in, dt, r);
       }
       bad |= not_finite(out);
       qout[o + v * P.sv] = out;
     }
   }
   if (bad && P.status) atomicOr(P.status, 1u);
+}
+
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const double* __restrict__ qin,
+                                                   const double* __restrict__ qbase, double* __restrict__ qout,
+                                                   const double dt, const int kind) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  stage_tile<ND, NF, WO, RT, TX, TY, NT>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
+                                         (ND > 1) ? blockIdx.y * TY : 0, smem_raw);
 }
 
 }  // namespace mfc

@@ -1,0 +1,221 @@
+// Directional sweep kernel for 3-D cases (the reference is 2-D; this is its
+// z-extension).  A 3-D RK stage is three launches, one per direction, each
+// computing that direction's part of s_compute_rhs (m_rhs.fpp:469-656):
+//
+//   x sweep: rhs  = 1/dx (F_{i-1/2} - F_{i+1/2});  rhs_a += 1/dx alpha (u*_{i+1/2} - u*_{i-1/2})
+//   y sweep: rhs += ... (same in y)
+//   z sweep: rhs += ... (same in z), then the RK combination (m_time_steppers.fpp)
+//
+// which is the reference's accumulation order, so the FP64 variant
+// reproduces the oracle bit for bit.  A block owns TA cells along the sweep
+// direction for TB x TC pencils; it loads them plus an H-cell halo along the
+// sweep (coalesced: x is always one of the fastest-varying thread indices),
+// converts to primitive variables, reconstructs every variable of the TA+2
+// cells that border the block's faces, solves TA+1 Riemann problems per
+// pencil and forms the flux divergence.  The partial RHS lives in a global
+// buffer (FP64, or FP32 on the split path) between the sweeps.
+#pragma once
+
+#include "mfc_device.cuh"
+#include "mfc_stage.cuh"
+
+namespace mfc {
+
+template <int NF, int WO, class RT, int DIR, int TA, int TB, int TC>
+struct SweepShape {
+  using Q = Eqs<3, NF>;
+  static constexpr int S = Q::S;
+  static constexpr int H = (WO + 1) / 2;
+  static constexpr int LA = TA + 2 * H;
+  static constexpr int NP = TB * TC;          // pencils per block
+  static constexpr int NQ = S * NP * LA;      // primitive tile [S][pencil][LA]
+  static constexpr int NW = S * NP * (TA + 2);
+  static constexpr int NFL = (S + 1) * NP * (TA + 1);
+  static constexpr int NCOEF = (sizeof(RT) == 4 && WO == 5) ? kNumCoef * (TA + 2) : 0;
+  static constexpr size_t kSmemBytes = sizeof(RT) * (size_t(NQ) + 2 * size_t(NW) + size_t(NFL) + size_t(NCOEF));
+};
+
+// Pencil p of a block and position a along the sweep -> global (x, y, z).
+// DIR 0: a = x, pencils over (y = b, z = c); DIR 1: a = y, pencils over
+// (x = b, z = c); DIR 2: a = z, pencils over (x = b, y = c).
+template <int DIR>
+__device__ __forceinline__ void sweep_coords(int a, int b, int c, int& x, int& y, int& z) {
+  if (DIR == 0) { x = a; y = b; z = c; }
+  else if (DIR == 1) { x = b; y = a; z = c; }
+  else { x = b; y = c; z = a; }
+}
+
+template <int NF, int WO, class RT, int DIR, int TA, int TB, int TC, int NT>
+__global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const double* __restrict__ qin,
+                                                   const double* __restrict__ qbase, double* __restrict__ qout,
+                                                   const double dt, const int kind) {
+  using Sh = SweepShape<NF, WO, RT, DIR, TA, TB, TC>;
+  using Q = Eqs<3, NF>;
+  constexpr int S = Sh::S, H = Sh::H, LA = Sh::LA, NP = Sh::NP;
+  constexpr bool kSplit = sizeof(RT) == 4;
+  using AT = RT;
+  constexpr int OA = DIR, OB = DIR == 0 ? 1 : 0, OC = DIR == 2 ? 1 : 2;  // axis index of a, b, c
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  RT* sq = reinterpret_cast<RT*>(smem_raw);
+  RT* wl = sq + Sh::NQ;
+  RT* wr = wl + Sh::NW;
+  RT* fl = wr + Sh::NW;
+  RT* sc = fl + Sh::NFL;
+
+  const int tid = threadIdx.x;
+  // block origin: blockIdx.x tiles the fastest non-sweep axis for DIR != 0
+  int a0, b0, c0;
+  if (DIR == 0) { a0 = blockIdx.x * TA; b0 = blockIdx.y * TB; c0 = blockIdx.z * TC; }
+  else { b0 = blockIdx.x * TB; a0 = blockIdx.y * TA; c0 = blockIdx.z * TC; }
+  const int na = P.n[OA], nb = P.n[OB], nc = P.n[OC];
+
+  RT gam_i[NF], pi_i[NF];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    gam_i[f] = RT(P.gammas[f]);
+    pi_i[f] = RT(P.pi_infs[f]);
+  }
+  const RT eps = RT(P.weno_eps);
+  const int64_t st[3] = {1, P.sy, P.sz};
+
+  // ---- load + BCs + cons -> prim ------------------------------------------------
+  // thread order: the a index fastest for the x sweep, the pencil b index
+  // fastest otherwise, so that global loads are coalesced along x
+  for (int it = tid; it < NP * LA; it += NT) {
+    int la, pb, pc;
+    if (DIR == 0) { la = it % LA; pb = (it / LA) % TB; pc = it / (LA * TB); }
+    else { pb = it % TB; la = (it / TB) % LA; pc = it / (TB * LA); }
+    bool fa = false, dummy = false;
+    const int ga = map_cell(a0 - H + la, na, P.bc_beg[OA], P.bc_end[OA], &fa);
+    const int gb = map_cell(b0 + pb, nb, P.bc_beg[OB], P.bc_end[OB], &dummy);
+    const int gc = map_cell(c0 + pc, nc, P.bc_beg[OC], P.bc_end[OC], &dummy);
+    const double* src = qin + ga * st[OA] + gb * st[OB] + gc * st[OC];
+    double q[S];
+#pragma unroll
+    for (int v = 0; v < S; ++v) q[v] = __ldg(src + v * P.sv);
+    if (fa) q[Q::MOM + DIR] = -q[Q::MOM + DIR];
+    const int p = pc * TB + pb;
+    if constexpr (kSplit) {
+      float pr[S];
+      cons_to_prim_split<3, NF>(q, P, pr);
+#pragma unroll
+      for (int v = 0; v < S; ++v) sq[(v * NP + p) * LA + la] = pr[v];
+    } else {
+      cons_to_prim<3, NF>(q, P);
+#pragma unroll
+      for (int v = 0; v < S; ++v) sq[(v * NP + p) * LA + la] = RT(q[v]);
+    }
+  }
+  if constexpr (Sh::NCOEF > 0) {
+    for (int it = tid; it < kNumCoef * (TA + 2); it += NT) {
+      const int ca = it % (TA + 2), k = it / (TA + 2);
+      sc[it] = d2f_bits(__ldg(P.coef[DIR] + k * P.cstride[DIR] + clamp_coef_index(a0 - 1 + ca, na) + P.coff));
+    }
+  }
+  __syncthreads();
+
+  // ---- WENO along the sweep for cells a0-1 .. a0+TA --------------------------------
+  constexpr int NCA = TA + 2;
+  for (int it = tid; it < S * NP * NCA; it += NT) {
+    const int ca = it % NCA;
+    const int r = it / NCA;
+    const int p = r % NP, v = r / NP;
+    const RT* line = sq + (v * NP + p) * LA;
+    const int la = ca + H - 1;
+    RT stc[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const int o = k - 2;
+      stc[k] = (o >= -(WO / 2) && o <= WO / 2) ? line[la + o] : RT(0);
+    }
+    RT c[kNumCoef];
+    if constexpr (Sh::NCOEF > 0) {
+#pragma unroll
+      for (int k = 0; k < kNumCoef; ++k) c[k] = sc[k * NCA + ca];
+    } else if constexpr (WO > 1) {
+      const int gi = clamp_coef_index(a0 - 1 + ca, na) + P.coff;
+#pragma unroll
+      for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(P.coef[DIR] + k * P.cstride[DIR] + gi));
+    }
+    RT vl, vr;
+    if constexpr (kSplit && WO == 5) weno5_cell_fast(c, stc, eps, vl, vr);
+    else weno_cell<WO, RT>(c, stc, eps, vl, vr);
+    wl[(v * NP + p) * NCA + ca] = vl;
+    wr[(v * NP + p) * NCA + ca] = vr;
+  }
+  __syncthreads();
+
+  // ---- HLLC on faces a0-1/2 .. a0+TA-1/2 ---------------------------------------------
+  constexpr int NFA = TA + 1;
+  for (int it = tid; it < NP * NFA; it += NT) {
+    const int f = it % NFA, p = it / NFA;
+    const int gface = a0 - 1 + f;
+    RT qL[S], qR[S], F[S], us;
+    const bool lfr = (gface == -1 && P.bc_beg[OA] == -4);
+    const bool rfl = (gface == na - 1 && P.bc_end[OA] == -4);
+#pragma unroll
+    for (int v = 0; v < S; ++v) {
+      const RT a = wr[(v * NP + p) * NCA + f];
+      const RT b = wl[(v * NP + p) * NCA + f + 1];
+      qL[v] = lfr ? b : a;
+      qR[v] = rfl ? a : b;
+    }
+    hllc_face<3, NF, DIR, RT>(qL, qR, gam_i, pi_i, F, us);
+#pragma unroll
+    for (int v = 0; v < S; ++v) fl[(v * NP + p) * NFA + f] = F[v];
+    fl[(S * NP + p) * NFA + f] = us;
+  }
+  __syncthreads();
+
+  // ---- flux divergence, accumulation, RK on the last sweep ---------------------------
+  AT* rhs_buf = reinterpret_cast<AT*>(P.work);
+  bool bad = false;
+  for (int it = tid; it < NP * TA; it += NT) {
+    int ta, pb, pc;
+    if (DIR == 0) { ta = it % TA; pb = (it / TA) % TB; pc = it / (TA * TB); }
+    else { pb = it % TB; ta = (it / TB) % TA; pc = it / (TB * TA); }
+    const int ga = a0 + ta, gb = b0 + pb, gc = c0 + pc;
+    if (ga >= na || gb >= nb || gc >= nc) continue;
+    const int p = pc * TB + pb;
+    int x, y, z;
+    sweep_coords<DIR>(ga, gb, gc, x, y, z);
+    const int64_t o = z * P.sz + y * P.sy + x;
+    const AT inv = narrow<AT>(__ldg(P.inv_d[DIR] + ga));
+    AT r[S];
+#pragma unroll
+    for (int v = 0; v < S; ++v) {
+      const AT d = inv * (AT(fl[(v * NP + p) * NFA + ta]) - AT(fl[(v * NP + p) * NFA + ta + 1]));
+      r[v] = (DIR == 0) ? d : rhs_buf[o + v * P.sv] + d;
+    }
+    const AT du = AT(fl[(S * NP + p) * NFA + ta + 1]) - AT(fl[(S * NP + p) * NFA + ta]);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      const AT a = AT(sq[((Q::ADV + f) * NP + p) * LA + ta + H]);
+      r[Q::ADV + f] = r[Q::ADV + f] + inv * a * du;
+    }
+    if (DIR < 2) {
+#pragma unroll
+      for (int v = 0; v < S; ++v) rhs_buf[o + v * P.sv] = r[v];
+      continue;
+    }
+#pragma unroll
+    for (int v = 0; v < S; ++v) {
+      const double rv = widen(r[v]);
+      double out;
+      if (kind == kRhsOnly) {
+        out = rv;
+      } else {
+        const double b = __ldg(qbase + o + v * P.sv);
+        const double in = (kind == kRkEuler) ? b : __ldg(qin + o + v * P.sv);
+        if constexpr (kSplit) out = rk_combine_split(kind, b, in, dt, rv);
+        else out = rk_combine(kind, b, in, dt, rv);
+      }
+      bad |= not_finite(out);
+      qout[o + v * P.sv] = out;
+    }
+  }
+  if (bad && P.status) atomicOr(P.status, 1u);
+}
+
+}  // namespace mfc

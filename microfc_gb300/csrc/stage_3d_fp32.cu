@@ -1,0 +1,13 @@
+// Instantiations of the 3-D directional sweeps, split precision.
+#include "mfc_launch.h"
+
+namespace mfc {
+
+void register_stage_3d_fp32(std::vector<StageEntry>& r) {
+  r.push_back(Sweep3D<2, 5, float, 32, 4, 2, 16, 32, 256>::entry());
+  r.push_back(Sweep3D<1, 5, float, 32, 4, 2, 16, 32, 256>::entry());
+  r.push_back(Sweep3D<2, 3, float, 32, 4, 2, 16, 32, 256>::entry());
+  r.push_back(Sweep3D<2, 1, float, 32, 4, 2, 16, 32, 256>::entry());
+}
+
+}  // namespace mfc

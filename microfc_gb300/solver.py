@@ -30,6 +30,29 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
+def make_params(case: Case, x_cb, y_cb=None, z_cb=None, device: int = 0):
+    """The mfc_params block of a case; returns (params, arrays it points to)."""
+    cb = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (x_cb, y_cb, z_cb)]
+    P = _lib.MfcParams()
+    P.m, P.n, P.p = case.m, case.n, case.p
+    P.num_fluids = case.num_fluids
+    P.weno_order = case.weno_order
+    P.weno_eps = case.weno_eps
+    P.time_stepper = case.time_stepper
+    P.bc_x_beg, P.bc_x_end = case.bc_x
+    P.bc_y_beg, P.bc_y_end = case.bc_y
+    P.bc_z_beg, P.bc_z_end = case.bc_z
+    for i in range(case.num_fluids):
+        P.gammas[i] = case.gammas[i]
+        P.pi_infs[i] = case.pi_infs[i]
+    P.x_cb = _dp(cb[0])
+    P.y_cb = _dp(cb[1]) if cb[1] is not None else None
+    P.z_cb = _dp(cb[2]) if cb[2] is not None else None
+    P.precision = _lib.MFC_PREC_SPLIT if case.precision == "split" else _lib.MFC_PREC_FP64
+    P.device = device
+    return P, cb
+
+
 class Simulation:
     """Device-resident state of one case (q_cons_ts, rhs, grid, WENO tables)."""
 
@@ -45,24 +68,7 @@ class Simulation:
             z_cb = gz if z_cb is None else z_cb
             q_cons = gq if q_cons is None else q_cons
         self.L = _lib.load()
-        self._cb = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (x_cb, y_cb, z_cb)]
-        P = _lib.MfcParams()
-        P.m, P.n, P.p = case.m, case.n, case.p
-        P.num_fluids = case.num_fluids
-        P.weno_order = case.weno_order
-        P.weno_eps = case.weno_eps
-        P.time_stepper = case.time_stepper
-        P.bc_x_beg, P.bc_x_end = case.bc_x
-        P.bc_y_beg, P.bc_y_end = case.bc_y
-        P.bc_z_beg, P.bc_z_end = case.bc_z
-        for i in range(case.num_fluids):
-            P.gammas[i] = case.gammas[i]
-            P.pi_infs[i] = case.pi_infs[i]
-        P.x_cb = _dp(self._cb[0])
-        P.y_cb = _dp(self._cb[1]) if self._cb[1] is not None else None
-        P.z_cb = _dp(self._cb[2]) if self._cb[2] is not None else None
-        P.precision = _lib.MFC_PREC_SPLIT if case.precision == "split" else _lib.MFC_PREC_FP64
-        P.device = device
+        P, self._cb = make_params(case, x_cb, y_cb, z_cb, device)
         self._params = P
         h = ctypes.c_void_p()
         _lib.check(self.L.mfc_gpu_init(ctypes.byref(P), ctypes.byref(h)))
@@ -129,6 +135,12 @@ class Simulation:
         _lib.check(self.L.mfc_gpu_run(self._h, int(a), int(b), ctypes.byref(dt)))
         self.dt = dt.value
         return dt.value
+
+    def tune(self, reps: int = 5):
+        """Autotune the tile variant (mfc_gpu_tune); returns (index, ms per stage)."""
+        v, ms = ctypes.c_int(-1), ctypes.c_double(0)
+        _lib.check(self.L.mfc_gpu_tune(self._h, int(reps), ctypes.byref(v), ctypes.byref(ms)))
+        return v.value, ms.value
 
     def status(self, clear: bool = False) -> int:
         f = ctypes.c_uint32(0)

@@ -85,12 +85,15 @@ def test_weno5_is_high_order_on_smooth_flow(oracle_lib):
     assert order > 4.5, (e1, e2, order)
 
 
-@pytest.mark.parametrize("nd", [1, 2])
+@pytest.mark.parametrize("nd", [1, 2, 3])
 def test_periodic_box_conserves_mass_momentum_energy(oracle_lib, nd):
     if nd == 1:
         case = cases.sod_1d(m=99, steps=40, dt=2e-4).replace(bc_x=(-1, -1))
-    else:
+    elif nd == 2:
         case = cases.shock_droplet_2d(nx=40, ny=32, steps=30).replace(bc_x=(-1, -1), bc_y=(-1, -1))
+    else:
+        case = cases.shock_bubble_3d(N=28, steps=8, precision="fp64").replace(
+            m=27, n=25, p=26, bc_x=(-1, -1), bc_y=(-1, -1), bc_z=(-1, -1))
     x_cb, y_cb, q0, q1 = _run(oracle_lib, case)
     for v in range(case.E_idx + 1):  # partial densities, momenta, energy are conserved
         s0, s1 = q0[v].sum(), q1[v].sum()
