@@ -56,6 +56,7 @@ extern "C" {
 /* Precision of the reconstruction/Riemann arithmetic. */
 #define MFC_PREC_FP64 0  /* plain FP64 everywhere (parity path)                       */
 #define MFC_PREC_SPLIT 1 /* FP32 WENO/HLLC; FP64 state, RK update, pressure recovery   */
+#define MFC_PREC_GATED 2 /* MFC_PREC_SPLIT + the learned WENO gate (2-D, WENO5)         */
 
 /*
  * Case parameters: the solver-relevant subset of the reference's &user_inputs
@@ -148,6 +149,33 @@ int mfc_gpu_finalize(mfc_gpu_ctx* ctx);
  * its index and per-launch time in milliseconds. */
 int mfc_gpu_tune(mfc_gpu_ctx* ctx, int reps, int* variant_out, double* ms_out);
 
+/* ---- Learned WENO gate (no reference counterpart).  A 10-32-32-1 MLP on a
+ * cell's alpha_1 and p stencils picks nonlinear WENO5 or the optimal linear
+ * weights per cell and direction (MFC_PREC_GATED).  Parameters are FP32
+ * vectors of mfc_gate_param_count() values (W1[10][32], b1[32], W2[32][32],
+ * b2[32], W3[32], b3); inference uses them rounded to FP16. */
+int mfc_gate_param_count(void);
+/* Floats of training workspace a batch needs. */
+int mfc_gate_workspace_floats(int batch);
+/* Sets the gate parameters (host FP32) of a MFC_PREC_GATED context; its
+ * time steps fail until this has been called. */
+int mfc_gpu_set_gate(mfc_gpu_ctx* ctx, const float* host_params);
+/* Training samples of the context's current state (register 0) along
+ * direction dir (0 = x, 1 = y) for all interior cells: features
+ * x_dev[cells][10] and the label statistic dev_dev[cells] = max_k
+ * |omega_k - d_k| over alpha_1, p and both faces.  Device pointers. */
+int mfc_gpu_gate_samples(mfc_gpu_ctx* ctx, int dir, float* x_dev, float* dev_dev);
+/* Forward + backward of a batch (device pointers): grad <- gradient of the
+ * mean weighted binary cross-entropy, *loss <- summed loss.  Synchronous. */
+int mfc_gate_gradients(const float* X, const float* T, int batch, const float* w, float pos_weight, float* grad,
+                       float* work, float* loss, void* stream);
+/* One Adam step on a batch (device pointers; asynchronous on stream). */
+int mfc_gate_train_step(const float* X, const float* T, int batch, float* w, float* grad, float* m, float* v,
+                        float* work, int step, float lr, float pos_weight, float* loss, void* stream);
+/* Tensor-core inference (FP16 weights, FP32 accumulation) of n inputs;
+ * wh_scratch holds mfc_gate_param_count() halves.  Synchronous. */
+int mfc_gate_infer(const float* X, int n, const float* w, void* wh_scratch, float* logits, void* stream);
+
 /* ---- Ensemble mode (no reference counterpart; the reference runs one case
  * per process).  Up to 96 independent 2-D cases that share num_fluids,
  * weno_order, precision, time_stepper (2 or 3) and device, each with its own
@@ -168,6 +196,8 @@ int mfc_gpu_ensemble_run(mfc_gpu_ensemble* ens, int t_step_start, int t_step_sto
 void* mfc_gpu_ensemble_stream(mfc_gpu_ensemble* ens);
 int64_t mfc_gpu_ensemble_launch_count(const mfc_gpu_ensemble* ens);
 int mfc_gpu_ensemble_finalize(mfc_gpu_ensemble* ens);
+/* Gate parameters for a MFC_PREC_GATED ensemble (see mfc_gpu_set_gate). */
+int mfc_gpu_ensemble_set_gate(mfc_gpu_ensemble* ens, const float* host_params);
 
 /* No counterpart in the reference.  One time step like mfc_gpu_tvd_rk, for
  * callers that cannot allocate device memory (their device memory belongs to

@@ -21,8 +21,10 @@ EXPORTS = (
     "mfc_gpu_launch_count", "mfc_gpu_finalize", "mfc_gpu_measure_peaks", "mfc_gpu_tvd_rk_noalloc",
     "mfc_gpu_tune", "mfc_gpu_ensemble_init", "mfc_gpu_ensemble_upload", "mfc_gpu_ensemble_download",
     "mfc_gpu_ensemble_tune", "mfc_gpu_ensemble_run", "mfc_gpu_ensemble_stream", "mfc_gpu_ensemble_launch_count",
-    "mfc_gpu_ensemble_finalize",
+    "mfc_gpu_ensemble_finalize", "mfc_gpu_ensemble_set_gate", "mfc_gate_param_count", "mfc_gate_workspace_floats",
+    "mfc_gpu_set_gate", "mfc_gpu_gate_samples", "mfc_gate_gradients", "mfc_gate_train_step", "mfc_gate_infer",
 )
+MFC_PREC_GATED = 2
 
 
 class MfcParams(ctypes.Structure):
@@ -104,6 +106,16 @@ def load(build_if_missing: bool = True):
     L.mfc_gpu_ensemble_launch_count.argtypes = [vp]
     L.mfc_gpu_ensemble_launch_count.restype = i64
     L.mfc_gpu_ensemble_finalize.argtypes = [vp]
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.mfc_gpu_ensemble_set_gate.argtypes = [vp, fp]
+    L.mfc_gate_param_count.restype = ctypes.c_int
+    L.mfc_gate_workspace_floats.argtypes = [ctypes.c_int]
+    L.mfc_gpu_set_gate.argtypes = [vp, fp]
+    L.mfc_gpu_gate_samples.argtypes = [vp, ctypes.c_int, vp, vp]
+    L.mfc_gate_gradients.argtypes = [vp, vp, ctypes.c_int, vp, ctypes.c_float, vp, vp, vp, vp]
+    L.mfc_gate_train_step.argtypes = [vp, vp, ctypes.c_int, vp, vp, vp, vp, vp, ctypes.c_int, ctypes.c_float,
+                                      ctypes.c_float, vp, vp]
+    L.mfc_gate_infer.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp]
     _lib = L
     return L
 

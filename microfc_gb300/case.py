@@ -58,7 +58,7 @@ class Case:
     gammas: tuple = ()                  # fluid_pp(i)%gamma  = 1/(gamma_i - 1)
     pi_infs: tuple = ()                 # fluid_pp(i)%pi_inf = gamma_i*pi_inf_i/(gamma_i - 1)
     patches: list = field(default_factory=list)
-    precision: str = "fp64"             # "fp64" or "split"
+    precision: str = "fp64"             # "fp64", "split" or "gated" (split + learned WENO gate)
     name: str = "case"
 
     # index layout, m_global_parameters.fpp:302-310
@@ -144,7 +144,7 @@ class Case:
                 bad("Unsupported value of fluid_pp(i)%gamma")
             if pi < 0:
                 bad("Unsupported value of fluid_pp(i)%pi_inf")
-        if self.precision not in ("fp64", "split"):
+        if self.precision not in ("fp64", "split", "gated"):
             bad("Unsupported value of precision mode")
 
     # -- case-file dictionary --------------------------------------------------

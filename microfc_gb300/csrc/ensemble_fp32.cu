@@ -12,3 +12,13 @@ void register_ensemble_fp32(std::vector<EnsembleEntry>& r) {
 }
 
 }  // namespace mfc
+
+namespace mfc {
+
+void register_ensemble_gated(std::vector<EnsembleEntry>& r) {
+  r.push_back(ensemble_entry<2, 5, float, 32, 16, 256, true>());
+  r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, true>());
+  r.push_back(ensemble_entry<2, 5, float, 32, 32, 512, true>());
+}
+
+}  // namespace mfc

@@ -71,6 +71,8 @@ struct mfc_gpu_ctx {
   double* reg[3] = {nullptr, nullptr, nullptr};
   double* rhs = nullptr;
   double* work = nullptr;       // 3-D: partial RHS between the directional sweeps
+  void* gate_w = nullptr;       // MFC_PREC_GATED: FP16 gate parameters
+  bool gate_ready = false;
   double* tables = nullptr;     // inv_d and coefficient tables
   uint32_t* status = nullptr;
   cudaStream_t stream = nullptr;
@@ -178,6 +180,8 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if ((e = cudaMalloc(&c->rhs, sizeof(double) * c->reg_elems)) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
+  if (p->precision == MFC_PREC_GATED && (e = cudaMalloc(&c->gate_w, 2 * mfc::kGateParams)) != cudaSuccess)
+    return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if (c->nd == 3 && (e = cudaMalloc(&c->work, sizeof(double) * c->reg_elems)) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if ((e = cudaMalloc(&c->status, sizeof(uint32_t))) != cudaSuccess)
@@ -218,6 +222,7 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
   D.coff = mfc::kCoefPad;
   D.status = c->status;
   D.work = c->work;
+  D.gate_w = c->gate_w;
 
   if ((e = c->stage->prepare()) != cudaSuccess) return cleanup(fail(MFC_ERR_CUDA, cudaGetErrorString(e)));
   if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cleanup(fail(MFC_ERR_CUDA, cudaGetErrorString(e)));
@@ -265,8 +270,25 @@ int mfc_gpu_download_state(mfc_gpu_ctx* c, double* host_q) {
   return MFC_OK;
 }
 
+int mfc_gpu_set_gate(mfc_gpu_ctx* c, const float* host_params) {
+  if (!c || !host_params) return fail(MFC_ERR_INVALID, "NULL argument");
+  if (!c->gate_w) return fail(MFC_ERR_INVALID, "the context was not created with MFC_PREC_GATED");
+  int rc = mfc::gate_upload(host_params, c->gate_w, c->stream);
+  if (rc) return rc;
+  c->gate_ready = true;
+  return MFC_OK;
+}
+
+int mfc_gpu_gate_samples(mfc_gpu_ctx* c, int dir, float* x_dev, float* dev_dev) {
+  if (!c || !x_dev || !dev_dev) return fail(MFC_ERR_INVALID, "NULL argument");
+  if (c->nd != 2 || dir < 0 || dir > 1) return fail(MFC_ERR_INVALID, "gate samples are taken from 2-D cases, dir 0 or 1");
+  if (c->prm.weno_order != 5) return fail(MFC_ERR_INVALID, "gate samples need WENO5 coefficients");
+  return mfc::gate_samples(c->dev, c->prm.num_fluids, c->reg[0], dir, x_dev, dev_dev, c->stream);
+}
+
 int mfc_gpu_compute_rhs(mfc_gpu_ctx* c, double* rhs_out, double* prim_out) {
   if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  if (c->gate_w && !c->gate_ready) return fail(MFC_ERR_INVALID, "gate parameters not set (mfc_gpu_set_gate)");
   int rc = launch_stage(c, c->reg[0], c->reg[0], c->rhs, 0.0, mfc::kRhsOnly);
   if (rc) return rc;
   const int64_t cells = (int64_t)c->n[0] * c->n[1] * c->n[2];
@@ -295,6 +317,7 @@ int mfc_gpu_compute_rhs(mfc_gpu_ctx* c, double* rhs_out, double* prim_out) {
 
 int mfc_gpu_tvd_rk(mfc_gpu_ctx* c, double dt, int last_step) {
   if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  if (c->gate_w && !c->gate_ready) return fail(MFC_ERR_INVALID, "gate parameters not set (mfc_gpu_set_gate)");
   if (last_step) return MFC_OK;  // s_compute_rhs returns before any update at t_step_stop
   int rc;
   double** R = c->reg;
@@ -400,6 +423,7 @@ int mfc_gpu_finalize(mfc_gpu_ctx* c) {
   cudaFree(c->tables);
   cudaFree(c->status);
   cudaFree(c->work);
+  cudaFree(c->gate_w);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return MFC_OK;

@@ -31,6 +31,7 @@ struct DevParams {
   int coff, cstride[3];
   uint32_t* status;
   void* work;  // 3-D: partial RHS between the directional sweeps ([S][z][y][x], RT)
+  const void* gate_w;  // learned WENO gate: FP16 MLP parameters (mfc_gate.cuh layout)
 };
 
 // Equation index layout, m_global_parameters.fpp:302-310 (0-based).

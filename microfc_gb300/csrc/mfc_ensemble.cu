@@ -24,6 +24,7 @@ void build_ens_registry() {
   std::call_once(g_once, [] {
     mfc::register_ensemble_fp64(g_ens);
     mfc::register_ensemble_fp32(g_ens);
+    mfc::register_ensemble_gated(g_ens);
   });
 }
 
@@ -51,6 +52,8 @@ struct mfc_gpu_ensemble {
   double* state = nullptr;
   double* tables = nullptr;
   uint32_t* status = nullptr;
+  void* gate_w = nullptr;  // MFC_PREC_GATED: FP16 gate parameters
+  bool gate_ready = false;
   cudaStream_t stream = nullptr;
   const mfc::EnsembleEntry* entry = nullptr;
   int grid = 0, total_tiles = 0;
@@ -195,7 +198,8 @@ int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_ca
   if ((err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (err = cudaMalloc(&e->state, sizeof(double) * state_elems)) != cudaSuccess ||
       (err = cudaMalloc(&e->tables, sizeof(double) * table_elems)) != cudaSuccess ||
-      (err = cudaMalloc(&e->status, sizeof(uint32_t))) != cudaSuccess)
+      (err = cudaMalloc(&e->status, sizeof(uint32_t))) != cudaSuccess ||
+      (c0.precision == MFC_PREC_GATED && (err = cudaMalloc(&e->gate_w, 2 * mfc::kGateParams)) != cudaSuccess))
     return cleanup(mfc::report_error(MFC_ERR_NOMEM, cudaGetErrorString(err)));
   cudaMemsetAsync(e->state, 0, sizeof(double) * state_elems, e->stream);
   cudaMemsetAsync(e->status, 0, sizeof(uint32_t), e->stream);
@@ -212,6 +216,7 @@ int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_ca
       C.P.coef[d] = tb + gts[i].off_coef[d];
     }
     C.P.status = e->status;
+    C.P.gate_w = e->gate_w;
     C.dt = e->dt[i];
     C.dt_last = e->dt[i];
   }
@@ -306,6 +311,8 @@ int mfc_gpu_ensemble_run(mfc_gpu_ensemble* e, int t_step_start, int t_step_stop,
   if (!e) return mfc::report_error(MFC_ERR_INVALID, "NULL ensemble");
   if (t_step_start < 0 || t_step_stop <= t_step_start)
     return mfc::report_error(MFC_ERR_INVALID, "Unsupported combination of values of t_step_start and t_step_stop");
+  if (e->gate_w && !e->gate_ready)
+    return mfc::report_error(MFC_ERR_INVALID, "gate parameters not set (mfc_gpu_ensemble_set_gate)");
   for (int i = 0; i < e->num; ++i) e->cases[i].dt_last = trimmed_last_dt(e->dt[i], t_step_start, t_step_stop);
   const int steps = t_step_stop - t_step_start;
   int rc = MFC_OK;
@@ -345,6 +352,15 @@ int mfc_gpu_ensemble_run(mfc_gpu_ensemble* e, int t_step_start, int t_step_stop,
   return MFC_OK;
 }
 
+int mfc_gpu_ensemble_set_gate(mfc_gpu_ensemble* e, const float* host_params) {
+  if (!e || !host_params) return mfc::report_error(MFC_ERR_INVALID, "NULL argument");
+  if (!e->gate_w) return mfc::report_error(MFC_ERR_INVALID, "the ensemble was not created with MFC_PREC_GATED");
+  int rc = mfc::gate_upload(host_params, e->gate_w, e->stream);
+  if (rc) return rc;
+  e->gate_ready = true;
+  return MFC_OK;
+}
+
 void* mfc_gpu_ensemble_stream(mfc_gpu_ensemble* e) { return e ? (void*)e->stream : nullptr; }
 
 int64_t mfc_gpu_ensemble_launch_count(const mfc_gpu_ensemble* e) { return e ? e->launches : 0; }
@@ -355,6 +371,7 @@ int mfc_gpu_ensemble_finalize(mfc_gpu_ensemble* e) {
   cudaFree(e->state);
   cudaFree(e->tables);
   cudaFree(e->status);
+  cudaFree(e->gate_w);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e->ep;
   delete e;

@@ -30,7 +30,7 @@ struct EnsParams {
 };
 static_assert(sizeof(EnsParams) <= 32764, "ensemble parameters must fit the kernel parameter space");
 
-template <int NF, int WO, class RT, int TX, int TY, int NT>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE>
 __global__ void __launch_bounds__(NT) ensemble_stage_kernel(const __grid_constant__ EnsParams E) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   for (int t = blockIdx.x; t < E.total_tiles; t += gridDim.x) {
@@ -55,8 +55,8 @@ __global__ void __launch_bounds__(NT) ensemble_stage_kernel(const __grid_constan
     } else {
       in = C.reg[2], out = C.reg[0], kind = kRk3Final;
     }
-    stage_tile<2, NF, WO, RT, TX, TY, NT>(C.P, in, C.reg[0], out, E.last_step ? C.dt_last : C.dt, kind, x0, y0,
-                                          smem_raw);
+    stage_tile<2, NF, WO, RT, TX, TY, NT, GATE>(C.P, in, C.reg[0], out, E.last_step ? C.dt_last : C.dt, kind, x0,
+                                                y0, smem_raw);
     __syncthreads();  // the next tile reuses the shared memory
   }
 }
@@ -68,22 +68,24 @@ struct EnsembleEntry {
   cudaError_t (*launch)(const EnsParams& E, int grid, cudaStream_t st);
 };
 
-template <int NF, int WO, class RT, int TX, int TY, int NT>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE>
 cudaError_t ensemble_launch(const EnsParams& E, int grid, cudaStream_t st) {
-  using Sh = StageShape<2, NF, WO, RT, TX, TY>;
-  ensemble_stage_kernel<NF, WO, RT, TX, TY, NT><<<grid, NT, Sh::kSmemBytes, st>>>(E);
+  ensemble_stage_kernel<NF, WO, RT, TX, TY, NT, GATE>
+      <<<grid, NT, stage_smem_bytes<2, NF, WO, RT, TX, TY, NT, GATE>(), st>>>(E);
   return cudaGetLastError();
 }
 
-template <int NF, int WO, class RT, int TX, int TY, int NT>
+// prec: 0 FP64, 1 split, 2 split with the learned gate
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
 EnsembleEntry ensemble_entry() {
-  using Sh = StageShape<2, NF, WO, RT, TX, TY>;
-  return EnsembleEntry{NF, WO, sizeof(RT) == 8 ? 0 : 1, TX, TY, NT, Sh::kSmemBytes,
-                       reinterpret_cast<const void*>(&ensemble_stage_kernel<NF, WO, RT, TX, TY, NT>),
-                       &ensemble_launch<NF, WO, RT, TX, TY, NT>};
+  return EnsembleEntry{NF, WO, sizeof(RT) == 8 ? 0 : (GATE ? 2 : 1), TX, TY, NT,
+                       stage_smem_bytes<2, NF, WO, RT, TX, TY, NT, GATE>(),
+                       reinterpret_cast<const void*>(&ensemble_stage_kernel<NF, WO, RT, TX, TY, NT, GATE>),
+                       &ensemble_launch<NF, WO, RT, TX, TY, NT, GATE>};
 }
 
 void register_ensemble_fp64(std::vector<EnsembleEntry>& r);
 void register_ensemble_fp32(std::vector<EnsembleEntry>& r);
+void register_ensemble_gated(std::vector<EnsembleEntry>& r);
 
 }  // namespace mfc

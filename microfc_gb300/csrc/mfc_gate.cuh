@@ -1,0 +1,198 @@
+// Learned WENO smoothness gate (no reference counterpart).
+//
+// A small MLP looks at one cell's 5-point stencils of alpha_1 and p in one
+// direction and decides whether the cell needs the full nonlinear WENO5
+// weights (m_weno.fpp:495-531) or can use the optimal linear weights d_k.
+//
+//   inputs  10: each stencil shifted by its minimum and divided by its range
+//               (max - min, floored at 1e-6 of the stencil's magnitude)
+//   layers  10 -> 32 (ReLU) -> 32 (ReLU) -> 1 (logit; sigmoid > 1/2 <=> logit > 0)
+//   label   max_k |omega_k - d_k| > 1e-3 for alpha_1 or p, left or right face
+//
+// Inference runs on the tensor cores with FP16 weights and FP32
+// accumulation (mma.sync m16n8k16, 16 cells per warp, the three layers
+// chained in registers: the accumulator fragment of one layer is the A
+// fragment of the next).  Training uses FP32 master weights.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mfc_device.cuh"
+
+namespace mfc {
+
+constexpr int kGateIn = 10, kGateH = 32;
+constexpr int kGW1 = 0, kGB1 = kGW1 + kGateIn * kGateH, kGW2 = kGB1 + kGateH, kGB2 = kGW2 + kGateH * kGateH,
+              kGW3 = kGB2 + kGateH, kGB3 = kGW3 + kGateH, kGateParams = kGB3 + 1;  // 1441
+constexpr float kGateLabelTol = 1e-3f;
+
+// One stencil of 5 values -> 5 normalised inputs.
+__device__ __forceinline__ void gate_norm5(const float (&s)[5], float* out) {
+  const float lo = fminf(fminf(fminf(s[0], s[1]), fminf(s[2], s[3])), s[4]);
+  const float hi = fmaxf(fmaxf(fmaxf(s[0], s[1]), fmaxf(s[2], s[3])), s[4]);
+  const float floor_ = fmaxf(fmaxf(fabsf(lo), fabsf(hi)) * 1e-6f, 1e-30f);
+  const float r = rcp_approx(fmaxf(hi - lo, floor_));
+#pragma unroll
+  for (int k = 0; k < 5; ++k) out[k] = (s[k] - lo) * r;
+}
+
+__device__ __forceinline__ void gate_features(const float (&a)[5], const float (&p)[5], float (&x)[kGateIn]) {
+  gate_norm5(a, x);
+  gate_norm5(p, x + 5);
+}
+
+// max_k |omega_k - d_k| over both faces of the FP32 WENO5 weights of one
+// stencil (the label of one variable).
+__device__ __forceinline__ float weno5_weight_deviation(const float* __restrict__ c, const float (&v)[5], float eps) {
+  const float d1 = v[4] - v[3], d0 = v[3] - v[2], dm1 = v[2] - v[1], dm2 = v[1] - v[0];
+  const float b0 = fmaf(d1, fmaf(c[kBeta + 0], d1, c[kBeta + 1] * d0), fmaf(c[kBeta + 2] * d0, d0, eps));
+  const float b1 = fmaf(d0, fmaf(c[kBeta + 3], d0, c[kBeta + 4] * dm1), fmaf(c[kBeta + 5] * dm1, dm1, eps));
+  const float b2 = fmaf(dm1, fmaf(c[kBeta + 6], dm1, c[kBeta + 7] * dm2), fmaf(c[kBeta + 8] * dm2, dm2, eps));
+  const float r0 = 1.0f / (b0 * b0), r1 = 1.0f / (b1 * b1), r2 = 1.0f / (b2 * b2);
+  float dev = 0.f;
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const float* d = c + (side ? kDR : kDL);
+    const float a0 = d[0] * r0, a1 = d[1] * r1, a2 = d[2] * r2;
+    const float is = 1.0f / (a0 + a1 + a2);
+    dev = fmaxf(dev, fmaxf(fabsf(a0 * is - d[0]), fmaxf(fabsf(a1 * is - d[1]), fabsf(a2 * is - d[2]))));
+  }
+  return dev;
+}
+
+// WENO5 with the optimal linear weights d_k (the gate's "smooth" branch).
+__device__ __forceinline__ void weno5_cell_linear(const float* __restrict__ c, const float (&v)[5], float& vL,
+                                                  float& vR) {
+  const float d1 = v[4] - v[3], d0 = v[3] - v[2], dm1 = v[2] - v[1], dm2 = v[1] - v[0];
+  {
+    const float p0 = fmaf(c[kPL + 1], d0, fmaf(c[kPL + 0], d1, v[2]));
+    const float p1 = fmaf(c[kPL + 3], dm1, fmaf(c[kPL + 2], d0, v[2]));
+    const float p2 = fmaf(c[kPL + 5], dm2, fmaf(c[kPL + 4], dm1, v[2]));
+    vL = fmaf(c[kDL + 2], p2, fmaf(c[kDL + 1], p1, c[kDL + 0] * p0));
+  }
+  {
+    const float p0 = fmaf(c[kPR + 1], d0, fmaf(c[kPR + 0], d1, v[2]));
+    const float p1 = fmaf(c[kPR + 3], dm1, fmaf(c[kPR + 2], d0, v[2]));
+    const float p2 = fmaf(c[kPR + 5], dm2, fmaf(c[kPR + 4], dm1, v[2]));
+    vR = fmaf(c[kDR + 2], p2, fmaf(c[kDR + 1], p1, c[kDR + 0] * p0));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core inference.  Weight fragments of one lane (m16n8k16 layouts:
+// lane = 4*g + t; A rows g, g+8 / cols 2t, 2t+1, 2t+8, 2t+9; B rows (k) 2t,
+// 2t+1, 2t+8, 2t+9 / col (n) g; C rows g, g+8 / cols 2t, 2t+1).
+struct GateFrags {
+  uint32_t w1[4][2];     // layer 1: k 0..15 (inputs, 10 used), n-tiles 0..3
+  uint32_t w2[2][4][2];  // layer 2: k-steps 0..1, n-tiles 0..3
+  uint32_t w3[2][2];     // layer 3: k-steps 0..1, n-tile 0 (only column 0 used)
+  float b1[4][2], b2[4][2], b3;
+};
+
+__device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
+  const __half2 h = __floats2half2_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+__device__ __forceinline__ uint32_t pack_h2_raw(__half lo, __half hi) {
+  __half2 h;
+  h.x = lo;
+  h.y = hi;
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// w: FP16 weights in the parameter layout (kGW1..kGB3), biases included.
+__device__ __forceinline__ void gate_load_frags(const __half* __restrict__ w, GateFrags& F) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  auto W1 = [&](int k, int n) { return k < kGateIn ? w[kGW1 + k * kGateH + n] : __float2half(0.f); };
+  auto W2 = [&](int k, int n) { return w[kGW2 + k * kGateH + n]; };
+  auto W3 = [&](int k, int n) { return n == 0 ? w[kGW3 + k] : __float2half(0.f); };
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int n = 8 * j + g;
+    F.w1[j][0] = pack_h2_raw(W1(2 * t, n), W1(2 * t + 1, n));
+    F.w1[j][1] = pack_h2_raw(W1(2 * t + 8, n), W1(2 * t + 9, n));
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      F.w2[s][j][0] = pack_h2_raw(W2(16 * s + 2 * t, n), W2(16 * s + 2 * t + 1, n));
+      F.w2[s][j][1] = pack_h2_raw(W2(16 * s + 2 * t + 8, n), W2(16 * s + 2 * t + 9, n));
+    }
+    F.b1[j][0] = __half2float(w[kGB1 + 8 * j + 2 * t]);
+    F.b1[j][1] = __half2float(w[kGB1 + 8 * j + 2 * t + 1]);
+    F.b2[j][0] = __half2float(w[kGB2 + 8 * j + 2 * t]);
+    F.b2[j][1] = __half2float(w[kGB2 + 8 * j + 2 * t + 1]);
+  }
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    F.w3[s][0] = pack_h2_raw(W3(16 * s + 2 * t, g), W3(16 * s + 2 * t + 1, g));
+    F.w3[s][1] = pack_h2_raw(W3(16 * s + 2 * t + 8, g), W3(16 * s + 2 * t + 9, g));
+  }
+  F.b3 = __half2float(w[kGB3]);
+}
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Logits of 16 cells.  xin: the cells' inputs, FP16, row stride 16 halves
+// (inputs 10..15 zero); the warp's lanes must all call this.  Returns, in
+// lanes with t == 0, the logits of cells g (lo) and g + 8 (hi).
+__device__ __forceinline__ void gate_mlp16(const __half* __restrict__ xin, const GateFrags& F, float& lo,
+                                           float& hi) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  uint32_t a[4];
+  const __half* r0 = xin + g * 16;
+  const __half* r1 = xin + (g + 8) * 16;
+  a[0] = pack_h2_raw(r0[2 * t], r0[2 * t + 1]);
+  a[1] = pack_h2_raw(r1[2 * t], r1[2 * t + 1]);
+  a[2] = pack_h2_raw(r0[2 * t + 8], r0[2 * t + 9]);
+  a[3] = pack_h2_raw(r1[2 * t + 8], r1[2 * t + 9]);
+  float h[4][4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    h[j][0] = F.b1[j][0];
+    h[j][1] = F.b1[j][1];
+    h[j][2] = F.b1[j][0];
+    h[j][3] = F.b1[j][1];
+    mma16816(h[j], a, F.w1[j][0], F.w1[j][1]);
+  }
+  float h2[4][4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    h2[j][0] = F.b2[j][0];
+    h2[j][1] = F.b2[j][1];
+    h2[j][2] = F.b2[j][0];
+    h2[j][3] = F.b2[j][1];
+  }
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    uint32_t as[4];
+    as[0] = pack_h2(fmaxf(h[2 * s][0], 0.f), fmaxf(h[2 * s][1], 0.f));
+    as[1] = pack_h2(fmaxf(h[2 * s][2], 0.f), fmaxf(h[2 * s][3], 0.f));
+    as[2] = pack_h2(fmaxf(h[2 * s + 1][0], 0.f), fmaxf(h[2 * s + 1][1], 0.f));
+    as[3] = pack_h2(fmaxf(h[2 * s + 1][2], 0.f), fmaxf(h[2 * s + 1][3], 0.f));
+#pragma unroll
+    for (int j = 0; j < 4; ++j) mma16816(h2[j], as, F.w2[s][j][0], F.w2[s][j][1]);
+  }
+  float o[4] = {t == 0 ? F.b3 : 0.f, 0.f, t == 0 ? F.b3 : 0.f, 0.f};
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    uint32_t as[4];
+    as[0] = pack_h2(fmaxf(h2[2 * s][0], 0.f), fmaxf(h2[2 * s][1], 0.f));
+    as[1] = pack_h2(fmaxf(h2[2 * s][2], 0.f), fmaxf(h2[2 * s][3], 0.f));
+    as[2] = pack_h2(fmaxf(h2[2 * s + 1][0], 0.f), fmaxf(h2[2 * s + 1][1], 0.f));
+    as[3] = pack_h2(fmaxf(h2[2 * s + 1][2], 0.f), fmaxf(h2[2 * s + 1][3], 0.f));
+    mma16816(o, as, F.w3[s][0], F.w3[s][1]);
+  }
+  lo = o[0];
+  hi = o[2];
+}
+
+}  // namespace mfc

@@ -190,7 +190,10 @@ inline std::string validate_params(const mfc_params* p) {
   if (p->n > 0 && !p->y_cb) return "y_cb is NULL";
   if (p->p > 0 && !p->z_cb) return "z_cb is NULL";
   if (p->p > 0 && p->p + 1 < stcls) return "Unsupported combination of values of p and weno_order";
-  if (p->precision != MFC_PREC_FP64 && p->precision != MFC_PREC_SPLIT) return "Unsupported precision";
+  if (p->precision != MFC_PREC_FP64 && p->precision != MFC_PREC_SPLIT && p->precision != MFC_PREC_GATED)
+    return "Unsupported precision";
+  if (p->precision == MFC_PREC_GATED && (p->n == 0 || p->p > 0 || p->weno_order != 5))
+    return "The learned gate runs on 2-D WENO5 cases";
   return "";
 }
 

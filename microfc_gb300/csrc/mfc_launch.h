@@ -26,27 +26,28 @@ struct StageEntry {
                         int kind, cudaStream_t st);
 };
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
 cudaError_t stage_prepare() {
-  using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
-  return cudaFuncSetAttribute(stage_kernel<ND, NF, WO, RT, TX, TY, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)Sh::kSmemBytes);
+  return cudaFuncSetAttribute(stage_kernel<ND, NF, WO, RT, TX, TY, NT, GATE>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE>());
 }
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
 cudaError_t stage_launch(const DevParams& P, const double* qin, const double* qbase, double* qout, double dt,
                          int kind, cudaStream_t st) {
-  using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
   const dim3 grid((unsigned)((P.n[0] + TX - 1) / TX), ND > 1 ? (unsigned)((P.n[1] + TY - 1) / TY) : 1u, 1u);
-  stage_kernel<ND, NF, WO, RT, TX, TY, NT><<<grid, NT, Sh::kSmemBytes, st>>>(P, qin, qbase, qout, dt, kind);
+  stage_kernel<ND, NF, WO, RT, TX, TY, NT, GATE>
+      <<<grid, NT, stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE>(), st>>>(P, qin, qbase, qout, dt, kind);
   return cudaGetLastError();
 }
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT>
+// prec of a registry entry: 0 FP64, 1 split, 2 split with the learned gate
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
 StageEntry stage_entry() {
-  using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
-  return StageEntry{ND, NF, WO, sizeof(RT) == 8 ? 0 : 1, TX, TY, NT, Sh::kSmemBytes, 1,
-                    &stage_prepare<ND, NF, WO, RT, TX, TY, NT>, &stage_launch<ND, NF, WO, RT, TX, TY, NT>};
+  return StageEntry{ND, NF, WO, sizeof(RT) == 8 ? 0 : (GATE ? 2 : 1), TX, TY, NT,
+                    stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE>(), 1,
+                    &stage_prepare<ND, NF, WO, RT, TX, TY, NT, GATE>, &stage_launch<ND, NF, WO, RT, TX, TY, NT, GATE>};
 }
 
 // 3-D: three directional sweeps per stage (mfc_sweep.cuh).  The x sweep uses
@@ -94,6 +95,12 @@ const StageEntry* find_stage(int nd, int nf, int wo, int prec);
 
 // Records msg as the calling thread's mfc_gpu_last_error() and returns code.
 int report_error(int code, const std::string& msg);
+
+// Gate training samples of a 2-D state (mfc_gate.cu).
+int gate_samples(const DevParams& P, int nf, const double* q, int dir, float* xout, float* dev_out, cudaStream_t st);
+
+// FP32 gate parameters (host) -> FP16 device copy (mfc_gate.cu).
+int gate_upload(const float* host_params, void* dev_half, cudaStream_t st);
 
 // Defined in the instantiation translation units.
 void register_stage_1d_fp64(std::vector<StageEntry>& r);

@@ -18,6 +18,7 @@
 #pragma once
 
 #include "mfc_device.cuh"
+#include "mfc_gate.cuh"
 
 namespace mfc {
 
@@ -58,11 +59,21 @@ struct StageShape {
 // single-case kernel (one tile per block) and by the ensemble kernel (many
 // tiles of many cases per persistent block).  smem_raw must hold
 // StageShape::kSmemBytes.
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT>
+// Extra shared memory of the learned gate: one 16x16 FP16 input block per
+// warp, then one flag per (cell, direction) reconstructed by the tile.
+template <int ND, int TX, int TY, int NT>
+struct GateShape {
+  static constexpr int NGX = (TX + 2) * ((ND > 1) ? TY : 1);
+  static constexpr int NGY = (ND > 1) ? TX * (TY + 2) : 0;
+  static constexpr size_t kBytes = size_t(NT / 32) * 512 + ((NGX + NGY + 15) / 16) * 16;
+};
+
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
 __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __restrict__ qin,
                                            const double* __restrict__ qbase, double* __restrict__ qout,
                                            const double dt, const int kind, const int x0, const int y0,
                                            unsigned char* smem_raw) {
+  static_assert(!GATE || (sizeof(RT) == 4 && WO == 5), "the learned gate runs on the split-precision WENO5 path");
   using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
   using Q = Eqs<ND, NF>;
   constexpr int S = Sh::S, H = Sh::H, LX = Sh::LX, LY = Sh::LY, TYE = Sh::TYE;
@@ -130,6 +141,56 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   }
   __syncthreads();
 
+  // ---- learned gate: one flag per (cell, direction), tensor-core MLP -------
+  const uint8_t* gflag = nullptr;
+  if constexpr (GATE) {
+    using G = GateShape<ND, TX, TY, NT>;
+    unsigned char* gbase = smem_raw + Sh::kSmemBytes;
+    __half* gin = reinterpret_cast<__half*>(gbase);
+    uint8_t* flags = gbase + (NT / 32) * 512;
+    const int warp = tid >> 5, lane = tid & 31;
+    GateFrags F;
+    gate_load_frags(reinterpret_cast<const __half*>(P.gate_w), F);
+    __half* my = gin + warp * 256;
+    constexpr int NG = G::NGX + G::NGY, NCH = (NG + 15) / 16;
+    for (int ch = warp; ch < NCH; ch += NT / 32) {
+      const int cell = ch * 16 + (lane & 15);
+      const int var = lane < 16 ? Q::ADV : Q::E;  // alpha_1 | pressure
+      float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      if (cell < G::NGX) {
+        const int cx = cell % (TX + 2), ty = cell / (TX + 2);
+        const RT* row = sq + (var * LY + ((ND > 1) ? ty + H : 0)) * LX + cx + H - 1;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) s[k] = row[k - 2];
+      } else if (cell < NG) {
+        const int c2 = cell - G::NGX, tx = c2 % TX, cy = c2 / TX;
+        const RT* col = sq + var * LY * LX + (cy + H - 1) * LX + tx + H;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) s[k] = col[(k - 2) * LX];
+      }
+      float xf[5];
+      gate_norm5(s, xf);
+      __half* r = my + (lane & 15) * 16;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) r[(lane < 16 ? 0 : 5) + k] = __float2half(xf[k]);
+      if (lane >= 16) {
+#pragma unroll
+        for (int k = 10; k < 16; ++k) r[k] = __float2half(0.f);
+      }
+      __syncwarp();
+      float lo, hi;
+      gate_mlp16(my, F, lo, hi);
+      if ((lane & 3) == 0) {
+        const int c_lo = ch * 16 + (lane >> 2), c_hi = c_lo + 8;
+        if (c_lo < NG) flags[c_lo] = lo > 0.f;
+        if (c_hi < NG) flags[c_hi] = hi > 0.f;
+      }
+      __syncwarp();
+    }
+    gflag = flags;
+    __syncthreads();
+  }
+
   // ---- phase 2: x WENO over cells x0-1 .. x0+TX of the interior rows -------
   {
     constexpr int NCX = TX + 2;
@@ -158,8 +219,14 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
       }
       RT vl, vr;
-      if constexpr (kSplit && WO == 5) weno5_cell_fast(c, st, eps, vl, vr);
-      else weno_cell<WO, RT>(c, st, eps, vl, vr);
+      if constexpr (GATE) {
+        if (gflag[ty * NCX + cx]) weno5_cell_fast(c, st, eps, vl, vr);
+        else weno5_cell_linear(c, st, vl, vr);
+      } else if constexpr (kSplit && WO == 5) {
+        weno5_cell_fast(c, st, eps, vl, vr);
+      } else {
+        weno_cell<WO, RT>(c, st, eps, vl, vr);
+      }
       wl[(v * TYE + ty) * NCX + cx] = vl;
       wr[(v * TYE + ty) * NCX + cx] = vr;
     }
@@ -236,8 +303,14 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
       }
       RT vl, vr;
-      if constexpr (kSplit && WO == 5) weno5_cell_fast(c, st, eps, vl, vr);
-      else weno_cell<WO, RT>(c, st, eps, vl, vr);
+      if constexpr (GATE) {
+        if (gflag[GateShape<ND, TX, TY, NT>::NGX + cy * TX + tx]) weno5_cell_fast(c, st, eps, vl, vr);
+        else weno5_cell_linear(c, st, vl, vr);
+      } else if constexpr (kSplit && WO == 5) {
+        weno5_cell_fast(c, st, eps, vl, vr);
+      } else {
+        weno_cell<WO, RT>(c, st, eps, vl, vr);
+      }
       wl[(v * NCY + cy) * TX + tx] = vl;
       wr[(v * NCY + cy) * TX + tx] = vr;
     }
@@ -314,13 +387,19 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   if (bad && P.status) atomicOr(P.status, 1u);
 }
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
 __global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const double* __restrict__ qin,
                                                    const double* __restrict__ qbase, double* __restrict__ qout,
                                                    const double dt, const int kind) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_tile<ND, NF, WO, RT, TX, TY, NT>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
-                                         (ND > 1) ? blockIdx.y * TY : 0, smem_raw);
+  stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
+                                               (ND > 1) ? blockIdx.y * TY : 0, smem_raw);
+}
+
+// Shared memory of one stage-kernel block (with the gate's share when on).
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE>
+constexpr size_t stage_smem_bytes() {
+  return StageShape<ND, NF, WO, RT, TX, TY>::kSmemBytes + (GATE ? GateShape<ND, TX, TY, NT>::kBytes : 0);
 }
 
 }  // namespace mfc

@@ -12,6 +12,11 @@ void register_stage_2d_fp32(std::vector<StageEntry>& r) {
   r.push_back(stage_entry<2, 2, 1, float, 32, 16, 256>());
   r.push_back(stage_entry<2, 1, 3, float, 32, 16, 256>());
   r.push_back(stage_entry<2, 1, 1, float, 32, 16, 256>());
+  // split precision with the learned WENO gate
+  r.push_back(stage_entry<2, 2, 5, float, 32, 16, 256, true>());
+  r.push_back(stage_entry<2, 2, 5, float, 16, 16, 256, true>());
+  r.push_back(stage_entry<2, 2, 5, float, 32, 32, 512, true>());
+  r.push_back(stage_entry<2, 1, 5, float, 32, 16, 256, true>());
 }
 
 }  // namespace mfc

@@ -48,7 +48,8 @@ def make_params(case: Case, x_cb, y_cb=None, z_cb=None, device: int = 0):
     P.x_cb = _dp(cb[0])
     P.y_cb = _dp(cb[1]) if cb[1] is not None else None
     P.z_cb = _dp(cb[2]) if cb[2] is not None else None
-    P.precision = _lib.MFC_PREC_SPLIT if case.precision == "split" else _lib.MFC_PREC_FP64
+    P.precision = {"fp64": _lib.MFC_PREC_FP64, "split": _lib.MFC_PREC_SPLIT,
+                   "gated": _lib.MFC_PREC_GATED}[case.precision]
     P.device = device
     return P, cb
 
@@ -141,6 +142,16 @@ class Simulation:
         v, ms = ctypes.c_int(-1), ctypes.c_double(0)
         _lib.check(self.L.mfc_gpu_tune(self._h, int(reps), ctypes.byref(v), ctypes.byref(ms)))
         return v.value, ms.value
+
+    def set_gate(self, params) -> None:
+        """Parameters (FP32, mfc_gate_param_count values) of the learned gate."""
+        w = np.ascontiguousarray(params, dtype=np.float32)
+        _lib.check(self.L.mfc_gpu_set_gate(self._h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+    def gate_samples(self, direction: int, x_dev_ptr: int, dev_dev_ptr: int) -> None:
+        """Gate training samples of the current state into device buffers."""
+        _lib.check(self.L.mfc_gpu_gate_samples(self._h, int(direction), ctypes.c_void_p(x_dev_ptr),
+                                               ctypes.c_void_p(dev_dev_ptr)))
 
     def status(self, clear: bool = False) -> int:
         f = ctypes.c_uint32(0)

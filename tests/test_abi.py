@@ -15,7 +15,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     text = open(os.path.join(ROOT, "include", "mfc_gpu.h")).read()
-    return sorted(set(re.findall(r"\b(mfc_gpu_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(mfc_(?:gpu|gate)_\w+)\s*\(", text)))
 
 
 def test_library_builds_and_exports_every_declared_symbol():
