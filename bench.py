@@ -170,6 +170,78 @@ def run_reference(args):
     return 0
 
 
+def _time_steps(sim, stream, flush, steps, warmup, dt):
+    """CUDA-event time (s) of `steps` time steps of a Simulation, L2 flushed between steps."""
+    import torch
+    for _ in range(warmup):
+        sim.tvd_rk(0, dt)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for i in range(steps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            sim.tvd_rk(0, dt)
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev) / 1e3
+
+
+def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
+    """Split precision, split + learned gate (the gated FP32 form) on the same
+    workload, and the 64-case ensemble of config 5 against 64 sequential
+    plain FP64 runs.  Accuracy of these modes against FP64 is asserted by
+    tests/test_gpu_parity.py, tests/test_gate.py and tests/test_ensemble.py."""
+    import torch
+    from microfc_gb300 import Simulation, gate
+    from microfc_gb300.ensemble import Ensemble, random_droplet_cases
+    out = {}
+    params = gate.load() if os.path.exists(gate.WEIGHTS_FILE) else None
+    modes = [("split", None)] + ([("gated", params)] if params is not None else [])
+    for prec, p in modes:
+        with Simulation(case.replace(precision=prec), x_cb, y_cb, q_cons=q0) as s:
+            if p is not None:
+                s.set_gate(p)
+            st = torch.cuda.ExternalStream(s.stream)
+            t = _time_steps(s, st, flush, args.steps, args.warmup, case.dt)
+            rate = case.cells * args.steps / t
+            out[prec] = {"value": rate, "unit": "cell-updates/s", "ms_per_step": 1e3 * t / args.steps,
+                         "vs_plain_fp64": rate / fp64_rate}
+    if params is None:
+        out["gated"] = {"unavailable": "no trained gate parameters (python -m microfc_gb300.gate)"}
+    # config 5: 64 cases, nx in {128,256,384,512}, ny = nx/2, seed 0
+    prec = "gated" if params is not None else "split"
+    cl = random_droplet_cases(count=64, seed=0, steps=500, precision=prec)
+    with Ensemble(cl) as ens:
+        if params is not None:
+            ens.set_gate(params)
+        variant, _ = ens.tune(reps=3)
+        ens.run(0, 3, use_graph=True)  # warm-up (advances the state; timing only)
+        torch.cuda.synchronize()
+        nsteps = 20
+        t0 = time.perf_counter()
+        ens.run(3, 3 + nsteps, use_graph=True)
+        torch.cuda.synchronize()
+        t_ens = time.perf_counter() - t0
+        ens_rate = ens.cells * nsteps / t_ens
+    # 64 sequential plain FP64 runs: measured per size class
+    seq_time = 0.0
+    per_class = {}
+    for c in cl:
+        key = c.m + 1
+        if key not in per_class:
+            with Simulation(c.replace(precision="fp64")) as s:
+                st = torch.cuda.ExternalStream(s.stream)
+                per_class[key] = _time_steps(s, st, flush, 2, 1, c.dt) / 2
+        seq_time += per_class[key]
+    seq_rate = sum(c.cells for c in cl) / seq_time
+    out["ensemble"] = {"cases": len(cl), "cells": int(sum(c.cells for c in cl)), "precision": prec,
+                       "value": ens_rate, "unit": "cell-updates/s", "steps": nsteps, "graph": True,
+                       "tile_variant": variant, "timing": "host wall clock around graph replays, synchronized",
+                       "sequential_plain_fp64": seq_rate, "vs_sequential_plain_fp64": ens_rate / seq_rate}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -180,6 +252,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--nx", type=int, default=NX, help="cells in x (profiling runs; the benchmark is 1024)")
     ap.add_argument("--ny", type=int, default=NY, help="cells in y (profiling runs; the benchmark is 512)")
+    ap.add_argument("--no-modes", action="store_true", help="skip the split/gated/ensemble figures")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -284,9 +357,11 @@ def main():
             "unit": "TFLOP/s", "frac": ach / peak, "flops_per_cell_update": flops,
             "peak_kind": "measured in-process (FMA chains, mfc_gpu_measure_peaks)",
             "peaks_measured": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak}}
+    sim.close()
+    if not args.no_modes and args.precision == "fp64":
+        line["modes"] = other_modes(args, case, x_cb, y_cb, q0, flush, value / ws)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
-    sim.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

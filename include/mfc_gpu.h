@@ -134,6 +134,22 @@ int mfc_gpu_run(mfc_gpu_ctx* ctx, int t_step_start, int t_step_stop, double* dt_
  * bits (MFC_FLAG_*) in *flags; clears them when clear != 0. */
 int mfc_gpu_status(mfc_gpu_ctx* ctx, uint32_t* flags, int clear);
 
+/* Run-time stability monitor, the reference's ICFL of s_write_run_time_information
+ * (src/simulation/m_data_output.fpp:178-310), fused into the last stage kernel
+ * of every step: ICFL = dt / min_d(dx_d / (|u_d| + c)), maximised over the cells
+ * of the step's new state.  mfc_gpu_set_monitor turns it on/off (and clears
+ * the maximum); with it on, mfc_gpu_run fails like the reference when the
+ * maximum is NaN or above 1.  mfc_gpu_icfl returns the maximum since the last
+ * reset.  The monitor reads the state only; it changes no result. */
+int mfc_gpu_set_monitor(mfc_gpu_ctx* ctx, int on);
+int mfc_gpu_icfl(mfc_gpu_ctx* ctx, double* icfl_max, int reset);
+
+/* No counterpart in the reference (whose dt is fixed by the case file).
+ * num_steps time steps with dt chosen from the monitored ICFL so that every
+ * step after the first runs at the given CFL number: dt_{n+1} = dt_n * cfl /
+ * ICFL_n.  *dt_inout: first dt in, next dt out; *time_inout is advanced. */
+int mfc_gpu_run_cfl(mfc_gpu_ctx* ctx, int num_steps, double cfl, double* dt_inout, double* time_inout);
+
 /* The CUDA stream (cudaStream_t) the context launches on, for event timing. */
 void* mfc_gpu_stream(mfc_gpu_ctx* ctx);
 

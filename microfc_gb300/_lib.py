@@ -23,6 +23,7 @@ EXPORTS = (
     "mfc_gpu_ensemble_tune", "mfc_gpu_ensemble_run", "mfc_gpu_ensemble_stream", "mfc_gpu_ensemble_launch_count",
     "mfc_gpu_ensemble_finalize", "mfc_gpu_ensemble_set_gate", "mfc_gate_param_count", "mfc_gate_workspace_floats",
     "mfc_gpu_set_gate", "mfc_gpu_gate_samples", "mfc_gate_gradients", "mfc_gate_train_step", "mfc_gate_infer",
+    "mfc_gpu_set_monitor", "mfc_gpu_icfl", "mfc_gpu_run_cfl",
 )
 MFC_PREC_GATED = 2
 
@@ -116,6 +117,9 @@ def load(build_if_missing: bool = True):
     L.mfc_gate_train_step.argtypes = [vp, vp, ctypes.c_int, vp, vp, vp, vp, vp, ctypes.c_int, ctypes.c_float,
                                       ctypes.c_float, vp, vp]
     L.mfc_gate_infer.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp]
+    L.mfc_gpu_set_monitor.argtypes = [vp, ctypes.c_int]
+    L.mfc_gpu_icfl.argtypes = [vp, dp, ctypes.c_int]
+    L.mfc_gpu_run_cfl.argtypes = [vp, ctypes.c_int, ctypes.c_double, dp, dp]
     _lib = L
     return L
 

@@ -73,6 +73,8 @@ struct mfc_gpu_ctx {
   double* work = nullptr;       // 3-D: partial RHS between the directional sweeps
   void* gate_w = nullptr;       // MFC_PREC_GATED: FP16 gate parameters
   bool gate_ready = false;
+  unsigned long long* monitor = nullptr;  // max ICFL of the monitored steps (double bits)
+  bool monitor_on = false;
   double* tables = nullptr;     // inv_d and coefficient tables
   uint32_t* status = nullptr;
   cudaStream_t stream = nullptr;
@@ -88,8 +90,11 @@ int validate(const mfc_params* p) {
   return why.empty() ? MFC_OK : fail(MFC_ERR_INVALID, why);
 }
 
-int launch_stage(mfc_gpu_ctx* c, const double* qin, const double* qbase, double* qout, double dt, int kind) {
-  cudaError_t e = c->stage->launch(c->dev, qin, qbase, qout, dt, kind, c->stream);
+int launch_stage(mfc_gpu_ctx* c, const double* qin, const double* qbase, double* qout, double dt, int kind,
+                 bool last_stage = false) {
+  mfc::DevParams P = c->dev;
+  if (last_stage && c->monitor_on) P.monitor = c->monitor;  // ICFL of the step's new state
+  cudaError_t e = c->stage->launch(P, qin, qbase, qout, dt, kind, c->stream);
   if (e != cudaSuccess) return fail(MFC_ERR_CUDA, std::string("stage launch: ") + cudaGetErrorString(e));
   c->launches += c->stage->kernels;
   return MFC_OK;
@@ -184,6 +189,9 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if (c->nd == 3 && (e = cudaMalloc(&c->work, sizeof(double) * c->reg_elems)) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
+  if ((e = cudaMalloc(&c->monitor, sizeof(unsigned long long))) != cudaSuccess)
+    return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
+  cudaMemsetAsync(c->monitor, 0, sizeof(unsigned long long), c->stream);
   if ((e = cudaMalloc(&c->status, sizeof(uint32_t))) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   cudaMemsetAsync(c->state, 0, sizeof(double) * c->reg_elems * 3, c->stream);
@@ -323,17 +331,60 @@ int mfc_gpu_tvd_rk(mfc_gpu_ctx* c, double dt, int last_step) {
   double** R = c->reg;
   switch (c->prm.time_stepper) {
     case 1:
-      if ((rc = launch_stage(c, R[0], R[0], R[1], dt, mfc::kRkEuler))) return rc;
+      if ((rc = launch_stage(c, R[0], R[0], R[1], dt, mfc::kRkEuler, true))) return rc;
       std::swap(R[0], R[1]);
       return MFC_OK;
     case 2:
       if ((rc = launch_stage(c, R[0], R[0], R[1], dt, mfc::kRkEuler))) return rc;
-      return launch_stage(c, R[1], R[0], R[0], dt, mfc::kRk2Final);
+      return launch_stage(c, R[1], R[0], R[0], dt, mfc::kRk2Final, true);
     default:
       if ((rc = launch_stage(c, R[0], R[0], R[1], dt, mfc::kRkEuler))) return rc;
       if ((rc = launch_stage(c, R[1], R[0], R[2], dt, mfc::kRk3Mid))) return rc;
-      return launch_stage(c, R[2], R[0], R[0], dt, mfc::kRk3Final);
+      return launch_stage(c, R[2], R[0], R[0], dt, mfc::kRk3Final, true);
   }
+}
+
+int mfc_gpu_set_monitor(mfc_gpu_ctx* c, int on) {
+  if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  c->monitor_on = on != 0;
+  MFC_CUDA(cudaMemsetAsync(c->monitor, 0, sizeof(unsigned long long), c->stream));
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  return MFC_OK;
+}
+
+int mfc_gpu_icfl(mfc_gpu_ctx* c, double* icfl_max, int reset) {
+  if (!c || !icfl_max) return fail(MFC_ERR_INVALID, "NULL argument");
+  unsigned long long bits = 0;
+  MFC_CUDA(cudaMemcpyAsync(&bits, c->monitor, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+  if (reset) MFC_CUDA(cudaMemsetAsync(c->monitor, 0, sizeof(unsigned long long), c->stream));
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  std::memcpy(icfl_max, &bits, sizeof(double));
+  return MFC_OK;
+}
+
+int mfc_gpu_run_cfl(mfc_gpu_ctx* c, int num_steps, double cfl, double* dt_inout, double* time_inout) {
+  if (!c || !dt_inout || !time_inout) return fail(MFC_ERR_INVALID, "NULL argument");
+  if (num_steps < 1 || !(cfl > 0.0) || !(*dt_inout > 0.0)) return fail(MFC_ERR_INVALID, "bad CFL run arguments");
+  const bool was_on = c->monitor_on;
+  c->monitor_on = true;
+  double dt = *dt_inout, t = *time_inout;
+  int rc = MFC_OK;
+  for (int s = 0; s < num_steps && !rc; ++s) {
+    double icfl = 0.0;
+    if ((rc = mfc_gpu_icfl(c, &icfl, 1))) break;
+    if ((rc = mfc_gpu_tvd_rk(c, dt, 0))) break;
+    t += dt;
+    if ((rc = mfc_gpu_icfl(c, &icfl, 0))) break;
+    if (!(icfl == icfl) || !(icfl > 0.0)) {
+      rc = fail(MFC_ERR_STATE, "ICFL is NaN. Exiting ...");
+      break;
+    }
+    dt = dt * (cfl / icfl);  // ICFL of the new state scales with dt
+  }
+  c->monitor_on = was_on;
+  *dt_inout = dt;
+  *time_inout = t;
+  return rc;
 }
 
 int mfc_gpu_run(mfc_gpu_ctx* c, int t_step_start, int t_step_stop, double* dt_inout) {
@@ -357,6 +408,12 @@ int mfc_gpu_run(mfc_gpu_ctx* c, int t_step_start, int t_step_stop, double* dt_in
   int rc = mfc_gpu_status(c, &flags, 0);
   if (rc) return rc;
   if (flags & MFC_FLAG_NAN) return fail(MFC_ERR_STATE, "NaN or Inf in the conservative state");
+  if (c->monitor_on) {  // m_data_output.fpp:296-306
+    double icfl = 0.0;
+    if ((rc = mfc_gpu_icfl(c, &icfl, 0))) return rc;
+    if (icfl != icfl) return fail(MFC_ERR_STATE, "ICFL is NaN. Exiting ...");
+    if (icfl > 1.0) return fail(MFC_ERR_STATE, "ICFL is greater than 1.0. Exiting ...");
+  }
   return MFC_OK;
 }
 
@@ -424,6 +481,7 @@ int mfc_gpu_finalize(mfc_gpu_ctx* c) {
   cudaFree(c->status);
   cudaFree(c->work);
   cudaFree(c->gate_w);
+  cudaFree(c->monitor);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return MFC_OK;

@@ -32,7 +32,9 @@ struct DevParams {
   uint32_t* status;
   void* work;  // 3-D: partial RHS between the directional sweeps ([S][z][y][x], RT)
   const void* gate_w;  // learned WENO gate: FP16 MLP parameters (mfc_gate.cuh layout)
+  unsigned long long* monitor;  // set on a step's last stage: max ICFL of the new state (double bits)
 };
+
 
 // Equation index layout, m_global_parameters.fpp:302-310 (0-based).
 template <int ND, int NF>
@@ -130,6 +132,45 @@ __device__ __forceinline__ void cons_to_prim(double (&q)[Eqs<ND, NF>::S], const 
     dyn = dyn + 0.5 * mom * vel;
   }
   q[Q::E] = (q[Q::E] - dyn - pinf) / gam;
+}
+
+// The reference's run-time stability criterion of one cell
+// (m_data_output.fpp:197-242): ICFL = dt / min_d(dx_d / (|u_d| + c)) with the
+// mixture sound speed c = sqrt(((gamma + 1) p + pi_inf) / (gamma rho)),
+// from the cell's conservative state.  Non-negative, so the bit patterns of
+// the doubles order like their values (atomicMax on the bits).
+template <int ND, int NF>
+__device__ __forceinline__ double cell_icfl(const double (&q)[Eqs<ND, NF>::S], const DevParams& P, double dt,
+                                            const double (&inv_d)[ND]) {
+  using Q = Eqs<ND, NF>;
+  double p[Q::S];
+#pragma unroll
+  for (int v = 0; v < Q::S; ++v) p[v] = q[v];
+  cons_to_prim<ND, NF>(p, P);
+  double rho = 0.0, gam = 0.0, pinf = 0.0;
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    rho = rho + p[f];
+    gam = gam + p[Q::ADV + f] * P.gammas[f];
+    pinf = pinf + p[Q::ADV + f] * P.pi_infs[f];
+  }
+  const double c = sqrt(((gam + 1.0) * p[Q::E] + pinf) / (gam * rho));
+  double rate = 0.0;
+#pragma unroll
+  for (int d = 0; d < ND; ++d) rate = fmax(rate, (fabs(p[Q::MOM + d]) + c) * inv_d[d]);
+  const double icfl = dt * rate;
+  return icfl != icfl ? __longlong_as_double(0x7ff8000000000000ll) : icfl;
+}
+
+__device__ __forceinline__ void monitor_max(unsigned long long* w, double v) {
+  // NaN (all exponent bits, nonzero mantissa) orders above +inf as unsigned bits
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long other = __shfl_down_sync(0xffffffffu, b, o);
+    b = other > b ? other : b;
+  }
+  if ((threadIdx.x & 31) == 0 && b) atomicMax(w, b);
 }
 
 // cons -> prim for the split-precision path.  What needs FP64 stays FP64:

@@ -33,6 +33,8 @@ __global__ void gate_sample_kernel(const mfc::DevParams P, const double* __restr
   const int64_t cells = (int64_t)nx * ny;
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < cells; c += (int64_t)gridDim.x * blockDim.x) {
     const int x = (int)(c % nx), y = (int)(c / nx);
+    // features from the split path's FP32 primitives (what the gated kernel
+    // sees); label from the FP64 WENO5 weights of those normalised stencils
     float a[5], p[5];
     for (int k = 0; k < 5; ++k) {
       bool flip = false;
@@ -50,11 +52,16 @@ __global__ void gate_sample_kernel(const mfc::DevParams P, const double* __restr
     float feat[mfc::kGateIn];
     mfc::gate_features(a, p, feat);
     for (int k = 0; k < mfc::kGateIn; ++k) xout[c * mfc::kGateIn + k] = feat[k];
-    float cf[mfc::kNumCoef];
+    double cf[mfc::kNumCoef];
     const int ci = (dir == 0 ? x : y) + P.coff;
-    for (int k = 0; k < mfc::kNumCoef; ++k) cf[k] = (float)P.coef[dir][k * P.cstride[dir] + ci];
-    const float eps = (float)P.weno_eps;
-    dev_out[c] = fmaxf(mfc::weno5_weight_deviation(cf, a, eps), mfc::weno5_weight_deviation(cf, p, eps));
+    for (int k = 0; k < mfc::kNumCoef; ++k) cf[k] = P.coef[dir][k * P.cstride[dir] + ci];
+    double na[5], np_[5];
+    for (int k = 0; k < 5; ++k) {
+      na[k] = feat[k];
+      np_[k] = feat[5 + k];
+    }
+    dev_out[c] = (float)fmax(mfc::weno5_weight_deviation(cf, na, mfc::kGateLabelEps),
+                             mfc::weno5_weight_deviation(cf, np_, mfc::kGateLabelEps));
   }
 }
 

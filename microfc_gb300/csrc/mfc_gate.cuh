@@ -5,10 +5,21 @@
 // weights (m_weno.fpp:495-531) or can use the optimal linear weights d_k.
 //
 //   inputs  10: each stencil shifted by its minimum and divided by its range
-//               (max - min, floored at 1e-6 of the stencil's magnitude)
+//               max - min, floored at 1e-2 of the stencil's magnitude for p
+//               and at 1e-2 for alpha_1 (a volume fraction is O(1)); below
+//               the floor the inputs shrink with the stencil's amplitude, so
+//               the network can tell a ripple from a jump
 //   layers  10 -> 32 (ReLU) -> 32 (ReLU) -> 1 (logit; sigmoid > 1/2 <=> logit > 0)
-//   label   max_k |omega_k - d_k| > 1e-3 for alpha_1 or p, left or right face
-//
+//   label   max_k |omega_k - d_k| > 1e-3 for alpha_1 or p, left or right face,
+//           with the WENO5 weights evaluated (in FP64) on those normalised
+//           stencils and epsilon = 1e-2: a unit jump has beta ~ 1, and
+//           variations under ~1e-3 of a variable's magnitude (beta below
+//           epsilon) count as flat.  On the raw fields with the case's
+//           epsilon = 1e-16 the weights react to any relative variation above
+//           ~1e-13, so the round-off of the stiffened-gas pressure recovery
+//           and the FP32 ripples of the split path would mark nearly every
+//           cell.
+
 // Inference runs on the tensor cores with FP16 weights and FP32
 // accumulation (mma.sync m16n8k16, 16 cells per warp, the three layers
 // chained in registers: the accumulator fragment of one layer is the A
@@ -28,37 +39,44 @@ constexpr int kGateIn = 10, kGateH = 32;
 constexpr int kGW1 = 0, kGB1 = kGW1 + kGateIn * kGateH, kGW2 = kGB1 + kGateH, kGB2 = kGW2 + kGateH * kGateH,
               kGW3 = kGB2 + kGateH, kGB3 = kGW3 + kGateH, kGateParams = kGB3 + 1;  // 1441
 constexpr float kGateLabelTol = 1e-3f;
+constexpr double kGateLabelEps = 1e-2;
+constexpr float kGateRelFloor = 1e-2f, kGateAlphaFloor = 1e-2f;
 
 // One stencil of 5 values -> 5 normalised inputs.
-__device__ __forceinline__ void gate_norm5(const float (&s)[5], float* out) {
+__device__ __forceinline__ void gate_norm5(const float (&s)[5], float* out, float abs_floor) {
   const float lo = fminf(fminf(fminf(s[0], s[1]), fminf(s[2], s[3])), s[4]);
   const float hi = fmaxf(fmaxf(fmaxf(s[0], s[1]), fmaxf(s[2], s[3])), s[4]);
-  const float floor_ = fmaxf(fmaxf(fabsf(lo), fabsf(hi)) * 1e-6f, 1e-30f);
+  const float floor_ = fmaxf(fmaxf(fabsf(lo), fabsf(hi)) * kGateRelFloor, abs_floor);
   const float r = rcp_approx(fmaxf(hi - lo, floor_));
 #pragma unroll
   for (int k = 0; k < 5; ++k) out[k] = (s[k] - lo) * r;
 }
 
-__device__ __forceinline__ void gate_features(const float (&a)[5], const float (&p)[5], float (&x)[kGateIn]) {
-  gate_norm5(a, x);
-  gate_norm5(p, x + 5);
+// var 0: alpha_1 stencil, var 1: pressure stencil
+__device__ __forceinline__ void gate_norm5_var(const float (&s)[5], float* out, int var) {
+  gate_norm5(s, out, var == 0 ? kGateAlphaFloor : 1e-30f);
 }
 
-// max_k |omega_k - d_k| over both faces of the FP32 WENO5 weights of one
-// stencil (the label of one variable).
-__device__ __forceinline__ float weno5_weight_deviation(const float* __restrict__ c, const float (&v)[5], float eps) {
-  const float d1 = v[4] - v[3], d0 = v[3] - v[2], dm1 = v[2] - v[1], dm2 = v[1] - v[0];
-  const float b0 = fmaf(d1, fmaf(c[kBeta + 0], d1, c[kBeta + 1] * d0), fmaf(c[kBeta + 2] * d0, d0, eps));
-  const float b1 = fmaf(d0, fmaf(c[kBeta + 3], d0, c[kBeta + 4] * dm1), fmaf(c[kBeta + 5] * dm1, dm1, eps));
-  const float b2 = fmaf(dm1, fmaf(c[kBeta + 6], dm1, c[kBeta + 7] * dm2), fmaf(c[kBeta + 8] * dm2, dm2, eps));
-  const float r0 = 1.0f / (b0 * b0), r1 = 1.0f / (b1 * b1), r2 = 1.0f / (b2 * b2);
-  float dev = 0.f;
+__device__ __forceinline__ void gate_features(const float (&a)[5], const float (&p)[5], float (&x)[kGateIn]) {
+  gate_norm5_var(a, x, 0);
+  gate_norm5_var(p, x + 5, 1);
+}
+
+// max_k |omega_k - d_k| over both faces of the FP64 WENO5 weights of one
+// stencil (m_weno.fpp:495-528; the label of one variable).
+__device__ __forceinline__ double weno5_weight_deviation(const double* __restrict__ c, const double (&v)[5],
+                                                         double eps) {
+  const double d1 = v[4] - v[3], d0 = v[3] - v[2], dm1 = v[2] - v[1], dm2 = v[1] - v[0];
+  const double b0 = c[kBeta + 0] * d1 * d1 + c[kBeta + 1] * d1 * d0 + c[kBeta + 2] * d0 * d0 + eps;
+  const double b1 = c[kBeta + 3] * d0 * d0 + c[kBeta + 4] * d0 * dm1 + c[kBeta + 5] * dm1 * dm1 + eps;
+  const double b2 = c[kBeta + 6] * dm1 * dm1 + c[kBeta + 7] * dm1 * dm2 + c[kBeta + 8] * dm2 * dm2 + eps;
+  double dev = 0.0;
 #pragma unroll
   for (int side = 0; side < 2; ++side) {
-    const float* d = c + (side ? kDR : kDL);
-    const float a0 = d[0] * r0, a1 = d[1] * r1, a2 = d[2] * r2;
-    const float is = 1.0f / (a0 + a1 + a2);
-    dev = fmaxf(dev, fmaxf(fabsf(a0 * is - d[0]), fmaxf(fabsf(a1 * is - d[1]), fabsf(a2 * is - d[2]))));
+    const double* d = c + (side ? kDR : kDL);
+    const double a0 = d[0] / (b0 * b0), a1 = d[1] / (b1 * b1), a2 = d[2] / (b2 * b2);
+    const double s = a0 + a1 + a2;
+    dev = fmax(dev, fmax(fabs(a0 / s - d[0]), fmax(fabs(a1 / s - d[1]), fabs(a2 / s - d[2]))));
   }
   return dev;
 }

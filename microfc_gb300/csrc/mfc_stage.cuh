@@ -169,7 +169,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         for (int k = 0; k < 5; ++k) s[k] = col[(k - 2) * LX];
       }
       float xf[5];
-      gate_norm5(s, xf);
+      gate_norm5_var(s, xf, lane < 16 ? 0 : 1);
       __half* r = my + (lane & 15) * 16;
 #pragma unroll
       for (int k = 0; k < 5; ++k) r[(lane < 16 ? 0 : 5) + k] = __float2half(xf[k]);
@@ -360,6 +360,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
 
   // ---- phase 6b: RK combination and store ------------------------------------
   bool bad = false;
+  double icfl = 0.0;
 #pragma unroll
   for (int k = 0; k < CPT; ++k) {
     const int e = tid + k * NT;
@@ -368,6 +369,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
     const int gx = x0 + tx, gy = y0 + ty;
     if (gx >= nx || (ND > 1 && gy >= ny)) continue;
     const int64_t o = gy * P.sy + gx;
+    double qn[S];
 #pragma unroll
     for (int v = 0; v < S; ++v) {
       const double r = widen(rhs[k][v]);
@@ -382,9 +384,18 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       }
       bad |= not_finite(out);
       qout[o + v * P.sv] = out;
+      qn[v] = out;
+    }
+    if (P.monitor) {
+      double inv[ND];
+      inv[0] = __ldg(P.inv_d[0] + gx);
+      if constexpr (ND > 1) inv[1] = __ldg(P.inv_d[1] + gy);
+      const double c = cell_icfl<ND, NF>(qn, P, dt, inv);
+      if (!(c <= icfl)) icfl = c;  // keeps NaN
     }
   }
   if (bad && P.status) atomicOr(P.status, 1u);
+  if (P.monitor) monitor_max(P.monitor, icfl);
 }
 
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>

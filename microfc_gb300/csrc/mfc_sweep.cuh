@@ -171,6 +171,7 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const doub
   // ---- flux divergence, accumulation, RK on the last sweep ---------------------------
   AT* rhs_buf = reinterpret_cast<AT*>(P.work);
   bool bad = false;
+  double icfl = 0.0;
   for (int it = tid; it < NP * TA; it += NT) {
     int ta, pb, pc;
     if (DIR == 0) { ta = it % TA; pb = (it / TA) % TB; pc = it / (TA * TB); }
@@ -199,6 +200,7 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const doub
       for (int v = 0; v < S; ++v) rhs_buf[o + v * P.sv] = r[v];
       continue;
     }
+    double qn[S];
 #pragma unroll
     for (int v = 0; v < S; ++v) {
       const double rv = widen(r[v]);
@@ -213,9 +215,16 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const doub
       }
       bad |= not_finite(out);
       qout[o + v * P.sv] = out;
+      qn[v] = out;
+    }
+    if (P.monitor) {
+      const double inv[3] = {__ldg(P.inv_d[0] + x), __ldg(P.inv_d[1] + y), __ldg(P.inv_d[2] + z)};
+      const double c = cell_icfl<3, NF>(qn, P, dt, inv);
+      if (!(c <= icfl)) icfl = c;  // keeps NaN
     }
   }
   if (bad && P.status) atomicOr(P.status, 1u);
+  if (DIR == 2 && P.monitor) monitor_max(P.monitor, icfl);
 }
 
 }  // namespace mfc

@@ -89,6 +89,11 @@ class Ensemble:
         _lib.check(self.L.mfc_gpu_ensemble_download(self._h, int(i), _dp(a)))
         return a
 
+    def set_gate(self, params) -> None:
+        """Parameters of the learned gate (precision "gated")."""
+        w = np.ascontiguousarray(params, dtype=np.float32)
+        _lib.check(self.L.mfc_gpu_ensemble_set_gate(self._h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
     def tune(self, reps: int = 5):
         v, ms = ctypes.c_int(-1), ctypes.c_double(0)
         _lib.check(self.L.mfc_gpu_ensemble_tune(self._h, int(reps), ctypes.byref(v), ctypes.byref(ms)))

@@ -4,7 +4,12 @@ The network (10 -> 32 -> 32 -> 1, ReLU, sigmoid) reads one cell's 5-point
 stencils of alpha_1 and p along one direction, each shifted by its minimum
 and divided by its range, and predicts whether the cell needs the nonlinear
 WENO5 weights.  Label: max_k |omega_k - d_k| > 1e-3 over alpha_1 and p and
-both faces (the FP32 weights of the split path).  Smooth cells then use the
+both faces, the weights evaluated in FP64 on those same normalised stencils
+with epsilon = 1e-2, so variations under ~1e-3 of a variable's magnitude
+count as flat (with the case's epsilon on the raw fields, round-off in the
+pressure recovery alone would flag nearly every cell); the inputs come
+from the split path's FP32 primitives, as the gated kernel sees them.  Smooth
+cells then use the
 optimal linear weights d_k; plain WENO everywhere stays the fallback
 (precision "split") and the judge (FP64, precision "fp64").
 
@@ -180,7 +185,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--cases", type=int, default=16)
     ap.add_argument("--steps", type=int, default=1000)
-    ap.add_argument("--per-snapshot", type=int, default=31250)  # 16 cases x 4 snapshots x 2 dirs -> 2e6
+    ap.add_argument("--per-snapshot", type=int, default=15625)  # 16 cases x 4 snapshots x 2 dirs -> 2e6
     ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--out", default=WEIGHTS_FILE)
     a = ap.parse_args()

@@ -143,6 +143,22 @@ class Simulation:
         _lib.check(self.L.mfc_gpu_tune(self._h, int(reps), ctypes.byref(v), ctypes.byref(ms)))
         return v.value, ms.value
 
+    def set_monitor(self, on: bool = True) -> None:
+        """Fused ICFL monitor (the reference's run-time information)."""
+        _lib.check(self.L.mfc_gpu_set_monitor(self._h, int(bool(on))))
+
+    def icfl(self, reset: bool = False) -> float:
+        v = ctypes.c_double(0)
+        _lib.check(self.L.mfc_gpu_icfl(self._h, ctypes.byref(v), int(bool(reset))))
+        return v.value
+
+    def run_cfl(self, num_steps: int, cfl: float, dt: float | None = None, time: float = 0.0):
+        """num_steps steps at a constant CFL number; returns (next dt, time)."""
+        d = ctypes.c_double(self.case.dt if dt is None else dt)
+        t = ctypes.c_double(time)
+        _lib.check(self.L.mfc_gpu_run_cfl(self._h, int(num_steps), float(cfl), ctypes.byref(d), ctypes.byref(t)))
+        return d.value, t.value
+
     def set_gate(self, params) -> None:
         """Parameters (FP32, mfc_gate_param_count values) of the learned gate."""
         w = np.ascontiguousarray(params, dtype=np.float32)

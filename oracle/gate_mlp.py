@@ -24,16 +24,32 @@ def unpack(p):
     return (p[W1:B1].reshape(N_IN, N_H), p[B1:W2], p[W2:B2].reshape(N_H, N_H), p[B2:W3], p[W3:B3], p[B3])
 
 
-def norm5(s):
-    """(s - min) / max(max - min, 1e-6 * max|s|) for stencils s[..., 5]."""
+def norm5(s, abs_floor):
+    """(s - min) / max(max - min, 1e-2 * max|s|, abs_floor) for stencils s[..., 5]."""
     s = np.asarray(s, dtype=np.float64)
     lo, hi = s.min(axis=-1, keepdims=True), s.max(axis=-1, keepdims=True)
-    fl = np.maximum(np.maximum(np.abs(lo), np.abs(hi)) * 1e-6, 1e-30)
+    fl = np.maximum(np.maximum(np.abs(lo), np.abs(hi)) * 1e-2, abs_floor)
     return (s - lo) / np.maximum(hi - lo, fl)
 
 
 def features(alpha5, p5):
-    return np.concatenate([norm5(alpha5), norm5(p5)], axis=-1)
+    return np.concatenate([norm5(alpha5, 1e-2), norm5(p5, 1e-30)], axis=-1)
+
+
+def weight_deviation(x5, eps=1e-2):
+    """max_k |omega_k - d_k| over both faces of the uniform-grid WENO5-JS
+    weights of normalised stencils x5[..., 5] (the label statistic)."""
+    v = [x5[..., k] for k in range(5)]
+    b0 = 13 / 12 * (v[2] - 2 * v[3] + v[4]) ** 2 + 0.25 * (3 * v[2] - 4 * v[3] + v[4]) ** 2
+    b1 = 13 / 12 * (v[1] - 2 * v[2] + v[3]) ** 2 + 0.25 * (v[1] - v[3]) ** 2
+    b2 = 13 / 12 * (v[0] - 2 * v[1] + v[2]) ** 2 + 0.25 * (v[0] - 4 * v[1] + 3 * v[2]) ** 2
+    out = np.zeros_like(b0)
+    for d in ((0.1, 0.6, 0.3), (0.3, 0.6, 0.1)):  # left face, right face
+        al = [d[k] / (b + eps) ** 2 for k, b in enumerate((b0, b1, b2))]
+        s = al[0] + al[1] + al[2]
+        for k in range(3):
+            out = np.maximum(out, np.abs(al[k] / s - d[k]))
+    return out
 
 
 def forward(X, p):

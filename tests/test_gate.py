@@ -28,6 +28,16 @@ def test_oracle_gradient_matches_finite_differences():
         assert abs(fd - g[i]) <= 1e-6 + 1e-5 * abs(fd), (i, fd, g[i])
 
 
+def test_label_separates_smooth_from_discontinuous_stencils():
+    x = np.linspace(-1, 1, 5)
+    smooth = np.stack([np.sin(0.05 * x + s) for s in np.linspace(0, 3, 20)])
+    step = np.stack([np.where(x > c, 1.0, 0.0) + 0.01 * x for c in (-0.6, -0.1, 0.1, 0.6)])
+    tiny = 1.0 + 1e-9 * np.random.default_rng(0).normal(size=(20, 5))  # round-off on a flat field
+    assert gate_mlp.weight_deviation(gate_mlp.norm5(smooth, 1e-30)).max() < 1e-3
+    assert gate_mlp.weight_deviation(gate_mlp.norm5(step, 1e-30)).min() > 1e-3
+    assert gate_mlp.weight_deviation(gate_mlp.norm5(tiny, 1e-30)).max() < 1e-3
+
+
 @pytest.mark.gpu
 def test_gpu_backward_kernels_match_oracle():
     from microfc_gb300 import gate
@@ -74,7 +84,11 @@ def test_gate_samples_match_oracle_features():
     idx = np.clip(np.arange(c.m + 1)[:, None] + np.arange(-2, 3)[None, :], 0, c.m)
     feat = gate_mlp.features(a[:, idx], pr[:, idx]).reshape(-1, 10)
     assert np.abs(Xg - feat).max() <= 2e-3
-    assert Dg.min() >= 0 and (Dg > 1e-3).mean() < 0.5
+    # labels: the FP64 weight deviation of the kernel's own normalised stencils
+    X64 = Xg.astype(np.float64)
+    dref = np.maximum(gate_mlp.weight_deviation(X64[:, :5]), gate_mlp.weight_deviation(X64[:, 5:]))
+    assert np.abs(Dg - dref).max() <= 1e-6
+    assert Dg.min() >= 0 and 0.01 < (Dg > 1e-3).mean() < 0.5
 
 
 @pytest.mark.gpu
