@@ -238,6 +238,13 @@ int mfc_gpu_tvd_rk_noalloc(const mfc_params* params, const double* q_in, double*
  * denominators of the compute roofline reported by the benchmark. */
 int mfc_gpu_measure_peaks(int device, double* fp64_tflops, double* fp32_tflops);
 
+/* Self-test with no reference counterpart: for i < n, q_fast[i] = a[i]/b[i]
+ * through the plain path's correctly rounded shared-divisor division and
+ * q_ieee[i] = a[i]/b[i] through the IEEE division; the two must agree bit
+ * for bit.  All pointers are device memory; asynchronous on `stream`. */
+int mfc_gpu_selftest_div(const double* a, const double* b, double* q_fast, double* q_ieee, long long n,
+                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,6 +19,7 @@ EXPORTS = (
     "mfc_gpu_upload", "mfc_gpu_download", "mfc_gpu_upload_state", "mfc_gpu_download_state",
     "mfc_gpu_compute_rhs", "mfc_gpu_tvd_rk", "mfc_gpu_run", "mfc_gpu_status", "mfc_gpu_stream",
     "mfc_gpu_launch_count", "mfc_gpu_finalize", "mfc_gpu_measure_peaks", "mfc_gpu_tvd_rk_noalloc",
+    "mfc_gpu_selftest_div",
     "mfc_gpu_tune", "mfc_gpu_ensemble_init", "mfc_gpu_ensemble_upload", "mfc_gpu_ensemble_download",
     "mfc_gpu_ensemble_tune", "mfc_gpu_ensemble_run", "mfc_gpu_ensemble_stream", "mfc_gpu_ensemble_launch_count",
     "mfc_gpu_ensemble_finalize", "mfc_gpu_ensemble_set_gate", "mfc_gate_param_count", "mfc_gate_workspace_floats",
@@ -94,6 +95,7 @@ def load(build_if_missing: bool = True):
     L.mfc_gpu_launch_count.restype = i64
     L.mfc_gpu_finalize.argtypes = [vp]
     L.mfc_gpu_measure_peaks.argtypes = [ctypes.c_int, dp, dp]
+    L.mfc_gpu_selftest_div.argtypes = [vp, vp, vp, vp, ctypes.c_longlong, vp]
     L.mfc_gpu_tvd_rk_noalloc.argtypes = [ctypes.POINTER(MfcParams), vp, vp, i64, ctypes.c_double, vp]
     ip = ctypes.POINTER(ctypes.c_int)
     L.mfc_gpu_tune.argtypes = [vp, ctypes.c_int, ip, dp]

@@ -103,6 +103,91 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return r;
 }
 
+// ---------------------------------------------------------------------------
+// Correctly rounded FP64 division with a shared divisor.
+//
+// GB300 issues two FP64 operations per SM and clock, and an IEEE division
+// costs several of them, so the WENO weights (alpha_k = d_k / b_k^2 for both
+// faces, omega_k = alpha_k / sum alpha) spend about half of the plain path's
+// FP64 issue on divisions.  The quotient must still be the correctly rounded
+// one (the plain path reproduces the CPU reference bit for bit), so this is
+// the textbook Newton-Raphson reciprocal with a Markstein-style correction
+// and an exact-residual rounding test (J.-M. Muller et al., Handbook of
+// Floating-Point Arithmetic, 2nd ed., ch. 4-5: division with an FMA, the
+// exactness of the remainder a - b*q for a faithful q, and the impossibility
+// of a quotient lying exactly halfway between two doubles):
+//
+//   divisor(b): y0 = rcp.approx.f32 of b's significand (|rel err| < 2^-21),
+//               rescaled by b's exponent with integer operations;
+//               y = y0 + y0 (1 - b y0)                 |y b - 1| < 2^-42
+//   div_rn(a):  q0 = a y;  r0 = a - b q0 (one rounding);  q1 = q0 + r0 y,
+//               so |q1 - a/b| < ulp(q1)/2 + 2^-80 |a/b| < ulp(q1) and
+//               r1 = a - b q1 is exact.  |a/b - q1| = |r1| / |b| is then
+//               compared, with integer operations on the bit patterns,
+//               against half the spacing of doubles from q1 towards a/b;
+//               beyond it the neighbour is the rounded quotient.
+//
+// A divisor costs 2 FP64 operations, each quotient 4 (one multiply and three
+// FMAs).  The argument holds while |a| and |b| lie in [2^-250, 2^251): then
+// every intermediate (q near 2^+-501, residuals near |b| ulp(q)) is a normal
+// double.  Anything else (zero, subnormal, huge, inf or NaN operands) takes
+// the ordinary IEEE division, except a zero numerator over an in-window
+// divisor, whose signed-zero quotient is written directly.
+constexpr uint32_t kDivExpLo = 1023u - 250u, kDivExpSpan = 501u;
+
+static __device__ __noinline__ double div_ieee(double a, double b) { return a / b; }
+
+struct DivisorF64 {
+  double b, y;
+  bool ok;
+};
+
+__device__ __forceinline__ DivisorF64 divisor(double b) {
+  const uint32_t hi = (uint32_t)__double2hiint(b), lo = (uint32_t)__double2loint(b);
+  const uint32_t eb = (hi >> 20) & 0x7ffu;
+  const float f = __uint_as_float(0x3f800000u | ((hi & 0xfffffu) << 3) | (lo >> 29));  // [1, 2)
+  const uint32_t rb = __float_as_uint(rcp_approx(f));                                    // (1/2, 1]
+  const uint32_t ey = (rb >> 23) + (2046u - 127u) - eb;  // exponent of y0 = r * 2^-(eb - 1023)
+  const double y0 = __hiloint2double((int)((hi & 0x80000000u) | (ey << 20) | ((rb & 0x7fffffu) >> 3)),
+                                     (int)(rb << 29));
+  const bool ok = eb - kDivExpLo < kDivExpSpan;
+  const double e = fma(-b, y0, 1.0);
+  return {b, fma(y0, e, y0), ok};
+}
+
+__device__ __forceinline__ double div_rn(double a, const DivisorF64& d) {
+  const int64_t ab = __double_as_longlong(a);
+  const uint32_t ea = (uint32_t)(ab >> 52) & 0x7ffu;
+  if (!d.ok || ea - kDivExpLo >= kDivExpSpan) {
+    if (d.ok && (ab & 0x7fffffffffffffffLL) == 0)
+      return __longlong_as_double((ab ^ __double_as_longlong(d.b)) & (int64_t)0x8000000000000000ULL);
+    return div_ieee(a, d.b);
+  }
+  const double q0 = a * d.y;
+  const double r0 = fma(-d.b, q0, a);
+  const double q1 = fma(r0, d.y, q0);
+  const double r1 = fma(-d.b, q1, a);
+  int64_t qb = __double_as_longlong(q1);
+  const int64_t rb = __double_as_longlong(r1);
+  const int64_t rmag = rb & 0x7fffffffffffffffLL;
+  const bool up = (rb ^ ab) >= 0;  // sign(r1) == sign(a): |a/b| > |q1|
+  const bool pow2 = (qb & 0xfffffffffffffLL) == 0;
+  // half the spacing towards a/b times |b|, as a bit pattern: |b| * 2^(E(q1) - 53), one less
+  // when stepping down from a power of two
+  const int64_t sh = ((qb >> 52) & 0x7ff) - (1023 + 53) - ((!up && pow2) ? 1 : 0);
+  const int64_t tb = (__double_as_longlong(d.b) & 0x7fffffffffffffffLL) + sh * ((int64_t)1 << 52);
+  if (rmag > tb) qb += up ? 1 : -1;
+  return __longlong_as_double(qb);
+}
+
+// FP32 counterparts (split path): the division itself, under the unit's
+// -prec-div setting.
+struct DivisorF32 {
+  float b;
+};
+__device__ __forceinline__ DivisorF32 divisor(float b) { return {b}; }
+__device__ __forceinline__ float div_rn(float a, const DivisorF32& d) { return a / d.b; }
+
 __device__ __forceinline__ bool not_finite(double x) {
   const uint32_t hi = (uint32_t)(__double_as_longlong(x) >> 32);
   return (hi & 0x7ff00000u) == 0x7ff00000u;
@@ -124,14 +209,15 @@ __device__ __forceinline__ void cons_to_prim(double (&q)[Eqs<ND, NF>::S], const 
     pinf = pinf + q[Q::ADV + f] * P.pi_infs[f];
   }
   rho = fmax(rho, 1e-16);
+  const DivisorF64 R = divisor(rho);
 #pragma unroll
   for (int d = 0; d < ND; ++d) {
     const double mom = q[Q::MOM + d];
-    const double vel = mom / rho;
+    const double vel = div_rn(mom, R);
     q[Q::MOM + d] = vel;
     dyn = dyn + 0.5 * mom * vel;
   }
-  q[Q::E] = (q[Q::E] - dyn - pinf) / gam;
+  q[Q::E] = div_rn(q[Q::E] - dyn - pinf, divisor(gam));
 }
 
 // The reference's run-time stability criterion of one cell
@@ -259,15 +345,16 @@ __device__ __forceinline__ void weno_cell(const RT* __restrict__ c, const RT (&v
     const RT b1 = c[kBeta + 3] * dm1 * dm1 + eps;
     RT p0 = v[2] + c[kPL + 0] * d0;
     RT p1 = v[2] + c[kPL + 2] * dm1;
-    RT a0 = c[kDL + 0] / (b0 * b0), a1 = c[kDL + 1] / (b1 * b1);
-    RT s = a0 + a1;
-    vL = (a0 / s) * p0 + (a1 / s) * p1;
+    const auto D0 = divisor(b0 * b0), D1 = divisor(b1 * b1);
+    RT a0 = div_rn(c[kDL + 0], D0), a1 = div_rn(c[kDL + 1], D1);
+    auto S = divisor(a0 + a1);
+    vL = div_rn(a0, S) * p0 + div_rn(a1, S) * p1;
     p0 = v[2] + c[kPR + 0] * d0;
     p1 = v[2] + c[kPR + 2] * dm1;
-    a0 = c[kDR + 0] / (b0 * b0);
-    a1 = c[kDR + 1] / (b1 * b1);
-    s = a0 + a1;
-    vR = (a0 / s) * p0 + (a1 / s) * p1;
+    a0 = div_rn(c[kDR + 0], D0);
+    a1 = div_rn(c[kDR + 1], D1);
+    S = divisor(a0 + a1);
+    vR = div_rn(a0, S) * p0 + div_rn(a1, S) * p1;
   } else {
     const RT d1 = v[4] - v[3];
     const RT d0 = v[3] - v[2];
@@ -276,22 +363,23 @@ __device__ __forceinline__ void weno_cell(const RT* __restrict__ c, const RT (&v
     const RT b0 = c[kBeta + 0] * d1 * d1 + c[kBeta + 1] * d1 * d0 + c[kBeta + 2] * d0 * d0 + eps;
     const RT b1 = c[kBeta + 3] * d0 * d0 + c[kBeta + 4] * d0 * dm1 + c[kBeta + 5] * dm1 * dm1 + eps;
     const RT b2 = c[kBeta + 6] * dm1 * dm1 + c[kBeta + 7] * dm1 * dm2 + c[kBeta + 8] * dm2 * dm2 + eps;
-    const RT bb0 = b0 * b0, bb1 = b1 * b1, bb2 = b2 * b2;
+    // b_k^2 is the divisor of both faces' alpha_k, sum(alpha) of the three omega_k of a face
+    const auto D0 = divisor(b0 * b0), D1 = divisor(b1 * b1), D2 = divisor(b2 * b2);
     {
       const RT p0 = v[2] + c[kPL + 0] * d1 + c[kPL + 1] * d0;
       const RT p1 = v[2] + c[kPL + 2] * d0 + c[kPL + 3] * dm1;
       const RT p2 = v[2] + c[kPL + 4] * dm1 + c[kPL + 5] * dm2;
-      const RT a0 = c[kDL + 0] / bb0, a1 = c[kDL + 1] / bb1, a2 = c[kDL + 2] / bb2;
-      const RT s = a0 + a1 + a2;
-      vL = (a0 / s) * p0 + (a1 / s) * p1 + (a2 / s) * p2;
+      const RT a0 = div_rn(c[kDL + 0], D0), a1 = div_rn(c[kDL + 1], D1), a2 = div_rn(c[kDL + 2], D2);
+      const auto S = divisor(a0 + a1 + a2);
+      vL = div_rn(a0, S) * p0 + div_rn(a1, S) * p1 + div_rn(a2, S) * p2;
     }
     {
       const RT p0 = v[2] + c[kPR + 0] * d1 + c[kPR + 1] * d0;
       const RT p1 = v[2] + c[kPR + 2] * d0 + c[kPR + 3] * dm1;
       const RT p2 = v[2] + c[kPR + 4] * dm1 + c[kPR + 5] * dm2;
-      const RT a0 = c[kDR + 0] / bb0, a1 = c[kDR + 1] / bb1, a2 = c[kDR + 2] / bb2;
-      const RT s = a0 + a1 + a2;
-      vR = (a0 / s) * p0 + (a1 / s) * p1 + (a2 / s) * p2;
+      const RT a0 = div_rn(c[kDR + 0], D0), a1 = div_rn(c[kDR + 1], D1), a2 = div_rn(c[kDR + 2], D2);
+      const auto S = divisor(a0 + a1 + a2);
+      vR = div_rn(a0, S) * p0 + div_rn(a1, S) * p1 + div_rn(a2, S) * p2;
     }
   }
 }
@@ -329,17 +417,18 @@ __device__ __forceinline__ void hllc_face(const RT (&qL)[Eqs<ND, NF>::S], const 
   }
   const RT EL = gamL * pL + piL + RT(0.5) * rhoL * rmsL;
   const RT ER = gamR * pR + piR + RT(0.5) * rhoR * rmsR;
-  const RT HL = (EL + pL) / rhoL;
-  const RT HR = (ER + pR) / rhoR;
-  const RT cL = sqrt((HL - RT(0.5) * rmsL) / gamL);
-  const RT cR = sqrt((HR - RT(0.5) * rmsR) / gamR);
+  const RT HL = div_rn(EL + pL, divisor(rhoL));
+  const RT HR = div_rn(ER + pR, divisor(rhoR));
+  const RT cL = sqrt(div_rn(HL - RT(0.5) * rmsL, divisor(gamL)));
+  const RT cR = sqrt(div_rn(HR - RT(0.5) * rmsR, divisor(gamR)));
   const RT uL = qL[Q::MOM + DIR], uR = qR[Q::MOM + DIR];
   const RT sL = fmin(uL - cL, uR - cR);
   const RT sR = fmax(uR + cR, uL + cL);
-  const RT sS = (pR - pL + rhoL * uL * (sL - uL) - rhoR * uR * (sR - uR)) / (rhoL * (sL - uL) - rhoR * (sR - uR));
+  const RT sS = div_rn(pR - pL + rhoL * uL * (sL - uL) - rhoR * uR * (sR - uR),
+                      divisor(rhoL * (sL - uL) - rhoR * (sR - uR)));
   if (!signbit(sS)) {  // xi_M = 1, xi_P = 0
     const RT sM = fmin(RT(0), sL);
-    const RT xi = (sL - uL) / (sL - sS);
+    const RT xi = div_rn(sL - uL, divisor(sL - sS));
     const RT w = uL + sM * (xi - RT(1));
 #pragma unroll
     for (int f = 0; f < NF; ++f) F[f] = qL[f] * w;
@@ -349,13 +438,13 @@ __device__ __forceinline__ void hllc_face(const RT (&qL)[Eqs<ND, NF>::S], const 
       if (d == DIR) F[Q::MOM + d] = rhoL * (uL * vd + sM * (xi * sS - vd)) + pL;
       else F[Q::MOM + d] = rhoL * (uL * vd + sM * (xi * vd - vd));
     }
-    F[Q::E] = uL * (EL + pL) + sM * (xi * (EL + (sS - uL) * (rhoL * sS + pL / (sL - uL))) - EL);
+    F[Q::E] = uL * (EL + pL) + sM * (xi * (EL + (sS - uL) * (rhoL * sS + div_rn(pL, divisor(sL - uL)))) - EL);
 #pragma unroll
     for (int f = 0; f < NF; ++f) F[Q::ADV + f] = qL[Q::ADV + f] * w;
     ustar = w;
   } else {  // xi_M = 0, xi_P = 1
     const RT sP = fmax(RT(0), sR);
-    const RT xi = (sR - uR) / (sR - sS);
+    const RT xi = div_rn(sR - uR, divisor(sR - sS));
     const RT w = uR + sP * (xi - RT(1));
 #pragma unroll
     for (int f = 0; f < NF; ++f) F[f] = qR[f] * w;
@@ -365,7 +454,7 @@ __device__ __forceinline__ void hllc_face(const RT (&qL)[Eqs<ND, NF>::S], const 
       if (d == DIR) F[Q::MOM + d] = rhoR * (uR * vd + sP * (xi * sS - vd)) + pR;
       else F[Q::MOM + d] = rhoR * (uR * vd + sP * (xi * vd - vd));
     }
-    F[Q::E] = uR * (ER + pR) + sP * (xi * (ER + (sS - uR) * (rhoR * sS + pR / (sR - uR))) - ER);
+    F[Q::E] = uR * (ER + pR) + sP * (xi * (ER + (sS - uR) * (rhoR * sS + div_rn(pR, divisor(sR - uR)))) - ER);
 #pragma unroll
     for (int f = 0; f < NF; ++f) F[Q::ADV + f] = qR[Q::ADV + f] * w;
     ustar = w;
@@ -387,7 +476,7 @@ __device__ __forceinline__ double rk_combine(int kind, double base, double in, d
     case kRkEuler: return base + dt * r;
     case kRk2Final: return (base + in + dt * r) / 2.0;
     case kRk3Mid: return (3.0 * base + in + dt * r) / 4.0;
-    case kRk3Final: return (base + 2.0 * in + 2.0 * dt * r) / 3.0;
+    case kRk3Final: return div_rn(base + 2.0 * in + 2.0 * dt * r, DivisorF64{3.0, 1.0 / 3.0, true});
     default: return r;
   }
 }

@@ -9,6 +9,7 @@
 #include <string>
 
 #include "../../include/mfc_gpu.h"
+#include "mfc_device.cuh"
 
 namespace {
 
@@ -53,7 +54,26 @@ double time_fma(int sms, int iters, cudaError_t* err) {
   return flops / (ms * 1e-3) / 1e12;
 }
 
+// div_rn (the plain path's shared-divisor division) beside the IEEE
+// division, element by element.
+__global__ void div_check_kernel(const double* __restrict__ a, const double* __restrict__ b,
+                                 double* __restrict__ q_fast, double* __restrict__ q_ieee, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    q_fast[i] = mfc::div_rn(a[i], mfc::divisor(b[i]));
+    q_ieee[i] = mfc::div_ieee(a[i], b[i]);
+  }
+}
+
 }  // namespace
+
+extern "C" int mfc_gpu_selftest_div(const double* a, const double* b, double* q_fast, double* q_ieee, long long n,
+                                    void* stream) {
+  if (n < 0 || (n > 0 && (!a || !b || !q_fast || !q_ieee))) return MFC_ERR_INVALID;
+  if (n == 0) return MFC_OK;
+  const long long blocks = (n + 255) / 256 < 152 * 64 ? (n + 255) / 256 : 152 * 64;
+  div_check_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(a, b, q_fast, q_ieee, n);
+  return cudaGetLastError() == cudaSuccess ? MFC_OK : MFC_ERR_CUDA;
+}
 
 extern "C" int mfc_gpu_measure_peaks(int device, double* fp64_tflops, double* fp32_tflops) {
   if (!fp64_tflops || !fp32_tflops) return MFC_ERR_INVALID;
