@@ -248,7 +248,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "split", "gated"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--nx", type=int, default=NX, help="cells in x (profiling runs; the benchmark is 1024)")
     ap.add_argument("--ny", type=int, default=NY, help="cells in y (profiling runs; the benchmark is 512)")
@@ -273,6 +273,9 @@ def main():
     case = cases.shock_droplet_2d(nx=args.nx, ny=args.ny, precision=args.precision)
     x_cb, y_cb, _, q0 = preprocess.generate(case)
     sim = Simulation(case, x_cb, y_cb, q_cons=q0, device=local)
+    if args.precision == "gated":
+        from microfc_gb300 import gate
+        sim.set_gate(gate.load())
     stream = torch.cuda.ExternalStream(sim.stream, device=torch.device("cuda", local))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -336,9 +339,10 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64 state / f32 WENO+HLLC",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64 state / f32 WENO+HLLC"
+        + (" + learned gate" if args.precision == "gated" else ""),
         "data": "synthetic (reference-style case inputs, generated in-process)",
-        "config": {"workload": WORKLOAD if args.precision == "fp64" else WORKLOAD.replace("plain FP64", "split"),
+        "config": {"workload": WORKLOAD if args.precision == "fp64" else WORKLOAD.replace("plain FP64", args.precision),
                    "cells": cells, "equations": case.sys_size, "dt": case.dt,
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": state_bytes,
