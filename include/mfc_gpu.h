@@ -215,6 +215,38 @@ int mfc_gpu_ensemble_finalize(mfc_gpu_ensemble* ens);
 /* Gate parameters for a MFC_PREC_GATED ensemble (see mfc_gpu_set_gate). */
 int mfc_gpu_ensemble_set_gate(mfc_gpu_ensemble* ens, const float* host_params);
 
+/* ---- Initial condition on the device: the reference's pre_process patches
+ * (src/pre_process/m_create_patches.fpp:47-313: line segment 1, circle 2,
+ * rectangle 3; sphere 8 and cuboid 9 are their 3-D analogues), the
+ * smoothed-patch blend (m_assign_patches.fpp:54-165) and prim -> cons
+ * (src/common/m_variables_conversion.fpp:385-443), on the uniform grid of
+ * m_grid.f90:54-70 over the given domain.  Fields mirror patch_icpp(i)%... of
+ * the case file; alter_patch[j] != 0 lets the patch overwrite cells owned by
+ * patch j (j = 0: no patch yet).  Writes register 0 (q_cons_ts(1)) directly:
+ * no host initial condition and no file round trip.  Same operation order
+ * as the CPU pre_process; only tanh (smoothed circles and spheres) may
+ * differ from the host's libm in the last bit. */
+#define MFC_MAX_PATCHES 10
+typedef struct mfc_patch {
+  int32_t geometry;                 /* 1, 2, 3, 8 or 9                                  */
+  double x_centroid, y_centroid, z_centroid;
+  double length_x, length_y, length_z;
+  double radius;
+  int32_t smoothen;                 /* circles/spheres: tanh-smoothed volume fraction   */
+  int32_t smooth_patch_id;          /* 1-based patch the smoothing blends into          */
+  double smooth_coeff;
+  int32_t alter_patch[MFC_MAX_PATCHES + 1];
+  double alpha_rho[MFC_MAX_FLUIDS];
+  double alpha[MFC_MAX_FLUIDS];
+  double vel[3];
+  double pres;
+} mfc_patch;
+
+/* domain: x_beg, x_end, y_beg, y_end, z_beg, z_end (unused directions ignored). */
+int mfc_gpu_generate_ic(mfc_gpu_ctx* ctx, const mfc_patch* patches, int num_patches, const double* domain);
+int mfc_gpu_ensemble_generate_ic(mfc_gpu_ensemble* ens, int case_index, const mfc_patch* patches, int num_patches,
+                                 const double* domain);
+
 /* No counterpart in the reference.  One time step like mfc_gpu_tvd_rk, for
  * callers that cannot allocate device memory (their device memory belongs to
  * another allocator -- a framework's caching pool, or an OpenACC runtime that

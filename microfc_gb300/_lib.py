@@ -24,7 +24,7 @@ EXPORTS = (
     "mfc_gpu_ensemble_tune", "mfc_gpu_ensemble_run", "mfc_gpu_ensemble_stream", "mfc_gpu_ensemble_launch_count",
     "mfc_gpu_ensemble_finalize", "mfc_gpu_ensemble_set_gate", "mfc_gate_param_count", "mfc_gate_workspace_floats",
     "mfc_gpu_set_gate", "mfc_gpu_gate_samples", "mfc_gate_gradients", "mfc_gate_train_step", "mfc_gate_infer",
-    "mfc_gpu_set_monitor", "mfc_gpu_icfl", "mfc_gpu_run_cfl",
+    "mfc_gpu_set_monitor", "mfc_gpu_icfl", "mfc_gpu_run_cfl", "mfc_gpu_generate_ic", "mfc_gpu_ensemble_generate_ic",
 )
 MFC_PREC_GATED = 2
 
@@ -46,6 +46,27 @@ class MfcParams(ctypes.Structure):
         ("z_cb", ctypes.POINTER(ctypes.c_double)),
         ("precision", ctypes.c_int32),
         ("device", ctypes.c_int32),
+    ]
+
+
+MFC_MAX_PATCHES = 10
+
+
+class MfcPatch(ctypes.Structure):
+    """mfc_patch: one patch_icpp(i) of the case file (device initial condition)."""
+    _fields_ = [
+        ("geometry", ctypes.c_int32),
+        ("x_centroid", ctypes.c_double), ("y_centroid", ctypes.c_double), ("z_centroid", ctypes.c_double),
+        ("length_x", ctypes.c_double), ("length_y", ctypes.c_double), ("length_z", ctypes.c_double),
+        ("radius", ctypes.c_double),
+        ("smoothen", ctypes.c_int32),
+        ("smooth_patch_id", ctypes.c_int32),
+        ("smooth_coeff", ctypes.c_double),
+        ("alter_patch", ctypes.c_int32 * (MFC_MAX_PATCHES + 1)),
+        ("alpha_rho", ctypes.c_double * MFC_MAX_FLUIDS),
+        ("alpha", ctypes.c_double * MFC_MAX_FLUIDS),
+        ("vel", ctypes.c_double * 3),
+        ("pres", ctypes.c_double),
     ]
 
 
@@ -101,6 +122,8 @@ def load(build_if_missing: bool = True):
     L.mfc_gpu_tune.argtypes = [vp, ctypes.c_int, ip, dp]
     L.mfc_gpu_ensemble_init.argtypes = [ctypes.POINTER(MfcParams), dp, ctypes.c_int, ctypes.POINTER(vp)]
     L.mfc_gpu_ensemble_upload.argtypes = [vp, ctypes.c_int, dp]
+    L.mfc_gpu_generate_ic.argtypes = [vp, ctypes.POINTER(MfcPatch), ctypes.c_int, dp]
+    L.mfc_gpu_ensemble_generate_ic.argtypes = [vp, ctypes.c_int, ctypes.POINTER(MfcPatch), ctypes.c_int, dp]
     L.mfc_gpu_ensemble_download.argtypes = [vp, ctypes.c_int, dp]
     L.mfc_gpu_ensemble_tune.argtypes = [vp, ctypes.c_int, ip, dp]
     L.mfc_gpu_ensemble_run.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]

@@ -18,6 +18,7 @@
 
 #include "../../include/mfc_gpu.h"
 #include "mfc_grid.h"
+#include "mfc_ic.h"
 #include "mfc_launch.h"
 
 namespace {
@@ -263,6 +264,16 @@ int mfc_gpu_upload_state(mfc_gpu_ctx* c, const double* host_q) {
     int rc = copy_var(c, c->reg[0], v, host_q + v * cells, nullptr, c->n[0], (int64_t)c->n[0] * c->n[1]);
     if (rc) return rc;
   }
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  return MFC_OK;
+}
+
+int mfc_gpu_generate_ic(mfc_gpu_ctx* c, const mfc_patch* patches, int num_patches, const double* domain) {
+  if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  mfc::IcTarget t{c->nd, c->prm.num_fluids, {c->n[0], c->n[1], c->n[2]}, c->sy, c->sz, c->sv,
+                  c->prm.gammas, c->prm.pi_infs, c->reg[0]};
+  const std::string why = mfc::generate_ic(t, patches, num_patches, domain, c->stream, &c->launches);
+  if (!why.empty()) return fail(MFC_ERR_INVALID, why);
   MFC_CUDA(cudaStreamSynchronize(c->stream));
   return MFC_OK;
 }

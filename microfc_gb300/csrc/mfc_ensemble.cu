@@ -13,6 +13,7 @@
 #include "../../include/mfc_gpu.h"
 #include "mfc_ensemble.cuh"
 #include "mfc_grid.h"
+#include "mfc_ic.h"
 #include "mfc_launch.h"
 
 namespace {
@@ -238,6 +239,17 @@ int mfc_gpu_ensemble_upload(mfc_gpu_ensemble* e, int i, const double* host_q) {
                                         (size_t)e->nx[i] * 8, (size_t)e->ny[i], cudaMemcpyHostToDevice, e->stream);
     if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
   }
+  cudaError_t err = cudaStreamSynchronize(e->stream);
+  return err == cudaSuccess ? MFC_OK : mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+}
+
+int mfc_gpu_ensemble_generate_ic(mfc_gpu_ensemble* e, int i, const mfc_patch* patches, int num_patches,
+                                 const double* domain) {
+  if (!e || i < 0 || i >= e->num) return mfc::report_error(MFC_ERR_INVALID, "bad ensemble case index");
+  const mfc::EnsCase& C = e->cases[i];
+  mfc::IcTarget t{2, e->nf, {e->nx[i], e->ny[i], 1}, C.P.sy, C.P.sz, C.P.sv, C.P.gammas, C.P.pi_infs, C.reg[0]};
+  const std::string why = mfc::generate_ic(t, patches, num_patches, domain, e->stream, &e->launches);
+  if (!why.empty()) return mfc::report_error(MFC_ERR_INVALID, why);
   cudaError_t err = cudaStreamSynchronize(e->stream);
   return err == cudaSuccess ? MFC_OK : mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
 }

@@ -35,29 +35,48 @@ def random_droplet_cases(count: int = 64, seed: int = 0, steps: int = 500, preci
 
 
 class Ensemble:
-    def __init__(self, case_list, states=None, device: int = 0):
+    def __init__(self, case_list, states=None, device: int = 0, ic: str = "host"):
+        """states: initial states per case; without them the cases' patches
+        give the initial condition, built on the host (ic="host") or written
+        in place by the device generator (ic="device", no host arrays)."""
+        if ic not in ("host", "device"):
+            raise ValueError("ic must be 'host' or 'device'")
         self.cases = list(case_list)
         self.L = _lib.load()
         params = (_lib.MfcParams * len(self.cases))()
         self._keep = []
         self.grids = []
         qs = []
+        on_device = states is None and ic == "device"
         for i, c in enumerate(self.cases):
             c.check()
-            x_cb, y_cb, _, q = preprocess.generate(c)
-            if states is not None:
-                q = states[i]
+            if on_device:
+                x_cb, y_cb, _ = preprocess.grid(c)
+                q = None
+            else:
+                x_cb, y_cb, _, q = preprocess.generate(c)
+                if states is not None:
+                    q = states[i]
+                q = np.ascontiguousarray(q, dtype=np.float64)
             P, cb = make_params(c, x_cb, y_cb, None, device)
             params[i] = P
             self._keep.append(cb)
             self.grids.append((x_cb, y_cb))
-            qs.append(np.ascontiguousarray(q, dtype=np.float64))
+            qs.append(q)
         dts = np.array([c.dt for c in self.cases], dtype=np.float64)
         h = ctypes.c_void_p()
         _lib.check(self.L.mfc_gpu_ensemble_init(params, _dp(dts), len(self.cases), ctypes.byref(h)))
         self._h = h
         for i, q in enumerate(qs):
-            self.upload(i, q)
+            if on_device:
+                self.generate_ic(i)
+            else:
+                self.upload(i, q)
+
+    def generate_ic(self, i: int) -> None:
+        """pre_process of case i on the device, straight into its state."""
+        arr, dom = preprocess.device_patches(self.cases[i])
+        _lib.check(self.L.mfc_gpu_ensemble_generate_ic(self._h, int(i), arr, len(arr), _dp(dom)))
 
     def close(self):
         if getattr(self, "_h", None):

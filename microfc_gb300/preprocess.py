@@ -99,6 +99,43 @@ def generate(case: Case):
     return x_cb, y_cb, z_cb, q
 
 
+def grid(case: Case):
+    """The uniform cell boundaries x_cb, y_cb, z_cb of a case (None when unused)."""
+    x_cb = uniform_grid(case.m, *case.x_domain)[0]
+    y_cb = uniform_grid(case.n, *case.y_domain)[0] if case.n > 0 else None
+    z_cb = uniform_grid(case.p, *case.z_domain)[0] if case.p > 0 else None
+    return x_cb, y_cb, z_cb
+
+
+def device_patches(case: Case):
+    """(mfc_patch array, domain[6]) of a case for the device generator
+    (mfc_gpu_generate_ic); the same patch semantics as generate()."""
+    from . import _lib
+    P = len(case.patches)
+    if not 1 <= P <= _lib.MFC_MAX_PATCHES:
+        raise ValueError(f"{P} patches; the device generator takes 1..{_lib.MFC_MAX_PATCHES}")
+    arr = (_lib.MfcPatch * P)()
+    for i, pt in enumerate(case.patches):
+        a = arr[i]
+        a.geometry = pt.geometry
+        a.x_centroid, a.y_centroid, a.z_centroid = pt.centroid
+        a.length_x, a.length_y, a.length_z = pt.length
+        a.radius = pt.radius
+        a.smoothen = int(pt.smoothen)
+        a.smooth_patch_id = pt.smooth_patch_id if pt.smooth_patch_id else i + 1
+        a.smooth_coeff = pt.smooth_coeff
+        for j in range(_lib.MFC_MAX_PATCHES + 1):
+            a.alter_patch[j] = 1 if (j == 0 or j in pt.alter_patch) else 0
+        for f in range(case.num_fluids):
+            a.alpha_rho[f] = pt.alpha_rho[f]
+            a.alpha[f] = pt.alpha[f]
+        for d in range(3):
+            a.vel[d] = pt.vel[d] if d < len(pt.vel) else 0.0
+        a.pres = pt.pres
+    dom = np.array([*case.x_domain, *case.y_domain, *case.z_domain], dtype=np.float64)
+    return arr, dom
+
+
 def to_primitive(case: Case, q: np.ndarray) -> np.ndarray:
     """cons -> prim (m_variables_conversion.fpp:326-373) of a whole state, FP64."""
     nf, nd = case.num_fluids, case.num_dims

@@ -58,11 +58,22 @@ class Simulation:
     """Device-resident state of one case (q_cons_ts, rhs, grid, WENO tables)."""
 
     def __init__(self, case: Case, x_cb=None, y_cb=None, z_cb=None, q_cons=None, device: int = 0,
-                 check: bool = True):
+                 check: bool = True, ic: str = "host"):
+        """ic: where the initial condition comes from when q_cons is None --
+        "host" (preprocess.generate, then an upload) or "device"
+        (mfc_gpu_generate_ic writes it in place)."""
         if check:
             case.check()
+        if ic not in ("host", "device"):
+            raise ValueError("ic must be 'host' or 'device'")
         self.case = case
-        if x_cb is None or q_cons is None:
+        on_device = q_cons is None and ic == "device"
+        if on_device:
+            gx, gy, gz = preprocess.grid(case)
+            x_cb = gx if x_cb is None else x_cb
+            y_cb = gy if y_cb is None else y_cb
+            z_cb = gz if z_cb is None else z_cb
+        elif x_cb is None or q_cons is None:
             gx, gy, gz, gq = preprocess.generate(case)
             x_cb = gx if x_cb is None else x_cb
             y_cb = gy if y_cb is None else y_cb
@@ -76,7 +87,15 @@ class Simulation:
         self._h = h
         self.S = self.L.mfc_gpu_sys_size(h)
         self.dt = case.dt
-        self.upload(q_cons)
+        if on_device:
+            self.generate_ic()
+        else:
+            self.upload(q_cons)
+
+    def generate_ic(self, case: Case | None = None) -> None:
+        """pre_process on the device: the case's patches straight into q_cons_ts(1)."""
+        arr, dom = preprocess.device_patches(case or self.case)
+        _lib.check(self.L.mfc_gpu_generate_ic(self._h, arr, len(arr), _dp(dom)))
 
     # -- life cycle -----------------------------------------------------------
     def close(self) -> None:
