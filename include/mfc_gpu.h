@@ -150,6 +150,17 @@ int mfc_gpu_icfl(mfc_gpu_ctx* ctx, double* icfl_max, int reset);
  * ICFL_n.  *dt_inout: first dt in, next dt out; *time_inout is advanced. */
 int mfc_gpu_run_cfl(mfc_gpu_ctx* ctx, int num_steps, double cfl, double* dt_inout, double* time_inout);
 
+/* Output without stalling the time loop (no counterpart in the reference,
+ * whose "!$acc update host" at every t_step_save blocks, p_main.fpp:291-296).
+ * mfc_gpu_snapshot copies register 0 at the current point of the context's
+ * stream to a device staging buffer, then to pinned host slot `slot` (0 or
+ * 1) on a second stream, so time steps launched afterwards run while the
+ * copy is in flight.  mfc_gpu_snapshot_wait blocks until that copy has
+ * landed and returns the slot's [S][p+1][n+1][m+1] array, valid until the
+ * slot's next snapshot or mfc_gpu_finalize. */
+int mfc_gpu_snapshot(mfc_gpu_ctx* ctx, int slot);
+int mfc_gpu_snapshot_wait(mfc_gpu_ctx* ctx, int slot, const double** host_q);
+
 /* The CUDA stream (cudaStream_t) the context launches on, for event timing. */
 void* mfc_gpu_stream(mfc_gpu_ctx* ctx);
 

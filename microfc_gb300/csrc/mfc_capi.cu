@@ -79,6 +79,12 @@ struct mfc_gpu_ctx {
   double* tables = nullptr;     // inv_d and coefficient tables
   uint32_t* status = nullptr;
   cudaStream_t stream = nullptr;
+  // asynchronous snapshots: per slot a device staging copy and a pinned host buffer
+  double* snap_dev[2] = {nullptr, nullptr};
+  double* snap_host[2] = {nullptr, nullptr};
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t snap_staged = nullptr, snap_done[2] = {nullptr, nullptr};
+  bool snap_pending[2] = {false, false};
   mfc::DevParams dev{};
   const mfc::StageEntry* stage = nullptr;
   int64_t launches = 0;
@@ -483,9 +489,69 @@ void* mfc_gpu_stream(mfc_gpu_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 int64_t mfc_gpu_launch_count(const mfc_gpu_ctx* c) { return c ? c->launches : 0; }
 
+int mfc_gpu_snapshot(mfc_gpu_ctx* c, int slot) {
+  if (!c || slot < 0 || slot > 1) return fail(MFC_ERR_INVALID, "bad snapshot slot");
+  const int64_t cells = (int64_t)c->n[0] * c->n[1] * c->n[2];
+  const size_t bytes = (size_t)c->S * cells * sizeof(double);
+  if (!c->copy_stream) {
+    MFC_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    MFC_CUDA(cudaEventCreateWithFlags(&c->snap_staged, cudaEventDisableTiming));
+  }
+  if (!c->snap_host[slot]) {
+    if (cudaMalloc(&c->snap_dev[slot], bytes) != cudaSuccess) return fail(MFC_ERR_NOMEM, "snapshot staging buffer");
+    if (cudaMallocHost(&c->snap_host[slot], bytes) != cudaSuccess) return fail(MFC_ERR_NOMEM, "pinned snapshot slot");
+    MFC_CUDA(cudaEventCreateWithFlags(&c->snap_done[slot], cudaEventDisableTiming));
+  }
+  // the slot's staging buffer is reused: its previous copy-out must have left it
+  if (c->snap_pending[slot]) MFC_CUDA(cudaStreamWaitEvent(c->stream, c->snap_done[slot], 0));
+  // register 0 -> contiguous staging copy, in stream order with the time steps
+  const bool planes_contiguous = c->sz == c->sy * c->n[1];
+  for (int v = 0; v < c->S; ++v) {
+    double* dst = c->snap_dev[slot] + v * cells;
+    if (planes_contiguous) {
+      MFC_CUDA(cudaMemcpy2DAsync(dst, (size_t)c->n[0] * 8, c->reg[0] + v * c->sv, (size_t)c->sy * 8,
+                                 (size_t)c->n[0] * 8, (size_t)c->n[1] * c->n[2], cudaMemcpyDeviceToDevice,
+                                 c->stream));
+    } else {
+      for (int z = 0; z < c->n[2]; ++z)
+        MFC_CUDA(cudaMemcpy2DAsync(dst + (int64_t)z * c->n[0] * c->n[1], (size_t)c->n[0] * 8,
+                                   c->reg[0] + v * c->sv + z * c->sz, (size_t)c->sy * 8, (size_t)c->n[0] * 8,
+                                   (size_t)c->n[1], cudaMemcpyDeviceToDevice, c->stream));
+    }
+  }
+  MFC_CUDA(cudaEventRecord(c->snap_staged, c->stream));
+  // staging -> pinned host on the copy stream; later steps on c->stream overlap with it
+  MFC_CUDA(cudaStreamWaitEvent(c->copy_stream, c->snap_staged, 0));
+  MFC_CUDA(cudaMemcpyAsync(c->snap_host[slot], c->snap_dev[slot], bytes, cudaMemcpyDeviceToHost, c->copy_stream));
+  MFC_CUDA(cudaEventRecord(c->snap_done[slot], c->copy_stream));
+  c->snap_pending[slot] = true;
+  return MFC_OK;
+}
+
+int mfc_gpu_snapshot_wait(mfc_gpu_ctx* c, int slot, const double** host_q) {
+  if (!c || slot < 0 || slot > 1 || !host_q) return fail(MFC_ERR_INVALID, "bad snapshot slot");
+  if (!c->snap_host[slot]) return fail(MFC_ERR_INVALID, "no snapshot was taken into this slot");
+  if (c->snap_pending[slot]) {
+    MFC_CUDA(cudaEventSynchronize(c->snap_done[slot]));
+    c->snap_pending[slot] = false;
+  }
+  *host_q = c->snap_host[slot];
+  return MFC_OK;
+}
+
 int mfc_gpu_finalize(mfc_gpu_ctx* c) {
   if (!c) return MFC_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
+  if (c->snap_staged) cudaEventDestroy(c->snap_staged);
+  for (int s2 = 0; s2 < 2; ++s2) {
+    if (c->snap_done[s2]) cudaEventDestroy(c->snap_done[s2]);
+    if (c->snap_host[s2]) cudaFreeHost(c->snap_host[s2]);
+    cudaFree(c->snap_dev[s2]);
+  }
   cudaFree(c->state);
   cudaFree(c->rhs);
   cudaFree(c->tables);

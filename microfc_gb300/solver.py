@@ -125,6 +125,18 @@ class Simulation:
         _lib.check(self.L.mfc_gpu_download_state(self._h, _dp(a)))
         return a
 
+    def snapshot(self, slot: int = 0) -> None:
+        """Start an asynchronous copy of the current state into pinned slot 0 or 1
+        (mfc_gpu_snapshot); time steps issued afterwards overlap with it."""
+        _lib.check(self.L.mfc_gpu_snapshot(self._h, int(slot)))
+
+    def snapshot_wait(self, slot: int = 0) -> np.ndarray:
+        """The state of the slot's last snapshot, once it has landed.  A view of
+        pinned memory, valid until the slot's next snapshot or close()."""
+        ptr = ctypes.POINTER(ctypes.c_double)()
+        _lib.check(self.L.mfc_gpu_snapshot_wait(self._h, int(slot), ctypes.byref(ptr)))
+        return np.ctypeslib.as_array(ptr, shape=self.case.shape)
+
     def upload_var(self, var: int, sf: np.ndarray, ld_y: int, ld_z: int = 0) -> None:
         """Copy one equation from a host array laid out like q_cons_vf(var)%sf."""
         _lib.check(self.L.mfc_gpu_upload(self._h, int(var), _dp(sf), int(ld_y), int(ld_z)))
