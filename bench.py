@@ -202,11 +202,12 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
         with Simulation(case.replace(precision=prec), x_cb, y_cb, q_cons=q0) as s:
             if p is not None:
                 s.set_gate(p)
+            variant, _ = s.tune(5)
             st = torch.cuda.ExternalStream(s.stream)
             t = _time_steps(s, st, flush, args.steps, args.warmup, case.dt)
             rate = case.cells * args.steps / t
             out[prec] = {"value": rate, "unit": "cell-updates/s", "ms_per_step": 1e3 * t / args.steps,
-                         "vs_plain_fp64": rate / fp64_rate}
+                         "vs_plain_fp64": rate / fp64_rate, "tile_variant": variant}
     if params is None:
         out["gated"] = {"unavailable": "no trained gate parameters (python -m microfc_gb300.gate)"}
     # config 5: 64 cases, nx in {128,256,384,512}, ny = nx/2, seed 0
@@ -231,8 +232,9 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
         key = c.m + 1
         if key not in per_class:
             with Simulation(c.replace(precision="fp64")) as s:
+                s.tune(3)
                 st = torch.cuda.ExternalStream(s.stream)
-                per_class[key] = _time_steps(s, st, flush, 2, 1, c.dt) / 2
+                per_class[key] = _time_steps(s, st, flush, 3, 3, c.dt) / 3
         seq_time += per_class[key]
     seq_rate = sum(c.cells for c in cl) / seq_time
     out["ensemble"] = {"cases": len(cl), "cells": int(sum(c.cells for c in cl)), "precision": prec,
@@ -253,6 +255,8 @@ def main():
     ap.add_argument("--nx", type=int, default=NX, help="cells in x (profiling runs; the benchmark is 1024)")
     ap.add_argument("--ny", type=int, default=NY, help="cells in y (profiling runs; the benchmark is 512)")
     ap.add_argument("--no-modes", action="store_true", help="skip the split/gated/ensemble figures")
+    ap.add_argument("--variant", type=int, default=None,
+                    help="pin this tile variant instead of running the autotuner (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -276,6 +280,12 @@ def main():
     if args.precision == "gated":
         from microfc_gb300 import gate
         sim.set_gate(gate.load())
+    if args.variant is None:
+        variant, _ = sim.tune(5)  # the library's autotuner picks the tile shape
+    else:
+        variant = args.variant
+        sim.select_variant(variant)
+    tile = sim.select_variant(variant)
     stream = torch.cuda.ExternalStream(sim.stream, device=torch.device("cuda", local))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -344,7 +354,8 @@ def main():
         "data": "synthetic (reference-style case inputs, generated in-process)",
         "config": {"workload": WORKLOAD if args.precision == "fp64" else WORKLOAD.replace("plain FP64", args.precision),
                    "cells": cells, "equations": case.sys_size, "dt": case.dt,
-                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}"},
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}",
+                   "tile": {"variant": variant, "tx": tile[0], "ty": tile[1], "threads": tile[2]}},
         "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes, "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,

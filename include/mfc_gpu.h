@@ -175,6 +175,10 @@ int mfc_gpu_finalize(mfc_gpu_ctx* ctx);
  * configuration (the state is not advanced), keeps the fastest and returns
  * its index and per-launch time in milliseconds. */
 int mfc_gpu_tune(mfc_gpu_ctx* ctx, int reps, int* variant_out, double* ms_out);
+/* Pins tile variant `variant` (the numbering mfc_gpu_tune reports) and
+ * returns its tile shape and threads per block; MFC_ERR_INVALID past the
+ * last variant of the context's configuration. */
+int mfc_gpu_select_variant(mfc_gpu_ctx* ctx, int variant, int* tx, int* ty, int* threads);
 
 /* ---- Learned WENO gate (no reference counterpart).  A 10-32-32-1 MLP on a
  * cell's alpha_1 and p stencils picks nonlinear WENO5 or the optimal linear

@@ -25,7 +25,7 @@ EXPORTS = (
     "mfc_gpu_ensemble_finalize", "mfc_gpu_ensemble_set_gate", "mfc_gate_param_count", "mfc_gate_workspace_floats",
     "mfc_gpu_set_gate", "mfc_gpu_gate_samples", "mfc_gate_gradients", "mfc_gate_train_step", "mfc_gate_infer",
     "mfc_gpu_set_monitor", "mfc_gpu_icfl", "mfc_gpu_run_cfl", "mfc_gpu_generate_ic", "mfc_gpu_ensemble_generate_ic",
-    "mfc_gpu_snapshot", "mfc_gpu_snapshot_wait",
+    "mfc_gpu_snapshot", "mfc_gpu_snapshot_wait", "mfc_gpu_select_variant",
 )
 MFC_PREC_GATED = 2
 
@@ -123,6 +123,8 @@ def load(build_if_missing: bool = True):
     L.mfc_gpu_tune.argtypes = [vp, ctypes.c_int, ip, dp]
     L.mfc_gpu_ensemble_init.argtypes = [ctypes.POINTER(MfcParams), dp, ctypes.c_int, ctypes.POINTER(vp)]
     L.mfc_gpu_ensemble_upload.argtypes = [vp, ctypes.c_int, dp]
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.mfc_gpu_select_variant.argtypes = [vp, ctypes.c_int, ip, ip, ip]
     L.mfc_gpu_snapshot.argtypes = [vp, ctypes.c_int]
     L.mfc_gpu_snapshot_wait.argtypes = [vp, ctypes.c_int, ctypes.POINTER(dp)]
     L.mfc_gpu_generate_ic.argtypes = [vp, ctypes.POINTER(MfcPatch), ctypes.c_int, dp]

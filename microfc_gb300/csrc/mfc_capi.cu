@@ -477,6 +477,23 @@ int mfc_gpu_tune(mfc_gpu_ctx* c, int reps, int* variant_out, double* ms_out) {
   return MFC_OK;
 }
 
+int mfc_gpu_select_variant(mfc_gpu_ctx* c, int variant, int* tx, int* ty, int* threads) {
+  if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  int idx = -1;
+  for (const auto& e : g_reg) {
+    if (e.nd != c->nd || e.nf != c->prm.num_fluids || e.wo != c->prm.weno_order || e.prec != c->prm.precision)
+      continue;
+    if (++idx != variant) continue;
+    if (e.prepare() != cudaSuccess) return fail(MFC_ERR_CUDA, "tile variant does not fit on this device");
+    c->stage = &e;
+    if (tx) *tx = e.tx;
+    if (ty) *ty = e.ty;
+    if (threads) *threads = e.nt;
+    return MFC_OK;
+  }
+  return fail(MFC_ERR_INVALID, "no such tile variant for this configuration");
+}
+
 int mfc_gpu_status(mfc_gpu_ctx* c, uint32_t* flags, int clear) {
   if (!c || !flags) return fail(MFC_ERR_INVALID, "NULL argument");
   MFC_CUDA(cudaMemcpyAsync(flags, c->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));

@@ -26,28 +26,36 @@ struct StageEntry {
                         int kind, cudaStream_t st);
 };
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
+// MINB > 1 selects the register-capped kernel (stage_kernel_mb).
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB>
+constexpr auto stage_func() {
+  if constexpr (MINB > 1) return &stage_kernel_mb<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>;
+  else return &stage_kernel<ND, NF, WO, RT, TX, TY, NT, GATE>;
+}
+
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1>
 cudaError_t stage_prepare() {
-  return cudaFuncSetAttribute(stage_kernel<ND, NF, WO, RT, TX, TY, NT, GATE>,
+  return cudaFuncSetAttribute(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>(),
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE>());
 }
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1>
 cudaError_t stage_launch(const DevParams& P, const double* qin, const double* qbase, double* qout, double dt,
                          int kind, cudaStream_t st) {
   const dim3 grid((unsigned)((P.n[0] + TX - 1) / TX), ND > 1 ? (unsigned)((P.n[1] + TY - 1) / TY) : 1u, 1u);
-  stage_kernel<ND, NF, WO, RT, TX, TY, NT, GATE>
+  stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>()
       <<<grid, NT, stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE>(), st>>>(P, qin, qbase, qout, dt, kind);
   return cudaGetLastError();
 }
 
 // prec of a registry entry: 0 FP64, 1 split, 2 split with the learned gate
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1>
 StageEntry stage_entry() {
   return StageEntry{ND, NF, WO, sizeof(RT) == 8 ? 0 : (GATE ? 2 : 1), TX, TY, NT,
                     stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE>(), 1,
-                    &stage_prepare<ND, NF, WO, RT, TX, TY, NT, GATE>, &stage_launch<ND, NF, WO, RT, TX, TY, NT, GATE>};
+                    &stage_prepare<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>,
+                    &stage_launch<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>};
 }
 
 // 3-D: three directional sweeps per stage (mfc_sweep.cuh).  The x sweep uses

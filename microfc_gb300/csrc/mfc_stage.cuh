@@ -22,6 +22,23 @@
 
 namespace mfc {
 
+// One cell's FP32 WENO coefficients from shared memory: kCoefRec floats,
+// 16-byte aligned, as float4 loads.
+constexpr int kCoefRec = 28;
+template <class RT>
+__device__ __forceinline__ void load_coef_record(const RT* __restrict__ rec, RT (&c)[kCoefRec]) {
+  if constexpr (sizeof(RT) == 4) {
+#pragma unroll
+    for (int k = 0; k < kCoefRec / 4; ++k) {
+      const float4 v = reinterpret_cast<const float4*>(rec)[k];
+      c[4 * k] = v.x;
+      c[4 * k + 1] = v.y;
+      c[4 * k + 2] = v.z;
+      c[4 * k + 3] = v.w;
+    }
+  }
+}
+
 // Precision changes of the accumulation type: identity for FP64, the
 // integer bit-field conversions for the split path's FP32.
 template <class T>
@@ -49,10 +66,15 @@ struct StageShape {
   static constexpr int NFX = (S + 1) * TYE * (TX + 1);
   static constexpr int NFY = (ND > 1) ? (S + 1) * (TY + 1) * TX : 0;
   static constexpr int NFL = NFX > NFY ? NFX : NFY;
-  // split precision: the tile's WENO coefficients, converted to FP32 once
+  // split precision: the tile's WENO coefficients, converted to FP32 once and
+  // stored as one 16-byte aligned record of kCoefRec floats per cell, so that
+  // a WENO evaluation loads them with 7 vector loads
   static constexpr int NCX = TX + 2, NCY = (ND > 1) ? TY + 2 : 0;
-  static constexpr int NCOEF = (sizeof(RT) == 4 && WO == 5) ? kNumCoef * (NCX + NCY) : 0;
-  static constexpr size_t kSmemBytes = sizeof(RT) * (size_t(NQ) + 2 * size_t(NW) + size_t(NFL) + size_t(NCOEF));
+  static constexpr int NCOEF = (sizeof(RT) == 4 && WO == 5) ? kCoefRec * (NCX + NCY) : 0;
+  // offsets (in RT elements) of the arrays, each rounded up to 16 bytes
+  static constexpr int align16(int n) { return (n * int(sizeof(RT)) + 15) / 16 * 16 / int(sizeof(RT)); }
+  static constexpr int OW = align16(NQ), OF = OW + 2 * align16(NW), OC = OF + align16(NFL);
+  static constexpr size_t kSmemBytes = sizeof(RT) * (size_t(OC) + size_t(NCOEF));
 };
 
 // One tile of one RK stage; the tile's first cell is (x0, y0).  Used by the
@@ -84,11 +106,11 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   using AT = RT;  // type of the flux-divergence accumulation
 
   RT* sq = reinterpret_cast<RT*>(smem_raw);  // [S][LY][LX] primitive
-  RT* wl = sq + Sh::NQ;                       // left-face values
-  RT* wr = wl + Sh::NW;                       // right-face values
-  RT* fl = wr + Sh::NW;                       // fluxes [S+1][...]
-  RT* scx = fl + Sh::NFL;                     // split: FP32 x coefficients [kNumCoef][TX+2]
-  RT* scy = scx + kNumCoef * Sh::NCX;         // split: FP32 y coefficients [kNumCoef][TY+2]
+  RT* wl = sq + Sh::OW;                       // left-face values
+  RT* wr = wl + Sh::align16(Sh::NW);          // right-face values
+  RT* fl = sq + Sh::OF;                       // fluxes [S+1][...]
+  RT* scx = sq + Sh::OC;                      // split: FP32 x coefficients [TX+2][kCoefRec]
+  RT* scy = scx + kCoefRec * Sh::NCX;         // split: FP32 y coefficients [TY+2][kCoefRec]
 
   const int tid = threadIdx.x;
   const int nx = P.n[0], ny = P.n[1];
@@ -128,14 +150,20 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
     }
   }
   if constexpr (Sh::NCOEF > 0) {
-    for (int it = tid; it < kNumCoef * Sh::NCX; it += NT) {
+    // global reads coalesced along the cells, records written per cell
+    for (int it = tid; it < kCoefRec * Sh::NCX; it += NT) {
       const int cx = it % Sh::NCX, k = it / Sh::NCX;
-      scx[it] = d2f_bits(__ldg(P.coef[0] + k * P.cstride[0] + clamp_coef_index(x0 - 1 + cx, nx) + P.coff));
+      scx[cx * kCoefRec + k] =
+          k < kNumCoef ? d2f_bits(__ldg(P.coef[0] + k * P.cstride[0] + clamp_coef_index(x0 - 1 + cx, nx) + P.coff))
+                       : 0.f;
     }
     if constexpr (ND > 1) {
-      for (int it = tid; it < kNumCoef * Sh::NCY; it += NT) {
+      for (int it = tid; it < kCoefRec * Sh::NCY; it += NT) {
         const int cy = it % Sh::NCY, k = it / Sh::NCY;
-        scy[it] = d2f_bits(__ldg(P.coef[1] + k * P.cstride[1] + clamp_coef_index(y0 - 1 + cy, ny) + P.coff));
+        scy[cy * kCoefRec + k] =
+            k < kNumCoef
+                ? d2f_bits(__ldg(P.coef[1] + k * P.cstride[1] + clamp_coef_index(y0 - 1 + cy, ny) + P.coff))
+                : 0.f;
       }
     }
   }
@@ -209,10 +237,9 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         const int o = k - 2;
         st[k] = (o >= -(WO / 2) && o <= WO / 2) ? row[lx + o] : RT(0);
       }
-      RT c[kNumCoef];
+      RT c[kCoefRec];
       if constexpr (Sh::NCOEF > 0) {
-#pragma unroll
-        for (int k = 0; k < kNumCoef; ++k) c[k] = scx[k * NCX + cx];
+        load_coef_record(scx + cx * kCoefRec, c);
       } else if constexpr (WO > 1) {
         const int gi = clamp_coef_index(x0 - 1 + cx, nx) + P.coff;
 #pragma unroll
@@ -293,10 +320,9 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         const int o = k - 2;
         st[k] = (o >= -(WO / 2) && o <= WO / 2) ? col[(ly + o) * LX] : RT(0);
       }
-      RT c[kNumCoef];
+      RT c[kCoefRec];
       if constexpr (Sh::NCOEF > 0) {
-#pragma unroll
-        for (int k = 0; k < kNumCoef; ++k) c[k] = scy[k * NCY + cy];
+        load_coef_record(scy + cy * kCoefRec, c);
       } else if constexpr (WO > 1) {
         const int gi = clamp_coef_index(y0 - 1 + cy, ny) + P.coff;
 #pragma unroll
@@ -402,6 +428,17 @@ template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = 
 __global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const double* __restrict__ qin,
                                                    const double* __restrict__ qbase, double* __restrict__ qout,
                                                    const double dt, const int kind) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
+                                               (ND > 1) ? blockIdx.y * TY : 0, smem_raw);
+}
+
+// The same kernel with its registers capped so that MINB blocks fit on an SM.
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB>
+__global__ void __launch_bounds__(NT, MINB) stage_kernel_mb(const DevParams P, const double* __restrict__ qin,
+                                                            const double* __restrict__ qbase,
+                                                            double* __restrict__ qout, const double dt,
+                                                            const int kind) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
                                                (ND > 1) ? blockIdx.y * TY : 0, smem_raw);

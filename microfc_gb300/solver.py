@@ -174,6 +174,13 @@ class Simulation:
         _lib.check(self.L.mfc_gpu_tune(self._h, int(reps), ctypes.byref(v), ctypes.byref(ms)))
         return v.value, ms.value
 
+    def select_variant(self, variant: int):
+        """Pin a tile variant (mfc_gpu_select_variant); returns (tx, ty, threads)."""
+        tx, ty, nt = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        _lib.check(self.L.mfc_gpu_select_variant(self._h, int(variant), ctypes.byref(tx), ctypes.byref(ty),
+                                                 ctypes.byref(nt)))
+        return tx.value, ty.value, nt.value
+
     def set_monitor(self, on: bool = True) -> None:
         """Fused ICFL monitor (the reference's run-time information)."""
         _lib.check(self.L.mfc_gpu_set_monitor(self._h, int(bool(on))))
