@@ -108,6 +108,26 @@ struct GateFrags {
   uint32_t w2[2][4][2];  // layer 2: k-steps 0..1, n-tiles 0..3
   uint32_t w3[2][2];     // layer 3: k-steps 0..1, n-tile 0 (only column 0 used)
   float b1[4][2], b2[4][2], b3;
+  __device__ uint32_t W1(int j, int r) const { return w1[j][r]; }
+  __device__ uint32_t W2(int s, int j, int r) const { return w2[s][j][r]; }
+  __device__ uint32_t W3(int s, int r) const { return w3[s][r]; }
+  __device__ float B1(int j, int c) const { return b1[j][c]; }
+  __device__ float B2(int j, int c) const { return b2[j][c]; }
+  __device__ float B3() const { return b3; }
+};
+
+// The same fragments kept in shared memory, word-major ([word][32 lanes]) so
+// that a warp reads one word of every lane conflict-free; the fused stage
+// kernel uses this form, which keeps its register count low.
+constexpr int kGateFragWords = 45;  // 8 (W1) + 16 (W2) + 4 (W3) + 8 (b1) + 8 (b2) + 1 (b3)
+struct GateFragsSmem {
+  const uint32_t* p;  // word 0 of this lane
+  __device__ uint32_t W1(int j, int r) const { return p[(2 * j + r) * 32]; }
+  __device__ uint32_t W2(int s, int j, int r) const { return p[(8 + 2 * (4 * s + j) + r) * 32]; }
+  __device__ uint32_t W3(int s, int r) const { return p[(24 + 2 * s + r) * 32]; }
+  __device__ float B1(int j, int c) const { return __uint_as_float(p[(28 + 2 * j + c) * 32]); }
+  __device__ float B2(int j, int c) const { return __uint_as_float(p[(36 + 2 * j + c) * 32]); }
+  __device__ float B3() const { return __uint_as_float(p[44 * 32]); }
 };
 
 __device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
@@ -151,6 +171,38 @@ __device__ __forceinline__ void gate_load_frags(const __half* __restrict__ w, Ga
   F.b3 = __half2float(w[kGB3]);
 }
 
+// One word of one lane's fragments (the GateFragsSmem numbering), computed
+// from the FP16 parameters exactly as gate_load_frags does.
+__device__ __forceinline__ uint32_t gate_frag_word(const __half* __restrict__ w, int lane, int word) {
+  const int g = lane >> 2, t = lane & 3;
+  auto W1 = [&](int k, int n) { return k < kGateIn ? w[kGW1 + k * kGateH + n] : __float2half(0.f); };
+  auto W2 = [&](int k, int n) { return w[kGW2 + k * kGateH + n]; };
+  auto W3 = [&](int k, int n) { return n == 0 ? w[kGW3 + k] : __float2half(0.f); };
+  if (word < 8) {
+    const int j = word >> 1, r = word & 1, n = 8 * j + g;
+    return r == 0 ? pack_h2_raw(W1(2 * t, n), W1(2 * t + 1, n)) : pack_h2_raw(W1(2 * t + 8, n), W1(2 * t + 9, n));
+  }
+  if (word < 24) {
+    const int q = word - 8, r = q & 1, sj = q >> 1, s = sj >> 2, j = sj & 3, n = 8 * j + g;
+    return r == 0 ? pack_h2_raw(W2(16 * s + 2 * t, n), W2(16 * s + 2 * t + 1, n))
+                  : pack_h2_raw(W2(16 * s + 2 * t + 8, n), W2(16 * s + 2 * t + 9, n));
+  }
+  if (word < 28) {
+    const int q = word - 24, s = q >> 1, r = q & 1;
+    return r == 0 ? pack_h2_raw(W3(16 * s + 2 * t, g), W3(16 * s + 2 * t + 1, g))
+                  : pack_h2_raw(W3(16 * s + 2 * t + 8, g), W3(16 * s + 2 * t + 9, g));
+  }
+  if (word < 36) {
+    const int q = word - 28, j = q >> 1, c = q & 1;
+    return __float_as_uint(__half2float(w[kGB1 + 8 * j + 2 * t + c]));
+  }
+  if (word < 44) {
+    const int q = word - 36, j = q >> 1, c = q & 1;
+    return __float_as_uint(__half2float(w[kGB2 + 8 * j + 2 * t + c]));
+  }
+  return __float_as_uint(__half2float(w[kGB3]));
+}
+
 __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -162,8 +214,8 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], 
 // Logits of 16 cells.  xin: the cells' inputs, FP16, row stride 16 halves
 // (inputs 10..15 zero); the warp's lanes must all call this.  Returns, in
 // lanes with t == 0, the logits of cells g (lo) and g + 8 (hi).
-__device__ __forceinline__ void gate_mlp16(const __half* __restrict__ xin, const GateFrags& F, float& lo,
-                                           float& hi) {
+template <class Frags>
+__device__ __forceinline__ void gate_mlp16(const __half* __restrict__ xin, const Frags& F, float& lo, float& hi) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   uint32_t a[4];
   const __half* r0 = xin + g * 16;
@@ -175,19 +227,19 @@ __device__ __forceinline__ void gate_mlp16(const __half* __restrict__ xin, const
   float h[4][4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    h[j][0] = F.b1[j][0];
-    h[j][1] = F.b1[j][1];
-    h[j][2] = F.b1[j][0];
-    h[j][3] = F.b1[j][1];
-    mma16816(h[j], a, F.w1[j][0], F.w1[j][1]);
+    h[j][0] = F.B1(j, 0);
+    h[j][1] = F.B1(j, 1);
+    h[j][2] = F.B1(j, 0);
+    h[j][3] = F.B1(j, 1);
+    mma16816(h[j], a, F.W1(j, 0), F.W1(j, 1));
   }
   float h2[4][4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    h2[j][0] = F.b2[j][0];
-    h2[j][1] = F.b2[j][1];
-    h2[j][2] = F.b2[j][0];
-    h2[j][3] = F.b2[j][1];
+    h2[j][0] = F.B2(j, 0);
+    h2[j][1] = F.B2(j, 1);
+    h2[j][2] = F.B2(j, 0);
+    h2[j][3] = F.B2(j, 1);
   }
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
@@ -197,9 +249,9 @@ __device__ __forceinline__ void gate_mlp16(const __half* __restrict__ xin, const
     as[2] = pack_h2(fmaxf(h[2 * s + 1][0], 0.f), fmaxf(h[2 * s + 1][1], 0.f));
     as[3] = pack_h2(fmaxf(h[2 * s + 1][2], 0.f), fmaxf(h[2 * s + 1][3], 0.f));
 #pragma unroll
-    for (int j = 0; j < 4; ++j) mma16816(h2[j], as, F.w2[s][j][0], F.w2[s][j][1]);
+    for (int j = 0; j < 4; ++j) mma16816(h2[j], as, F.W2(s, j, 0), F.W2(s, j, 1));
   }
-  float o[4] = {t == 0 ? F.b3 : 0.f, 0.f, t == 0 ? F.b3 : 0.f, 0.f};
+  float o[4] = {t == 0 ? F.B3() : 0.f, 0.f, t == 0 ? F.B3() : 0.f, 0.f};
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
     uint32_t as[4];
@@ -207,7 +259,7 @@ __device__ __forceinline__ void gate_mlp16(const __half* __restrict__ xin, const
     as[1] = pack_h2(fmaxf(h2[2 * s][2], 0.f), fmaxf(h2[2 * s][3], 0.f));
     as[2] = pack_h2(fmaxf(h2[2 * s + 1][0], 0.f), fmaxf(h2[2 * s + 1][1], 0.f));
     as[3] = pack_h2(fmaxf(h2[2 * s + 1][2], 0.f), fmaxf(h2[2 * s + 1][3], 0.f));
-    mma16816(o, as, F.w3[s][0], F.w3[s][1]);
+    mma16816(o, as, F.W3(s, 0), F.W3(s, 1));
   }
   lo = o[0];
   hi = o[2];

@@ -83,11 +83,15 @@ struct StageShape {
 // StageShape::kSmemBytes.
 // Extra shared memory of the learned gate: one 16x16 FP16 input block per
 // warp, then one flag per (cell, direction) reconstructed by the tile.
+// The MLP's lane fragments (kGateFragWords words per lane, word-major)
+// follow, then the flags.
 template <int ND, int TX, int TY, int NT>
 struct GateShape {
   static constexpr int NGX = (TX + 2) * ((ND > 1) ? TY : 1);
   static constexpr int NGY = (ND > 1) ? TX * (TY + 2) : 0;
-  static constexpr size_t kBytes = size_t(NT / 32) * 512 + ((NGX + NGY + 15) / 16) * 16;
+  static constexpr size_t kFragOff = size_t(NT / 32) * 512;
+  static constexpr size_t kFlagOff = kFragOff + size_t(kGateFragWords) * 32 * 4;
+  static constexpr size_t kBytes = kFlagOff + ((NGX + NGY + 15) / 16) * 16;
 };
 
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
@@ -175,10 +179,13 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
     using G = GateShape<ND, TX, TY, NT>;
     unsigned char* gbase = smem_raw + Sh::kSmemBytes;
     __half* gin = reinterpret_cast<__half*>(gbase);
-    uint8_t* flags = gbase + (NT / 32) * 512;
+    uint32_t* frag = reinterpret_cast<uint32_t*>(gbase + G::kFragOff);
+    uint8_t* flags = gbase + G::kFlagOff;
     const int warp = tid >> 5, lane = tid & 31;
-    GateFrags F;
-    gate_load_frags(reinterpret_cast<const __half*>(P.gate_w), F);
+    for (int i = tid; i < kGateFragWords * 32; i += NT)
+      frag[i] = gate_frag_word(reinterpret_cast<const __half*>(P.gate_w), i & 31, i >> 5);
+    __syncthreads();
+    const GateFragsSmem F{frag + lane};
     __half* my = gin + warp * 256;
     constexpr int NG = G::NGX + G::NGY, NCH = (NG + 15) / 16;
     for (int ch = warp; ch < NCH; ch += NT / 32) {
