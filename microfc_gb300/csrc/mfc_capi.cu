@@ -192,7 +192,7 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if ((e = cudaMalloc(&c->rhs, sizeof(double) * c->reg_elems)) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
-  if (p->precision == MFC_PREC_GATED && (e = cudaMalloc(&c->gate_w, 2 * mfc::kGateParams)) != cudaSuccess)
+  if (p->precision == MFC_PREC_GATED && (e = cudaMalloc(&c->gate_w, mfc::kGateBufferBytes)) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if (c->nd == 3 && (e = cudaMalloc(&c->work, sizeof(double) * c->reg_elems)) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));

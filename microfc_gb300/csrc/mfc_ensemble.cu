@@ -200,7 +200,7 @@ int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_ca
       (err = cudaMalloc(&e->state, sizeof(double) * state_elems)) != cudaSuccess ||
       (err = cudaMalloc(&e->tables, sizeof(double) * table_elems)) != cudaSuccess ||
       (err = cudaMalloc(&e->status, sizeof(uint32_t))) != cudaSuccess ||
-      (c0.precision == MFC_PREC_GATED && (err = cudaMalloc(&e->gate_w, 2 * mfc::kGateParams)) != cudaSuccess))
+      (c0.precision == MFC_PREC_GATED && (err = cudaMalloc(&e->gate_w, mfc::kGateBufferBytes)) != cudaSuccess))
     return cleanup(mfc::report_error(MFC_ERR_NOMEM, cudaGetErrorString(err)));
   cudaMemsetAsync(e->state, 0, sizeof(double) * state_elems, e->stream);
   cudaMemsetAsync(e->status, 0, sizeof(uint32_t), e->stream);

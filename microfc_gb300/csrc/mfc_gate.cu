@@ -171,6 +171,12 @@ __global__ void gate_adam_kernel(float* __restrict__ w, const float* __restrict_
   w[i] -= lr * mh / (sqrtf(vh) + eps);
 }
 
+// Lane fragments [kGateFragWords][32] of the FP16 parameters (GateFragsSmem layout).
+__global__ void gate_frag_kernel(const __half* __restrict__ wh, uint32_t* __restrict__ frag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < mfc::kGateFragWords * 32) frag[i] = mfc::gate_frag_word(wh, i & 31, i >> 5);
+}
+
 __global__ void gate_to_half_kernel(const float* __restrict__ w, __half* __restrict__ h) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < mfc::kGateParams) h[i] = __float2half_rn(w[i]);
@@ -276,13 +282,19 @@ int gate_samples(const DevParams& P, int nf, const double* q, int dir, float* xo
   return e == cudaSuccess ? MFC_OK : cuda_fail(e);
 }
 
-int gate_upload(const float* host_params, void* dev_half, cudaStream_t st) {
+int gate_upload(const float* host_params, void* dev_buf, cudaStream_t st) {
   std::vector<__half> h(kGateParams);
   for (int i = 0; i < kGateParams; ++i) {
     if (!std::isfinite(host_params[i])) return report_error(MFC_ERR_INVALID, "gate parameters must be finite");
     h[i] = __float2half_rn(host_params[i]);
   }
-  cudaError_t e = cudaMemcpyAsync(dev_half, h.data(), sizeof(__half) * kGateParams, cudaMemcpyHostToDevice, st);
+  cudaError_t e = cudaMemcpyAsync(dev_buf, h.data(), sizeof(__half) * kGateParams, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(e);
+  // the fused stage kernel's per-lane MMA fragments, computed once here
+  gate_frag_kernel<<<(kGateFragWords * 32 + 255) / 256, 256, 0, st>>>(
+      static_cast<const __half*>(dev_buf),
+      reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(dev_buf) + kGateFragOffset));
+  e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return e == cudaSuccess ? MFC_OK : cuda_fail(e);
 }

@@ -120,6 +120,10 @@ struct GateFrags {
 // that a warp reads one word of every lane conflict-free; the fused stage
 // kernel uses this form, which keeps its register count low.
 constexpr int kGateFragWords = 45;  // 8 (W1) + 16 (W2) + 4 (W3) + 8 (b1) + 8 (b2) + 1 (b3)
+// Device buffer of a gated context: the FP16 parameters, then (16-byte
+// aligned) the precomputed lane fragments [kGateFragWords][32].
+constexpr size_t kGateFragOffset = (2 * size_t(kGateParams) + 15) / 16 * 16;
+constexpr size_t kGateBufferBytes = kGateFragOffset + size_t(kGateFragWords) * 32 * 4;
 struct GateFragsSmem {
   const uint32_t* p;  // word 0 of this lane
   __device__ uint32_t W1(int j, int r) const { return p[(2 * j + r) * 32]; }

@@ -182,8 +182,9 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
     uint32_t* frag = reinterpret_cast<uint32_t*>(gbase + G::kFragOff);
     uint8_t* flags = gbase + G::kFlagOff;
     const int warp = tid >> 5, lane = tid & 31;
-    for (int i = tid; i < kGateFragWords * 32; i += NT)
-      frag[i] = gate_frag_word(reinterpret_cast<const __half*>(P.gate_w), i & 31, i >> 5);
+    const uint32_t* gsrc =
+        reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(P.gate_w) + kGateFragOffset);
+    for (int i = tid; i < kGateFragWords * 32; i += NT) frag[i] = __ldg(gsrc + i);
     __syncthreads();
     const GateFragsSmem F{frag + lane};
     __half* my = gin + warp * 256;
