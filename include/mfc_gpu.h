@@ -124,6 +124,31 @@ int mfc_gpu_compute_rhs(mfc_gpu_ctx* ctx, double* rhs_out, double* prim_out);
  * return at t_step == t_step_stop (m_rhs.fpp:452).  Asynchronous. */
 int mfc_gpu_tvd_rk(mfc_gpu_ctx* ctx, double dt, int last_step);
 
+/* ---- Processor boundaries (domain decomposition, m_mpi_proxy.fpp:468-979).
+ * A boundary value >= 0 in mfc_params (the neighbouring subdomain, as the
+ * reference's bc_x%beg = rank) makes that side read its ghost cells from a
+ * halo receive buffer instead of a physical boundary condition (1-D and
+ * 2-D; the neighbour's ghost cell widths come from mfc_gpu_set_halo_widths,
+ * as the reference exchanges them).  Such a context is stepped stage
+ * by stage: before stage s, every subdomain packs the strip next to each of
+ * its processor boundaries from that stage's input (mfc_gpu_halo_pack) into
+ * the neighbour's receive buffer (mfc_gpu_halo_buffer) -- directly when both
+ * live on one GPU, or through a send/receive pair across GPUs -- and then
+ * runs mfc_gpu_rk_stage.  mfc_gpu_tvd_rk and mfc_gpu_run refuse such a
+ * context.  Layouts (depth d = 0 next to the boundary, H = (weno_order+1)/2):
+ * x sides [S][n+1][H], y sides [S][H][m+1]. */
+int mfc_gpu_rk_stage(mfc_gpu_ctx* ctx, int stage, double dt);
+int mfc_gpu_halo_buffer(mfc_gpu_ctx* ctx, int dir, int side, double** dev_ptr, int64_t* count);
+/* The neighbour's cell widths beyond a processor boundary (widths[i] = ghost
+ * cell at depth i, count >= buff_size = (weno_order-1)/2 + 2), as the
+ * reference exchanges its grid buffers (m_mpi_proxy.fpp); without them the
+ * ghost cells repeat the edge cell's width.  Rebuilds the WENO tables. */
+int mfc_gpu_set_halo_widths(mfc_gpu_ctx* ctx, int dir, int side, const double* widths, int count);
+/* Packs, on the context's stream, the strip that the neighbour across
+ * (dir, side) needs for stage `stage` into dst (device memory, layout of the
+ * neighbour's receive buffer for its opposite side). */
+int mfc_gpu_halo_pack(mfc_gpu_ctx* ctx, int stage, int dir, int side, double* dst);
+
 /* The time loop of p_main (p_main.fpp:196-318) from t_step_start to
  * t_step_stop, including the trim of dt at the last step of the CPU build.
  * *dt_inout carries dt in and the final (possibly trimmed) dt out.

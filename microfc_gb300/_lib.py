@@ -26,6 +26,7 @@ EXPORTS = (
     "mfc_gpu_set_gate", "mfc_gpu_gate_samples", "mfc_gate_gradients", "mfc_gate_train_step", "mfc_gate_infer",
     "mfc_gpu_set_monitor", "mfc_gpu_icfl", "mfc_gpu_run_cfl", "mfc_gpu_generate_ic", "mfc_gpu_ensemble_generate_ic",
     "mfc_gpu_snapshot", "mfc_gpu_snapshot_wait", "mfc_gpu_select_variant",
+    "mfc_gpu_rk_stage", "mfc_gpu_halo_buffer", "mfc_gpu_halo_pack", "mfc_gpu_set_halo_widths",
 )
 MFC_PREC_GATED = 2
 
@@ -125,6 +126,11 @@ def load(build_if_missing: bool = True):
     L.mfc_gpu_ensemble_upload.argtypes = [vp, ctypes.c_int, dp]
     ip = ctypes.POINTER(ctypes.c_int)
     L.mfc_gpu_select_variant.argtypes = [vp, ctypes.c_int, ip, ip, ip]
+    L.mfc_gpu_rk_stage.argtypes = [vp, ctypes.c_int, ctypes.c_double]
+    L.mfc_gpu_halo_buffer.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                                      ctypes.POINTER(ctypes.c_int64)]
+    L.mfc_gpu_halo_pack.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
+    L.mfc_gpu_set_halo_widths.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int]
     L.mfc_gpu_snapshot.argtypes = [vp, ctypes.c_int]
     L.mfc_gpu_snapshot_wait.argtypes = [vp, ctypes.c_int, ctypes.POINTER(dp)]
     L.mfc_gpu_generate_ic.argtypes = [vp, ctypes.POINTER(MfcPatch), ctypes.c_int, dp]

@@ -85,6 +85,14 @@ struct mfc_gpu_ctx {
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t snap_staged = nullptr, snap_done[2] = {nullptr, nullptr};
   bool snap_pending[2] = {false, false};
+  // processor boundaries: receive buffers per side ([2*dir + side]) and their device table
+  bool has_proc = false;
+  int H = 0;
+  double* halo_buf[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  int64_t halo_count[6] = {0, 0, 0, 0, 0, 0};
+  const double** halo_table = nullptr;
+  std::vector<double> cb_host[3];      // the cell boundaries passed at init
+  std::vector<double> ghost_w[3][2];   // neighbour widths of processor boundaries
   mfc::DevParams dev{};
   const mfc::StageEntry* stage = nullptr;
   int64_t launches = 0;
@@ -93,7 +101,7 @@ struct mfc_gpu_ctx {
 namespace {
 
 int validate(const mfc_params* p) {
-  const std::string why = mfc::validate_params(p);
+  const std::string why = mfc::validate_params(p, /*allow_processor=*/true);
   return why.empty() ? MFC_OK : fail(MFC_ERR_INVALID, why);
 }
 
@@ -123,6 +131,31 @@ __global__ void prim_kernel(const mfc::DevParams P, const double* __restrict__ q
     mfc::cons_to_prim<ND, NF>(v, P);
 #pragma unroll
     for (int k = 0; k < Q::S; ++k) out[o + k * P.sv] = v[k];
+  }
+}
+
+// Boundary strip of a stage input for the neighbour across (dir, side):
+// depth d = 0 is the cell next to the boundary.  dir 0: dst[S][ny][H],
+// dir 1: dst[S][H][nx] (the neighbour's halo layout).
+__global__ void halo_pack_kernel(const double* __restrict__ q, int S, int nx, int ny, int64_t sy, int64_t sv, int H,
+                                 int dir, int side, double* __restrict__ dst) {
+  const int across = dir == 0 ? ny : nx;
+  const int64_t total = (int64_t)S * H * across;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    int v, a, d;
+    if (dir == 0) {
+      d = (int)(i % H);
+      a = (int)((i / H) % across);
+      v = (int)(i / ((int64_t)H * across));
+      const int x = side == 0 ? d : nx - 1 - d;
+      dst[i] = q[v * sv + a * sy + x];
+    } else {
+      a = (int)(i % across);
+      d = (int)((i / across) % H);
+      v = (int)(i / ((int64_t)H * across));
+      const int y = side == 0 ? d : ny - 1 - d;
+      dst[i] = q[v * sv + y * sy + a];
+    }
   }
 }
 
@@ -217,7 +250,32 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
   if ((e = cudaMemcpy(c->tables, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
     return cleanup(fail(MFC_ERR_CUDA, cudaGetErrorString(e)));
 
+  {
+    const double* cbs[3] = {p->x_cb, p->y_cb, p->z_cb};
+    for (int d = 0; d < c->nd; ++d) c->cb_host[d].assign(cbs[d], cbs[d] + c->n[d] + 1);
+  }
+  // halo receive buffers of the processor boundaries
+  c->H = (p->weno_order + 1) / 2;
+  for (int d = 0; d < c->nd; ++d) {
+    for (int side = 0; side < 2; ++side) {
+      if ((side == 0 ? bcb[d] : bce[d]) < 0) continue;
+      c->has_proc = true;
+      const int k = 2 * d + side;
+      c->halo_count[k] = (int64_t)c->S * c->H * (d == 0 ? c->n[1] : c->n[0]);
+      if ((e = cudaMalloc(&c->halo_buf[k], sizeof(double) * c->halo_count[k])) != cudaSuccess)
+        return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
+      cudaMemsetAsync(c->halo_buf[k], 0, sizeof(double) * c->halo_count[k], c->stream);
+    }
+  }
+  if (c->has_proc) {
+    if ((e = cudaMalloc(&c->halo_table, sizeof(double*) * 6)) != cudaSuccess)
+      return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
+    if ((e = cudaMemcpy(c->halo_table, c->halo_buf, sizeof(double*) * 6, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return cleanup(fail(MFC_ERR_CUDA, cudaGetErrorString(e)));
+  }
+
   mfc::DevParams& D = c->dev;
+  D.halo = c->halo_table;
   for (int d = 0; d < 3; ++d) {
     D.n[d] = c->n[d];
     D.bc_beg[d] = bcb[d];
@@ -342,6 +400,8 @@ int mfc_gpu_compute_rhs(mfc_gpu_ctx* c, double* rhs_out, double* prim_out) {
 
 int mfc_gpu_tvd_rk(mfc_gpu_ctx* c, double dt, int last_step) {
   if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  if (c->has_proc)
+    return fail(MFC_ERR_INVALID, "processor boundaries: step with mfc_gpu_rk_stage and a halo exchange per stage");
   if (c->gate_w && !c->gate_ready) return fail(MFC_ERR_INVALID, "gate parameters not set (mfc_gpu_set_gate)");
   if (last_step) return MFC_OK;  // s_compute_rhs returns before any update at t_step_stop
   int rc;
@@ -359,6 +419,69 @@ int mfc_gpu_tvd_rk(mfc_gpu_ctx* c, double dt, int last_step) {
       if ((rc = launch_stage(c, R[1], R[0], R[2], dt, mfc::kRk3Mid))) return rc;
       return launch_stage(c, R[2], R[0], R[0], dt, mfc::kRk3Final, true);
   }
+}
+
+int mfc_gpu_rk_stage(mfc_gpu_ctx* c, int stage, double dt) {
+  if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  if (c->gate_w && !c->gate_ready) return fail(MFC_ERR_INVALID, "gate parameters not set (mfc_gpu_set_gate)");
+  const int ts = c->prm.time_stepper;
+  if (stage < 0 || stage >= ts) return fail(MFC_ERR_INVALID, "stage out of range for the time stepper");
+  double** R = c->reg;
+  const bool last = stage == ts - 1;
+  if (ts == 1) {
+    int rc = launch_stage(c, R[0], R[0], R[1], dt, mfc::kRkEuler, true);
+    if (!rc) std::swap(R[0], R[1]);
+    return rc;
+  }
+  if (stage == 0) return launch_stage(c, R[0], R[0], R[1], dt, mfc::kRkEuler);
+  if (ts == 2) return launch_stage(c, R[1], R[0], R[0], dt, mfc::kRk2Final, true);
+  if (stage == 1) return launch_stage(c, R[1], R[0], R[2], dt, mfc::kRk3Mid);
+  return launch_stage(c, R[2], R[0], R[0], dt, mfc::kRk3Final, last);
+}
+
+int mfc_gpu_halo_buffer(mfc_gpu_ctx* c, int dir, int side, double** dev_ptr, int64_t* count) {
+  if (!c || !dev_ptr || dir < 0 || dir > 2 || side < 0 || side > 1) return fail(MFC_ERR_INVALID, "bad halo side");
+  *dev_ptr = c->halo_buf[2 * dir + side];
+  if (count) *count = c->halo_count[2 * dir + side];
+  if (!*dev_ptr) return fail(MFC_ERR_INVALID, "that side is not a processor boundary");
+  return MFC_OK;
+}
+
+int mfc_gpu_set_halo_widths(mfc_gpu_ctx* c, int dir, int side, const double* widths, int count) {
+  if (!c || !widths || dir < 0 || dir >= c->nd || side < 0 || side > 1) return fail(MFC_ERR_INVALID, "bad halo side");
+  if (!c->halo_buf[2 * dir + side]) return fail(MFC_ERR_INVALID, "that side is not a processor boundary");
+  if (count < c->b) return fail(MFC_ERR_INVALID, "need buff_size = (weno_order-1)/2 + 2 ghost widths");
+  for (int i = 0; i < c->b; ++i)
+    if (!(widths[i] > 0.0)) return fail(MFC_ERR_INVALID, "ghost widths must be positive");
+  c->ghost_w[dir][side].assign(widths, widths + c->b);
+  // rebuild this context's grid tables with the neighbour's widths
+  mfc_params q = c->prm;
+  q.x_cb = c->cb_host[0].data();
+  q.y_cb = c->nd > 1 ? c->cb_host[1].data() : nullptr;
+  q.z_cb = c->nd > 2 ? c->cb_host[2].data() : nullptr;
+  const double* gw[3][2];
+  for (int d = 0; d < 3; ++d)
+    for (int e = 0; e < 2; ++e) gw[d][e] = c->ghost_w[d][e].empty() ? nullptr : c->ghost_w[d][e].data();
+  mfc::GridTables gt;
+  const std::string why = mfc::build_grid_tables(&q, c->nd, c->n, c->b, gt, gw);
+  if (!why.empty()) return fail(MFC_ERR_INVALID, why);
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  MFC_CUDA(cudaMemcpy(c->tables, gt.host.data(), sizeof(double) * gt.host.size(), cudaMemcpyHostToDevice));
+  return MFC_OK;
+}
+
+int mfc_gpu_halo_pack(mfc_gpu_ctx* c, int stage, int dir, int side, double* dst) {
+  if (!c || !dst || dir < 0 || dir >= c->nd || dir > 1 || side < 0 || side > 1)
+    return fail(MFC_ERR_INVALID, "bad halo pack arguments");
+  if (stage < 0 || stage >= c->prm.time_stepper) return fail(MFC_ERR_INVALID, "stage out of range");
+  const double* q = stage == 0 ? c->reg[0] : stage == 1 ? c->reg[1] : c->reg[2];
+  const int across = dir == 0 ? c->n[1] : c->n[0];
+  const int64_t total = (int64_t)c->S * c->H * across;
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 8);
+  halo_pack_kernel<<<blocks, 256, 0, c->stream>>>(q, c->S, c->n[0], c->n[1], c->sy, c->sv, c->H, dir, side, dst);
+  MFC_CUDA(cudaGetLastError());
+  c->launches += 1;
+  return MFC_OK;
 }
 
 int mfc_gpu_set_monitor(mfc_gpu_ctx* c, int on) {
@@ -564,6 +687,8 @@ int mfc_gpu_finalize(mfc_gpu_ctx* c) {
     cudaStreamDestroy(c->copy_stream);
   }
   if (c->snap_staged) cudaEventDestroy(c->snap_staged);
+  for (int k = 0; k < 6; ++k) cudaFree(c->halo_buf[k]);
+  cudaFree(c->halo_table);
   for (int s2 = 0; s2 < 2; ++s2) {
     if (c->snap_done[s2]) cudaEventDestroy(c->snap_done[s2]);
     if (c->snap_host[s2]) cudaFreeHost(c->snap_host[s2]);

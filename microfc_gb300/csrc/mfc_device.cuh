@@ -33,6 +33,12 @@ struct DevParams {
   void* work;  // 3-D: partial RHS between the directional sweeps ([S][z][y][x], RT)
   const void* gate_w;  // learned WENO gate: FP16 MLP parameters (mfc_gate.cuh layout)
   unsigned long long* monitor;  // set on a step's last stage: max ICFL of the new state (double bits)
+  // processor boundaries (bc >= 0): device table of 6 halo buffers, [2*dir + side]
+  // (NULL where the side is a physical boundary); the whole table is NULL
+  // when the context has no processor boundary.  x sides: [S][ny][H] (depth
+  // fastest), y sides: [S][H][nx]; depth d = 0 is the ghost cell next to the
+  // boundary.
+  const double* const* halo;
 };
 
 

@@ -7,6 +7,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -24,12 +25,17 @@ struct AxisHost {
 
 // Widths and boundaries of the ghost cells (cell centres are not used by the
 // hot path).
-inline void grid_ghosts(AxisHost& a, int bcb, int bce) {
+// Processor boundaries (bc >= 0) take the neighbour's widths when given
+// (wb/we[i] = width of the ghost cell at depth i, as the reference exchanges
+// them in s_mpi_sendrecv_grid_variables_buffers), else the edge width.
+inline void grid_ghosts(AxisHost& a, int bcb, int bce, const double* wb = nullptr, const double* we = nullptr) {
   const int s = a.s, b = a.b;
   for (int i = 0; i <= s; ++i) a.D(i) = a.CB(i) - a.CB(i - 1);
-  for (int i = 1; i <= b; ++i) a.D(-i) = bcb <= -3 ? a.D(0) : bcb == -2 ? a.D(i - 1) : a.D(s - (i - 1));
+  for (int i = 1; i <= b; ++i)
+    a.D(-i) = (bcb >= 0 && wb) ? wb[i - 1] : (bcb <= -3 || bcb >= 0) ? a.D(0) : bcb == -2 ? a.D(i - 1) : a.D(s - (i - 1));
   for (int i = 1; i <= b; ++i) a.CB(-1 - i) = a.CB(-i) - a.D(-i);
-  for (int i = 1; i <= b; ++i) a.D(s + i) = bce <= -3 ? a.D(s) : bce == -2 ? a.D(s - (i - 1)) : a.D(i - 1);
+  for (int i = 1; i <= b; ++i)
+    a.D(s + i) = (bce >= 0 && we) ? we[i - 1] : (bce <= -3 || bce >= 0) ? a.D(s) : bce == -2 ? a.D(s - (i - 1)) : a.D(i - 1);
   for (int i = 1; i <= b; ++i) a.CB(s + i) = a.CB(s + (i - 1)) + a.D(s + i);
 }
 
@@ -124,7 +130,9 @@ struct GridTables {
   int cstride[3] = {0, 0, 0};
 };
 
-inline std::string build_grid_tables(const mfc_params* p, int nd, const int* n, int b, GridTables& t) {
+// ghost[d][side]: neighbour widths for processor boundaries (b values), or NULL
+inline std::string build_grid_tables(const mfc_params* p, int nd, const int* n, int b, GridTables& t,
+                                     const double* const (*ghost)[2] = nullptr) {
   const double* cbs[3] = {p->x_cb, p->y_cb, p->z_cb};
   const int bcb[3] = {p->bc_x_beg, p->bc_y_beg, p->bc_z_beg};
   const int bce[3] = {p->bc_x_end, p->bc_y_end, p->bc_z_end};
@@ -137,7 +145,7 @@ inline std::string build_grid_tables(const mfc_params* p, int nd, const int* n, 
     a.cb.assign((size_t)(a.s + 2 * a.b + 2), 0.0);
     a.d.assign((size_t)(a.s + 2 * a.b + 1), 0.0);
     for (int i = -1; i <= a.s; ++i) a.CB(i) = cbs[d][i + 1];
-    grid_ghosts(a, bcb[d], bce[d]);
+    grid_ghosts(a, bcb[d], bce[d], ghost ? ghost[d][0] : nullptr, ghost ? ghost[d][1] : nullptr);
     for (int i = 0; i <= a.s; ++i)
       if (!(a.D(i) > 0.0)) return "cell boundaries must increase";
     t.off_inv[d] = t.host.size();
@@ -161,7 +169,9 @@ inline std::string build_grid_tables(const mfc_params* p, int nd, const int* n, 
 }
 
 // The checks of s_check_input_file that apply to the hot path.
-inline std::string validate_params(const mfc_params* p) {
+// allow_processor: boundary values >= 0 (a neighbouring subdomain, exchanged
+// through halo buffers) are accepted, in 1-D and 2-D.
+inline std::string validate_params(const mfc_params* p, bool allow_processor = false) {
   if (!p) return "params is NULL";
   if (p->m <= 0) return "Unsupported value of m";
   if (p->n < 0 || p->p < 0) return "Unsupported value of n or p";
@@ -178,10 +188,15 @@ inline std::string validate_params(const mfc_params* p) {
   for (int d = 0; d < ndim; ++d) {
     for (int e = 0; e < 2; ++e) {
       const int bc = bcs[2 * d + e];
-      if (bc < -12 || bc > -1) return "Unsupported boundary condition (processor boundaries need a halo exchange)";
+      if (bc >= 0 && !allow_processor)
+        return "Unsupported boundary condition (processor boundaries need a context with halo buffers)";
+      if (bc < -12 || (bc > -1 && !allow_processor)) return "Unsupported boundary condition";
     }
     if ((bcs[2 * d] == -1) != (bcs[2 * d + 1] == -1)) return "Periodic boundaries must be set at both ends";
   }
+  const bool proc = bcs[0] >= 0 || bcs[1] >= 0 || (ndim > 1 && (bcs[2] >= 0 || bcs[3] >= 0)) ||
+                    (ndim > 2 && (bcs[4] >= 0 || bcs[5] >= 0));
+  if (proc && ndim > 2) return "processor boundaries are supported in 1-D and 2-D";
   for (int f = 0; f < p->num_fluids; ++f) {
     if (!(p->gammas[f] > 0.0)) return "Unsupported value of fluid_pp%gamma";
     if (p->pi_infs[f] < 0.0) return "Unsupported value of fluid_pp%pi_inf";

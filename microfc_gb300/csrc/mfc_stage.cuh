@@ -134,12 +134,31 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
     const bool hy = (ND > 1) && (ly < H || ly >= H + TY);
     if (hx && hy) continue;  // corners are never read
     bool fx = false, fy = false;
-    const int gx = map_cell(x0 - H + lx, nx, P.bc_beg[0], P.bc_end[0], &fx);
-    const int gy = (ND > 1) ? map_cell(y0 - H + ly, ny, P.bc_beg[1], P.bc_end[1], &fy) : 0;
-    const double* src = qin + gy * P.sy + gx;
+    const int rx = x0 - H + lx, ry = (ND > 1) ? y0 - H + ly : 0;
+    // processor boundaries: ghost cells come from the neighbour's halo buffer
+    const int px = rx < 0 ? (P.bc_beg[0] >= 0 ? 0 : -1) : (rx >= nx && P.bc_end[0] >= 0 ? 1 : -1);
+    const int py = (ND > 1) ? (ry < 0 ? (P.bc_beg[1] >= 0 ? 0 : -1) : (ry >= ny && P.bc_end[1] >= 0 ? 1 : -1)) : -1;
+    const double* src;
+    int64_t vs = P.sv;
+    if (px >= 0) {
+      // cells of partial edge tiles beyond the first H ghosts are never stored: clamp
+      const int d = min(px == 0 ? -1 - rx : rx - nx, H - 1);
+      const int yy = ry < 0 ? 0 : (ry >= ny ? ny - 1 : ry);  // rows beyond the domain are never stored
+      src = P.halo[px] + (int64_t)yy * H + d;
+      vs = (int64_t)ny * H;
+    } else if (py >= 0) {
+      const int d = min(py == 0 ? -1 - ry : ry - ny, H - 1);
+      const int xx = rx < 0 ? 0 : (rx >= nx ? nx - 1 : rx);
+      src = P.halo[2 + py] + (int64_t)d * nx + xx;
+      vs = (int64_t)H * nx;
+    } else {
+      const int gx = map_cell(rx, nx, P.bc_beg[0], P.bc_end[0], &fx);
+      const int gy = (ND > 1) ? map_cell(ry, ny, P.bc_beg[1], P.bc_end[1], &fy) : 0;
+      src = qin + gy * P.sy + gx;
+    }
     double q[S];
 #pragma unroll
-    for (int v = 0; v < S; ++v) q[v] = __ldg(src + v * P.sv);
+    for (int v = 0; v < S; ++v) q[v] = __ldg(src + v * vs);
     if (fx) q[Q::MOM] = -q[Q::MOM];
     if (ND > 1 && fy) q[Q::MOM + 1] = -q[Q::MOM + 1];
     if constexpr (kSplit) {

@@ -1,0 +1,198 @@
+"""Domain decomposition with halo exchange, on one GPU or across ranks.
+
+``decompose`` splits a case the way s_mpi_decompose_computational_domain
+does (src/simulation/m_mpi_proxy.fpp:134-328): (m+1) // p cells per
+subdomain, the first (m+1) % p subdomains one more, subdomains ordered x
+fastest, a processor boundary (the neighbour's rank, >= 0) wherever a
+subdomain meets another one, and the physical boundary conditions (a
+periodic one wrapping around to the far subdomain) elsewhere.
+
+Every RK stage needs the neighbours' strips of that stage's input (the
+halo exchange of s_populate_conservative_variables_buffers, m_rhs.fpp:434
+and m_mpi_proxy.fpp:468-979).  ``MultiDomain`` runs all subdomains on one
+GPU: each subdomain packs its strips straight into the neighbours' receive
+buffers (mfc_gpu_halo_pack / mfc_gpu_halo_buffer), then every subdomain
+runs the stage (mfc_gpu_rk_stage).  ``exchange`` is the rank-to-rank form:
+send/receive pairs of packed strips through torch.distributed (NCCL between
+GPUs, gloo on the host).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .case import Case
+from .solver import _dp
+
+
+@dataclass
+class Subdomain:
+    rank: int
+    coords: tuple            # (ix, iy)
+    start: tuple             # first global cell (x, y)
+    case: Case               # the subdomain's case: local m, n and boundary conditions
+    x_cb: np.ndarray
+    y_cb: np.ndarray | None
+    neighbors: dict = field(default_factory=dict)  # (dir, side) -> rank
+
+    def window(self):
+        """Slices of the global [S, 1, n+1, m+1] state this subdomain holds."""
+        sx, sy = self.start
+        return (slice(None), slice(None), slice(sy, sy + self.case.n + 1), slice(sx, sx + self.case.m + 1))
+
+
+def _split(count: int, parts: int):
+    base, rem = divmod(count, parts)
+    sizes = [base + (1 if i < rem else 0) for i in range(parts)]
+    starts = [sum(sizes[:i]) for i in range(parts)]
+    return sizes, starts
+
+
+def decompose(case: Case, x_cb, y_cb=None, px: int = 2, py: int = 1) -> list[Subdomain]:
+    """Subdomains of a 1-D or 2-D case on a px x py process grid."""
+    if case.p > 0:
+        raise ValueError("decomposition is supported for 1-D and 2-D cases")
+    if case.n == 0 and py != 1:
+        raise ValueError("a 1-D case decomposes along x only")
+    sx, ox = _split(case.m + 1, px)
+    sy, oy = _split(case.n + 1, py)
+    if min(sx) < 5 * case.weno_order or (case.n > 0 and min(sy) < 5 * case.weno_order):
+        raise ValueError("subdomains too small for the WENO stencil")
+    subs = []
+    for iy in range(py):
+        for ix in range(px):
+            rank = iy * px + ix
+            bx, by = list(case.bc_x), list(case.bc_y)
+            nb = {}
+
+            def link(d, side, coord, count, bc, other):
+                if (side == 0 and coord > 0) or (side == 1 and coord < count - 1) or (bc[side] == -1 and count > 1):
+                    nb[(d, side)] = other
+                    bc[side] = other
+
+            link(0, 0, ix, px, bx, iy * px + (ix - 1) % px)
+            link(0, 1, ix, px, bx, iy * px + (ix + 1) % px)
+            if case.n > 0:
+                link(1, 0, iy, py, by, ((iy - 1) % py) * px + ix)
+                link(1, 1, iy, py, by, ((iy + 1) % py) * px + ix)
+            sub_case = case.replace(m=sx[ix] - 1, n=(sy[iy] - 1) if case.n > 0 else 0, bc_x=tuple(bx),
+                                    bc_y=tuple(by), name=f"{case.name}_p{rank}")
+            xs = np.asarray(x_cb)[ox[ix]:ox[ix] + sx[ix] + 1]
+            ys = None if y_cb is None or case.n == 0 else np.asarray(y_cb)[oy[iy]:oy[iy] + sy[iy] + 1]
+            subs.append(Subdomain(rank, (ix, iy), (ox[ix], oy[iy]), sub_case, xs, ys, nb))
+    return subs
+
+
+def halo_strip(sub: Subdomain, q_local: np.ndarray, d: int, side: int, H: int) -> np.ndarray:
+    """Host restatement of mfc_gpu_halo_pack: the strip of a local state
+    [S, 1, n+1, m+1] that the neighbour across (d, side) needs, in its
+    receive-buffer layout (x: [S][n+1][H], y: [S][H][m+1]; depth 0 next to
+    the boundary)."""
+    q = q_local[:, 0]
+    if d == 0:
+        cols = [k if side == 0 else q.shape[2] - 1 - k for k in range(H)]
+        return np.stack([q[:, :, c] for c in cols], axis=-1)
+    rows = [k if side == 0 else q.shape[1] - 1 - k for k in range(H)]
+    return np.stack([q[:, r, :] for r in rows], axis=1)
+
+
+def ghost_widths(neighbor: Subdomain, d: int, side: int, b: int) -> np.ndarray:
+    """The b cell widths of `neighbor` next to the boundary it shares with a
+    subdomain whose side `side` faces it (depth 0 first): what the reference
+    sends in s_mpi_sendrecv_grid_variables_buffers (m_mpi_proxy.fpp:338-458)."""
+    w = np.diff(np.asarray(neighbor.x_cb if d == 0 else neighbor.y_cb))
+    return np.ascontiguousarray(w[::-1][:b] if side == 0 else w[:b])
+
+
+def exchange(sub: Subdomain, strips: dict, group=None) -> dict:
+    """Rank-to-rank halo exchange: sends strips[(d, side)] to the neighbour
+    across (d, side) and returns what each neighbour sent, keyed by the side
+    it arrives on.  Tensors may live on the host (gloo) or the GPU (NCCL);
+    every send is matched by the neighbour's receive on its opposite side, so
+    the pattern is the same on every rank and cannot deadlock."""
+    import torch
+    import torch.distributed as dist
+    reqs, out = [], {}
+    for (d, side), peer in sorted(sub.neighbors.items()):
+        t = strips[(d, side)]
+        buf = torch.empty_like(t)
+        out[(d, side)] = buf
+        reqs.append(dist.isend(t.contiguous(), dst=peer, group=group, tag=2 * d + side))
+        reqs.append(dist.irecv(buf, src=peer, group=group, tag=2 * d + (1 - side)))
+    for r in reqs:
+        r.wait()
+    return out
+
+
+class MultiDomain:
+    """All subdomains of a decomposed case on one GPU, stepped with a halo
+    exchange before every RK stage; bit-identical to the undecomposed run."""
+
+    def __init__(self, case: Case, x_cb, y_cb=None, q_cons=None, px: int = 2, py: int = 1, device: int = 0):
+        from .solver import Simulation
+        self.case = case
+        self.subs = decompose(case, x_cb, y_cb, px, py)
+        self.sims = []
+        for s in self.subs:
+            q = None if q_cons is None else np.ascontiguousarray(q_cons[s.window()])
+            self.sims.append(Simulation(s.case, s.x_cb, s.y_cb, q_cons=q, device=device, check=False))
+        self.H = (case.weno_order + 1) // 2
+        self.L = _lib.load()
+        b = (case.weno_order - 1) // 2 + 2  # buff_size
+        for s, sim in zip(self.subs, self.sims):
+            for (d, side), peer in s.neighbors.items():
+                w = ghost_widths(self.subs[peer], d, side, b)
+                _lib.check(self.L.mfc_gpu_set_halo_widths(sim._h, d, side, _dp(w), b))
+
+    def close(self):
+        for s in self.sims:
+            s.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _buffer(self, rank: int, d: int, side: int) -> int:
+        p = ctypes.c_void_p()
+        n = ctypes.c_int64()
+        _lib.check(self.L.mfc_gpu_halo_buffer(self.sims[rank]._h, d, side, ctypes.byref(p), ctypes.byref(n)))
+        return p.value
+
+    def step(self, dt: float) -> None:
+        import torch
+        for stage in range(self.case.time_stepper):
+            for s, sim in zip(self.subs, self.sims):
+                for (d, side), peer in s.neighbors.items():
+                    dst = self._buffer(peer, d, 1 - side)
+                    _lib.check(self.L.mfc_gpu_halo_pack(sim._h, stage, d, side, ctypes.c_void_p(dst)))
+            torch.cuda.synchronize()
+            for sim in self.sims:
+                _lib.check(self.L.mfc_gpu_rk_stage(sim._h, stage, float(dt)))
+            torch.cuda.synchronize()
+
+    def run(self, t_step_start: int, t_step_stop: int, dt: float | None = None) -> float:
+        """The p_main loop (with its last-step dt trim) over the subdomains."""
+        dt = self.case.dt if dt is None else dt
+        t_step = t_step_start
+        mytime = 0.0 if t_step == 0 else t_step * dt
+        finaltime = t_step_stop * dt
+        while True:
+            mytime = mytime + dt
+            if t_step == t_step_stop:
+                break
+            self.step(dt)
+            if (mytime + dt) >= finaltime:
+                dt = finaltime - mytime
+            t_step = t_step + 1
+        return dt
+
+    def download(self) -> np.ndarray:
+        q = np.empty(self.case.shape)
+        for s, sim in zip(self.subs, self.sims):
+            q[s.window()] = sim.download()
+        return q

@@ -52,7 +52,7 @@ def _params(case, x_cb, y_cb=None):
     ("weno_order", 4, "weno_order"),
     ("weno_eps", 1e-3, "weno_eps"),
     ("time_stepper", 4, "time_stepper"),
-    ("bc_x_beg", 0, "processor boundaries"),
+    ("bc_x_beg", -13, "Unsupported boundary condition"),
     ("bc_x_beg", -1, "Periodic"),
     ("num_fluids", 5, "num_fluids"),
 ])
@@ -67,6 +67,19 @@ def test_init_rejects_invalid_cases_without_touching_the_device(field, value, ms
     assert rc == _lib.MFC_ERR_INVALID
     assert not h.value
     assert msg in L.mfc_gpu_last_error().decode()
+
+
+def test_processor_boundaries_are_1d_and_2d_only():
+    L = _lib.load()
+    case = cases.shock_bubble_3d(N=28, steps=2, precision="fp64")
+    x_cb, y_cb, z_cb, _ = preprocess.generate(case)
+    P = _params(case, x_cb, y_cb)
+    P.p = case.p
+    P.z_cb = z_cb.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    P.bc_x_end = 1  # neighbouring subdomain
+    h = ctypes.c_void_p()
+    assert L.mfc_gpu_init(ctypes.byref(P), ctypes.byref(h)) == _lib.MFC_ERR_INVALID
+    assert "1-D and 2-D" in L.mfc_gpu_last_error().decode()
 
 
 def test_null_context_calls_fail_cleanly():
