@@ -1,0 +1,50 @@
+"""Every compiled tile variant the autotuner can pick gives the same bits: the
+per-cell arithmetic does not depend on the tile shape, so a tuned run must
+equal the default one (and, for FP64, the CPU oracle) exactly.  Ragged grids
+exercise partial edge tiles.  (The FP32 units are compiled with FMA
+contraction, so a variant whose register cap made the compiler fuse
+differently would fail here; one such 16x8 variant was dropped.)"""
+import numpy as np
+import pytest
+
+from microfc_gb300 import cases, gate, preprocess
+
+pytestmark = pytest.mark.gpu
+
+
+def _variant_runs(case, steps, params=None):
+    from microfc_gb300 import Simulation
+    from microfc_gb300._lib import MfcError
+    x, y, z, q = preprocess.generate(case)
+    outs, shapes = [], []
+    v = 0
+    while True:
+        with Simulation(case, x, y, z, q_cons=q) as sim:
+            if params is not None:
+                sim.set_gate(params)
+            try:
+                shapes.append(sim.select_variant(v))
+            except MfcError:
+                break
+            sim.run(0, steps)
+            outs.append(sim.download())
+        v += 1
+    return outs, shapes
+
+
+@pytest.mark.parametrize("kind", ["1d_fp64", "1d_split", "2d_fp64", "2d_split", "2d_gated", "3d_fp64", "3d_split"])
+def test_all_tile_variants_agree_bitwise(kind):
+    nd, prec = kind.split("_")
+    params = None
+    if nd == "1d":
+        c = cases.sod_1d(m=299, steps=6, dt=1e-4).replace(precision=prec)
+    elif nd == "2d":
+        c = cases.shock_droplet_2d(nx=100, ny=60, steps=6, precision=prec)
+        if prec == "gated":
+            params = gate.load()
+    else:
+        c = cases.shock_bubble_3d(N=28, steps=6, precision=prec).replace(m=28, n=26, p=27)
+    outs, shapes = _variant_runs(c, 6, params)
+    assert len(outs) >= 1
+    for o, s in zip(outs[1:], shapes[1:]):
+        assert np.array_equal(o.view(np.uint64), outs[0].view(np.uint64)), s
