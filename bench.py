@@ -371,7 +371,11 @@ def main():
             "bound": "fp64" if args.precision == "fp64" else "fp32", "achieved": ach, "peak": peak,
             "unit": "TFLOP/s", "frac": ach / peak, "flops_per_cell_update": flops,
             "peak_kind": "measured in-process (FMA chains, mfc_gpu_measure_peaks)",
-            "peaks_measured": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak}}
+            "peaks_measured": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak},
+            # the peak counts an FMA as 2 flops; the bit-faithful path may fuse
+            # nothing, so each algorithmic add, mul, div or sqrt needs at least
+            # one pipe instruction: its ceiling is half the flop peak
+            "issue_frac": ach / (peak / 2.0)}
     sim.close()
     if not args.no_modes and args.precision == "fp64":
         line["modes"] = other_modes(args, case, x_cb, y_cb, q0, flush, value / ws)
