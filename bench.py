@@ -116,6 +116,19 @@ def _dist():
     return ws, rank, local
 
 
+def replica_rate(seconds: float, units_per_rank: int, ws: int, device: str = "cuda"):
+    """Whole-job rate of N independent replicas: every rank processed
+    units_per_rank cell-updates; the job took as long as its slowest rank.
+    Returns (units of all ranks / max seconds, max seconds)."""
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        tt = torch.tensor([seconds], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        seconds = float(tt.item())
+    return ws * units_per_rank / seconds, seconds
+
+
 def cpu_baseline(steps: int = 2, ny: int = 64):
     """The oracle on a 1024 x ny strip of the workload, all host cores."""
     import oracle
@@ -311,12 +324,8 @@ def main():
     launches = sim.launches - l0
     ms = [a.elapsed_time(b) for a, b in ev]
     t_total = sum(ms) / 1e3
-    if ws > 1:
-        tt = torch.tensor([t_total], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total = float(tt.item())
     cells = case.cells
-    value = ws * cells * args.steps / t_total
+    value, t_total = replica_rate(t_total, cells * args.steps, ws)
     ms_step = 1e3 * t_total / args.steps
     if sim.status() != 0:
         raise RuntimeError("device flagged a non-finite state during the benchmark")
@@ -333,11 +342,7 @@ def main():
         sim.tvd_rk(0, case.dt)
         sim.download(host)
     t_e2e = time.perf_counter() - t0
-    if ws > 1:
-        tt = torch.tensor([t_e2e], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
-    e2e = ws * cells * e2e_steps / t_e2e
+    e2e, t_e2e = replica_rate(t_e2e, cells * e2e_steps, ws)
     state_bytes = int(np.prod(case.shape)) * 8
 
     # ---- rooflines ---------------------------------------------------------------------
