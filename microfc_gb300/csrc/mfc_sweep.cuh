@@ -31,8 +31,11 @@ struct SweepShape {
   static constexpr int NQ = S * NP * LA;      // primitive tile [S][pencil][LA]
   static constexpr int NW = S * NP * (TA + 2);
   static constexpr int NFL = (S + 1) * NP * (TA + 1);
-  static constexpr int NCOEF = (sizeof(RT) == 4 && WO == 5) ? kNumCoef * (TA + 2) : 0;
-  static constexpr size_t kSmemBytes = sizeof(RT) * (size_t(NQ) + 2 * size_t(NW) + size_t(NFL) + size_t(NCOEF));
+  // split precision: FP32 coefficient records of kCoefRec floats per cell (float4 loads)
+  static constexpr int NCOEF = (sizeof(RT) == 4 && WO == 5) ? kCoefRec * (TA + 2) : 0;
+  static constexpr int align16(int n) { return (n * int(sizeof(RT)) + 15) / 16 * 16 / int(sizeof(RT)); }
+  static constexpr int OC = align16(NQ + 2 * NW + NFL);
+  static constexpr size_t kSmemBytes = sizeof(RT) * (size_t(OC) + size_t(NCOEF));
 };
 
 // Pencil p of a block and position a along the sweep -> global (x, y, z).
@@ -61,7 +64,7 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const doub
   RT* wl = sq + Sh::NQ;
   RT* wr = wl + Sh::NW;
   RT* fl = wr + Sh::NW;
-  RT* sc = fl + Sh::NFL;
+  RT* sc = sq + Sh::OC;  // 16-byte aligned coefficient records
 
   const int tid = threadIdx.x;
   // block origin: blockIdx.x tiles the fastest non-sweep axis for DIR != 0
@@ -108,9 +111,12 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const doub
     }
   }
   if constexpr (Sh::NCOEF > 0) {
-    for (int it = tid; it < kNumCoef * (TA + 2); it += NT) {
+    for (int it = tid; it < kCoefRec * (TA + 2); it += NT) {
       const int ca = it % (TA + 2), k = it / (TA + 2);
-      sc[it] = d2f_bits(__ldg(P.coef[DIR] + k * P.cstride[DIR] + clamp_coef_index(a0 - 1 + ca, na) + P.coff));
+      sc[ca * kCoefRec + k] =
+          k < kNumCoef
+              ? d2f_bits(__ldg(P.coef[DIR] + k * P.cstride[DIR] + clamp_coef_index(a0 - 1 + ca, na) + P.coff))
+              : 0.f;
     }
   }
   __syncthreads();
@@ -129,10 +135,9 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const doub
       const int o = k - 2;
       stc[k] = (o >= -(WO / 2) && o <= WO / 2) ? line[la + o] : RT(0);
     }
-    RT c[kNumCoef];
+    RT c[kCoefRec];
     if constexpr (Sh::NCOEF > 0) {
-#pragma unroll
-      for (int k = 0; k < kNumCoef; ++k) c[k] = sc[k * NCA + ca];
+      load_coef_record(sc + ca * kCoefRec, c);
     } else if constexpr (WO > 1) {
       const int gi = clamp_coef_index(a0 - 1 + ca, na) + P.coff;
 #pragma unroll

@@ -91,7 +91,7 @@ def _exchange_worker(rank, world, port, out):
 def test_rank_to_rank_exchange_over_gloo():
     import torch.multiprocessing as mp
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of a threaded process
         out = m.dict()
         mp.spawn(_exchange_worker, args=(2, port, out), nprocs=2, join=True)
         assert dict(out) == {0: True, 1: True}

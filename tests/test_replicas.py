@@ -25,7 +25,7 @@ def _worker(rank, world, port, out):
 
 def test_replica_rate_is_total_work_over_the_slowest_rank():
     import torch.multiprocessing as mp
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of a threaded process
         out = m.dict()
         mp.spawn(_worker, args=(2, _free_port(), out), nprocs=2, join=True)
         assert dict(out) == {0: (2000 / 3.0, 3.0), 1: (2000 / 3.0, 3.0)}
