@@ -233,10 +233,13 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
         ens.run(0, 3, use_graph=True)  # warm-up (advances the state; timing only)
         torch.cuda.synchronize()
         nsteps = 20
-        t0 = time.perf_counter()
+        est = torch.cuda.ExternalStream(ens.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(est)  # 64 states (0.7 GB) exceed the L2: no flush needed
         ens.run(3, 3 + nsteps, use_graph=True)
+        e1.record(est)
         torch.cuda.synchronize()
-        t_ens = time.perf_counter() - t0
+        t_ens = e0.elapsed_time(e1) / 1e3
         ens_rate = ens.cells * nsteps / t_ens
     # 64 sequential plain FP64 runs: measured per size class
     seq_time = 0.0
@@ -252,7 +255,7 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
     seq_rate = sum(c.cells for c in cl) / seq_time
     out["ensemble"] = {"cases": len(cl), "cells": int(sum(c.cells for c in cl)), "precision": prec,
                        "value": ens_rate, "unit": "cell-updates/s", "steps": nsteps, "graph": True,
-                       "tile_variant": variant, "timing": "host wall clock around graph replays, synchronized",
+                       "tile_variant": variant, "timing": "CUDA events on the ensemble stream around 20 graph-replayed steps",
                        "sequential_plain_fp64": seq_rate, "vs_sequential_plain_fp64": ens_rate / seq_rate}
     return out
 
