@@ -127,16 +127,17 @@ int mfc_gpu_tvd_rk(mfc_gpu_ctx* ctx, double dt, int last_step);
 /* ---- Processor boundaries (domain decomposition, m_mpi_proxy.fpp:468-979).
  * A boundary value >= 0 in mfc_params (the neighbouring subdomain, as the
  * reference's bc_x%beg = rank) makes that side read its ghost cells from a
- * halo receive buffer instead of a physical boundary condition (1-D and
- * 2-D; the neighbour's ghost cell widths come from mfc_gpu_set_halo_widths,
- * as the reference exchanges them).  Such a context is stepped stage
+ * halo receive buffer instead of a physical boundary condition (the
+ * neighbour's ghost cell widths come from mfc_gpu_set_halo_widths, as the
+ * reference exchanges them).  Such a context is stepped stage
  * by stage: before stage s, every subdomain packs the strip next to each of
  * its processor boundaries from that stage's input (mfc_gpu_halo_pack) into
  * the neighbour's receive buffer (mfc_gpu_halo_buffer) -- directly when both
  * live on one GPU, or through a send/receive pair across GPUs -- and then
  * runs mfc_gpu_rk_stage.  mfc_gpu_tvd_rk and mfc_gpu_run refuse such a
  * context.  Layouts (depth d = 0 next to the boundary, H = (weno_order+1)/2):
- * x sides [S][n+1][H], y sides [S][H][m+1]. */
+ * x sides [S][p+1][n+1][H], y sides [S][p+1][H][m+1], z sides
+ * [S][H][n+1][m+1]. */
 int mfc_gpu_rk_stage(mfc_gpu_ctx* ctx, int stage, double dt);
 int mfc_gpu_halo_buffer(mfc_gpu_ctx* ctx, int dir, int side, double** dev_ptr, int64_t* count);
 /* The neighbour's cell widths beyond a processor boundary (widths[i] = ghost

@@ -134,28 +134,34 @@ __global__ void prim_kernel(const mfc::DevParams P, const double* __restrict__ q
   }
 }
 
-// Boundary strip of a stage input for the neighbour across (dir, side):
-// depth d = 0 is the cell next to the boundary.  dir 0: dst[S][ny][H],
-// dir 1: dst[S][H][nx] (the neighbour's halo layout).
-__global__ void halo_pack_kernel(const double* __restrict__ q, int S, int nx, int ny, int64_t sy, int64_t sv, int H,
-                                 int dir, int side, double* __restrict__ dst) {
-  const int across = dir == 0 ? ny : nx;
-  const int64_t total = (int64_t)S * H * across;
+// Boundary strip of a stage input for the neighbour across (dir, side), in
+// the neighbour's halo layout (depth d = 0 is the cell next to the
+// boundary): dir 0 [S][nz][ny][H], dir 1 [S][nz][H][nx], dir 2 [S][H][ny][nx].
+__global__ void halo_pack_kernel(const double* __restrict__ q, int S, int nx, int ny, int nz, int64_t sy, int64_t sz,
+                                 int64_t sv, int H, int dir, int side, double* __restrict__ dst) {
+  const int64_t total = (int64_t)S * H * (dir == 0 ? (int64_t)ny * nz : dir == 1 ? (int64_t)nx * nz : (int64_t)nx * ny);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    int v, a, d;
+    int x, y, z, d, v;
     if (dir == 0) {
       d = (int)(i % H);
-      a = (int)((i / H) % across);
-      v = (int)(i / ((int64_t)H * across));
-      const int x = side == 0 ? d : nx - 1 - d;
-      dst[i] = q[v * sv + a * sy + x];
+      y = (int)((i / H) % ny);
+      z = (int)((i / ((int64_t)H * ny)) % nz);
+      v = (int)(i / ((int64_t)H * ny * nz));
+      x = side == 0 ? d : nx - 1 - d;
+    } else if (dir == 1) {
+      x = (int)(i % nx);
+      d = (int)((i / nx) % H);
+      z = (int)((i / ((int64_t)nx * H)) % nz);
+      v = (int)(i / ((int64_t)nx * H * nz));
+      y = side == 0 ? d : ny - 1 - d;
     } else {
-      a = (int)(i % across);
-      d = (int)((i / across) % H);
-      v = (int)(i / ((int64_t)H * across));
-      const int y = side == 0 ? d : ny - 1 - d;
-      dst[i] = q[v * sv + y * sy + a];
+      x = (int)(i % nx);
+      y = (int)((i / nx) % ny);
+      d = (int)((i / ((int64_t)nx * ny)) % H);
+      v = (int)(i / ((int64_t)nx * ny * H));
+      z = side == 0 ? d : nz - 1 - d;
     }
+    dst[i] = q[v * sv + z * sz + y * sy + x];
   }
 }
 
@@ -261,7 +267,8 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
       if ((side == 0 ? bcb[d] : bce[d]) < 0) continue;
       c->has_proc = true;
       const int k = 2 * d + side;
-      c->halo_count[k] = (int64_t)c->S * c->H * (d == 0 ? c->n[1] : c->n[0]);
+      c->halo_count[k] = (int64_t)c->S * c->H * (d == 0 ? (int64_t)c->n[1] * c->n[2]
+                                                 : d == 1 ? (int64_t)c->n[0] * c->n[2] : (int64_t)c->n[0] * c->n[1]);
       if ((e = cudaMalloc(&c->halo_buf[k], sizeof(double) * c->halo_count[k])) != cudaSuccess)
         return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
       cudaMemsetAsync(c->halo_buf[k], 0, sizeof(double) * c->halo_count[k], c->stream);
@@ -471,14 +478,18 @@ int mfc_gpu_set_halo_widths(mfc_gpu_ctx* c, int dir, int side, const double* wid
 }
 
 int mfc_gpu_halo_pack(mfc_gpu_ctx* c, int stage, int dir, int side, double* dst) {
-  if (!c || !dst || dir < 0 || dir >= c->nd || dir > 1 || side < 0 || side > 1)
+  if (!c || !dst || dir < 0 || dir >= c->nd || side < 0 || side > 1)
     return fail(MFC_ERR_INVALID, "bad halo pack arguments");
   if (stage < 0 || stage >= c->prm.time_stepper) return fail(MFC_ERR_INVALID, "stage out of range");
   const double* q = stage == 0 ? c->reg[0] : stage == 1 ? c->reg[1] : c->reg[2];
-  const int across = dir == 0 ? c->n[1] : c->n[0];
-  const int64_t total = (int64_t)c->S * c->H * across;
+  const int64_t total = c->halo_count[2 * dir + side] > 0
+                            ? c->halo_count[2 * dir + side]
+                            : (int64_t)c->S * c->H *
+                                  (dir == 0 ? (int64_t)c->n[1] * c->n[2]
+                                            : dir == 1 ? (int64_t)c->n[0] * c->n[2] : (int64_t)c->n[0] * c->n[1]);
   const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 8);
-  halo_pack_kernel<<<blocks, 256, 0, c->stream>>>(q, c->S, c->n[0], c->n[1], c->sy, c->sv, c->H, dir, side, dst);
+  halo_pack_kernel<<<blocks, 256, 0, c->stream>>>(q, c->S, c->n[0], c->n[1], c->n[2], c->sy, c->sz, c->sv, c->H,
+                                                  dir, side, dst);
   MFC_CUDA(cudaGetLastError());
   c->launches += 1;
   return MFC_OK;

@@ -170,7 +170,7 @@ inline std::string build_grid_tables(const mfc_params* p, int nd, const int* n, 
 
 // The checks of s_check_input_file that apply to the hot path.
 // allow_processor: boundary values >= 0 (a neighbouring subdomain, exchanged
-// through halo buffers) are accepted, in 1-D and 2-D.
+// through halo buffers) are accepted.
 inline std::string validate_params(const mfc_params* p, bool allow_processor = false) {
   if (!p) return "params is NULL";
   if (p->m <= 0) return "Unsupported value of m";
@@ -194,9 +194,6 @@ inline std::string validate_params(const mfc_params* p, bool allow_processor = f
     }
     if ((bcs[2 * d] == -1) != (bcs[2 * d + 1] == -1)) return "Periodic boundaries must be set at both ends";
   }
-  const bool proc = bcs[0] >= 0 || bcs[1] >= 0 || (ndim > 1 && (bcs[2] >= 0 || bcs[3] >= 0)) ||
-                    (ndim > 2 && (bcs[4] >= 0 || bcs[5] >= 0));
-  if (proc && ndim > 2) return "processor boundaries are supported in 1-D and 2-D";
   for (int f = 0; f < p->num_fluids; ++f) {
     if (!(p->gammas[f] > 0.0)) return "Unsupported value of fluid_pp%gamma";
     if (p->pi_infs[f] < 0.0) return "Unsupported value of fluid_pp%pi_inf";

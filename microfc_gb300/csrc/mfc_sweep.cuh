@@ -90,13 +90,31 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const doub
     if (DIR == 0) { la = it % LA; pb = (it / LA) % TB; pc = it / (LA * TB); }
     else { pb = it % TB; la = (it / TB) % LA; pc = it / (TB * LA); }
     bool fa = false, dummy = false;
-    const int ga = map_cell(a0 - H + la, na, P.bc_beg[OA], P.bc_end[OA], &fa);
+    const int ra = a0 - H + la;
+    // processor boundary along the sweep: the ghost cell comes from the
+    // neighbour's halo buffer (x: [S][nz][ny][H], y: [S][nz][H][nx],
+    // z: [S][H][ny][nx]; depth 0 next to the boundary)
+    const int side = ra < 0 ? (P.bc_beg[OA] >= 0 ? 0 : -1) : (ra >= na && P.bc_end[OA] >= 0 ? 1 : -1);
     const int gb = map_cell(b0 + pb, nb, P.bc_beg[OB], P.bc_end[OB], &dummy);
     const int gc = map_cell(c0 + pc, nc, P.bc_beg[OC], P.bc_end[OC], &dummy);
-    const double* src = qin + ga * st[OA] + gb * st[OB] + gc * st[OC];
+    const double* src;
+    int64_t vs = P.sv;
+    if (side >= 0) {
+      const int d = min(side == 0 ? -1 - ra : ra - na, H - 1);  // deeper cells of partial tiles are never stored
+      int x, y, z;
+      sweep_coords<DIR>(d, gb, gc, x, y, z);
+      const int nx = P.n[0], ny = P.n[1], nz = P.n[2];
+      const double* h = P.halo[2 * DIR + side];
+      if (DIR == 0) { src = h + ((int64_t)z * ny + y) * H + d; vs = (int64_t)nz * ny * H; }
+      else if (DIR == 1) { src = h + ((int64_t)z * H + d) * nx + x; vs = (int64_t)nz * H * nx; }
+      else { src = h + ((int64_t)d * ny + y) * nx + x; vs = (int64_t)H * ny * nx; }
+    } else {
+      const int ga = map_cell(ra, na, P.bc_beg[OA], P.bc_end[OA], &fa);
+      src = qin + ga * st[OA] + gb * st[OB] + gc * st[OC];
+    }
     double q[S];
 #pragma unroll
-    for (int v = 0; v < S; ++v) q[v] = __ldg(src + v * P.sv);
+    for (int v = 0; v < S; ++v) q[v] = __ldg(src + v * vs);
     if (fa) q[Q::MOM + DIR] = -q[Q::MOM + DIR];
     const int p = pc * TB + pb;
     if constexpr (kSplit) {

@@ -3,9 +3,10 @@
 ``decompose`` splits a case the way s_mpi_decompose_computational_domain
 does (src/simulation/m_mpi_proxy.fpp:134-328): (m+1) // p cells per
 subdomain, the first (m+1) % p subdomains one more, subdomains ordered x
-fastest, a processor boundary (the neighbour's rank, >= 0) wherever a
-subdomain meets another one, and the physical boundary conditions (a
-periodic one wrapping around to the far subdomain) elsewhere.
+fastest, then y, then z, a processor boundary (the neighbour's rank, >= 0)
+wherever a subdomain meets another one, and the physical boundary
+conditions (a periodic one wrapping around to the far subdomain) elsewhere.
+The reference decomposes in x and y; z follows the same rule.
 
 Every RK stage needs the neighbours' strips of that stage's input (the
 halo exchange of s_populate_conservative_variables_buffers, m_rhs.fpp:434
@@ -31,17 +32,19 @@ from .solver import _dp
 @dataclass
 class Subdomain:
     rank: int
-    coords: tuple            # (ix, iy)
-    start: tuple             # first global cell (x, y)
-    case: Case               # the subdomain's case: local m, n and boundary conditions
+    coords: tuple            # (ix, iy, iz)
+    start: tuple             # first global cell (x, y, z)
+    case: Case               # the subdomain's case: local m, n, p and boundary conditions
     x_cb: np.ndarray
     y_cb: np.ndarray | None
+    z_cb: np.ndarray | None = None
     neighbors: dict = field(default_factory=dict)  # (dir, side) -> rank
 
     def window(self):
-        """Slices of the global [S, 1, n+1, m+1] state this subdomain holds."""
-        sx, sy = self.start
-        return (slice(None), slice(None), slice(sy, sy + self.case.n + 1), slice(sx, sx + self.case.m + 1))
+        """Slices of the global [S, p+1, n+1, m+1] state this subdomain holds."""
+        sx, sy, sz = self.start
+        c = self.case
+        return (slice(None), slice(sz, sz + c.p + 1), slice(sy, sy + c.n + 1), slice(sx, sx + c.m + 1))
 
 
 def _split(count: int, parts: int):
@@ -51,59 +54,67 @@ def _split(count: int, parts: int):
     return sizes, starts
 
 
-def decompose(case: Case, x_cb, y_cb=None, px: int = 2, py: int = 1) -> list[Subdomain]:
-    """Subdomains of a 1-D or 2-D case on a px x py process grid."""
-    if case.p > 0:
-        raise ValueError("decomposition is supported for 1-D and 2-D cases")
+def decompose(case: Case, x_cb, y_cb=None, px: int = 2, py: int = 1, pz: int = 1, z_cb=None) -> list[Subdomain]:
+    """Subdomains of a case on a px x py x pz process grid."""
     if case.n == 0 and py != 1:
         raise ValueError("a 1-D case decomposes along x only")
-    sx, ox = _split(case.m + 1, px)
-    sy, oy = _split(case.n + 1, py)
-    if min(sx) < 5 * case.weno_order or (case.n > 0 and min(sy) < 5 * case.weno_order):
-        raise ValueError("subdomains too small for the WENO stencil")
+    if case.p == 0 and pz != 1:
+        raise ValueError("a 2-D case does not decompose along z")
+    parts = (px, py, pz)
+    counts = (case.m + 1, case.n + 1, case.p + 1)
+    used = (True, case.n > 0, case.p > 0)
+    splits = [_split(counts[d], parts[d]) for d in range(3)]
+    for d in range(3):
+        if used[d] and min(splits[d][0]) < 5 * case.weno_order:
+            raise ValueError("subdomains too small for the WENO stencil")
+    cbs = (x_cb, y_cb, z_cb)
     subs = []
-    for iy in range(py):
-        for ix in range(px):
-            rank = iy * px + ix
-            bx, by = list(case.bc_x), list(case.bc_y)
-            nb = {}
-
-            def link(d, side, coord, count, bc, other):
-                if (side == 0 and coord > 0) or (side == 1 and coord < count - 1) or (bc[side] == -1 and count > 1):
-                    nb[(d, side)] = other
-                    bc[side] = other
-
-            link(0, 0, ix, px, bx, iy * px + (ix - 1) % px)
-            link(0, 1, ix, px, bx, iy * px + (ix + 1) % px)
-            if case.n > 0:
-                link(1, 0, iy, py, by, ((iy - 1) % py) * px + ix)
-                link(1, 1, iy, py, by, ((iy + 1) % py) * px + ix)
-            sub_case = case.replace(m=sx[ix] - 1, n=(sy[iy] - 1) if case.n > 0 else 0, bc_x=tuple(bx),
-                                    bc_y=tuple(by), name=f"{case.name}_p{rank}")
-            xs = np.asarray(x_cb)[ox[ix]:ox[ix] + sx[ix] + 1]
-            ys = None if y_cb is None or case.n == 0 else np.asarray(y_cb)[oy[iy]:oy[iy] + sy[iy] + 1]
-            subs.append(Subdomain(rank, (ix, iy), (ox[ix], oy[iy]), sub_case, xs, ys, nb))
+    for iz in range(pz):
+        for iy in range(py):
+            for ix in range(px):
+                coords = (ix, iy, iz)
+                rank = (iz * py + iy) * px + ix
+                bcs = [list(case.bc_x), list(case.bc_y), list(case.bc_z)]
+                nb = {}
+                for d in range(3):
+                    if not used[d]:
+                        continue
+                    for side in (0, 1):
+                        c, n = coords[d], parts[d]
+                        inner = (side == 0 and c > 0) or (side == 1 and c < n - 1)
+                        if inner or (bcs[d][side] == -1 and n > 1):
+                            o = list(coords)
+                            o[d] = (c - 1) % n if side == 0 else (c + 1) % n
+                            other = (o[2] * py + o[1]) * px + o[0]
+                            nb[(d, side)] = other
+                            bcs[d][side] = other
+                sizes = [splits[d][0][coords[d]] for d in range(3)]
+                starts = [splits[d][1][coords[d]] for d in range(3)]
+                sub_case = case.replace(m=sizes[0] - 1, n=(sizes[1] - 1) if used[1] else 0,
+                                        p=(sizes[2] - 1) if used[2] else 0, bc_x=tuple(bcs[0]), bc_y=tuple(bcs[1]),
+                                        bc_z=tuple(bcs[2]), name=f"{case.name}_p{rank}")
+                loc = [None if (cbs[d] is None or not used[d]) else
+                       np.asarray(cbs[d])[starts[d]:starts[d] + sizes[d] + 1] for d in range(3)]
+                subs.append(Subdomain(rank, coords, tuple(starts), sub_case, loc[0], loc[1], loc[2], nb))
     return subs
 
 
 def halo_strip(sub: Subdomain, q_local: np.ndarray, d: int, side: int, H: int) -> np.ndarray:
     """Host restatement of mfc_gpu_halo_pack: the strip of a local state
-    [S, 1, n+1, m+1] that the neighbour across (d, side) needs, in its
-    receive-buffer layout (x: [S][n+1][H], y: [S][H][m+1]; depth 0 next to
-    the boundary)."""
-    q = q_local[:, 0]
-    if d == 0:
-        cols = [k if side == 0 else q.shape[2] - 1 - k for k in range(H)]
-        return np.stack([q[:, :, c] for c in cols], axis=-1)
-    rows = [k if side == 0 else q.shape[1] - 1 - k for k in range(H)]
-    return np.stack([q[:, r, :] for r in rows], axis=1)
+    [S, p+1, n+1, m+1] that the neighbour across (d, side) needs, in its
+    receive-buffer layout (depth 0 next to the boundary): x [S][p+1][n+1][H],
+    y [S][p+1][H][m+1], z [S][H][n+1][m+1]."""
+    axis = 3 - d  # array axis of direction d
+    n = q_local.shape[axis]
+    idx = [k if side == 0 else n - 1 - k for k in range(H)]
+    return np.ascontiguousarray(np.take(q_local, idx, axis=axis))  # depth replaces the axis
 
 
 def ghost_widths(neighbor: Subdomain, d: int, side: int, b: int) -> np.ndarray:
     """The b cell widths of `neighbor` next to the boundary it shares with a
     subdomain whose side `side` faces it (depth 0 first): what the reference
     sends in s_mpi_sendrecv_grid_variables_buffers (m_mpi_proxy.fpp:338-458)."""
-    w = np.diff(np.asarray(neighbor.x_cb if d == 0 else neighbor.y_cb))
+    w = np.diff(np.asarray((neighbor.x_cb, neighbor.y_cb, neighbor.z_cb)[d]))
     return np.ascontiguousarray(w[::-1][:b] if side == 0 else w[:b])
 
 
@@ -131,15 +142,15 @@ class MultiDomain:
     """All subdomains of a decomposed case on one GPU, stepped with a halo
     exchange before every RK stage; bit-identical to the undecomposed run."""
 
-    def __init__(self, case: Case, x_cb, y_cb=None, q_cons=None, px: int = 2, py: int = 1, device: int = 0):
+    def __init__(self, case: Case, x_cb, y_cb=None, q_cons=None, px: int = 2, py: int = 1, pz: int = 1,
+                 z_cb=None, device: int = 0):
         from .solver import Simulation
         self.case = case
-        self.subs = decompose(case, x_cb, y_cb, px, py)
+        self.subs = decompose(case, x_cb, y_cb, px, py, pz, z_cb)
         self.sims = []
         for s in self.subs:
             q = None if q_cons is None else np.ascontiguousarray(q_cons[s.window()])
-            self.sims.append(Simulation(s.case, s.x_cb, s.y_cb, q_cons=q, device=device, check=False))
-        self.H = (case.weno_order + 1) // 2
+            self.sims.append(Simulation(s.case, s.x_cb, s.y_cb, s.z_cb, q_cons=q, device=device, check=False))
         self.L = _lib.load()
         b = (case.weno_order - 1) // 2 + 2  # buff_size
         for s, sim in zip(self.subs, self.sims):

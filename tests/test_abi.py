@@ -69,19 +69,6 @@ def test_init_rejects_invalid_cases_without_touching_the_device(field, value, ms
     assert msg in L.mfc_gpu_last_error().decode()
 
 
-def test_processor_boundaries_are_1d_and_2d_only():
-    L = _lib.load()
-    case = cases.shock_bubble_3d(N=28, steps=2, precision="fp64")
-    x_cb, y_cb, z_cb, _ = preprocess.generate(case)
-    P = _params(case, x_cb, y_cb)
-    P.p = case.p
-    P.z_cb = z_cb.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-    P.bc_x_end = 1  # neighbouring subdomain
-    h = ctypes.c_void_p()
-    assert L.mfc_gpu_init(ctypes.byref(P), ctypes.byref(h)) == _lib.MFC_ERR_INVALID
-    assert "1-D and 2-D" in L.mfc_gpu_last_error().decode()
-
-
 def test_null_context_calls_fail_cleanly():
     L = _lib.load()
     assert L.mfc_gpu_tvd_rk(None, 1.0, 0) == _lib.MFC_ERR_INVALID

@@ -36,7 +36,7 @@ def test_2d_grid_of_subdomains_and_halo_strips():
     c = cases.shock_droplet_2d(nx=128, ny=64, steps=2)
     x_cb, y_cb, _, q = preprocess.generate(c)
     subs = decomp.decompose(c, x_cb, y_cb, px=2, py=2)
-    assert [s.coords for s in subs] == [(0, 0), (1, 0), (0, 1), (1, 1)]
+    assert [s.coords for s in subs] == [(0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0)]
     assert subs[0].neighbors == {(0, 1): 1, (1, 1): 2}
     assert subs[3].neighbors == {(0, 0): 2, (1, 0): 1}
     H = 3
@@ -50,11 +50,11 @@ def test_2d_grid_of_subdomains_and_halo_strips():
                 if d == 0:
                     gx = o.start[0] - 1 - k if side == 1 else o.start[0] + o.case.m + 1 + k
                     ref = q[:, 0, o.start[1]:o.start[1] + o.case.n + 1, gx]
-                    assert np.array_equal(strip[:, :, k], ref)
+                    assert np.array_equal(strip[:, 0, :, k], ref)
                 else:
                     gy = o.start[1] - 1 - k if side == 1 else o.start[1] + o.case.n + 1 + k
                     ref = q[:, 0, gy, o.start[0]:o.start[0] + o.case.m + 1]
-                    assert np.array_equal(strip[:, k, :], ref)
+                    assert np.array_equal(strip[:, 0, k, :], ref)
 
 
 def _free_port():
@@ -118,6 +118,34 @@ def test_subdomains_on_one_gpu_reproduce_the_whole_domain(kind):
         md.run(0, 20)
         got = md.download()
     assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "split"])
+def test_3d_subdomains_reproduce_the_whole_domain(prec):
+    from microfc_gb300 import Simulation
+    c = cases.shock_bubble_3d(N=52, steps=5, precision=prec).replace(m=53, n=51, p=52)
+    x_cb, y_cb, z_cb, q = preprocess.generate(c)
+    with Simulation(c, x_cb, y_cb, z_cb, q_cons=q) as sim:
+        sim.run(0, 5)
+        ref = sim.download()
+    with decomp.MultiDomain(c, x_cb, y_cb, q_cons=q, px=2, py=1, pz=2, z_cb=z_cb) as md:
+        md.run(0, 5)
+        got = md.download()
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+
+
+def test_3d_split_and_strips():
+    c = cases.shock_bubble_3d(N=52, steps=2, precision="fp64").replace(m=53, n=51, p=52)
+    x_cb, y_cb, z_cb, q = preprocess.generate(c)
+    subs = decomp.decompose(c, x_cb, y_cb, px=2, py=2, pz=2, z_cb=z_cb)
+    assert len(subs) == 8 and subs[7].coords == (1, 1, 1) and subs[7].start == (27, 26, 27)
+    assert subs[0].neighbors == {(0, 1): 1, (1, 1): 2, (2, 1): 4}
+    s, o = subs[0], subs[4]  # z neighbours
+    strip = decomp.halo_strip(s, q[s.window()], 2, 1, 3)
+    assert strip.shape == (c.sys_size, 3, s.case.n + 1, s.case.m + 1)
+    for k in range(3):
+        assert np.array_equal(strip[:, k], q[:, o.start[2] - 1 - k, :s.case.n + 1, :s.case.m + 1])
 
 
 @pytest.mark.gpu
