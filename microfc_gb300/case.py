@@ -57,11 +57,17 @@ class Case:
     bc_z: tuple = (DFLT_INT, DFLT_INT)
     gammas: tuple = ()                  # fluid_pp(i)%gamma  = 1/(gamma_i - 1)
     pi_infs: tuple = ()                 # fluid_pp(i)%pi_inf = gamma_i*pi_inf_i/(gamma_i - 1)
+    re_shear: tuple = ()                # fluid_pp(i)%Re(1), shear Reynolds number (<= 0 or absent: inviscid)
+    re_bulk: tuple = ()                 # fluid_pp(i)%Re(2), bulk Reynolds number
     patches: list = field(default_factory=list)
     precision: str = "fp64"             # "fp64", "split" or "gated" (split + learned WENO gate)
     name: str = "case"
 
     # index layout, m_global_parameters.fpp:302-310
+    @property
+    def viscous(self) -> bool:
+        return any(r > 0 for r in tuple(self.re_shear) + tuple(self.re_bulk))
+
     @property
     def num_dims(self) -> int:
         return 1 + min(1, self.n) + min(1, self.p)
@@ -168,10 +174,18 @@ class Case:
         nf = int(g.get("num_fluids", 1))
         gam = [0.0] * nf
         pinf = [0.0] * nf
+        res = [[0.0] * nf, [0.0] * nf]
         patches: dict[int, dict] = {}
         rx = re.compile(r"patch_icpp\((\d+)\)%(\w+)(?:\((\d+)\))?")
         rf = re.compile(r"fluid_pp\((\d+)\)%(\w+)")
+        rre = re.compile(r"fluid_pp\((\d+)\)%Re\(([12])\)")
         for k, v in g.items():
+            mr = rre.fullmatch(k)
+            if mr:
+                i = int(mr.group(1)) - 1
+                if i < nf:
+                    res[int(mr.group(2)) - 1][i] = float(v)
+                continue
             mf = rf.fullmatch(k)
             if mf:
                 i = int(mf.group(1)) - 1
@@ -223,7 +237,7 @@ class Case:
             num_fluids=nf, time_stepper=int(g.get("time_stepper", 3)),
             weno_order=int(g.get("weno_order", 5)), weno_eps=float(g.get("weno_eps", 1e-16)),
             bc_x=(int(g.get("bc_x%beg", -3)), int(g.get("bc_x%end", -3))), bc_y=bcy, bc_z=bcz,
-            gammas=tuple(gam), pi_infs=tuple(pinf), patches=plist,
+            gammas=tuple(gam), pi_infs=tuple(pinf), re_shear=tuple(res[0]), re_bulk=tuple(res[1]), patches=plist,
             precision=str(g.get("gpu_precision", "fp64")), name=str(g.get("case_name", "case")))
 
     def to_namelist(self) -> str:

@@ -37,6 +37,8 @@ class MfoParams(ctypes.Structure):
         ("bc_z_beg", ctypes.c_int), ("bc_z_end", ctypes.c_int),
         ("gammas", ctypes.c_double * MAX_FLUIDS),
         ("pi_infs", ctypes.c_double * MAX_FLUIDS),
+        ("re_shear", ctypes.c_double * MAX_FLUIDS),
+        ("re_bulk", ctypes.c_double * MAX_FLUIDS),
     ]
 
 
@@ -121,6 +123,10 @@ def params_from_case(case) -> MfoParams:
     for i, (g, pi) in enumerate(zip(case.gammas, case.pi_infs)):
         q.gammas[i] = g
         q.pi_infs[i] = pi
+    for i, r in enumerate(getattr(case, "re_shear", ())):
+        q.re_shear[i] = r
+    for i, r in enumerate(getattr(case, "re_bulk", ())):
+        q.re_bulk[i] = r
     return q
 
 

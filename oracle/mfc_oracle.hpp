@@ -57,10 +57,25 @@ struct Params {
   int bc_z_beg = -3, bc_z_end = -3;
   double gammas[kMaxFluids] = {0};   // fluid_pp(i)%gamma  = 1/(gamma_i - 1)
   double pi_infs[kMaxFluids] = {0};  // fluid_pp(i)%pi_inf = gamma_i pi_inf_i/(gamma_i - 1)
+  double re[2][kMaxFluids] = {};     // fluid_pp(i)%Re(1:2), shear and bulk; <= 0: none
 
   int num_dims() const { return 1 + (n > 0) + (p > 0); }
   int weno_polyn() const { return (weno_order - 1) / 2; }
-  int buff_size() const { return weno_polyn() + 2; }  // m_global_parameters.fpp:356-360 (inviscid)
+  // Re_size / Re_idx of m_global_parameters.fpp:300-336: the fluids with a
+  // positive Reynolds number, in index order
+  int re_size(int i) const {
+    int c = 0;
+    for (int f = 0; f < num_fluids; ++f) c += re[i][f] > 0.0;
+    return c;
+  }
+  int re_idx(int i, int q) const {
+    for (int f = 0; f < num_fluids; ++f)
+      if (re[i][f] > 0.0 && q-- == 0) return f;
+    return -1;
+  }
+  bool viscous() const { return re_size(0) > 0 || re_size(1) > 0; }
+  // m_global_parameters.fpp:354-359
+  int buff_size() const { return viscous() ? 2 * weno_polyn() + 2 : weno_polyn() + 2; }
   int cont_end() const { return num_fluids; }          // contxe
   int mom_beg() const { return num_fluids + 1; }       // momxb (1-based)
   int E_idx() const { return num_fluids + num_dims() + 1; }
@@ -218,6 +233,7 @@ struct Solver {
   std::vector<Field<R>> vL, vR;        // WENO face values, one direction at a time
   std::vector<Field<R>> flux;          // flux at face j+1/2 stored at j
   Field<R> fsrc;                       // interface velocity at face j+1/2
+  Field<R> vflux[3];                   // viscous source flux at face j+1/2: x-momentum, y-momentum, energy
   double dt = 0;
 
   void init(const Params& p, const double* x_cb, const double* y_cb, const double* z_cb) {
@@ -257,6 +273,86 @@ struct Solver {
       rhs[v].alloc(0, P.m, 0, P.n, 0, P.p);
     }
     fsrc.alloc(xb, xe, yb, ye, zb, ze);
+    if (P.viscous())
+      for (auto& f : vflux) f.alloc(xb, xe, yb, ye, zb, ze);
+  }
+
+  // Velocity component c of a cell (primitive, after cons_to_prim).
+  R U(int c, int i, int j) const { return qp[P.mom_beg() - 1 + c](i, j, 0); }
+  // The one-sided velocity gradients of s_get_viscous (m_viscous.fpp:212-264,
+  // weno_Re_flux = F): dqL_prim_dx_n(1) = L, dqR_prim_dx_n(1) = R.
+  R Lx(int c, int i, int j) { return (U(c, i, j) - U(c, i - 1, j)) / (ax[0].CC(i) - ax[0].CC(i - 1)); }
+  R Rx(int c, int i, int j) { return (U(c, i + 1, j) - U(c, i, j)) / (ax[0].CC(i + 1) - ax[0].CC(i)); }
+  R Ly(int c, int i, int j) { return (U(c, i, j) - U(c, i, j - 1)) / (ax[1].CC(j) - ax[1].CC(j - 1)); }
+  R Ry(int c, int i, int j) { return (U(c, i, j + 1) - U(c, i, j)) / (ax[1].CC(j + 1) - ax[1].CC(j)); }
+
+  // Viscous source flux of the face between (i,j) and its neighbour along dir,
+  // s_compute_viscous_source_flux (m_riemann_solvers.fpp:683-902), with the
+  // face gradients of s_get_viscous (m_viscous.fpp:159-370): the arithmetic
+  // means of the left and right face values, which are the same numbers, and
+  // the cross derivatives averaged over four one-sided gradients
+  // (m_viscous.fpp:266-332).  re_avg: Re_avg(1:2); vs: vel_src(1:2).
+  void viscous_flux(int dir, int i, int j, const R (&re_avg)[2], const R (&vs)[3], R (&out)[3]) {
+    R dx[2] = {R(0), R(0)}, dy[2] = {R(0), R(0)};
+    const int ndv = nd;
+    if (dir == 0) {
+      for (int c = 0; c < ndv; ++c) dx[c] = R(0.5) * (Rx(c, i, j) + Lx(c, i + 1, j));
+      if (nd > 1)
+        for (int c = 0; c < ndv; ++c) {
+          const R A = R(0.25) * (Ly(c, i + 1, j) + Ry(c, i + 1, j) + Ly(c, i, j) + Ry(c, i, j));
+          dy[c] = R(0.5) * (A + A);
+        }
+    } else {
+      for (int c = 0; c < ndv; ++c) {
+        const R A = R(0.25) * (Lx(c, i, j + 1) + Rx(c, i, j + 1) + Lx(c, i, j) + Rx(c, i, j));
+        dx[c] = R(0.5) * (A + A);
+        dy[c] = R(0.5) * (Ry(c, i, j) + Ly(c, i, j + 1));
+      }
+    }
+    R fm[2] = {R(0), R(0)}, fe = R(0);
+    const bool shear = P.re_size(0) > 0, bulk = P.re_size(1) > 0;
+    if (dir == 0) {
+      if (shear) {
+        const R tau = R(4.0 / 3.0) * dx[0] / re_avg[0];
+        fm[0] = fm[0] - tau;
+        fe = fe - vs[0] * tau;
+      }
+      if (bulk) {
+        const R tau = dx[0] / re_avg[1];
+        fm[0] = fm[0] - tau;
+        fe = fe - vs[0] * tau;
+      }
+      if (nd > 1) {
+        if (shear) {
+          const R t[2] = {-(R(2.0 / 3.0) * dy[1] / re_avg[0]), (dy[0] + dx[1]) / re_avg[0]};
+          for (int c = 0; c < 2; ++c) {
+            fm[c] = fm[c] - t[c];
+            fe = fe - vs[c] * t[c];
+          }
+        }
+        if (bulk) {
+          const R tau = dy[1] / re_avg[1];
+          fm[0] = fm[0] - tau;
+          fe = fe - vs[0] * tau;
+        }
+      }
+    } else {
+      if (shear) {
+        const R t[2] = {(dy[0] + dx[1]) / re_avg[0], (R(4) * dy[1] - R(2) * dx[0]) / (R(3) * re_avg[0])};
+        for (int c = 0; c < 2; ++c) {
+          fm[c] = fm[c] - t[c];
+          fe = fe - vs[c] * t[c];
+        }
+      }
+      if (bulk) {
+        const R tau = (dx[0] + dy[1]) / re_avg[1];
+        fm[1] = fm[1] - tau;
+        fe = fe - vs[1] * tau;
+      }
+    }
+    out[0] = fm[0];
+    out[1] = fm[1];
+    out[2] = fe;
   }
 
   // Ghost-cell fill of q_cons_qp, m_rhs.fpp:686-908, extended to z.
@@ -477,6 +573,29 @@ struct Solver {
             flux[ab + f](i, j, k) = xiM * QL(ab + f) * (uL + sM * (xiL - R(1))) + xiP * QR(ab + f) * (uR + sP * (xiR - R(1)));
           // vel_src(idx1) -> flux_src(advxb)
           fsrc(i, j, k) = xiM * (uL + R(1) * sM * (xiL - R(1))) + xiP * (uR + R(1) * sP * (xiR - R(1)));
+          if (P.viscous()) {
+            // Re_L/Re_R (m_riemann_solvers.fpp:169-199), Re_avg (:225-230),
+            // vel_src of every component (:314-324)
+            R re_avg[2], vs[3] = {R(0), R(0), R(0)}, vf[3];
+            for (int r = 0; r < 2; ++r) {
+              R reL = R(-1e6), reR = R(-1e6);
+              if (P.re_size(r) > 0) reL = reR = R(0);
+              for (int q = 0; q < P.re_size(r); ++q) {
+                const int f = P.re_idx(r, q);
+                reL = QL(ab + f) / R(P.re[r][f]) + reL;
+                reR = QR(ab + f) / R(P.re[r][f]) + reR;
+              }
+              reL = R(1) / std::max(reL, R(kSgmEps));
+              reR = R(1) / std::max(reR, R(kSgmEps));
+              re_avg[r] = R(2) / (R(1) / reL + R(1) / reR);
+            }
+            for (int d = 0; d < nd; ++d) {
+              const R flg = d == dir ? R(1) : R(0);
+              vs[d] = xiM * (velL[d] + flg * sM * (xiL - R(1))) + xiP * (velR[d] + flg * sP * (xiR - R(1)));
+            }
+            viscous_flux(dir, i, j, re_avg, vs, vf);
+            for (int t = 0; t < 3; ++t) vflux[t](i, j, k) = vf[t];
+          }
         }
   }
 
@@ -501,6 +620,14 @@ struct Solver {
           for (int f = 0; f < nf; ++f)
             rhs[ab + f](i, j, k) =
                 rhs[ab + f](i, j, k) + inv * qp[ab + f](i, j, k) * (fsrc(i, j, k) - fsrc(i - di, j - dj, k - dk));
+          if (P.viscous()) {  // m_rhs.fpp:591-603, 639-651: momentum .. energy
+            const int mb = P.mom_beg() - 1;
+            for (int t = 0; t <= nd; ++t) {
+              const int v = t < nd ? mb + t : P.E_idx() - 1;
+              const Field<R>& F = vflux[t < nd ? t : 2];
+              rhs[v](i, j, k) = rhs[v](i, j, k) + inv * (F(i - di, j - dj, k - dk) - F(i, j, k));
+            }
+          }
         }
   }
 

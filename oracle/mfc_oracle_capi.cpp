@@ -29,6 +29,8 @@ struct mfo_params {
   int bc_x_beg, bc_x_end, bc_y_beg, bc_y_end, bc_z_beg, bc_z_end;
   double gammas[kMaxFluids];
   double pi_infs[kMaxFluids];
+  double re_shear[kMaxFluids];  // fluid_pp(i)%Re(1); <= 0: inviscid
+  double re_bulk[kMaxFluids];   // fluid_pp(i)%Re(2)
 };
 
 static Params to_params(const mfo_params* q) {
@@ -42,6 +44,7 @@ static Params to_params(const mfo_params* q) {
   P.bc_y_beg = q->bc_y_beg; P.bc_y_end = q->bc_y_end;
   P.bc_z_beg = q->bc_z_beg; P.bc_z_end = q->bc_z_end;
   for (int i = 0; i < kMaxFluids; ++i) { P.gammas[i] = q->gammas[i]; P.pi_infs[i] = q->pi_infs[i]; }
+  for (int i = 0; i < kMaxFluids; ++i) { P.re[0][i] = q->re_shear[i]; P.re[1][i] = q->re_bulk[i]; }
   return P;
 }
 

@@ -164,3 +164,68 @@ def test_time_loop_trims_the_last_dt_like_the_cpu_build(oracle_lib):
             dt = final - mytime
         t_step += 1
     assert dt_final == dt
+
+
+def _shear_wave(nx=64, ny=25, re=100.0, amp=0.01, bulk=0.0, steps=250, dt=2e-3):
+    """Periodic box, rho = p = 1 (gamma 1.4), v = amp sin(2 pi x): a viscous
+    shear wave that decays as exp(-(2 pi)^2 t / (Re rho)) (tau = grad u / Re)."""
+    g, pi = cases.stiffened(1.4)
+    box = Patch(geometry=3, centroid=(0.5, 0.5 * ny / nx, 0), length=(1.0, ny / nx, 0),
+                alpha_rho=(1.0,), alpha=(1.0,), vel=(0.0, 0.0, 0), pres=1.0)
+    c = Case(m=nx - 1, n=ny - 1, x_domain=(0.0, 1.0), y_domain=(0.0, ny / nx), dt=dt, t_step_stop=steps,
+             t_step_save=steps, num_fluids=1, time_stepper=3, weno_order=5, weno_eps=1e-16, bc_x=(-1, -1),
+             bc_y=(-1, -1), gammas=(g,), pi_infs=(pi,), re_shear=(re,), re_bulk=(bulk,), patches=[box],
+             name="shear_wave")
+    x_cb, y_cb, _, q = preprocess.generate(c)
+    xc = 0.5 * (x_cb[1:] + x_cb[:-1])
+    v = amp * np.sin(2 * np.pi * xc)
+    q[c.mom_idx + 1, 0] = v[None, :] * q[0, 0]               # rho v
+    q[c.E_idx, 0] = q[c.E_idx, 0] + 0.5 * q[0, 0] * v[None, :] ** 2
+    return c, x_cb, y_cb, q, xc
+
+
+def test_viscous_shear_wave_decays_at_the_kinematic_viscosity(oracle_lib):
+    c, x_cb, y_cb, q, xc = _shear_wave()
+    o = oracle_lib.Oracle(c, x_cb, y_cb)
+    o.set_state(q)
+    o.run(0, c.t_step_stop, c.dt)
+    out = o.get_state()
+    v = out[c.mom_idx + 1, 0] / out[0, 0]
+    amp = 2 * np.mean(v * np.sin(2 * np.pi * xc)[None, :])
+    t = c.t_step_stop * c.dt
+    expect = 0.01 * np.exp(-(2 * np.pi) ** 2 * t / 100.0)
+    assert amp == pytest.approx(expect, rel=5e-3), (amp, expect, 0.01)
+    # only viscous heating (second order in the amplitude) drives any x-motion
+    assert np.abs(out[c.mom_idx, 0]).max() < 1e-6
+    # inviscid, the wave keeps its amplitude up to WENO dissipation
+    ci = c.replace(re_shear=(0.0,))
+    oi = oracle_lib.Oracle(ci, x_cb, y_cb)
+    oi.set_state(q)
+    oi.run(0, ci.t_step_stop, ci.dt)
+    vi = oi.get_state()[c.mom_idx + 1, 0] / oi.get_state()[0, 0]
+    assert 2 * np.mean(vi * np.sin(2 * np.pi * xc)[None, :]) == pytest.approx(0.01, rel=2e-3)
+
+
+def test_bulk_viscosity_damps_an_acoustic_wave(oracle_lib):
+    """1-D: u = amp sin(2 pi x) launches sound waves; bulk viscosity (tau =
+    div u / Re_2) removes kinetic energy that the inviscid run keeps."""
+    c2, x_cb, y_cb, q, xc = _shear_wave()
+    ke = []
+    for bulk in (0.0, 50.0):
+        g, pi = cases.stiffened(1.4)
+        box = Patch(geometry=1, centroid=(0.5, 0, 0), length=(1.0, 0, 0), alpha_rho=(1.0,), alpha=(1.0,),
+                    vel=(0.0, 0, 0), pres=1.0)
+        c = Case(m=99, x_domain=(0.0, 1.0), dt=1e-3, t_step_stop=200, t_step_save=200, num_fluids=1,
+                 time_stepper=3, weno_order=5, weno_eps=1e-16, bc_x=(-1, -1), gammas=(g,), pi_infs=(pi,),
+                 re_bulk=(bulk,), patches=[box])
+        xb, _, _, q1 = preprocess.generate(c)
+        xcc = 0.5 * (xb[1:] + xb[:-1])
+        u = 0.01 * np.sin(2 * np.pi * xcc)
+        q1[c.mom_idx, 0, 0] = u * q1[0, 0, 0]
+        q1[c.E_idx, 0, 0] = q1[c.E_idx, 0, 0] + 0.5 * q1[0, 0, 0] * u ** 2
+        o = oracle_lib.Oracle(c, xb)
+        o.set_state(q1)
+        o.run(0, c.t_step_stop, c.dt)
+        s = o.get_state()
+        ke.append(float(np.sum(0.5 * s[c.mom_idx, 0, 0] ** 2 / s[0, 0, 0])))
+    assert ke[1] < 0.95 * ke[0], ke
