@@ -160,6 +160,15 @@ int mfc_gpu_run(mfc_gpu_ctx* ctx, int t_step_start, int t_step_stop, double* dt_
  * bits (MFC_FLAG_*) in *flags; clears them when clear != 0. */
 int mfc_gpu_status(mfc_gpu_ctx* ctx, uint32_t* flags, int clear);
 
+/* Viscous terms (m_viscous.fpp, the viscous source flux of
+ * m_riemann_solvers.fpp:683-902 and its divergence in m_rhs.fpp:591-651):
+ * re_shear[i] / re_bulk[i] are fluid_pp(i+1)%Re(1) / %Re(2) for the
+ * context's fluids (NULL or values <= 0: none).  The velocity gradients are
+ * the reference's one-sided face differences (weno_Re_flux = F).  1-D and
+ * 2-D contexts without processor boundaries; all-zero Reynolds numbers switch
+ * back to the inviscid kernels.  Call before stepping. */
+int mfc_gpu_set_viscosity(mfc_gpu_ctx* ctx, const double* re_shear, const double* re_bulk);
+
 /* Run-time stability monitor, the reference's ICFL of s_write_run_time_information
  * (src/simulation/m_data_output.fpp:178-310), fused into the last stage kernel
  * of every step: ICFL = dt / min_d(dx_d / (|u_d| + c)), maximised over the cells

@@ -47,16 +47,18 @@ void build_registry() {
     mfc::register_stage_2d_fp32(g_reg);
     mfc::register_stage_3d_fp64(g_reg);
     mfc::register_stage_3d_fp32(g_reg);
+    mfc::register_stage_visc_fp64(g_reg);
+    mfc::register_stage_visc_fp32(g_reg);
   });
 }
 
 }  // namespace
 
 namespace mfc {
-const StageEntry* find_stage(int nd, int nf, int wo, int prec) {
+const StageEntry* find_stage(int nd, int nf, int wo, int prec, bool visc) {
   build_registry();
   for (const auto& e : g_reg)
-    if (e.nd == nd && e.nf == nf && e.wo == wo && e.prec == prec) return &e;
+    if (e.nd == nd && e.nf == nf && e.wo == wo && e.prec == prec && e.visc == visc) return &e;
   return nullptr;
 }
 
@@ -93,6 +95,8 @@ struct mfc_gpu_ctx {
   const double** halo_table = nullptr;
   std::vector<double> cb_host[3];      // the cell boundaries passed at init
   std::vector<double> ghost_w[3][2];   // neighbour widths of processor boundaries
+  mfc::ViscParams* visc = nullptr;     // device copy (viscous cases)
+  size_t off_dcc[3] = {0, 0, 0};       // spacing tables inside `tables`
   mfc::DevParams dev{};
   const mfc::StageEntry* stage = nullptr;
   int64_t launches = 0;
@@ -281,6 +285,7 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
       return cleanup(fail(MFC_ERR_CUDA, cudaGetErrorString(e)));
   }
 
+  for (int d = 0; d < 3; ++d) c->off_dcc[d] = gt.off_dcc[d];
   mfc::DevParams& D = c->dev;
   D.halo = c->halo_table;
   for (int d = 0; d < 3; ++d) {
@@ -495,6 +500,39 @@ int mfc_gpu_halo_pack(mfc_gpu_ctx* c, int stage, int dir, int side, double* dst)
   return MFC_OK;
 }
 
+int mfc_gpu_set_viscosity(mfc_gpu_ctx* c, const double* re_shear, const double* re_bulk) {
+  if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  mfc::ViscParams V{};
+  const int nf = c->prm.num_fluids;
+  for (int f = 0; f < nf; ++f) {
+    V.res[0][f] = re_shear ? re_shear[f] : 0.0;
+    V.res[1][f] = re_bulk ? re_bulk[f] : 0.0;
+  }
+  for (int r = 0; r < 2; ++r)
+    for (int f = 0; f < nf; ++f)
+      if (V.res[r][f] > 0.0) V.re_idx[r][V.re_size[r]++] = f;
+  const bool on = V.re_size[0] > 0 || V.re_size[1] > 0;
+  if (!on) {  // back to the inviscid kernels
+    cudaFree(c->visc);
+    c->visc = nullptr;
+    c->dev.visc = nullptr;
+    c->stage = mfc::find_stage(c->nd, nf, c->prm.weno_order, c->prm.precision);
+    return MFC_OK;
+  }
+  if (c->nd > 2) return fail(MFC_ERR_INVALID, "viscous terms are built for 1-D and 2-D cases");
+  if (c->has_proc) return fail(MFC_ERR_INVALID, "viscous terms with processor boundaries are not supported");
+  const mfc::StageEntry* e = mfc::find_stage(c->nd, nf, c->prm.weno_order, c->prm.precision, true);
+  if (!e) return fail(MFC_ERR_INVALID, "no viscous kernel compiled for this fluid count / WENO order / precision");
+  for (int d = 0; d < c->nd; ++d) V.dcc[d] = c->tables + c->off_dcc[d];
+  if (!c->visc && cudaMalloc(&c->visc, sizeof(mfc::ViscParams)) != cudaSuccess)
+    return fail(MFC_ERR_NOMEM, "viscous parameters");
+  MFC_CUDA(cudaMemcpy(c->visc, &V, sizeof(V), cudaMemcpyHostToDevice));
+  if (e->prepare() != cudaSuccess) return fail(MFC_ERR_CUDA, "viscous kernel does not fit on this device");
+  c->dev.visc = c->visc;
+  c->stage = e;
+  return MFC_OK;
+}
+
 int mfc_gpu_set_monitor(mfc_gpu_ctx* c, int on) {
   if (!c) return fail(MFC_ERR_INVALID, "NULL context");
   c->monitor_on = on != 0;
@@ -581,7 +619,8 @@ int mfc_gpu_tune(mfc_gpu_ctx* c, int reps, int* variant_out, double* ms_out) {
   MFC_CUDA(cudaEventCreate(&a));
   MFC_CUDA(cudaEventCreate(&b));
   for (const auto& e : g_reg) {
-    if (e.nd != c->nd || e.nf != c->prm.num_fluids || e.wo != c->prm.weno_order || e.prec != c->prm.precision)
+    if (e.nd != c->nd || e.nf != c->prm.num_fluids || e.wo != c->prm.weno_order || e.prec != c->prm.precision ||
+        e.visc != (c->visc != nullptr))
       continue;
     ++idx;
     if (e.prepare() != cudaSuccess) continue;
@@ -615,7 +654,8 @@ int mfc_gpu_select_variant(mfc_gpu_ctx* c, int variant, int* tx, int* ty, int* t
   if (!c) return fail(MFC_ERR_INVALID, "NULL context");
   int idx = -1;
   for (const auto& e : g_reg) {
-    if (e.nd != c->nd || e.nf != c->prm.num_fluids || e.wo != c->prm.weno_order || e.prec != c->prm.precision)
+    if (e.nd != c->nd || e.nf != c->prm.num_fluids || e.wo != c->prm.weno_order || e.prec != c->prm.precision ||
+        e.visc != (c->visc != nullptr))
       continue;
     if (++idx != variant) continue;
     if (e.prepare() != cudaSuccess) return fail(MFC_ERR_CUDA, "tile variant does not fit on this device");
@@ -700,6 +740,7 @@ int mfc_gpu_finalize(mfc_gpu_ctx* c) {
   if (c->snap_staged) cudaEventDestroy(c->snap_staged);
   for (int k = 0; k < 6; ++k) cudaFree(c->halo_buf[k]);
   cudaFree(c->halo_table);
+  cudaFree(c->visc);
   for (int s2 = 0; s2 < 2; ++s2) {
     if (c->snap_done[s2]) cudaEventDestroy(c->snap_done[s2]);
     if (c->snap_host[s2]) cudaFreeHost(c->snap_host[s2]);

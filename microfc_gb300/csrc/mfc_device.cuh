@@ -39,6 +39,19 @@ struct DevParams {
   // fastest), y sides: [S][H][nx]; depth d = 0 is the ghost cell next to the
   // boundary.
   const double* const* halo;
+  const struct ViscParams* visc;  // viscous cases: Reynolds numbers and spacing tables (NULL: inviscid)
+};
+
+// Viscous parameters: fluid_pp(i)%Re(1:2) as the reference's Re_size, Re_idx
+// and Res (m_global_parameters.fpp:300-336, m_viscous.fpp:33-45), and the
+// cell-centre spacings of the velocity gradients, dcc[d][i] = x_cc(i) -
+// x_cc(i-1) for i = 0 .. n_d (m_start_up.fpp:342-343 and the ghost centres of
+// s_populate_grid_variables_buffers).
+struct ViscParams {
+  double res[2][kMaxFluids];
+  int re_size[2];
+  int re_idx[2][kMaxFluids];
+  const double* dcc[3];
 };
 
 
@@ -398,10 +411,14 @@ __device__ __forceinline__ void weno_cell(const RT* __restrict__ c, const RT (&v
 // xi_M and xi_P of the reference are exactly 1/0 or 0/1 (0.5 +- sign(0.5,
 // s_S)), so the flux is the upwind side's term alone; evaluating only that
 // side gives the same values and halves the arithmetic.
-template <int ND, int NF, int DIR, class RT>
+//
+// VS: also return vel_src of every component, m_riemann_solvers.fpp:314-324,
+// with both sides' terms exactly as the reference writes them (the viscous
+// energy flux needs the tangential components).
+template <int ND, int NF, int DIR, class RT, bool VS = false>
 __device__ __forceinline__ void hllc_face(const RT (&qL)[Eqs<ND, NF>::S], const RT (&qR)[Eqs<ND, NF>::S],
                                           const RT (&gam_i)[NF], const RT (&pi_i)[NF], RT (&F)[Eqs<ND, NF>::S],
-                                          RT& ustar) {
+                                          RT& ustar, RT* vsrc = nullptr) {
   using Q = Eqs<ND, NF>;
   RT rmsL = RT(0), rmsR = RT(0);
 #pragma unroll
@@ -431,6 +448,18 @@ __device__ __forceinline__ void hllc_face(const RT (&qL)[Eqs<ND, NF>::S], const 
   const RT sR = fmax(uR + cR, uL + cL);
   const RT sS = div_rn(pR - pL + rhoL * uL * (sL - uL) - rhoR * uR * (sR - uR),
                       divisor(rhoL * (sL - uL) - rhoR * (sR - uR)));
+  if constexpr (VS) {
+    const RT sM = fmin(RT(0), sL), sP = fmax(RT(0), sR);
+    const RT xiL = div_rn(sL - uL, divisor(sL - sS));
+    const RT xiR = div_rn(sR - uR, divisor(sR - sS));
+    const RT xiM = RT(0.5) + copysign(RT(0.5), sS);
+    const RT xiP = RT(0.5) - copysign(RT(0.5), sS);
+#pragma unroll
+    for (int d = 0; d < ND; ++d) {
+      const RT flg = d == DIR ? RT(1) : RT(0);
+      vsrc[d] = xiM * (qL[Q::MOM + d] + flg * sM * (xiL - RT(1))) + xiP * (qR[Q::MOM + d] + flg * sP * (xiR - RT(1)));
+    }
+  }
   if (!signbit(sS)) {  // xi_M = 1, xi_P = 0
     const RT sM = fmin(RT(0), sL);
     const RT xi = div_rn(sL - uL, divisor(sL - sS));
@@ -464,6 +493,79 @@ __device__ __forceinline__ void hllc_face(const RT (&qL)[Eqs<ND, NF>::S], const 
     for (int f = 0; f < NF; ++f) F[Q::ADV + f] = qR[Q::ADV + f] * w;
     ustar = w;
   }
+}
+
+// Viscous source flux of one face, s_compute_viscous_source_flux
+// (m_riemann_solvers.fpp:683-902), from the face's left/right states (for the
+// mixture Reynolds numbers, :169-230), vel_src vs and the face velocity
+// gradients dx[c] = d u_c/dx, dy[c] = d u_c/dy (m_viscous.fpp:159-370).
+// out: the x-momentum, y-momentum and energy source fluxes.
+template <int ND, int NF, int DIR, class RT>
+__device__ __forceinline__ void viscous_face_flux(const RT (&qL)[Eqs<ND, NF>::S], const RT (&qR)[Eqs<ND, NF>::S],
+                                                  const ViscParams& V, const RT (&vs)[ND], const RT (&dx)[2],
+                                                  const RT (&dy)[2], RT (&out)[3]) {
+  using Q = Eqs<ND, NF>;
+  RT re_avg[2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    RT reL = RT(-1e6), reR = RT(-1e6);
+    if (V.re_size[r] > 0) reL = reR = RT(0);
+    for (int q = 0; q < V.re_size[r]; ++q) {
+      const int f = V.re_idx[r][q];
+      const auto D = divisor(RT(V.res[r][f]));
+      reL = div_rn(qL[Q::ADV + f], D) + reL;
+      reR = div_rn(qR[Q::ADV + f], D) + reR;
+    }
+    reL = div_rn(RT(1), divisor(reL < RT(1e-16) ? RT(1e-16) : reL));
+    reR = div_rn(RT(1), divisor(reR < RT(1e-16) ? RT(1e-16) : reR));
+    re_avg[r] = div_rn(RT(2), divisor(div_rn(RT(1), divisor(reL)) + div_rn(RT(1), divisor(reR))));
+  }
+  const bool shear = V.re_size[0] > 0, bulk = V.re_size[1] > 0;
+  RT fm[2] = {RT(0), RT(0)}, fe = RT(0);
+  if (DIR == 0) {
+    if (shear) {
+      const RT tau = div_rn(RT(4.0 / 3.0) * dx[0], divisor(re_avg[0]));
+      fm[0] = fm[0] - tau;
+      fe = fe - vs[0] * tau;
+    }
+    if (bulk) {
+      const RT tau = div_rn(dx[0], divisor(re_avg[1]));
+      fm[0] = fm[0] - tau;
+      fe = fe - vs[0] * tau;
+    }
+    if constexpr (ND > 1) {
+      if (shear) {
+        const RT t0 = -div_rn(RT(2.0 / 3.0) * dy[1], divisor(re_avg[0]));
+        const RT t1 = div_rn(dy[0] + dx[1], divisor(re_avg[0]));
+        fm[0] = fm[0] - t0;
+        fe = fe - vs[0] * t0;
+        fm[1] = fm[1] - t1;
+        fe = fe - vs[1] * t1;
+      }
+      if (bulk) {
+        const RT tau = div_rn(dy[1], divisor(re_avg[1]));
+        fm[0] = fm[0] - tau;
+        fe = fe - vs[0] * tau;
+      }
+    }
+  } else if constexpr (ND > 1) {
+    if (shear) {
+      const RT t0 = div_rn(dy[0] + dx[1], divisor(re_avg[0]));
+      const RT t1 = div_rn(RT(4) * dy[1] - RT(2) * dx[0], divisor(RT(3) * re_avg[0]));
+      fm[0] = fm[0] - t0;
+      fe = fe - vs[0] * t0;
+      fm[1] = fm[1] - t1;
+      fe = fe - vs[1] * t1;
+    }
+    if (bulk) {
+      const RT tau = div_rn(dx[0] + dy[1], divisor(re_avg[1]));
+      fm[1] = fm[1] - tau;
+      fe = fe - vs[1] * tau;
+    }
+  }
+  out[0] = fm[0];
+  out[1] = fm[1];
+  out[2] = fe;
 }
 
 // RK stage combinations, m_time_steppers.fpp:163-348, in the reference's

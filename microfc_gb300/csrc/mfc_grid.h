@@ -126,7 +126,7 @@ inline void weno_record(AxisHost& a, int i, int wo, double* r) {
 // empty string on success, else the reason.
 struct GridTables {
   std::vector<double> host;
-  size_t off_inv[3] = {0, 0, 0}, off_coef[3] = {0, 0, 0};
+  size_t off_inv[3] = {0, 0, 0}, off_coef[3] = {0, 0, 0}, off_dcc[3] = {0, 0, 0};
   int cstride[3] = {0, 0, 0};
 };
 
@@ -150,6 +150,17 @@ inline std::string build_grid_tables(const mfc_params* p, int nd, const int* n, 
       if (!(a.D(i) > 0.0)) return "cell boundaries must increase";
     t.off_inv[d] = t.host.size();
     for (int i = 0; i <= a.s; ++i) t.host.push_back(1.0 / a.D(i));
+    // cell centres x_cc(-1 .. s+1) (m_start_up.fpp:342-343 and the ghost
+    // centres of s_populate_grid_variables_buffers), then their spacings
+    // dcc(i) = x_cc(i) - x_cc(i-1), i = 0 .. s+1, for the viscous gradients
+    {
+      std::vector<double> cc((size_t)a.s + 3);  // cc[i + 1] = x_cc(i)
+      for (int i = 0; i <= a.s; ++i) cc[(size_t)i + 1] = a.CB(i - 1) + a.D(i) / 2.0;
+      cc[0] = cc[1] - (a.D(0) + a.D(-1)) / 2.0;
+      cc[(size_t)a.s + 2] = cc[(size_t)a.s + 1] + (a.D(a.s) + a.D(a.s + 1)) / 2.0;
+      t.off_dcc[d] = t.host.size();
+      for (int i = 0; i <= a.s + 1; ++i) t.host.push_back(cc[(size_t)i + 1] - cc[(size_t)i]);
+    }
     const int pad = kCoefPad;
     t.cstride[d] = n[d] + 2 * pad;
     t.off_coef[d] = t.host.size();

@@ -24,38 +24,40 @@ struct StageEntry {
   cudaError_t (*prepare)();
   cudaError_t (*launch)(const DevParams& P, const double* qin, const double* qbase, double* qout, double dt,
                         int kind, cudaStream_t st);
+  bool visc = false;  // compiled with the viscous terms
 };
 
 // MINB > 1 selects the register-capped kernel (stage_kernel_mb).
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool VISC>
 constexpr auto stage_func() {
+  static_assert(MINB == 1 || !VISC, "register-capped variants are inviscid");
   if constexpr (MINB > 1) return &stage_kernel_mb<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>;
-  else return &stage_kernel<ND, NF, WO, RT, TX, TY, NT, GATE>;
+  else return &stage_kernel<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>;
 }
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false>
 cudaError_t stage_prepare() {
-  return cudaFuncSetAttribute(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>(),
+  return cudaFuncSetAttribute(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>(),
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE>());
+                              (int)stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>());
 }
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false>
 cudaError_t stage_launch(const DevParams& P, const double* qin, const double* qbase, double* qout, double dt,
                          int kind, cudaStream_t st) {
   const dim3 grid((unsigned)((P.n[0] + TX - 1) / TX), ND > 1 ? (unsigned)((P.n[1] + TY - 1) / TY) : 1u, 1u);
-  stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>()
-      <<<grid, NT, stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE>(), st>>>(P, qin, qbase, qout, dt, kind);
+  stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>()
+      <<<grid, NT, stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>(), st>>>(P, qin, qbase, qout, dt, kind);
   return cudaGetLastError();
 }
 
 // prec of a registry entry: 0 FP64, 1 split, 2 split with the learned gate
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false>
 StageEntry stage_entry() {
   return StageEntry{ND, NF, WO, sizeof(RT) == 8 ? 0 : (GATE ? 2 : 1), TX, TY, NT,
-                    stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE>(), 1,
-                    &stage_prepare<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>,
-                    &stage_launch<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>};
+                    stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>(), 1,
+                    &stage_prepare<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>,
+                    &stage_launch<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>, VISC};
 }
 
 // 3-D: three directional sweeps per stage (mfc_sweep.cuh).  The x sweep uses
@@ -99,7 +101,7 @@ struct Sweep3D {
 };
 
 // The default (first registered) launcher of a configuration, or nullptr.
-const StageEntry* find_stage(int nd, int nf, int wo, int prec);
+const StageEntry* find_stage(int nd, int nf, int wo, int prec, bool visc = false);
 
 // Records msg as the calling thread's mfc_gpu_last_error() and returns code.
 int report_error(int code, const std::string& msg);
@@ -117,5 +119,7 @@ void register_stage_2d_fp64(std::vector<StageEntry>& r);
 void register_stage_2d_fp32(std::vector<StageEntry>& r);
 void register_stage_3d_fp64(std::vector<StageEntry>& r);
 void register_stage_3d_fp32(std::vector<StageEntry>& r);
+void register_stage_visc_fp64(std::vector<StageEntry>& r);
+void register_stage_visc_fp32(std::vector<StageEntry>& r);
 
 }  // namespace mfc

@@ -49,7 +49,7 @@ __device__ __forceinline__ T narrow(double x) {
 __device__ __forceinline__ double widen(double x) { return x; }
 __device__ __forceinline__ double widen(float x) { return f2d_bits(x); }
 
-template <int ND, int NF, int WO, class RT, int TX, int TY>
+template <int ND, int NF, int WO, class RT, int TX, int TY, bool VISC = false>
 struct StageShape {
   using Q = Eqs<ND, NF>;
   static constexpr int S = Q::S;
@@ -62,9 +62,11 @@ struct StageShape {
   static constexpr int NWX = S * TYE * (TX + 2);
   static constexpr int NWY = (ND > 1) ? S * (TY + 2) * TX : 0;
   static constexpr int NW = NWX > NWY ? NWX : NWY;
-  // fluxes + interface velocity
-  static constexpr int NFX = (S + 1) * TYE * (TX + 1);
-  static constexpr int NFY = (ND > 1) ? (S + 1) * (TY + 1) * TX : 0;
+  // fluxes + interface velocity (+ the viscous x-momentum, y-momentum and
+  // energy source fluxes)
+  static constexpr int NR = S + 1 + (VISC ? 3 : 0);
+  static constexpr int NFX = NR * TYE * (TX + 1);
+  static constexpr int NFY = (ND > 1) ? NR * (TY + 1) * TX : 0;
   static constexpr int NFL = NFX > NFY ? NFX : NFY;
   // split precision: the tile's WENO coefficients, converted to FP32 once and
   // stored as one 16-byte aligned record of kCoefRec floats per cell, so that
@@ -94,13 +96,14 @@ struct GateShape {
   static constexpr size_t kBytes = kFlagOff + ((NGX + NGY + 15) / 16) * 16;
 };
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, bool VISC = false>
 __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __restrict__ qin,
                                            const double* __restrict__ qbase, double* __restrict__ qout,
                                            const double dt, const int kind, const int x0, const int y0,
                                            unsigned char* smem_raw) {
   static_assert(!GATE || (sizeof(RT) == 4 && WO == 5), "the learned gate runs on the split-precision WENO5 path");
-  using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
+  static_assert(!(GATE && VISC), "the gated kernel is inviscid");
+  using Sh = StageShape<ND, NF, WO, RT, TX, TY, VISC>;
   using Q = Eqs<ND, NF>;
   constexpr int S = Sh::S, H = Sh::H, LX = Sh::LX, LY = Sh::LY, TYE = Sh::TYE;
   constexpr int CPT = (TX * TYE + NT - 1) / NT;  // interior cells per thread
@@ -132,7 +135,9 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
     const int lx = c % LX, ly = c / LX;
     const bool hx = lx < H || lx >= H + TX;
     const bool hy = (ND > 1) && (ly < H || ly >= H + TY);
-    if (hx && hy) continue;  // corners are never read
+    // corners are never read, except the four diagonal neighbours of the
+    // tile that the viscous cross derivatives use
+    if (hx && hy && !(VISC && (lx == H - 1 || lx == H + TX) && (ly == H - 1 || ly == H + TY))) continue;
     bool fx = false, fy = false;
     const int rx = x0 - H + lx, ry = (ND > 1) ? y0 - H + ly : 0;
     // processor boundaries: ghost cells come from the neighbour's halo buffer
@@ -303,7 +308,35 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         qL[v] = lfr ? b : a;
         qR[v] = rfl ? a : b;
       }
-      hllc_face<ND, NF, 0, RT>(qL, qR, gam_i, pi_i, F, us);
+      if constexpr (VISC) {
+        RT vs[ND], dxv[2] = {RT(0), RT(0)}, dyv[2] = {RT(0), RT(0)}, vf[3];
+        hllc_face<ND, NF, 0, RT, true>(qL, qR, gam_i, pi_i, F, us, vs);
+        const ViscParams& V = *P.visc;
+        const int ly = (ND > 1) ? ty + H : 0, lx = f + H - 1;  // the face's left cell
+        auto U = [&](int c, int x, int y) { return sq[((Q::MOM + c) * LY + y) * LX + x]; };
+        const auto Dx = divisor(narrow<RT>(__ldg(V.dcc[0] + min(x0 + f, nx))));  // x_cc(j+1) - x_cc(j)
+#pragma unroll
+        for (int c = 0; c < ND; ++c) {
+          const RT g = div_rn(U(c, lx + 1, ly) - U(c, lx, ly), Dx);
+          dxv[c] = RT(0.5) * (g + g);
+        }
+        if constexpr (ND > 1) {
+          const int gy = min(y0 + ty, ny - 1);
+          const auto D0 = divisor(narrow<RT>(__ldg(V.dcc[1] + gy))), D1 = divisor(narrow<RT>(__ldg(V.dcc[1] + gy + 1)));
+#pragma unroll
+          for (int c = 0; c < ND; ++c) {
+            auto Ly = [&](int x) { return div_rn(U(c, x, ly) - U(c, x, ly - 1), D0); };
+            auto Ry = [&](int x) { return div_rn(U(c, x, ly + 1) - U(c, x, ly), D1); };
+            const RT A = RT(0.25) * (Ly(lx + 1) + Ry(lx + 1) + Ly(lx) + Ry(lx));
+            dyv[c] = RT(0.5) * (A + A);
+          }
+        }
+        viscous_face_flux<ND, NF, 0, RT>(qL, qR, V, vs, dxv, dyv, vf);
+#pragma unroll
+        for (int t = 0; t < 3; ++t) fl[((S + 1 + t) * TYE + ty) * NFXr + f] = vf[t];
+      } else {
+        hllc_face<ND, NF, 0, RT>(qL, qR, gam_i, pi_i, F, us);
+      }
 #pragma unroll
       for (int v = 0; v < S; ++v) fl[(v * TYE + ty) * NFXr + f] = F[v];
       fl[(S * TYE + ty) * NFXr + f] = us;
@@ -329,6 +362,13 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
     for (int f = 0; f < NF; ++f) {
       const AT a = AT(sq[((Q::ADV + f) * LY + (ND > 1 ? ty + H : 0)) * LX + tx + H]);
       rhs[k][Q::ADV + f] = rhs[k][Q::ADV + f] + inv * a * du;
+    }
+    if constexpr (VISC) {  // m_rhs.fpp:591-603: momentum .. energy
+#pragma unroll
+      for (int t = 0; t <= ND; ++t) {
+        const int v = t < ND ? Q::MOM + t : Q::E, r = S + 1 + (t < ND ? t : 2);
+        rhs[k][v] = rhs[k][v] + inv * (AT(fl[(r * TYE + ty) * NFXr + tx]) - AT(fl[(r * TYE + ty) * NFXr + tx + 1]));
+      }
     }
   }
   if constexpr (ND > 1) {
@@ -384,7 +424,30 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         qL[v] = lfr ? b : a;
         qR[v] = rfl ? a : b;
       }
-      hllc_face<ND, NF, 1, RT>(qL, qR, gam_i, pi_i, F, us);
+      if constexpr (VISC) {
+        RT vs[ND], dxv[2], dyv[2], vf[3];
+        hllc_face<ND, NF, 1, RT, true>(qL, qR, gam_i, pi_i, F, us, vs);
+        const ViscParams& V = *P.visc;
+        const int ly = f + H - 1, lx = tx + H;  // the face's lower cell
+        auto U = [&](int c, int x, int y) { return sq[((Q::MOM + c) * LY + y) * LX + x]; };
+        const auto Dy = divisor(narrow<RT>(__ldg(V.dcc[1] + min(y0 + f, ny))));  // y_cc(k+1) - y_cc(k)
+        const int gx = min(x0 + tx, nx - 1);
+        const auto D0 = divisor(narrow<RT>(__ldg(V.dcc[0] + gx))), D1 = divisor(narrow<RT>(__ldg(V.dcc[0] + gx + 1)));
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          auto Lx = [&](int y) { return div_rn(U(c, lx, y) - U(c, lx - 1, y), D0); };
+          auto Rx = [&](int y) { return div_rn(U(c, lx + 1, y) - U(c, lx, y), D1); };
+          const RT A = RT(0.25) * (Lx(ly + 1) + Rx(ly + 1) + Lx(ly) + Rx(ly));
+          dxv[c] = RT(0.5) * (A + A);
+          const RT g = div_rn(U(c, lx, ly + 1) - U(c, lx, ly), Dy);
+          dyv[c] = RT(0.5) * (g + g);
+        }
+        viscous_face_flux<ND, NF, 1, RT>(qL, qR, V, vs, dxv, dyv, vf);
+#pragma unroll
+        for (int t = 0; t < 3; ++t) fl[((S + 1 + t) * NFYr + f) * TX + tx] = vf[t];
+      } else {
+        hllc_face<ND, NF, 1, RT>(qL, qR, gam_i, pi_i, F, us);
+      }
 #pragma unroll
       for (int v = 0; v < S; ++v) fl[(v * NFYr + f) * TX + tx] = F[v];
       fl[(S * NFYr + f) * TX + tx] = us;
@@ -407,6 +470,13 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       for (int f = 0; f < NF; ++f) {
         const AT a = AT(sq[((Q::ADV + f) * LY + ty + H) * LX + tx + H]);
         rhs[k][Q::ADV + f] = rhs[k][Q::ADV + f] + inv * a * du;
+      }
+      if constexpr (VISC) {  // m_rhs.fpp:639-651
+#pragma unroll
+        for (int t = 0; t <= ND; ++t) {
+          const int v = t < ND ? Q::MOM + t : Q::E, r = S + 1 + (t < ND ? t : 2);
+          rhs[k][v] = rhs[k][v] + inv * (AT(fl[(r * NFYr + ty) * TX + tx]) - AT(fl[(r * NFYr + ty + 1) * TX + tx]));
+        }
       }
     }
   }
@@ -451,13 +521,13 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   if (P.monitor) monitor_max(P.monitor, icfl);
 }
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, bool VISC = false>
 __global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const double* __restrict__ qin,
                                                    const double* __restrict__ qbase, double* __restrict__ qout,
                                                    const double dt, const int kind) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
-                                               (ND > 1) ? blockIdx.y * TY : 0, smem_raw);
+  stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
+                                                     (ND > 1) ? blockIdx.y * TY : 0, smem_raw);
 }
 
 // The same kernel with its registers capped so that MINB blocks fit on an SM.
@@ -472,9 +542,9 @@ __global__ void __launch_bounds__(NT, MINB) stage_kernel_mb(const DevParams P, c
 }
 
 // Shared memory of one stage-kernel block (with the gate's share when on).
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool VISC = false>
 constexpr size_t stage_smem_bytes() {
-  return StageShape<ND, NF, WO, RT, TX, TY>::kSmemBytes + (GATE ? GateShape<ND, TX, TY, NT>::kBytes : 0);
+  return StageShape<ND, NF, WO, RT, TX, TY, VISC>::kSmemBytes + (GATE ? GateShape<ND, TX, TY, NT>::kBytes : 0);
 }
 
 }  // namespace mfc

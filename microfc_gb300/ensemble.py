@@ -50,6 +50,8 @@ class Ensemble:
         on_device = states is None and ic == "device"
         for i, c in enumerate(self.cases):
             c.check()
+            if c.viscous:
+                raise ValueError("the ensemble kernels are inviscid")
             if on_device:
                 x_cb, y_cb, _ = preprocess.grid(c)
                 q = None

@@ -87,6 +87,8 @@ class Simulation:
         self._h = h
         self.S = self.L.mfc_gpu_sys_size(h)
         self.dt = case.dt
+        if case.viscous:
+            self.set_viscosity(case.re_shear, case.re_bulk)
         if on_device:
             self.generate_ic()
         else:
@@ -173,6 +175,16 @@ class Simulation:
         v, ms = ctypes.c_int(-1), ctypes.c_double(0)
         _lib.check(self.L.mfc_gpu_tune(self._h, int(reps), ctypes.byref(v), ctypes.byref(ms)))
         return v.value, ms.value
+
+    def set_viscosity(self, re_shear=(), re_bulk=()) -> None:
+        """fluid_pp(i)%Re(1:2) of the case's fluids (mfc_gpu_set_viscosity);
+        all zero switches back to the inviscid kernels."""
+        nf = self.case.num_fluids
+        a = np.zeros(nf)
+        b = np.zeros(nf)
+        a[:len(re_shear)] = re_shear
+        b[:len(re_bulk)] = re_bulk
+        _lib.check(self.L.mfc_gpu_set_viscosity(self._h, _dp(a), _dp(b)))
 
     def select_variant(self, variant: int):
         """Pin a tile variant (mfc_gpu_select_variant); returns (tx, ty, threads)."""

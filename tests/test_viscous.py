@@ -1,0 +1,95 @@
+"""Viscous terms on the GPU against the oracle: bit for bit in FP64 (1-D
+and 2-D, several boundary conditions), within tolerance in split
+precision; switching the viscosity off restores the inviscid kernels."""
+import numpy as np
+import pytest
+
+from conftest import rel_l1
+from microfc_gb300 import cases, preprocess
+
+pytestmark = pytest.mark.gpu
+
+
+def _shear_wave(nx=64, ny=25, re=100.0, bulk=0.0, steps=40, dt=2e-3, precision="fp64"):
+    from test_oracle_pins import _shear_wave as sw
+    c, x_cb, y_cb, q, _ = sw(nx, ny, re, 0.01, bulk, steps, dt)
+    return c.replace(precision=precision), x_cb, y_cb, q
+
+
+def _viscous_droplet(bc=(-3, -3), precision="fp64", steps=20):
+    c = cases.shock_droplet_2d(nx=96, ny=48, steps=steps, precision=precision)
+    # water (fluid 1) and air (fluid 2), Re = 1 / mu in the case's units, raised
+    # so that the viscous terms are visible within a few steps on this grid
+    return c.replace(bc_x=bc, bc_y=bc, re_shear=(1.0 / 1e-1, 1.0 / 2e-3), re_bulk=(0.0, 1.0 / 5e-3))
+
+
+def _gpu_and_oracle(oracle_lib, case, x_cb, y_cb, q, steps):
+    from microfc_gb300 import Simulation
+    with Simulation(case, x_cb, y_cb, q_cons=q) as sim:
+        sim.run(0, steps)
+        got = sim.download()
+    o = oracle_lib.Oracle(case.replace(precision="fp64"), x_cb, y_cb)
+    o.set_state(q)
+    o.run(0, steps, case.dt)
+    return got, o.get_state()
+
+
+def test_shear_wave_matches_oracle_bitwise(oracle_lib):
+    c, x_cb, y_cb, q = _shear_wave(re=100.0, bulk=40.0)
+    got, ref = _gpu_and_oracle(oracle_lib, c, x_cb, y_cb, q, c.t_step_stop)
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.parametrize("bc", [(-3, -3), (-2, -2), (-1, -1), (-4, -4), (-2, -3)])
+def test_viscous_droplet_matches_oracle_bitwise(oracle_lib, bc):
+    c = _viscous_droplet(bc)
+    x_cb, y_cb, _, q = preprocess.generate(c)
+    got, ref = _gpu_and_oracle(oracle_lib, c, x_cb, y_cb, q, c.t_step_stop)
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64)), rel_l1(got, ref)
+
+
+def test_viscous_sod_1d_matches_oracle_bitwise(oracle_lib):
+    c = cases.sod_1d(m=199, steps=40, dt=1e-4).replace(re_shear=(50.0, 80.0), re_bulk=(30.0, 0.0))
+    x_cb, _, _, q = preprocess.generate(c)
+    got, ref = _gpu_and_oracle(oracle_lib, c, x_cb, None, q, c.t_step_stop)
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+
+
+def test_viscosity_changes_the_result_and_can_be_switched_off(oracle_lib):
+    from microfc_gb300 import Simulation
+    c = _viscous_droplet()
+    x_cb, y_cb, _, q = preprocess.generate(c)
+    inv = c.replace(re_shear=(), re_bulk=())
+    with Simulation(inv, x_cb, y_cb, q_cons=q) as sim:
+        sim.run(0, c.t_step_stop)
+        q_inv = sim.download()
+    with Simulation(c, x_cb, y_cb, q_cons=q) as sim:
+        sim.set_viscosity((0.0, 0.0), (0.0, 0.0))
+        sim.run(0, c.t_step_stop)
+        assert np.array_equal(sim.download(), q_inv)
+    with Simulation(c, x_cb, y_cb, q_cons=q) as sim:
+        sim.run(0, c.t_step_stop)
+        assert rel_l1(sim.download(), q_inv)[c.mom_idx] > 1e-8
+
+
+def test_split_precision_viscous_error_bounded(oracle_lib):
+    c = _viscous_droplet(precision="split")
+    x_cb, y_cb, _, q = preprocess.generate(c)
+    got, ref = _gpu_and_oracle(oracle_lib, c, x_cb, y_cb, q, c.t_step_stop)
+    err = rel_l1(got, ref)
+    assert err[[0, 1, c.adv_idx, c.adv_idx + 1]].max() <= 1e-3, err
+
+
+def test_viscous_refusals():
+    from microfc_gb300 import Simulation, decomp
+    from microfc_gb300._lib import MfcError
+    c = cases.sod_1d(m=99, steps=2)
+    x_cb, _, _, q = preprocess.generate(c)
+    s = decomp.decompose(c, x_cb, px=2)[0]
+    with Simulation(s.case, s.x_cb, q_cons=np.ascontiguousarray(q[s.window()]), check=False) as sim:
+        with pytest.raises(MfcError, match="processor boundaries"):
+            sim.set_viscosity((10.0, 10.0))
+    b = cases.shock_bubble_3d(N=28, steps=2, precision="fp64")
+    with Simulation(b) as sim:
+        with pytest.raises(MfcError, match="1-D and 2-D"):
+            sim.set_viscosity((10.0, 10.0))
