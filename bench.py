@@ -72,30 +72,37 @@ class ClockSampler:
     Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, period_ms: int = 50):
         self.index = index
+        self.period_ms = period_ms
         self.samples = []
-        self._stop = threading.Event()
+        self._proc = None
         self._t = threading.Thread(target=self._run, daemon=True)
 
     def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
-                                     timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([s.strip() for s in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        # one nvidia-smi process streaming a line every period_ms
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                           "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            for line in self._proc.stdout:
+                if line.strip():
+                    self.samples.append([v.strip() for v in line.split(",")])
+        except Exception:
+            pass
 
     def __enter__(self):
         self._t.start()
+        time.sleep(0.1)  # the first line is out before the timed region starts
         return self
 
     def __exit__(self, *exc):
-        self._stop.set()
+        if self._proc is not None:
+            self._proc.terminate()  # the process this sampler started
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
         self._t.join(timeout=10)
 
     def summary(self):
@@ -263,7 +270,7 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "split", "gated"])
