@@ -169,6 +169,14 @@ int mfc_gpu_status(mfc_gpu_ctx* ctx, uint32_t* flags, int clear);
  * back to the inviscid kernels.  Call before stepping. */
 int mfc_gpu_set_viscosity(mfc_gpu_ctx* ctx, const double* re_shear, const double* re_bulk);
 
+/* Split and gated WENO5 on a uniform grid (no reference counterpart): when
+ * every cell of a direction has the same FP32 coefficient record, the
+ * kernels read that one record from their parameters instead of staging
+ * per-cell records in shared memory, with identical results.  On by default;
+ * enable = 0 forces the per-cell records.  *in_use (may be NULL) receives a
+ * bit per direction (x = 1, y = 2, z = 4) that now uses the shared record. */
+int mfc_gpu_set_uniform_coefficients(mfc_gpu_ctx* ctx, int enable, int* in_use);
+
 /* Run-time stability monitor, the reference's ICFL of s_write_run_time_information
  * (src/simulation/m_data_output.fpp:178-310), fused into the last stage kernel
  * of every step: ICFL = dt / min_d(dx_d / (|u_d| + c)), maximised over the cells

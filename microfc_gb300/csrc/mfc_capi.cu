@@ -98,6 +98,9 @@ struct mfc_gpu_ctx {
   mfc::ViscParams* visc = nullptr;     // device copy (viscous cases)
   size_t off_dcc[3] = {0, 0, 0};       // spacing tables inside `tables`
   mfc::DevParams dev{};
+  mfc::UniformCoef ucoef{};        // uniform grids: the split kernels' shared coefficient records
+  mfc::UniformCoef ucoef_found{};  // what the grid tables allow
+  bool ucoef_enabled = true;       // ucoef = ucoef_found when enabled, else all off
   const mfc::StageEntry* stage = nullptr;
   int64_t launches = 0;
 };
@@ -113,7 +116,7 @@ int launch_stage(mfc_gpu_ctx* c, const double* qin, const double* qbase, double*
                  bool last_stage = false) {
   mfc::DevParams P = c->dev;
   if (last_stage && c->monitor_on) P.monitor = c->monitor;  // ICFL of the step's new state
-  cudaError_t e = c->stage->launch(P, qin, qbase, qout, dt, kind, c->stream);
+  cudaError_t e = c->stage->launch(P, c->ucoef, qin, qbase, qout, dt, kind, c->stream);
   if (e != cudaSuccess) return fail(MFC_ERR_CUDA, std::string("stage launch: ") + cudaGetErrorString(e));
   c->launches += c->stage->kernels;
   return MFC_OK;
@@ -304,6 +307,9 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
     D.pi_infs[f] = f < p->num_fluids ? p->pi_infs[f] : 0.0;
   }
   D.weno_eps = p->weno_eps;
+  mfc::set_fp32_constants(D);
+  mfc::uniform_records(gt, c->nd, c->n, p->weno_order, p->precision, c->ucoef_found);
+  c->ucoef = c->ucoef_found;
   D.coff = mfc::kCoefPad;
   D.status = c->status;
   D.work = c->work;
@@ -479,6 +485,8 @@ int mfc_gpu_set_halo_widths(mfc_gpu_ctx* c, int dir, int side, const double* wid
   if (!why.empty()) return fail(MFC_ERR_INVALID, why);
   MFC_CUDA(cudaStreamSynchronize(c->stream));
   MFC_CUDA(cudaMemcpy(c->tables, gt.host.data(), sizeof(double) * gt.host.size(), cudaMemcpyHostToDevice));
+  mfc::uniform_records(gt, c->nd, c->n, q.weno_order, q.precision, c->ucoef_found);
+  c->ucoef = c->ucoef_enabled ? c->ucoef_found : mfc::UniformCoef{};
   return MFC_OK;
 }
 
@@ -530,6 +538,14 @@ int mfc_gpu_set_viscosity(mfc_gpu_ctx* c, const double* re_shear, const double* 
   if (e->prepare() != cudaSuccess) return fail(MFC_ERR_CUDA, "viscous kernel does not fit on this device");
   c->dev.visc = c->visc;
   c->stage = e;
+  return MFC_OK;
+}
+
+int mfc_gpu_set_uniform_coefficients(mfc_gpu_ctx* c, int enable, int* in_use) {
+  if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  c->ucoef_enabled = enable != 0;
+  c->ucoef = c->ucoef_enabled ? c->ucoef_found : mfc::UniformCoef{};
+  if (in_use) *in_use = c->ucoef.on[0] | (c->ucoef.on[1] << 1) | (c->ucoef.on[2] << 2);
   return MFC_OK;
 }
 
@@ -625,9 +641,11 @@ int mfc_gpu_tune(mfc_gpu_ctx* c, int reps, int* variant_out, double* ms_out) {
     ++idx;
     if (e.prepare() != cudaSuccess) continue;
     // first-stage launches read register 0 and write register 1 only
-    if (e.launch(c->dev, c->reg[0], c->reg[0], c->reg[1], 0.0, mfc::kRkEuler, c->stream) != cudaSuccess) continue;
+    if (e.launch(c->dev, c->ucoef, c->reg[0], c->reg[0], c->reg[1], 0.0, mfc::kRkEuler, c->stream) != cudaSuccess)
+      continue;
     cudaEventRecord(a, c->stream);
-    for (int r = 0; r < reps; ++r) e.launch(c->dev, c->reg[0], c->reg[0], c->reg[1], 0.0, mfc::kRkEuler, c->stream);
+    for (int r = 0; r < reps; ++r)
+      e.launch(c->dev, c->ucoef, c->reg[0], c->reg[0], c->reg[1], 0.0, mfc::kRkEuler, c->stream);
     cudaEventRecord(b, c->stream);
     if (cudaEventSynchronize(b) != cudaSuccess) break;
     float ms = 0.f;

@@ -18,6 +18,8 @@ constexpr int kMaxFluids = 4;
 constexpr int kNumCoef = 27;  // per cell: polyL[3][2], polyR[3][2], dL[3], dR[3], beta[3][3]
 // offsets inside one coefficient record
 constexpr int kPL = 0, kPR = 6, kDL = 12, kDR = 15, kBeta = 18;
+// split precision: one cell's FP32 coefficients padded to a 16-byte record
+constexpr int kCoefRec = 28;
 
 struct DevParams {
   int n[3];             // interior cells per direction (m+1, n+1, p+1); 1 when unused
@@ -25,6 +27,8 @@ struct DevParams {
   int bc_beg[3], bc_end[3];
   double gammas[kMaxFluids], pi_infs[kMaxFluids];
   double weno_eps;
+  // the same constants rounded to FP32 (split path), set by set_fp32_constants
+  float gammas_f[kMaxFluids], pi_infs_f[kMaxFluids], weno_eps_f;
   const double* inv_d[3];  // 1/dx(i) for i = 0 .. n-1 (per direction)
   const double* coef[3];   // WENO coefficients, SoA: coef[k * cstride + (i + coff)],
                            // cells i = -kCoefPad .. n-1+kCoefPad, coff = kCoefPad
@@ -40,6 +44,26 @@ struct DevParams {
   // boundary.
   const double* const* halo;
   const struct ViscParams* visc;  // viscous cases: Reynolds numbers and spacing tables (NULL: inviscid)
+};
+
+// Rounds the EOS and WENO constants to FP32 once on the host (the split
+// path's reconstruction and Riemann solve read them as floats).
+inline void set_fp32_constants(DevParams& D) {
+  for (int f = 0; f < kMaxFluids; ++f) {
+    D.gammas_f[f] = (float)D.gammas[f];
+    D.pi_infs_f[f] = (float)D.pi_infs[f];
+  }
+  D.weno_eps_f = (float)D.weno_eps;
+}
+
+// Split precision on a grid whose FP32 coefficient records are the same for
+// every cell of a direction (uniform spacing): that one record per
+// direction.  The single-case kernels receive it by value, so the
+// reconstruction takes its coefficients from the constant bank instead of
+// staging one record per cell in shared memory.  on[d] = 0: per-cell records.
+struct UniformCoef {
+  int on[3];
+  float rec[3][kCoefRec];
 };
 
 // Viscous parameters: fluid_pp(i)%Re(1:2) as the reference's Re_size, Re_idx
@@ -207,9 +231,14 @@ struct DivisorF32 {
 __device__ __forceinline__ DivisorF32 divisor(float b) { return {b}; }
 __device__ __forceinline__ float div_rn(float a, const DivisorF32& d) { return a / d.b; }
 
+// True for an infinity or NaN: the exponent field of the high word is all
+// ones.  The mask is applied in inline PTX so that the test stays an integer
+// operation (an equivalent floating-point comparison would occupy GB300's
+// narrow FP64 pipe).
 __device__ __forceinline__ bool not_finite(double x) {
-  const uint32_t hi = (uint32_t)(__double_as_longlong(x) >> 32);
-  return (hi & 0x7ff00000u) == 0x7ff00000u;
+  uint32_t e;
+  asm("and.b32 %0, %1, 0x7ff00000;" : "=r"(e) : "r"(__double2hiint(x)));
+  return e == 0x7ff00000u;
 }
 
 // cons -> prim of one cell, m_variables_conversion.fpp:326-373 and

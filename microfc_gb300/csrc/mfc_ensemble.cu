@@ -189,6 +189,7 @@ int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_ca
       D.pi_infs[f] = f < p.num_fluids ? p.pi_infs[f] : 0.0;
     }
     D.weno_eps = p.weno_eps;
+    mfc::set_fp32_constants(D);
     D.coff = mfc::kCoefPad;
     const int S = 2 * p.num_fluids + 3;
     reg_off[i] = state_elems;

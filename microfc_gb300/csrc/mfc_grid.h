@@ -8,6 +8,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -177,6 +179,49 @@ inline std::string build_grid_tables(const mfc_params* p, int nd, const int* n, 
     }
   }
   return "";
+}
+
+// The device's truncating double -> float conversion (d2f_bits in
+// mfc_device.cuh), restated on the host bit for bit.
+inline float d2f_trunc(double x) {
+  uint64_t b;
+  std::memcpy(&b, &x, sizeof b);
+  const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+  const uint32_t sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  const uint32_t mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const uint32_t r = e <= 0 ? sign : (e >= 255 ? (sign | 0x7f800000u) : (sign | ((uint32_t)e << 23) | mant));
+  float f;
+  std::memcpy(&f, &r, sizeof f);
+  return f;
+}
+
+// Split-precision WENO5 on a uniform grid: fills U.rec[d] and sets U.on[d]
+// for every direction whose cells -kCoefPad .. n-1+kCoefPad all have the same
+// FP32 coefficient record (the one the kernels would stage per cell), so
+// that the kernels may use that one record everywhere with identical results.
+inline void uniform_records(const GridTables& t, int nd, const int* n, int weno_order, int precision,
+                            UniformCoef& U) {
+  U = UniformCoef{};
+  if (precision == MFC_PREC_FP64 || weno_order != 5) return;
+  for (int d = 0; d < nd; ++d) {
+    const int cells = n[d] + 2 * kCoefPad;
+    auto bits = [](float f) {
+      uint32_t u;
+      std::memcpy(&u, &f, sizeof u);
+      return u;
+    };
+    bool same = true;
+    float rec[kCoefRec] = {};
+    for (int k = 0; k < kNumCoef && same; ++k) {
+      const double* row = t.host.data() + t.off_coef[d] + (size_t)k * t.cstride[d];
+      rec[k] = d2f_trunc(row[0]);
+      for (int i = 1; i < cells && same; ++i) same = bits(d2f_trunc(row[i])) == bits(rec[k]);
+    }
+    if (!same) continue;
+    U.on[d] = 1;
+    for (int k = 0; k < kCoefRec; ++k) U.rec[d][k] = rec[k];
+  }
 }
 
 // The checks of s_check_input_file that apply to the hot path.

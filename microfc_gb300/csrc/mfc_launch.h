@@ -22,8 +22,8 @@ struct StageEntry {
   size_t smem;
   int kernels;  // kernel launches per RK stage (1 in 1-D/2-D, 3 sweeps in 3-D)
   cudaError_t (*prepare)();
-  cudaError_t (*launch)(const DevParams& P, const double* qin, const double* qbase, double* qout, double dt,
-                        int kind, cudaStream_t st);
+  cudaError_t (*launch)(const DevParams& P, const UniformCoef& U, const double* qin, const double* qbase,
+                        double* qout, double dt, int kind, cudaStream_t st);
   bool visc = false;  // compiled with the viscous terms
 };
 
@@ -43,11 +43,12 @@ cudaError_t stage_prepare() {
 }
 
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false>
-cudaError_t stage_launch(const DevParams& P, const double* qin, const double* qbase, double* qout, double dt,
-                         int kind, cudaStream_t st) {
+cudaError_t stage_launch(const DevParams& P, const UniformCoef& U, const double* qin, const double* qbase,
+                         double* qout, double dt, int kind, cudaStream_t st) {
   const dim3 grid((unsigned)((P.n[0] + TX - 1) / TX), ND > 1 ? (unsigned)((P.n[1] + TY - 1) / TY) : 1u, 1u);
   stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>()
-      <<<grid, NT, stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>(), st>>>(P, qin, qbase, qout, dt, kind);
+      <<<grid, NT, stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>(), st>>>(P, U, qin, qbase, qout, dt,
+                                                                                       kind);
   return cudaGetLastError();
 }
 
@@ -84,15 +85,15 @@ struct Sweep3D {
     if (e == cudaSuccess) e = prep<2>();
     return e;
   }
-  static cudaError_t launch(const DevParams& P, const double* qin, const double* qbase, double* qout, double dt,
-                            int kind, cudaStream_t st) {
+  static cudaError_t launch(const DevParams& P, const UniformCoef& U, const double* qin, const double* qbase,
+                            double* qout, double dt, int kind, cudaStream_t st) {
     const unsigned nx = P.n[0], ny = P.n[1], nz = P.n[2];
     const dim3 g0((nx + TA0 - 1) / TA0, (ny + TB0 - 1) / TB0, (nz + TC0 - 1) / TC0);
     const dim3 g1((nx + TB1 - 1) / TB1, (ny + TA1 - 1) / TA1, nz);
     const dim3 g2((nx + TB1 - 1) / TB1, (nz + TA1 - 1) / TA1, ny);
-    sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT><<<g0, NT, K<0>::kSmemBytes, st>>>(P, qin, qbase, qout, dt, kind);
-    sweep_kernel<NF, WO, RT, 1, TA1, TB1, 1, NT><<<g1, NT, K<1>::kSmemBytes, st>>>(P, qin, qbase, qout, dt, kind);
-    sweep_kernel<NF, WO, RT, 2, TA1, TB1, 1, NT><<<g2, NT, K<2>::kSmemBytes, st>>>(P, qin, qbase, qout, dt, kind);
+    sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT><<<g0, NT, K<0>::kSmemBytes, st>>>(P, U, qin, qbase, qout, dt, kind);
+    sweep_kernel<NF, WO, RT, 1, TA1, TB1, 1, NT><<<g1, NT, K<1>::kSmemBytes, st>>>(P, U, qin, qbase, qout, dt, kind);
+    sweep_kernel<NF, WO, RT, 2, TA1, TB1, 1, NT><<<g2, NT, K<2>::kSmemBytes, st>>>(P, U, qin, qbase, qout, dt, kind);
     return cudaGetLastError();
   }
   static StageEntry entry() {

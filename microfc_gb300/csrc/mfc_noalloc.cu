@@ -137,8 +137,11 @@ extern "C" int mfc_gpu_tvd_rk_noalloc(const mfc_params* p, const double* q_in, d
     D.pi_infs[f] = f < p->num_fluids ? p->pi_infs[f] : 0.0;
   }
   D.weno_eps = p->weno_eps;
+  mfc::set_fp32_constants(D);
   D.coff = mfc::kCoefPad;
   D.status = status;
+  mfc::UniformCoef U;
+  mfc::uniform_records(gt, nd, n, p->weno_order, p->precision, U);
 
   if ((e = stage->prepare()) != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(e));
   if ((e = cudaMemcpyAsync(tables, gt.host.data(), sizeof(double) * gt.host.size(), cudaMemcpyHostToDevice, st)) !=
@@ -151,16 +154,16 @@ extern "C" int mfc_gpu_tvd_rk_noalloc(const mfc_params* p, const double* q_in, d
   // A stage never writes the register it reads its halo from.
   switch (p->time_stepper) {
     case 1:
-      e = stage->launch(D, q_in, q_in, q_out, dt, mfc::kRkEuler, st);
+      e = stage->launch(D, U, q_in, q_in, q_out, dt, mfc::kRkEuler, st);
       break;
     case 2:
-      e = stage->launch(D, q_in, q_in, reg, dt, mfc::kRkEuler, st);
-      if (e == cudaSuccess) e = stage->launch(D, reg, q_in, q_out, dt, mfc::kRk2Final, st);
+      e = stage->launch(D, U, q_in, q_in, reg, dt, mfc::kRkEuler, st);
+      if (e == cudaSuccess) e = stage->launch(D, U, reg, q_in, q_out, dt, mfc::kRk2Final, st);
       break;
     default:
-      e = stage->launch(D, q_in, q_in, q_out, dt, mfc::kRkEuler, st);
-      if (e == cudaSuccess) e = stage->launch(D, q_out, q_in, reg, dt, mfc::kRk3Mid, st);
-      if (e == cudaSuccess) e = stage->launch(D, reg, q_in, q_out, dt, mfc::kRk3Final, st);
+      e = stage->launch(D, U, q_in, q_in, q_out, dt, mfc::kRkEuler, st);
+      if (e == cudaSuccess) e = stage->launch(D, U, q_out, q_in, reg, dt, mfc::kRk3Mid, st);
+      if (e == cudaSuccess) e = stage->launch(D, U, reg, q_in, q_out, dt, mfc::kRk3Final, st);
       break;
   }
   if (e != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(e));

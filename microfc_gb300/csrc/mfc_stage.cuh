@@ -24,7 +24,6 @@ namespace mfc {
 
 // One cell's FP32 WENO coefficients from shared memory: kCoefRec floats,
 // 16-byte aligned, as float4 loads.
-constexpr int kCoefRec = 28;
 template <class RT>
 __device__ __forceinline__ void load_coef_record(const RT* __restrict__ rec, RT (&c)[kCoefRec]) {
   if constexpr (sizeof(RT) == 4) {
@@ -100,7 +99,7 @@ template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = 
 __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __restrict__ qin,
                                            const double* __restrict__ qbase, double* __restrict__ qout,
                                            const double dt, const int kind, const int x0, const int y0,
-                                           unsigned char* smem_raw) {
+                                           unsigned char* smem_raw, const UniformCoef* U = nullptr) {
   static_assert(!GATE || (sizeof(RT) == 4 && WO == 5), "the learned gate runs on the split-precision WENO5 path");
   static_assert(!(GATE && VISC), "the gated kernel is inviscid");
   using Sh = StageShape<ND, NF, WO, RT, TX, TY, VISC>;
@@ -125,10 +124,23 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   RT gam_i[NF], pi_i[NF];
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
-    gam_i[f] = RT(P.gammas[f]);
-    pi_i[f] = RT(P.pi_infs[f]);
+    if constexpr (kSplit) {
+      gam_i[f] = P.gammas_f[f];
+      pi_i[f] = P.pi_infs_f[f];
+    } else {
+      gam_i[f] = P.gammas[f];
+      pi_i[f] = P.pi_infs[f];
+    }
   }
-  const RT eps = RT(P.weno_eps);
+  RT eps;
+  if constexpr (kSplit) eps = P.weno_eps_f;
+  else eps = P.weno_eps;
+  // split WENO5 on a uniform grid: every cell of a direction shares one
+  // coefficient record, read from the kernel parameters
+  const bool ux = Sh::NCOEF > 0 && U != nullptr && U->on[0];
+  const bool uy = Sh::NCOEF > 0 && ND > 1 && U != nullptr && U->on[1];
+  (void)ux;
+  (void)uy;
 
   // ---- phase 1: load + BCs + cons -> prim --------------------------------
   for (int c = tid; c < LX * LY; c += NT) {
@@ -179,14 +191,14 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   }
   if constexpr (Sh::NCOEF > 0) {
     // global reads coalesced along the cells, records written per cell
-    for (int it = tid; it < kCoefRec * Sh::NCX; it += NT) {
+    for (int it = ux ? kCoefRec * Sh::NCX : tid; it < kCoefRec * Sh::NCX; it += NT) {
       const int cx = it % Sh::NCX, k = it / Sh::NCX;
       scx[cx * kCoefRec + k] =
           k < kNumCoef ? d2f_bits(__ldg(P.coef[0] + k * P.cstride[0] + clamp_coef_index(x0 - 1 + cx, nx) + P.coff))
                        : 0.f;
     }
     if constexpr (ND > 1) {
-      for (int it = tid; it < kCoefRec * Sh::NCY; it += NT) {
+      for (int it = uy ? kCoefRec * Sh::NCY : tid; it < kCoefRec * Sh::NCY; it += NT) {
         const int cy = it % Sh::NCY, k = it / Sh::NCY;
         scy[cy * kCoefRec + k] =
             k < kNumCoef
@@ -269,22 +281,33 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         const int o = k - 2;
         st[k] = (o >= -(WO / 2) && o <= WO / 2) ? row[lx + o] : RT(0);
       }
-      RT c[kCoefRec];
-      if constexpr (Sh::NCOEF > 0) {
-        load_coef_record(scx + cx * kCoefRec, c);
-      } else if constexpr (WO > 1) {
-        const int gi = clamp_coef_index(x0 - 1 + cx, nx) + P.coff;
-#pragma unroll
-        for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
-      }
       RT vl, vr;
-      if constexpr (GATE) {
-        if (gflag[ty * NCX + cx]) weno5_cell_fast(c, st, eps, vl, vr);
-        else weno5_cell_linear(c, st, vl, vr);
-      } else if constexpr (kSplit && WO == 5) {
-        weno5_cell_fast(c, st, eps, vl, vr);
+      auto recon = [&](const RT* __restrict__ c) {
+        if constexpr (GATE) {
+          if (gflag[ty * NCX + cx]) weno5_cell_fast(c, st, eps, vl, vr);
+          else weno5_cell_linear(c, st, vl, vr);
+        } else if constexpr (kSplit && WO == 5) {
+          weno5_cell_fast(c, st, eps, vl, vr);
+        } else {
+          weno_cell<WO, RT>(c, st, eps, vl, vr);
+        }
+      };
+      if constexpr (Sh::NCOEF > 0) {
+        if (ux) {
+          recon(U->rec[0]);
+        } else {
+          RT c[kCoefRec];
+          load_coef_record(scx + cx * kCoefRec, c);
+          recon(c);
+        }
       } else {
-        weno_cell<WO, RT>(c, st, eps, vl, vr);
+        RT c[kCoefRec];
+        if constexpr (WO > 1) {
+          const int gi = clamp_coef_index(x0 - 1 + cx, nx) + P.coff;
+#pragma unroll
+          for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
+        }
+        recon(c);
       }
       wl[(v * TYE + ty) * NCX + cx] = vl;
       wr[(v * TYE + ty) * NCX + cx] = vr;
@@ -387,22 +410,33 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         const int o = k - 2;
         st[k] = (o >= -(WO / 2) && o <= WO / 2) ? col[(ly + o) * LX] : RT(0);
       }
-      RT c[kCoefRec];
-      if constexpr (Sh::NCOEF > 0) {
-        load_coef_record(scy + cy * kCoefRec, c);
-      } else if constexpr (WO > 1) {
-        const int gi = clamp_coef_index(y0 - 1 + cy, ny) + P.coff;
-#pragma unroll
-        for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
-      }
       RT vl, vr;
-      if constexpr (GATE) {
-        if (gflag[GateShape<ND, TX, TY, NT>::NGX + cy * TX + tx]) weno5_cell_fast(c, st, eps, vl, vr);
-        else weno5_cell_linear(c, st, vl, vr);
-      } else if constexpr (kSplit && WO == 5) {
-        weno5_cell_fast(c, st, eps, vl, vr);
+      auto recon = [&](const RT* __restrict__ c) {
+        if constexpr (GATE) {
+          if (gflag[GateShape<ND, TX, TY, NT>::NGX + cy * TX + tx]) weno5_cell_fast(c, st, eps, vl, vr);
+          else weno5_cell_linear(c, st, vl, vr);
+        } else if constexpr (kSplit && WO == 5) {
+          weno5_cell_fast(c, st, eps, vl, vr);
+        } else {
+          weno_cell<WO, RT>(c, st, eps, vl, vr);
+        }
+      };
+      if constexpr (Sh::NCOEF > 0) {
+        if (uy) {
+          recon(U->rec[1]);
+        } else {
+          RT c[kCoefRec];
+          load_coef_record(scy + cy * kCoefRec, c);
+          recon(c);
+        }
       } else {
-        weno_cell<WO, RT>(c, st, eps, vl, vr);
+        RT c[kCoefRec];
+        if constexpr (WO > 1) {
+          const int gi = clamp_coef_index(y0 - 1 + cy, ny) + P.coff;
+#pragma unroll
+          for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
+        }
+        recon(c);
       }
       wl[(v * NCY + cy) * TX + tx] = vl;
       wr[(v * NCY + cy) * TX + tx] = vr;
@@ -522,23 +556,24 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
 }
 
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, bool VISC = false>
-__global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const double* __restrict__ qin,
-                                                   const double* __restrict__ qbase, double* __restrict__ qout,
-                                                   const double dt, const int kind) {
+__global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const __grid_constant__ UniformCoef U,
+                                                   const double* __restrict__ qin, const double* __restrict__ qbase,
+                                                   double* __restrict__ qout, const double dt, const int kind) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
-                                                     (ND > 1) ? blockIdx.y * TY : 0, smem_raw);
+                                                     (ND > 1) ? blockIdx.y * TY : 0, smem_raw, &U);
 }
 
 // The same kernel with its registers capped so that MINB blocks fit on an SM.
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB>
-__global__ void __launch_bounds__(NT, MINB) stage_kernel_mb(const DevParams P, const double* __restrict__ qin,
+__global__ void __launch_bounds__(NT, MINB) stage_kernel_mb(const DevParams P, const __grid_constant__ UniformCoef U,
+                                                            const double* __restrict__ qin,
                                                             const double* __restrict__ qbase,
                                                             double* __restrict__ qout, const double dt,
                                                             const int kind) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
-                                               (ND > 1) ? blockIdx.y * TY : 0, smem_raw);
+                                               (ND > 1) ? blockIdx.y * TY : 0, smem_raw, &U);
 }
 
 // Shared memory of one stage-kernel block (with the gate's share when on).

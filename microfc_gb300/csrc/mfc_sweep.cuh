@@ -49,9 +49,9 @@ __device__ __forceinline__ void sweep_coords(int a, int b, int c, int& x, int& y
 }
 
 template <int NF, int WO, class RT, int DIR, int TA, int TB, int TC, int NT>
-__global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const double* __restrict__ qin,
-                                                   const double* __restrict__ qbase, double* __restrict__ qout,
-                                                   const double dt, const int kind) {
+__global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __grid_constant__ UniformCoef U,
+                                                   const double* __restrict__ qin, const double* __restrict__ qbase,
+                                                   double* __restrict__ qout, const double dt, const int kind) {
   using Sh = SweepShape<NF, WO, RT, DIR, TA, TB, TC>;
   using Q = Eqs<3, NF>;
   constexpr int S = Sh::S, H = Sh::H, LA = Sh::LA, NP = Sh::NP;
@@ -76,10 +76,20 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const doub
   RT gam_i[NF], pi_i[NF];
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
-    gam_i[f] = RT(P.gammas[f]);
-    pi_i[f] = RT(P.pi_infs[f]);
+    if constexpr (kSplit) {
+      gam_i[f] = P.gammas_f[f];
+      pi_i[f] = P.pi_infs_f[f];
+    } else {
+      gam_i[f] = P.gammas[f];
+      pi_i[f] = P.pi_infs[f];
+    }
   }
-  const RT eps = RT(P.weno_eps);
+  RT eps;
+  if constexpr (kSplit) eps = P.weno_eps_f;
+  else eps = P.weno_eps;
+  // split WENO5 on a uniform grid: one coefficient record for the whole sweep
+  const bool ua = Sh::NCOEF > 0 && U.on[DIR];
+  (void)ua;
   const int64_t st[3] = {1, P.sy, P.sz};
 
   // ---- load + BCs + cons -> prim ------------------------------------------------
@@ -129,7 +139,7 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const doub
     }
   }
   if constexpr (Sh::NCOEF > 0) {
-    for (int it = tid; it < kCoefRec * (TA + 2); it += NT) {
+    for (int it = ua ? kCoefRec * (TA + 2) : tid; it < kCoefRec * (TA + 2); it += NT) {
       const int ca = it % (TA + 2), k = it / (TA + 2);
       sc[ca * kCoefRec + k] =
           k < kNumCoef
@@ -153,17 +163,24 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const doub
       const int o = k - 2;
       stc[k] = (o >= -(WO / 2) && o <= WO / 2) ? line[la + o] : RT(0);
     }
-    RT c[kCoefRec];
-    if constexpr (Sh::NCOEF > 0) {
-      load_coef_record(sc + ca * kCoefRec, c);
-    } else if constexpr (WO > 1) {
-      const int gi = clamp_coef_index(a0 - 1 + ca, na) + P.coff;
-#pragma unroll
-      for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(P.coef[DIR] + k * P.cstride[DIR] + gi));
-    }
     RT vl, vr;
-    if constexpr (kSplit && WO == 5) weno5_cell_fast(c, stc, eps, vl, vr);
-    else weno_cell<WO, RT>(c, stc, eps, vl, vr);
+    if constexpr (Sh::NCOEF > 0) {
+      if (ua) {
+        weno5_cell_fast(U.rec[DIR], stc, eps, vl, vr);
+      } else {
+        RT c[kCoefRec];
+        load_coef_record(sc + ca * kCoefRec, c);
+        weno5_cell_fast(c, stc, eps, vl, vr);
+      }
+    } else {
+      RT c[kCoefRec];
+      if constexpr (WO > 1) {
+        const int gi = clamp_coef_index(a0 - 1 + ca, na) + P.coff;
+#pragma unroll
+        for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(P.coef[DIR] + k * P.cstride[DIR] + gi));
+      }
+      weno_cell<WO, RT>(c, stc, eps, vl, vr);
+    }
     wl[(v * NP + p) * NCA + ca] = vl;
     wr[(v * NP + p) * NCA + ca] = vr;
   }

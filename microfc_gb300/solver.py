@@ -186,6 +186,14 @@ class Simulation:
         b[:len(re_bulk)] = re_bulk
         _lib.check(self.L.mfc_gpu_set_viscosity(self._h, _dp(a), _dp(b)))
 
+    def set_uniform_coefficients(self, enable: bool = True) -> int:
+        """Split/gated WENO5 on a uniform grid reads one shared coefficient
+        record per direction (on by default, identical results); returns the
+        directions using it as a bit mask (x 1, y 2, z 4)."""
+        used = ctypes.c_int(0)
+        _lib.check(self.L.mfc_gpu_set_uniform_coefficients(self._h, int(bool(enable)), ctypes.byref(used)))
+        return used.value
+
     def select_variant(self, variant: int):
         """Pin a tile variant (mfc_gpu_select_variant); returns (tx, ty, threads)."""
         tx, ty, nt = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)

@@ -48,3 +48,31 @@ def test_all_tile_variants_agree_bitwise(kind):
     assert len(outs) >= 1
     for o, s in zip(outs[1:], shapes[1:]):
         assert np.array_equal(o.view(np.uint64), outs[0].view(np.uint64)), s
+
+
+@pytest.mark.parametrize("kind", ["1d_split", "2d_split", "2d_gated", "3d_split"])
+def test_uniform_coefficient_record_matches_per_cell_records(kind):
+    """On a uniform grid the split kernels read one shared coefficient record
+    per direction from their parameters; the per-cell records give the same
+    bits."""
+    from microfc_gb300 import Simulation
+    nd, prec = kind.split("_")
+    params = None
+    if nd == "1d":
+        c = cases.sod_1d(m=299, steps=6, dt=1e-4).replace(precision=prec)
+    elif nd == "2d":
+        c = cases.shock_droplet_2d(nx=100, ny=60, steps=6, precision=prec)
+        params = gate.load() if prec == "gated" else None
+    else:
+        c = cases.shock_bubble_3d(N=28, steps=6, precision=prec).replace(m=28, n=26, p=27)
+    full = {"1d": 1, "2d": 3, "3d": 7}[nd]
+    x, y, z, q = preprocess.generate(c)
+    outs = []
+    for enable in (True, False):
+        with Simulation(c, x, y, z, q_cons=q) as sim:
+            if params is not None:
+                sim.set_gate(params)
+            assert sim.set_uniform_coefficients(enable) == (full if enable else 0)
+            sim.run(0, 6)
+            outs.append(sim.download())
+    assert np.array_equal(outs[0].view(np.uint64), outs[1].view(np.uint64))
