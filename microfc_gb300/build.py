@@ -26,11 +26,14 @@ def unit_flags(src: str) -> list[str]:
     reference's operation order, so its device code is compiled without FMA
     contraction (-fmad=false); host code never contracts (-ffp-contract=off,
     which matters on aarch64 hosts where GCC contracts by default).  The
-    split-precision units keep contraction and use the approximate FP32
-    division and square root (their FP32 results are checked against the
-    FP64 oracle at a stated tolerance, not bit for bit)."""
+    split-precision units use the approximate FP32 division and square root
+    (their FP32 results are checked against the FP64 oracle at a stated
+    tolerance).  They are compiled without automatic contraction as well and
+    write their fused multiply-adds out as fmaf: contraction left to the
+    compiler depends on the surrounding code, so two tile shapes or two code
+    paths of one kernel could round the same cell differently."""
     if src.endswith("_fp32.cu"):
-        return ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
+        return ["-prec-div=false", "-prec-sqrt=false", "-ftz=true", "-fmad=false"]
     return ["-fmad=false"]
 
 

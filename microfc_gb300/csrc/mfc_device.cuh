@@ -119,23 +119,38 @@ __device__ __forceinline__ int clamp_coef_index(int c, int n) {
 // float truncates the significand (error < 1 ulp of float), flushes results
 // below the smallest normal float to signed zero and maps everything above
 // the float range (and NaN) to infinity; float -> double is exact for
-// normal numbers and zero (denormal floats are flushed to zero, as the split
-// units run with -ftz=true).
+// normal numbers, zero, infinities and NaNs (denormal floats are flushed to
+// zero, as the split units run with -ftz=true).
+//
+// Bit-level forms, shared by host and device.  double -> float from the high
+// and low words: |x| >= 2^-126 and below 2^128 gives (E - 896) << 23 | the top
+// 23 significand bits; the subtraction is done before the shift so that the
+// exponent and significand move together (4 integer operations plus the two
+// range selects).
+__host__ __device__ __forceinline__ uint32_t d2f_trunc_word(uint32_t hi, uint32_t lo) {
+  const uint32_t a = hi & 0x7fffffffu;
+  const uint32_t t = ((a - 0x38000000u) << 3) | (lo >> 29);
+  const uint32_t r = a < 0x38100000u ? 0u : (a >= 0x47f00000u ? 0x7f800000u : t);
+  return r | (hi & 0x80000000u);
+}
+
+// float -> double high word (the low word is the float's bits << 29 for
+// normal floats, 0 otherwise): the exponent is rebiased by +896, or moved
+// from all ones to all ones, so that infinities and NaNs stay what they are.
+__host__ __device__ __forceinline__ uint32_t f2d_high_word(uint32_t b) {
+  const uint32_t a = b & 0x7fffffffu;
+  const uint32_t t = (a >> 3) + (a >= 0x7f800000u ? 0x70000000u : 0x38000000u);
+  return (a < 0x00800000u ? 0u : t) | (b & 0x80000000u);
+}
+
 __device__ __forceinline__ float d2f_bits(double x) {
-  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
-  const uint32_t sign = hi & 0x80000000u;
-  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-  const uint32_t mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
-  const uint32_t r = e <= 0 ? sign : (e >= 255 ? (sign | 0x7f800000u) : (sign | ((uint32_t)e << 23) | mant));
-  return __uint_as_float(r);
+  return __uint_as_float(d2f_trunc_word((uint32_t)__double2hiint(x), (uint32_t)__double2loint(x)));
 }
 
 __device__ __forceinline__ double f2d_bits(float f) {
   const uint32_t b = __float_as_uint(f);
-  const uint32_t sign = b & 0x80000000u, e = (b >> 23) & 0xffu, mant = b & 0x7fffffu;
-  const uint32_t hi = e == 0 ? sign : (sign | ((e + (1023u - 127u)) << 20) | (mant >> 3));
-  const uint32_t lo = e == 0 ? 0u : (mant << 29);
-  return __hiloint2double((int)hi, (int)lo);
+  const uint32_t lo = (b & 0x7fffffffu) < 0x00800000u ? 0u : (b << 29);
+  return __hiloint2double((int)f2d_high_word(b), (int)lo);
 }
 
 // Approximate FP32 reciprocal (PTX rcp.approx.ftz.f32); the split path
@@ -522,6 +537,73 @@ __device__ __forceinline__ void hllc_face(const RT (&qL)[Eqs<ND, NF>::S], const 
     for (int f = 0; f < NF; ++f) F[Q::ADV + f] = qR[Q::ADV + f] * w;
     ustar = w;
   }
+}
+
+// r + a*b: one fused multiply-add on the split path; on the FP64 path the
+// reference's rounded product followed by the rounded sum.
+__device__ __forceinline__ float mul_add(float a, float b, float r) { return fmaf(a, b, r); }
+__device__ __forceinline__ double mul_add(double a, double b, double r) { return r + a * b; }
+
+// HLLC for the split-precision path: the same wave speeds, star state and
+// upwind flux as hllc_face (same cases, same sign test on s_S), in FP32 with
+// every fused multiply-add written out as fmaf and the quotients as fast
+// reciprocal divisions.  The split units are compiled without automatic
+// contraction, so every tile shape and code path rounds identically.
+// Tangential momentum flux: rho v_d (u + s_M (xi - 1)) = rho v_d w.
+template <int ND, int NF, int DIR>
+__device__ __forceinline__ void hllc_face_fast(const float (&qL)[Eqs<ND, NF>::S], const float (&qR)[Eqs<ND, NF>::S],
+                                               const float (&gam_i)[NF], const float (&pi_i)[NF],
+                                               float (&F)[Eqs<ND, NF>::S], float& ustar) {
+  using Q = Eqs<ND, NF>;
+  float rmsL = qL[Q::MOM] * qL[Q::MOM], rmsR = qR[Q::MOM] * qR[Q::MOM];
+#pragma unroll
+  for (int d = 1; d < ND; ++d) {
+    rmsL = fmaf(qL[Q::MOM + d], qL[Q::MOM + d], rmsL);
+    rmsR = fmaf(qR[Q::MOM + d], qR[Q::MOM + d], rmsR);
+  }
+  const float pL = qL[Q::E], pR = qR[Q::E];
+  float rhoL = qL[0], gamL = qL[Q::ADV] * gam_i[0], piL = qL[Q::ADV] * pi_i[0];
+  float rhoR = qR[0], gamR = qR[Q::ADV] * gam_i[0], piR = qR[Q::ADV] * pi_i[0];
+#pragma unroll
+  for (int f = 1; f < NF; ++f) {
+    rhoL = rhoL + qL[f];
+    gamL = fmaf(qL[Q::ADV + f], gam_i[f], gamL);
+    piL = fmaf(qL[Q::ADV + f], pi_i[f], piL);
+    rhoR = rhoR + qR[f];
+    gamR = fmaf(qR[Q::ADV + f], gam_i[f], gamR);
+    piR = fmaf(qR[Q::ADV + f], pi_i[f], piR);
+  }
+  const float EL = fmaf(0.5f * rhoL, rmsL, fmaf(gamL, pL, piL));
+  const float ER = fmaf(0.5f * rhoR, rmsR, fmaf(gamR, pR, piR));
+  const float HL = __fdividef(EL + pL, rhoL), HR = __fdividef(ER + pR, rhoR);
+  const float cL = sqrtf(__fdividef(fmaf(-0.5f, rmsL, HL), gamL));
+  const float cR = sqrtf(__fdividef(fmaf(-0.5f, rmsR, HR), gamR));
+  const float uL = qL[Q::MOM + DIR], uR = qR[Q::MOM + DIR];
+  const float sL = fminf(uL - cL, uR - cR);
+  const float sR = fmaxf(uR + cR, uL + cL);
+  const float mL = rhoL * (sL - uL), mR = rhoR * (sR - uR);
+  const float sS = __fdividef(fmaf(-mR, uR, fmaf(mL, uL, pR - pL)), mL - mR);
+  const bool left = !signbit(sS);  // xi_M = 1, xi_P = 0
+  const float rho = left ? rhoL : rhoR, u = left ? uL : uR, p = left ? pL : pR, E = left ? EL : ER;
+  const float s = left ? fminf(0.f, sL) : fmaxf(0.f, sR);  // s_M or s_P
+  const float sk = left ? sL : sR;
+  const float xi = __fdividef(sk - u, sk - sS);
+  const float w = fmaf(s, xi - 1.f, u);
+  const float(&q)[Eqs<ND, NF>::S] = left ? qL : qR;
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    F[f] = q[f] * w;
+    F[Q::ADV + f] = q[Q::ADV + f] * w;
+  }
+#pragma unroll
+  for (int d = 0; d < ND; ++d) {
+    const float vd = q[Q::MOM + d];
+    if (d == DIR) F[Q::MOM + d] = fmaf(rho, fmaf(u, vd, s * fmaf(xi, sS, -vd)), p);
+    else F[Q::MOM + d] = rho * vd * w;
+  }
+  const float t = fmaf(rho, sS, __fdividef(p, sk - u));
+  F[Q::E] = fmaf(s, fmaf(xi, fmaf(sS - u, t, E), -E), u * (E + p));
+  ustar = w;
 }
 
 // Viscous source flux of one face, s_compute_viscous_source_flux

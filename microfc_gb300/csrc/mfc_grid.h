@@ -182,15 +182,11 @@ inline std::string build_grid_tables(const mfc_params* p, int nd, const int* n, 
 }
 
 // The device's truncating double -> float conversion (d2f_bits in
-// mfc_device.cuh), restated on the host bit for bit.
+// mfc_device.cuh) on the host, through the same bit-level function.
 inline float d2f_trunc(double x) {
   uint64_t b;
   std::memcpy(&b, &x, sizeof b);
-  const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
-  const uint32_t sign = hi & 0x80000000u;
-  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-  const uint32_t mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
-  const uint32_t r = e <= 0 ? sign : (e >= 255 ? (sign | 0x7f800000u) : (sign | ((uint32_t)e << 23) | mant));
+  const uint32_t r = d2f_trunc_word((uint32_t)(b >> 32), (uint32_t)b);
   float f;
   std::memcpy(&f, &r, sizeof f);
   return f;

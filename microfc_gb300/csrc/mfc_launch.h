@@ -46,9 +46,12 @@ template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = 
 cudaError_t stage_launch(const DevParams& P, const UniformCoef& U, const double* qin, const double* qbase,
                          double* qout, double dt, int kind, cudaStream_t st) {
   const dim3 grid((unsigned)((P.n[0] + TX - 1) / TX), ND > 1 ? (unsigned)((P.n[1] + TY - 1) / TY) : 1u, 1u);
-  stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>()
-      <<<grid, NT, stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>(), st>>>(P, U, qin, qbase, qout, dt,
-                                                                                       kind);
+  // a uniform grid stages no coefficient records: launch without their share
+  const bool shared_coef = U.on[0] && (ND < 2 || U.on[1]);
+  const size_t smem = shared_coef ? stage_smem_bytes_shared_coef<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>()
+                                  : stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>();
+  stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>()<<<grid, NT, smem, st>>>(P, U, qin, qbase, qout, dt,
+                                                                                      kind);
   return cudaGetLastError();
 }
 

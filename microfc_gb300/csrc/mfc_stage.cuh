@@ -48,6 +48,25 @@ __device__ __forceinline__ T narrow(double x) {
 __device__ __forceinline__ double widen(double x) { return x; }
 __device__ __forceinline__ double widen(float x) { return f2d_bits(x); }
 
+// Work distribution of a split WENO5 phase: NPOS positions (cells of the
+// tile's rows or columns) times S variables.  Each full pass gives a thread
+// one position with all S variables, so that the position's index
+// arithmetic, gate flag and coefficient record serve S reconstructions; the
+// NPOS % NT positions left over are dealt out per (position, variable), so
+// that no thread does more than ceil(S * NPOS / NT) reconstructions.
+// f(p, v, all): position p, all variables when all, else variable v.
+template <int NPOS, int S, int NT, class F>
+__device__ __forceinline__ void deal_positions(const int tid, F&& f) {
+  constexpr int FULL = (NPOS / NT) * NT, REM = NPOS - FULL;
+  for (int p = tid; p < FULL; p += NT) f(p, 0, true);
+  if constexpr (REM > 0) {
+    for (int it = tid; it < REM * S; it += NT) {
+      const int v = it / REM;
+      f(FULL + (it - v * REM), v, false);
+    }
+  }
+}
+
 template <int ND, int NF, int WO, class RT, int TX, int TY, bool VISC = false>
 struct StageShape {
   using Q = Eqs<ND, NF>;
@@ -75,26 +94,33 @@ struct StageShape {
   // offsets (in RT elements) of the arrays, each rounded up to 16 bytes
   static constexpr int align16(int n) { return (n * int(sizeof(RT)) + 15) / 16 * 16 / int(sizeof(RT)); }
   static constexpr int OW = align16(NQ), OF = OW + 2 * align16(NW), OC = OF + align16(NFL);
-  static constexpr size_t kSmemBytes = sizeof(RT) * (size_t(OC) + size_t(NCOEF));
+  // layout: [primitive tile, WENO values, fluxes][learned gate][coefficient
+  // records]; the records come last so that a uniform grid, which never
+  // stages them, can launch without their share
+  static constexpr size_t kMainBytes = sizeof(RT) * size_t(OC);
+  static constexpr size_t kCoefBytes = sizeof(RT) * size_t(NCOEF);
+  static constexpr size_t kSmemBytes = kMainBytes + kCoefBytes;
 };
 
-// One tile of one RK stage; the tile's first cell is (x0, y0).  Used by the
-// single-case kernel (one tile per block) and by the ensemble kernel (many
-// tiles of many cases per persistent block).  smem_raw must hold
-// StageShape::kSmemBytes.
-// Extra shared memory of the learned gate: one 16x16 FP16 input block per
-// warp, then one flag per (cell, direction) reconstructed by the tile.
-// The MLP's lane fragments (kGateFragWords words per lane, word-major)
-// follow, then the flags.
+// Shared memory of the learned gate.  Its own region holds one flag per
+// (cell, direction) reconstructed by the tile.  The gate phase's scratch --
+// one 16x16 FP16 input block per warp, then the MLP's lane fragments
+// (kGateFragWords words per lane, word-major) -- lives in the WENO value
+// arrays, which are not written before the gate phase ends.
 template <int ND, int TX, int TY, int NT>
 struct GateShape {
   static constexpr int NGX = (TX + 2) * ((ND > 1) ? TY : 1);
   static constexpr int NGY = (ND > 1) ? TX * (TY + 2) : 0;
   static constexpr size_t kFragOff = size_t(NT / 32) * 512;
-  static constexpr size_t kFlagOff = kFragOff + size_t(kGateFragWords) * 32 * 4;
-  static constexpr size_t kBytes = kFlagOff + ((NGX + NGY + 15) / 16) * 16;
+  static constexpr size_t kScratchBytes = kFragOff + size_t(kGateFragWords) * 32 * 4;
+  static constexpr size_t kBytes = ((NGX + NGY + 15) / 16) * 16;
 };
 
+// One tile of one RK stage; the tile's first cell is (x0, y0).  Used by the
+// single-case kernel (one tile per block) and by the ensemble kernel (many
+// tiles of many cases per persistent block).  smem_raw must hold
+// stage_smem_bytes() (or stage_smem_bytes_shared_coef() when U covers every
+// direction).
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, bool VISC = false>
 __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __restrict__ qin,
                                            const double* __restrict__ qbase, double* __restrict__ qout,
@@ -115,7 +141,8 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   RT* wl = sq + Sh::OW;                       // left-face values
   RT* wr = wl + Sh::align16(Sh::NW);          // right-face values
   RT* fl = sq + Sh::OF;                       // fluxes [S+1][...]
-  RT* scx = sq + Sh::OC;                      // split: FP32 x coefficients [TX+2][kCoefRec]
+  // split: FP32 x coefficients [TX+2][kCoefRec], after the gate's share
+  RT* scx = reinterpret_cast<RT*>(smem_raw + Sh::kMainBytes + (GATE ? GateShape<ND, TX, TY, NT>::kBytes : 0));
   RT* scy = scx + kCoefRec * Sh::NCX;         // split: FP32 y coefficients [TY+2][kCoefRec]
 
   const int tid = threadIdx.x;
@@ -213,10 +240,12 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   const uint8_t* gflag = nullptr;
   if constexpr (GATE) {
     using G = GateShape<ND, TX, TY, NT>;
-    unsigned char* gbase = smem_raw + Sh::kSmemBytes;
-    __half* gin = reinterpret_cast<__half*>(gbase);
-    uint32_t* frag = reinterpret_cast<uint32_t*>(gbase + G::kFragOff);
-    uint8_t* flags = gbase + G::kFlagOff;
+    static_assert(G::kScratchBytes <= 2 * sizeof(RT) * size_t(Sh::align16(Sh::NW)),
+                  "the gate's scratch must fit the WENO value arrays");
+    unsigned char* scratch = reinterpret_cast<unsigned char*>(wl);
+    __half* gin = reinterpret_cast<__half*>(scratch);
+    uint32_t* frag = reinterpret_cast<uint32_t*>(scratch + G::kFragOff);
+    uint8_t* flags = smem_raw + Sh::kMainBytes;
     const int warp = tid >> 5, lane = tid & 31;
     const uint32_t* gsrc =
         reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(P.gate_w) + kGateFragOffset);
@@ -266,51 +295,66 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   // ---- phase 2: x WENO over cells x0-1 .. x0+TX of the interior rows -------
   {
     constexpr int NCX = TX + 2;
-    const double* cf = P.coef[0];
-    const int cs = P.cstride[0];
-    for (int it = tid; it < S * TYE * NCX; it += NT) {
-      const int cx = it % NCX;
-      const int r = it / NCX;
-      const int ty = r % TYE, v = r / TYE;
-      const int ly = (ND > 1) ? ty + H : 0;
-      const int lx = cx + H - 1;
-      const RT* row = sq + (v * LY + ly) * LX;
+    // variable v of the cell at (cx, ty); c: the cell's coefficient record
+    auto x_recon = [&](const RT* __restrict__ c, const int cx, const int ty, const int v, const bool nonlin) {
+      const RT* row = sq + (v * LY + ((ND > 1) ? ty + H : 0)) * LX + cx + H - 1;
       RT st[5];
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         const int o = k - 2;
-        st[k] = (o >= -(WO / 2) && o <= WO / 2) ? row[lx + o] : RT(0);
+        st[k] = (o >= -(WO / 2) && o <= WO / 2) ? row[o] : RT(0);
       }
       RT vl, vr;
-      auto recon = [&](const RT* __restrict__ c) {
-        if constexpr (GATE) {
-          if (gflag[ty * NCX + cx]) weno5_cell_fast(c, st, eps, vl, vr);
-          else weno5_cell_linear(c, st, vl, vr);
-        } else if constexpr (kSplit && WO == 5) {
-          weno5_cell_fast(c, st, eps, vl, vr);
-        } else {
-          weno_cell<WO, RT>(c, st, eps, vl, vr);
-        }
-      };
-      if constexpr (Sh::NCOEF > 0) {
-        if (ux) {
-          recon(U->rec[0]);
-        } else {
-          RT c[kCoefRec];
-          load_coef_record(scx + cx * kCoefRec, c);
-          recon(c);
-        }
+      if constexpr (GATE) {
+        if (nonlin) weno5_cell_fast(c, st, eps, vl, vr);
+        else weno5_cell_linear(c, st, vl, vr);
+      } else if constexpr (kSplit && WO == 5) {
+        weno5_cell_fast(c, st, eps, vl, vr);
       } else {
+        weno_cell<WO, RT>(c, st, eps, vl, vr);
+      }
+      wl[(v * TYE + ty) * NCX + cx] = vl;
+      wr[(v * TYE + ty) * NCX + cx] = vr;
+    };
+    if constexpr (Sh::NCOEF > 0) {
+      deal_positions<TYE * NCX, S, NT>(tid, [&](const int p, const int v, const bool all) {
+        const int cx = p % NCX, ty = p / NCX;
+        bool nonlin = true;
+        if constexpr (GATE) nonlin = gflag[p] != 0;
+        // the shared record of a uniform grid, else the cell's staged record
+        // (reloaded per variable: keeping it live across them costs registers)
+        auto one = [&](const int w) {
+          if (ux) {
+            x_recon(U->rec[0], cx, ty, w, nonlin);
+          } else {
+            RT c[kCoefRec];
+            load_coef_record(scx + cx * kCoefRec, c);
+            x_recon(c, cx, ty, w, nonlin);
+          }
+        };
+        if (all) {
+#pragma unroll 1
+          for (int w = 0; w < S; ++w) one(w);
+        } else {
+          one(v);
+        }
+      });
+    } else {
+      // FP64 (and split WENO1/3): coefficients per reconstruction from global memory
+      const double* cf = P.coef[0];
+      const int cs = P.cstride[0];
+      for (int it = tid; it < S * TYE * NCX; it += NT) {
+        const int cx = it % NCX;
+        const int r = it / NCX;
+        const int ty = r % TYE, v = r / TYE;
         RT c[kCoefRec];
         if constexpr (WO > 1) {
           const int gi = clamp_coef_index(x0 - 1 + cx, nx) + P.coff;
 #pragma unroll
           for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
         }
-        recon(c);
+        x_recon(c, cx, ty, v, true);
       }
-      wl[(v * TYE + ty) * NCX + cx] = vl;
-      wr[(v * TYE + ty) * NCX + cx] = vr;
     }
   }
   __syncthreads();
@@ -357,6 +401,8 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         viscous_face_flux<ND, NF, 0, RT>(qL, qR, V, vs, dxv, dyv, vf);
 #pragma unroll
         for (int t = 0; t < 3; ++t) fl[((S + 1 + t) * TYE + ty) * NFXr + f] = vf[t];
+      } else if constexpr (kSplit) {
+        hllc_face_fast<ND, NF, 0>(qL, qR, gam_i, pi_i, F, us);
       } else {
         hllc_face<ND, NF, 0, RT>(qL, qR, gam_i, pi_i, F, us);
       }
@@ -384,62 +430,77 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
       const AT a = AT(sq[((Q::ADV + f) * LY + (ND > 1 ? ty + H : 0)) * LX + tx + H]);
-      rhs[k][Q::ADV + f] = rhs[k][Q::ADV + f] + inv * a * du;
+      rhs[k][Q::ADV + f] = mul_add(inv * a, du, rhs[k][Q::ADV + f]);
     }
     if constexpr (VISC) {  // m_rhs.fpp:591-603: momentum .. energy
 #pragma unroll
       for (int t = 0; t <= ND; ++t) {
         const int v = t < ND ? Q::MOM + t : Q::E, r = S + 1 + (t < ND ? t : 2);
-        rhs[k][v] = rhs[k][v] + inv * (AT(fl[(r * TYE + ty) * NFXr + tx]) - AT(fl[(r * TYE + ty) * NFXr + tx + 1]));
+        rhs[k][v] = mul_add(inv, AT(fl[(r * TYE + ty) * NFXr + tx]) - AT(fl[(r * TYE + ty) * NFXr + tx + 1]), rhs[k][v]);
       }
     }
   }
   if constexpr (ND > 1) {
     constexpr int NCY = TY + 2;
-    const double* cf = P.coef[1];
-    const int cs = P.cstride[1];
-    for (int it = tid; it < S * NCY * TX; it += NT) {
-      const int tx = it % TX;
-      const int r = it / TX;
-      const int cy = r % NCY, v = r / NCY;
-      const int ly = cy + H - 1, lx = tx + H;
-      const RT* col = sq + v * LY * LX + lx;
+    // variable v of the cell at (tx, cy)
+    auto y_recon = [&](const RT* __restrict__ c, const int tx, const int cy, const int v, const bool nonlin) {
+      const RT* col = sq + (v * LY + cy + H - 1) * LX + tx + H;
       RT st[5];
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         const int o = k - 2;
-        st[k] = (o >= -(WO / 2) && o <= WO / 2) ? col[(ly + o) * LX] : RT(0);
+        st[k] = (o >= -(WO / 2) && o <= WO / 2) ? col[o * LX] : RT(0);
       }
       RT vl, vr;
-      auto recon = [&](const RT* __restrict__ c) {
-        if constexpr (GATE) {
-          if (gflag[GateShape<ND, TX, TY, NT>::NGX + cy * TX + tx]) weno5_cell_fast(c, st, eps, vl, vr);
-          else weno5_cell_linear(c, st, vl, vr);
-        } else if constexpr (kSplit && WO == 5) {
-          weno5_cell_fast(c, st, eps, vl, vr);
-        } else {
-          weno_cell<WO, RT>(c, st, eps, vl, vr);
-        }
-      };
-      if constexpr (Sh::NCOEF > 0) {
-        if (uy) {
-          recon(U->rec[1]);
-        } else {
-          RT c[kCoefRec];
-          load_coef_record(scy + cy * kCoefRec, c);
-          recon(c);
-        }
+      if constexpr (GATE) {
+        if (nonlin) weno5_cell_fast(c, st, eps, vl, vr);
+        else weno5_cell_linear(c, st, vl, vr);
+      } else if constexpr (kSplit && WO == 5) {
+        weno5_cell_fast(c, st, eps, vl, vr);
       } else {
+        weno_cell<WO, RT>(c, st, eps, vl, vr);
+      }
+      wl[(v * NCY + cy) * TX + tx] = vl;
+      wr[(v * NCY + cy) * TX + tx] = vr;
+    };
+    if constexpr (Sh::NCOEF > 0) {
+      deal_positions<NCY * TX, S, NT>(tid, [&](const int p, const int v, const bool all) {
+        const int tx = p % TX, cy = p / TX;
+        bool nonlin = true;
+        if constexpr (GATE) nonlin = gflag[GateShape<ND, TX, TY, NT>::NGX + p] != 0;
+        // the shared record of a uniform grid, else the cell's staged record
+        // (reloaded per variable: keeping it live across them costs registers)
+        auto one = [&](const int w) {
+          if (uy) {
+            y_recon(U->rec[1], tx, cy, w, nonlin);
+          } else {
+            RT c[kCoefRec];
+            load_coef_record(scy + cy * kCoefRec, c);
+            y_recon(c, tx, cy, w, nonlin);
+          }
+        };
+        if (all) {
+#pragma unroll 1
+          for (int w = 0; w < S; ++w) one(w);
+        } else {
+          one(v);
+        }
+      });
+    } else {
+      const double* cf = P.coef[1];
+      const int cs = P.cstride[1];
+      for (int it = tid; it < S * NCY * TX; it += NT) {
+        const int tx = it % TX;
+        const int r = it / TX;
+        const int cy = r % NCY, v = r / NCY;
         RT c[kCoefRec];
         if constexpr (WO > 1) {
           const int gi = clamp_coef_index(y0 - 1 + cy, ny) + P.coff;
 #pragma unroll
           for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
         }
-        recon(c);
+        y_recon(c, tx, cy, v, true);
       }
-      wl[(v * NCY + cy) * TX + tx] = vl;
-      wr[(v * NCY + cy) * TX + tx] = vr;
     }
     __syncthreads();
 
@@ -479,6 +540,8 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         viscous_face_flux<ND, NF, 1, RT>(qL, qR, V, vs, dxv, dyv, vf);
 #pragma unroll
         for (int t = 0; t < 3; ++t) fl[((S + 1 + t) * NFYr + f) * TX + tx] = vf[t];
+      } else if constexpr (kSplit) {
+        hllc_face_fast<ND, NF, 1>(qL, qR, gam_i, pi_i, F, us);
       } else {
         hllc_face<ND, NF, 1, RT>(qL, qR, gam_i, pi_i, F, us);
       }
@@ -498,18 +561,18 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       const AT inv = narrow<AT>(__ldg(P.inv_d[1] + (gy < ny ? gy : ny - 1)));
 #pragma unroll
       for (int v = 0; v < S; ++v)
-        rhs[k][v] = rhs[k][v] + inv * (AT(fl[(v * NFYr + ty) * TX + tx]) - AT(fl[(v * NFYr + ty + 1) * TX + tx]));
+        rhs[k][v] = mul_add(inv, AT(fl[(v * NFYr + ty) * TX + tx]) - AT(fl[(v * NFYr + ty + 1) * TX + tx]), rhs[k][v]);
       const AT du = AT(fl[(S * NFYr + ty + 1) * TX + tx]) - AT(fl[(S * NFYr + ty) * TX + tx]);
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
         const AT a = AT(sq[((Q::ADV + f) * LY + ty + H) * LX + tx + H]);
-        rhs[k][Q::ADV + f] = rhs[k][Q::ADV + f] + inv * a * du;
+        rhs[k][Q::ADV + f] = mul_add(inv * a, du, rhs[k][Q::ADV + f]);
       }
       if constexpr (VISC) {  // m_rhs.fpp:639-651
 #pragma unroll
         for (int t = 0; t <= ND; ++t) {
           const int v = t < ND ? Q::MOM + t : Q::E, r = S + 1 + (t < ND ? t : 2);
-          rhs[k][v] = rhs[k][v] + inv * (AT(fl[(r * NFYr + ty) * TX + tx]) - AT(fl[(r * NFYr + ty + 1) * TX + tx]));
+          rhs[k][v] = mul_add(inv, AT(fl[(r * NFYr + ty) * TX + tx]) - AT(fl[(r * NFYr + ty + 1) * TX + tx]), rhs[k][v]);
         }
       }
     }
@@ -580,6 +643,14 @@ __global__ void __launch_bounds__(NT, MINB) stage_kernel_mb(const DevParams P, c
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool VISC = false>
 constexpr size_t stage_smem_bytes() {
   return StageShape<ND, NF, WO, RT, TX, TY, VISC>::kSmemBytes + (GATE ? GateShape<ND, TX, TY, NT>::kBytes : 0);
+}
+
+// The same without the coefficient records, for launches on a uniform grid
+// (every direction reads the shared record).
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool VISC = false>
+constexpr size_t stage_smem_bytes_shared_coef() {
+  return stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>() -
+         StageShape<ND, NF, WO, RT, TX, TY, VISC>::kCoefBytes;
 }
 
 }  // namespace mfc

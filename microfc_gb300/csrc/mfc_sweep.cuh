@@ -151,38 +151,54 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
 
   // ---- WENO along the sweep for cells a0-1 .. a0+TA --------------------------------
   constexpr int NCA = TA + 2;
-  for (int it = tid; it < S * NP * NCA; it += NT) {
-    const int ca = it % NCA;
-    const int r = it / NCA;
-    const int p = r % NP, v = r / NP;
-    const RT* line = sq + (v * NP + p) * LA;
-    const int la = ca + H - 1;
+  // variable v of cell ca of pencil p; c: the cell's coefficient record
+  auto recon = [&](const RT* __restrict__ c, const int ca, const int p, const int v) {
+    const RT* line = sq + (v * NP + p) * LA + ca + H - 1;
     RT stc[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
       const int o = k - 2;
-      stc[k] = (o >= -(WO / 2) && o <= WO / 2) ? line[la + o] : RT(0);
+      stc[k] = (o >= -(WO / 2) && o <= WO / 2) ? line[o] : RT(0);
     }
     RT vl, vr;
-    if constexpr (Sh::NCOEF > 0) {
-      if (ua) {
-        weno5_cell_fast(U.rec[DIR], stc, eps, vl, vr);
+    if constexpr (kSplit && WO == 5) weno5_cell_fast(c, stc, eps, vl, vr);
+    else weno_cell<WO, RT>(c, stc, eps, vl, vr);
+    wl[(v * NP + p) * NCA + ca] = vl;
+    wr[(v * NP + p) * NCA + ca] = vr;
+  };
+  if constexpr (Sh::NCOEF > 0) {
+    deal_positions<NP * NCA, S, NT>(tid, [&](const int q, const int v, const bool all) {
+      const int ca = q % NCA, p = q / NCA;
+      // the shared record of a uniform grid, else the cell's staged record
+      auto one = [&](const int w) {
+        if (ua) {
+          recon(U.rec[DIR], ca, p, w);
+        } else {
+          RT c[kCoefRec];
+          load_coef_record(sc + ca * kCoefRec, c);
+          recon(c, ca, p, w);
+        }
+      };
+      if (all) {
+#pragma unroll 1
+        for (int w = 0; w < S; ++w) one(w);
       } else {
-        RT c[kCoefRec];
-        load_coef_record(sc + ca * kCoefRec, c);
-        weno5_cell_fast(c, stc, eps, vl, vr);
+        one(v);
       }
-    } else {
+    });
+  } else {
+    for (int it = tid; it < S * NP * NCA; it += NT) {
+      const int ca = it % NCA;
+      const int r = it / NCA;
+      const int p = r % NP, v = r / NP;
       RT c[kCoefRec];
       if constexpr (WO > 1) {
         const int gi = clamp_coef_index(a0 - 1 + ca, na) + P.coff;
 #pragma unroll
         for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(P.coef[DIR] + k * P.cstride[DIR] + gi));
       }
-      weno_cell<WO, RT>(c, stc, eps, vl, vr);
+      recon(c, ca, p, v);
     }
-    wl[(v * NP + p) * NCA + ca] = vl;
-    wr[(v * NP + p) * NCA + ca] = vr;
   }
   __syncthreads();
 
@@ -201,7 +217,8 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
       qL[v] = lfr ? b : a;
       qR[v] = rfl ? a : b;
     }
-    hllc_face<3, NF, DIR, RT>(qL, qR, gam_i, pi_i, F, us);
+    if constexpr (kSplit) hllc_face_fast<3, NF, DIR>(qL, qR, gam_i, pi_i, F, us);
+    else hllc_face<3, NF, DIR, RT>(qL, qR, gam_i, pi_i, F, us);
 #pragma unroll
     for (int v = 0; v < S; ++v) fl[(v * NP + p) * NFA + f] = F[v];
     fl[(S * NP + p) * NFA + f] = us;
@@ -226,14 +243,14 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
     AT r[S];
 #pragma unroll
     for (int v = 0; v < S; ++v) {
-      const AT d = inv * (AT(fl[(v * NP + p) * NFA + ta]) - AT(fl[(v * NP + p) * NFA + ta + 1]));
-      r[v] = (DIR == 0) ? d : rhs_buf[o + v * P.sv] + d;
+      const AT diff = AT(fl[(v * NP + p) * NFA + ta]) - AT(fl[(v * NP + p) * NFA + ta + 1]);
+      r[v] = (DIR == 0) ? inv * diff : mul_add(inv, diff, rhs_buf[o + v * P.sv]);
     }
     const AT du = AT(fl[(S * NP + p) * NFA + ta + 1]) - AT(fl[(S * NP + p) * NFA + ta]);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
       const AT a = AT(sq[((Q::ADV + f) * NP + p) * LA + ta + H]);
-      r[Q::ADV + f] = r[Q::ADV + f] + inv * a * du;
+      r[Q::ADV + f] = mul_add(inv * a, du, r[Q::ADV + f]);
     }
     if (DIR < 2) {
 #pragma unroll

@@ -218,11 +218,12 @@ def test_bubble_3d_split_precision_error_bounded(oracle_lib):
     assert err[dens_alpha].max() <= TOL_SPLIT, err
 
 
-def test_status_flags_nan_and_clear():
+@pytest.mark.parametrize("prec", ["fp64", "split"])
+def test_status_flags_nan_and_clear(prec):
     """A NaN planted in the uploaded state is flagged by the stage kernel and
     reported as an error by the run loop (the reference aborts on NaN)."""
     from microfc_gb300._lib import MfcError, MFC_FLAG_NAN
-    case = cases.sod_1d(m=99, steps=2, dt=1e-4)
+    case = cases.sod_1d(m=99, steps=2, dt=1e-4).replace(precision=prec)
     x_cb, _, _, q = preprocess.generate(case)
     q[0, 0, 0, 50] = np.nan
     with Simulation(case, x_cb, q_cons=q) as sim:
