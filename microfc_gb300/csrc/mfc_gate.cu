@@ -171,10 +171,13 @@ __global__ void gate_adam_kernel(float* __restrict__ w, const float* __restrict_
   w[i] -= lr * mh / (sqrtf(vh) + eps);
 }
 
-// Lane fragments [kGateFragWords][32] of the FP16 parameters (GateFragsSmem layout).
+// Lane fragments of the FP16 parameters in the GateFragsSmem layout.
 __global__ void gate_frag_kernel(const __half* __restrict__ wh, uint32_t* __restrict__ frag) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < mfc::kGateFragWords * 32) frag[i] = mfc::gate_frag_word(wh, i & 31, i >> 5);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // (word, lane)
+  if (i < mfc::kGateFragWords * 32) {
+    const int word = i >> 5, lane = i & 31;
+    frag[mfc::gate_frag_index(lane, word)] = mfc::gate_frag_word(wh, lane, word);
+  }
 }
 
 __global__ void gate_to_half_kernel(const float* __restrict__ w, __half* __restrict__ h) {
@@ -185,16 +188,16 @@ __global__ void gate_to_half_kernel(const float* __restrict__ w, __half* __restr
 // Tensor-core inference of n inputs (16 per warp); logits out.
 __global__ void gate_infer_kernel(const float* __restrict__ X, int n, const __half* __restrict__ wh,
                                   float* __restrict__ logits) {
-  __shared__ __half buf[8][16 * 16];
+  __shared__ __align__(16) __half buf[8][16 * 16];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   mfc::GateFrags F;
   mfc::gate_load_frags(wh, F);
   const int base = (blockIdx.x * 8 + warp) * 16;
   __half* my = buf[warp];
   for (int k = lane; k < 256; k += 32) {
-    const int r = k / 16, col = k % 16;
+    const int r = k / 16, f = mfc::gate_feature_of_col(k % 16);
     const int b = base + r;
-    my[k] = __float2half((b < n && col < mfc::kGateIn) ? X[b * mfc::kGateIn + col] : 0.f);
+    my[k] = __float2half((b < n && f >= 0) ? X[b * mfc::kGateIn + f] : 0.f);
   }
   __syncwarp();
   float lo, hi;

@@ -249,9 +249,10 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
     const int warp = tid >> 5, lane = tid & 31;
     const uint32_t* gsrc =
         reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(P.gate_w) + kGateFragOffset);
-    for (int i = tid; i < kGateFragWords * 32; i += NT) frag[i] = __ldg(gsrc + i);
+    for (int i = tid; i < kGateFragWords * 8; i += NT)
+      reinterpret_cast<uint4*>(frag)[i] = __ldg(reinterpret_cast<const uint4*>(gsrc) + i);
     __syncthreads();
-    const GateFragsSmem F{frag + lane};
+    const GateFragsSmem F{frag + 4 * lane};
     __half* my = gin + warp * 256;
     constexpr int NG = G::NGX + G::NGY, NCH = (NG + 15) / 16;
     for (int ch = warp; ch < NCH; ch += NT / 32) {
@@ -271,13 +272,10 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       }
       float xf[5];
       gate_norm5_var(s, xf, lane < 16 ? 0 : 1);
-      __half* r = my + (lane & 15) * 16;
-#pragma unroll
-      for (int k = 0; k < 5; ++k) r[(lane < 16 ? 0 : 5) + k] = __float2half(xf[k]);
-      if (lane >= 16) {
-#pragma unroll
-        for (int k = 10; k < 16; ++k) r[k] = __float2half(0.f);
-      }
+      // columns 0..7 (alpha_1) or 8..15 (pressure) of the cell's row: five
+      // features and three zeros, one 16-byte store
+      const uint4 half8 = make_uint4(pack_h2(xf[0], xf[1]), pack_h2(xf[2], xf[3]), pack_h2(xf[4], 0.f), 0u);
+      reinterpret_cast<uint4*>(my + (lane & 15) * 16)[lane >> 4] = half8;
       __syncwarp();
       float lo, hi;
       gate_mlp16(my, F, lo, hi);
