@@ -209,7 +209,8 @@ def _time_steps(sim, stream, flush, steps, warmup, dt):
 
 def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
     """Split precision, split + learned gate (the gated FP32 form) on the same
-    workload, and the 64-case ensemble of config 5 against 64 sequential
+    workload, the 3-D shock-bubble of config 3 in split precision against
+    plain FP64, and the 64-case ensemble of config 5 against 64 sequential
     plain FP64 runs.  Accuracy of these modes against FP64 is asserted by
     tests/test_gpu_parity.py, tests/test_gate.py and tests/test_ensemble.py."""
     import torch
@@ -230,6 +231,20 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
                          "vs_plain_fp64": rate / fp64_rate, "tile_variant": variant}
     if params is None:
         out["gated"] = {"unavailable": "no trained gate parameters (python -m microfc_gb300.gate)"}
+    # config 3: the 3-D air/helium shock-bubble at 256^3, split precision,
+    # against plain FP64 on the same case (states of 1 GB per register: no
+    # L2 reuse between steps)
+    from microfc_gb300 import cases
+    c3 = cases.shock_bubble_3d(N=256, steps=500, precision="split")
+    r3, v3 = {}, {}
+    for prec3, n3 in (("split", 10), ("fp64", 2)):
+        with Simulation(c3.replace(precision=prec3), ic="device") as s:
+            v3[prec3], _ = s.tune(2)
+            st = torch.cuda.ExternalStream(s.stream)
+            r3[prec3] = c3.cells * n3 / _time_steps(s, st, flush, n3, 2, c3.dt)
+    out["split_3d"] = {"workload": "3-D air/helium shock-bubble 256^3, 2 fluids, WENO5-JS + HLLC + TVD-RK3",
+                       "value": r3["split"], "unit": "cell-updates/s", "steps": 10, "tile_variant": v3["split"],
+                       "plain_fp64": r3["fp64"], "vs_plain_fp64": r3["split"] / r3["fp64"]}
     # config 5: 64 cases, nx in {128,256,384,512}, ny = nx/2, seed 0
     prec = "gated" if params is not None else "split"
     cl = random_droplet_cases(count=64, seed=0, steps=500, precision=prec)
