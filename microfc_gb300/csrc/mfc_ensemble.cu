@@ -58,6 +58,8 @@ struct mfc_gpu_ensemble {
   cudaStream_t stream = nullptr;
   const mfc::EnsembleEntry* entry = nullptr;
   int grid = 0, total_tiles = 0;
+  size_t smem = 0;
+  mfc::UniformCoef U{};  // the shared coefficient record of all cases (split WENO5, uniform grids)
   int64_t launches = 0;
   mfc::EnsParams* ep = nullptr;  // host staging of the kernel parameters
 };
@@ -67,8 +69,9 @@ namespace {
 int configure(mfc_gpu_ensemble* e, const mfc::EnsembleEntry* en) {
   cudaError_t err = cudaFuncSetAttribute(en->func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)en->smem);
   if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+  const size_t smem = (e->U.on[0] && e->U.on[1]) ? en->smem_shared_coef : en->smem;
   int bps = 0, sms = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, en->func, en->nt, en->smem);
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, en->func, en->nt, smem);
   if (err == cudaSuccess) err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, e->device);
   if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
   if (bps < 1) return mfc::report_error(MFC_ERR_INVALID, "ensemble tile variant does not fit on an SM");
@@ -81,6 +84,7 @@ int configure(mfc_gpu_ensemble* e, const mfc::EnsembleEntry* en) {
   }
   e->total_tiles = base;
   e->grid = std::min(base, bps * sms);
+  e->smem = smem;
   e->entry = en;
   return MFC_OK;
 }
@@ -92,8 +96,9 @@ int launch_stage(mfc_gpu_ensemble* e, int stage, int last) {
   E.stage = stage;
   E.time_stepper = e->ts;
   E.last_step = last;
+  E.U = e->U;
   for (int i = 0; i < e->num; ++i) E.c[i] = e->cases[i];
-  cudaError_t err = e->entry->launch(E, e->grid, e->stream);
+  cudaError_t err = e->entry->launch(E, e->grid, e->smem, e->stream);
   if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
   e->launches += 1;
   return MFC_OK;
@@ -191,6 +196,11 @@ int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_ca
     D.weno_eps = p.weno_eps;
     mfc::set_fp32_constants(D);
     D.coff = mfc::kCoefPad;
+    // one shared record when every case's grid gives the same uniform record
+    mfc::UniformCoef u;
+    mfc::uniform_records(gts[i], 2, n, p.weno_order, p.precision, u);
+    if (i == 0) e->U = u;
+    else if (std::memcmp(&u, &e->U, sizeof(u)) != 0) e->U = mfc::UniformCoef{};
     const int S = 2 * p.num_fluids + 3;
     reg_off[i] = state_elems;
     state_elems += 3 * D.sv * S;

@@ -26,6 +26,10 @@ struct EnsCase {
 
 struct EnsParams {
   int num_cases, total_tiles, stage, time_stepper, last_step;
+  // split WENO5: the coefficient record every cell of every case shares when
+  // all cases have uniform grids (the FP32 records of a uniform grid do not
+  // depend on its spacing); all off otherwise
+  UniformCoef U;
   EnsCase c[kMaxEnsemble];
 };
 static_assert(sizeof(EnsParams) <= 32764, "ensemble parameters must fit the kernel parameter space");
@@ -56,22 +60,21 @@ __global__ void __launch_bounds__(NT) ensemble_stage_kernel(const __grid_constan
       in = C.reg[2], out = C.reg[0], kind = kRk3Final;
     }
     stage_tile<2, NF, WO, RT, TX, TY, NT, GATE>(C.P, in, C.reg[0], out, E.last_step ? C.dt_last : C.dt, kind, x0,
-                                                y0, smem_raw);
+                                                y0, smem_raw, &E.U);
     __syncthreads();  // the next tile reuses the shared memory
   }
 }
 
 struct EnsembleEntry {
   int nf, wo, prec, tx, ty, nt;
-  size_t smem;
+  size_t smem, smem_shared_coef;  // dynamic shared memory: per-cell records / shared record
   const void* func;
-  cudaError_t (*launch)(const EnsParams& E, int grid, cudaStream_t st);
+  cudaError_t (*launch)(const EnsParams& E, int grid, size_t smem, cudaStream_t st);
 };
 
 template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE>
-cudaError_t ensemble_launch(const EnsParams& E, int grid, cudaStream_t st) {
-  ensemble_stage_kernel<NF, WO, RT, TX, TY, NT, GATE>
-      <<<grid, NT, stage_smem_bytes<2, NF, WO, RT, TX, TY, NT, GATE>(), st>>>(E);
+cudaError_t ensemble_launch(const EnsParams& E, int grid, size_t smem, cudaStream_t st) {
+  ensemble_stage_kernel<NF, WO, RT, TX, TY, NT, GATE><<<grid, NT, smem, st>>>(E);
   return cudaGetLastError();
 }
 
@@ -80,6 +83,7 @@ template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
 EnsembleEntry ensemble_entry() {
   return EnsembleEntry{NF, WO, sizeof(RT) == 8 ? 0 : (GATE ? 2 : 1), TX, TY, NT,
                        stage_smem_bytes<2, NF, WO, RT, TX, TY, NT, GATE>(),
+                       stage_smem_bytes_shared_coef<2, NF, WO, RT, TX, TY, NT, GATE>(),
                        reinterpret_cast<const void*>(&ensemble_stage_kernel<NF, WO, RT, TX, TY, NT, GATE>),
                        &ensemble_launch<NF, WO, RT, TX, TY, NT, GATE>};
 }
