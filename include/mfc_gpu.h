@@ -136,8 +136,13 @@ int mfc_gpu_tvd_rk(mfc_gpu_ctx* ctx, double dt, int last_step);
  * live on one GPU, or through a send/receive pair across GPUs -- and then
  * runs mfc_gpu_rk_stage.  mfc_gpu_tvd_rk and mfc_gpu_run refuse such a
  * context.  Layouts (depth d = 0 next to the boundary, H = (weno_order+1)/2):
- * x sides [S][p+1][n+1][H], y sides [S][p+1][H][m+1], z sides
- * [S][H][n+1][m+1]. */
+ * x sides [S][p+1][n+1][H], y sides [S][p+1][H][m+1] in 3-D and [S][H][m+3]
+ * in 2-D, z sides [S][H][n+1][m+1].  A 2-D y strip carries the sender's x
+ * ghost cells -1 and m+1 of each row in its first and last column (from its
+ * own x receive buffers at processor boundaries): the diagonal neighbours'
+ * cells that the viscous corner gradients read.  So in 2-D the x strips of a
+ * stage are exchanged first and the y strips packed after they arrived, as
+ * the reference exchanges x before y (m_mpi_proxy.fpp). */
 int mfc_gpu_rk_stage(mfc_gpu_ctx* ctx, int stage, double dt);
 int mfc_gpu_halo_buffer(mfc_gpu_ctx* ctx, int dir, int side, double** dev_ptr, int64_t* count);
 /* The neighbour's cell widths beyond a processor boundary (widths[i] = ghost
@@ -165,8 +170,8 @@ int mfc_gpu_status(mfc_gpu_ctx* ctx, uint32_t* flags, int clear);
  * re_shear[i] / re_bulk[i] are fluid_pp(i+1)%Re(1) / %Re(2) for the
  * context's fluids (NULL or values <= 0: none).  The velocity gradients are
  * the reference's one-sided face differences (weno_Re_flux = F).  1-D and
- * 2-D contexts without processor boundaries; all-zero Reynolds numbers switch
- * back to the inviscid kernels.  Call before stepping. */
+ * 2-D contexts, with or without processor boundaries; all-zero Reynolds
+ * numbers switch back to the inviscid kernels.  Call before stepping. */
 int mfc_gpu_set_viscosity(mfc_gpu_ctx* ctx, const double* re_shear, const double* re_bulk);
 
 /* Split and gated WENO5 on a uniform grid (no reference counterpart): when

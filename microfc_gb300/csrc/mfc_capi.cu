@@ -144,9 +144,18 @@ __global__ void prim_kernel(const mfc::DevParams P, const double* __restrict__ q
 // Boundary strip of a stage input for the neighbour across (dir, side), in
 // the neighbour's halo layout (depth d = 0 is the cell next to the
 // boundary): dir 0 [S][nz][ny][H], dir 1 [S][nz][H][nx], dir 2 [S][H][ny][nx].
+// Strip of one processor boundary for the neighbour's receive buffer.  In
+// 2-D the y strips are widened by one column on each side (wy = nx + 2): the
+// x ghost cells -1 and nx of the packed rows, taken from this subdomain's own
+// x receive buffers (xh0/xh1, depth 0) where x is a processor boundary, else
+// from its x boundary condition.  They carry the diagonal neighbour's cells
+// to the y neighbour, whose viscous corner gradients read them; the x
+// strips must therefore have arrived before the y strips are packed.
 __global__ void halo_pack_kernel(const double* __restrict__ q, int S, int nx, int ny, int nz, int64_t sy, int64_t sz,
-                                 int64_t sv, int H, int dir, int side, double* __restrict__ dst) {
-  const int64_t total = (int64_t)S * H * (dir == 0 ? (int64_t)ny * nz : dir == 1 ? (int64_t)nx * nz : (int64_t)nx * ny);
+                                 int64_t sv, int H, int dir, int side, int wy, const double* __restrict__ xh0,
+                                 const double* __restrict__ xh1, int bcx_beg, int bcx_end, int mom,
+                                 double* __restrict__ dst) {
+  const int64_t total = (int64_t)S * H * (dir == 0 ? (int64_t)ny * nz : dir == 1 ? (int64_t)wy * nz : (int64_t)nx * ny);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
     int x, y, z, d, v;
     if (dir == 0) {
@@ -156,11 +165,23 @@ __global__ void halo_pack_kernel(const double* __restrict__ q, int S, int nx, in
       v = (int)(i / ((int64_t)H * ny * nz));
       x = side == 0 ? d : nx - 1 - d;
     } else if (dir == 1) {
-      x = (int)(i % nx);
-      d = (int)((i / nx) % H);
-      z = (int)((i / ((int64_t)nx * H)) % nz);
-      v = (int)(i / ((int64_t)nx * H * nz));
+      x = (int)(i % wy) - (wy - nx) / 2;
+      d = (int)((i / wy) % H);
+      z = (int)((i / ((int64_t)wy * H)) % nz);
+      v = (int)(i / ((int64_t)wy * H * nz));
       y = side == 0 ? d : ny - 1 - d;
+      if (x < 0 || x >= nx) {  // widened 2-D strip: an x ghost cell of row y
+        const double* xh = x < 0 ? xh0 : xh1;
+        if (xh) {
+          dst[i] = xh[(int64_t)(v * ny + y) * H];
+        } else {
+          bool flip = false;
+          const int gx = mfc::map_cell(x, nx, bcx_beg, bcx_end, &flip);
+          const double val = q[v * sv + y * sy + gx];
+          dst[i] = (flip && v == mom) ? -val : val;
+        }
+        continue;
+      }
     } else {
       x = (int)(i % nx);
       y = (int)((i / nx) % ny);
@@ -170,6 +191,14 @@ __global__ void halo_pack_kernel(const double* __restrict__ q, int S, int nx, in
     }
     dst[i] = q[v * sv + z * sz + y * sy + x];
   }
+}
+
+// Elements of the strip across direction dir (2-D y strips are widened by
+// the two x ghost cells).
+int64_t strip_elems(const mfc_gpu_ctx* c, int dir) {
+  const int64_t wy = c->nd == 2 ? c->n[0] + 2 : c->n[0];
+  return (int64_t)c->S * c->H *
+         (dir == 0 ? (int64_t)c->n[1] * c->n[2] : dir == 1 ? wy * c->n[2] : (int64_t)c->n[0] * c->n[1]);
 }
 
 int copy_var(mfc_gpu_ctx* c, double* dev_reg, int var, const double* host, double* host_out, int64_t ld_y,
@@ -274,8 +303,7 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
       if ((side == 0 ? bcb[d] : bce[d]) < 0) continue;
       c->has_proc = true;
       const int k = 2 * d + side;
-      c->halo_count[k] = (int64_t)c->S * c->H * (d == 0 ? (int64_t)c->n[1] * c->n[2]
-                                                 : d == 1 ? (int64_t)c->n[0] * c->n[2] : (int64_t)c->n[0] * c->n[1]);
+      c->halo_count[k] = strip_elems(c, d);
       if ((e = cudaMalloc(&c->halo_buf[k], sizeof(double) * c->halo_count[k])) != cudaSuccess)
         return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
       cudaMemsetAsync(c->halo_buf[k], 0, sizeof(double) * c->halo_count[k], c->stream);
@@ -495,14 +523,12 @@ int mfc_gpu_halo_pack(mfc_gpu_ctx* c, int stage, int dir, int side, double* dst)
     return fail(MFC_ERR_INVALID, "bad halo pack arguments");
   if (stage < 0 || stage >= c->prm.time_stepper) return fail(MFC_ERR_INVALID, "stage out of range");
   const double* q = stage == 0 ? c->reg[0] : stage == 1 ? c->reg[1] : c->reg[2];
-  const int64_t total = c->halo_count[2 * dir + side] > 0
-                            ? c->halo_count[2 * dir + side]
-                            : (int64_t)c->S * c->H *
-                                  (dir == 0 ? (int64_t)c->n[1] * c->n[2]
-                                            : dir == 1 ? (int64_t)c->n[0] * c->n[2] : (int64_t)c->n[0] * c->n[1]);
+  const int64_t total = strip_elems(c, dir);
   const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 8);
+  const int wy = c->nd == 2 ? c->n[0] + 2 : c->n[0];
   halo_pack_kernel<<<blocks, 256, 0, c->stream>>>(q, c->S, c->n[0], c->n[1], c->n[2], c->sy, c->sz, c->sv, c->H,
-                                                  dir, side, dst);
+                                                  dir, side, wy, c->halo_buf[0], c->halo_buf[1], c->prm.bc_x_beg,
+                                                  c->prm.bc_x_end, c->prm.num_fluids, dst);
   MFC_CUDA(cudaGetLastError());
   c->launches += 1;
   return MFC_OK;
@@ -528,7 +554,6 @@ int mfc_gpu_set_viscosity(mfc_gpu_ctx* c, const double* re_shear, const double* 
     return MFC_OK;
   }
   if (c->nd > 2) return fail(MFC_ERR_INVALID, "viscous terms are built for 1-D and 2-D cases");
-  if (c->has_proc) return fail(MFC_ERR_INVALID, "viscous terms with processor boundaries are not supported");
   const mfc::StageEntry* e = mfc::find_stage(c->nd, nf, c->prm.weno_order, c->prm.precision, true);
   if (!e) return fail(MFC_ERR_INVALID, "no viscous kernel compiled for this fluid count / WENO order / precision");
   for (int d = 0; d < c->nd; ++d) V.dcc[d] = c->tables + c->off_dcc[d];

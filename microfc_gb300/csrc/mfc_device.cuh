@@ -39,9 +39,10 @@ struct DevParams {
   unsigned long long* monitor;  // set on a step's last stage: max ICFL of the new state (double bits)
   // processor boundaries (bc >= 0): device table of 6 halo buffers, [2*dir + side]
   // (NULL where the side is a physical boundary); the whole table is NULL
-  // when the context has no processor boundary.  x sides: [S][ny][H] (depth
-  // fastest), y sides: [S][H][nx]; depth d = 0 is the ghost cell next to the
-  // boundary.
+  // when the context has no processor boundary.  x sides: [S][nz][ny][H]
+  // (depth fastest), y sides: [S][H][nx + 2] in 2-D (the x ghost cells -1
+  // and nx of each row first and last), [S][nz][H][nx] in 3-D, z sides:
+  // [S][H][ny][nx]; depth d = 0 is the ghost cell next to the boundary.
   const double* const* halo;
   const struct ViscParams* visc;  // viscous cases: Reynolds numbers and spacing tables (NULL: inviscid)
 };

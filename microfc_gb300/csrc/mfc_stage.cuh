@@ -184,17 +184,25 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
     const int py = (ND > 1) ? (ry < 0 ? (P.bc_beg[1] >= 0 ? 0 : -1) : (ry >= ny && P.bc_end[1] >= 0 ? 1 : -1)) : -1;
     const double* src;
     int64_t vs = P.sv;
-    if (px >= 0) {
-      // cells of partial edge tiles beyond the first H ghosts are never stored: clamp
+    // cells of partial edge tiles beyond the first H ghosts are never stored:
+    // their depth is clamped.  y strips are nx + 2 wide (the x ghost cells
+    // -1 and nx of the neighbour's rows come first and last).
+    if (px >= 0 && py >= 0) {
+      // between two processor boundaries (the viscous corner cells): the
+      // diagonal neighbour's cell, forwarded by the y neighbour
+      const int d = min(py == 0 ? -1 - ry : ry - ny, H - 1);
+      src = P.halo[2 + py] + (int64_t)d * (nx + 2) + (px == 0 ? 0 : nx + 1);
+      vs = (int64_t)H * (nx + 2);
+    } else if (px >= 0) {
       const int d = min(px == 0 ? -1 - rx : rx - nx, H - 1);
-      const int yy = ry < 0 ? 0 : (ry >= ny ? ny - 1 : ry);  // rows beyond the domain are never stored
+      const int yy = (ND > 1) ? map_cell(ry, ny, P.bc_beg[1], P.bc_end[1], &fy) : 0;
       src = P.halo[px] + (int64_t)yy * H + d;
       vs = (int64_t)ny * H;
     } else if (py >= 0) {
       const int d = min(py == 0 ? -1 - ry : ry - ny, H - 1);
-      const int xx = rx < 0 ? 0 : (rx >= nx ? nx - 1 : rx);
-      src = P.halo[2 + py] + (int64_t)d * nx + xx;
-      vs = (int64_t)H * nx;
+      const int xx = map_cell(rx, nx, P.bc_beg[0], P.bc_end[0], &fx);
+      src = P.halo[2 + py] + (int64_t)d * (nx + 2) + xx + 1;
+      vs = (int64_t)H * (nx + 2);
     } else {
       const int gx = map_cell(rx, nx, P.bc_beg[0], P.bc_end[0], &fx);
       const int gy = (ND > 1) ? map_cell(ry, ny, P.bc_beg[1], P.bc_end[1], &fy) : 0;

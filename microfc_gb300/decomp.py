@@ -12,8 +12,8 @@ Every RK stage needs the neighbours' strips of that stage's input (the
 halo exchange of s_populate_conservative_variables_buffers, m_rhs.fpp:434
 and m_mpi_proxy.fpp:468-979).  ``MultiDomain`` runs all subdomains on one
 GPU: each subdomain packs its strips straight into the neighbours' receive
-buffers (mfc_gpu_halo_pack / mfc_gpu_halo_buffer), then every subdomain
-runs the stage (mfc_gpu_rk_stage).  ``exchange`` is the rank-to-rank form:
+buffers (mfc_gpu_halo_pack / mfc_gpu_halo_buffer), x strips before y
+strips, then every subdomain runs the stage (mfc_gpu_rk_stage).  ``exchange`` is the rank-to-rank form:
 send/receive pairs of packed strips through torch.distributed (NCCL between
 GPUs, gloo on the host).
 """
@@ -99,15 +99,49 @@ def decompose(case: Case, x_cb, y_cb=None, px: int = 2, py: int = 1, pz: int = 1
     return subs
 
 
-def halo_strip(sub: Subdomain, q_local: np.ndarray, d: int, side: int, H: int) -> np.ndarray:
+def _map_x(c: int, n: int, bcb: int, bce: int):
+    """Ghost index mapping of one x index (mfc::map_cell): (cell, flip)."""
+    if c < 0:
+        flip = bcb == -2
+        c = c + n if bcb == -1 else (-c - 1 if bcb == -2 else 0)
+    elif c >= n:
+        flip = bce == -2
+        c = c - n if bce == -1 else (2 * n - 1 - c if bce == -2 else n - 1)
+    else:
+        flip = False
+    return min(max(c, 0), n - 1), flip
+
+
+def halo_strip(sub: Subdomain, q_local: np.ndarray, d: int, side: int, H: int, x_ghosts=None) -> np.ndarray:
     """Host restatement of mfc_gpu_halo_pack: the strip of a local state
     [S, p+1, n+1, m+1] that the neighbour across (d, side) needs, in its
     receive-buffer layout (depth 0 next to the boundary): x [S][p+1][n+1][H],
-    y [S][p+1][H][m+1], z [S][H][n+1][m+1]."""
+    y [S][p+1][H][m+1] in 3-D, z [S][H][n+1][m+1].  A 2-D y strip is
+    [S][1][H][m+3]: its first and last columns are the x ghost cells -1 and
+    m+1 of the packed rows -- x_ghosts = (left, right), each [S, n+1], the
+    depth-0 columns this subdomain received across its x processor
+    boundaries (None on a side with a physical boundary, which the x
+    boundary condition fills)."""
     axis = 3 - d  # array axis of direction d
     n = q_local.shape[axis]
     idx = [k if side == 0 else n - 1 - k for k in range(H)]
-    return np.ascontiguousarray(np.take(q_local, idx, axis=axis))  # depth replaces the axis
+    strip = np.take(q_local, idx, axis=axis)  # depth replaces the axis
+    c = sub.case
+    if d == 1 and c.p == 0:
+        m1 = q_local.shape[3]
+        cols = []
+        for j, x in enumerate((-1, m1)):
+            g = None if x_ghosts is None else x_ghosts[j]
+            if g is not None:
+                col = np.asarray(g)[:, idx]
+            else:
+                gx, flip = _map_x(x, m1, c.bc_x[0], c.bc_x[1])
+                col = q_local[:, 0, idx, gx].copy()
+                if flip:
+                    col[c.num_fluids] = -col[c.num_fluids]
+            cols.append(col[:, None, :, None])
+        strip = np.concatenate([cols[0], strip, cols[1]], axis=3)
+    return np.ascontiguousarray(strip)
 
 
 def ghost_widths(neighbor: Subdomain, d: int, side: int, b: int) -> np.ndarray:
@@ -123,11 +157,15 @@ def exchange(sub: Subdomain, strips: dict, group=None) -> dict:
     across (d, side) and returns what each neighbour sent, keyed by the side
     it arrives on.  Tensors may live on the host (gloo) or the GPU (NCCL);
     every send is matched by the neighbour's receive on its opposite side, so
-    the pattern is the same on every rank and cannot deadlock."""
+    the pattern is the same on every rank and cannot deadlock.  Only the
+    sides in `strips` are exchanged: a 2-D run exchanges its x strips first
+    and packs its y strips after they arrived (the y strips forward the
+    diagonal neighbours' cells), as the reference exchanges x before y."""
     import torch
     import torch.distributed as dist
     reqs, out = [], {}
-    for (d, side), peer in sorted(sub.neighbors.items()):
+    for (d, side) in sorted(strips):
+        peer = sub.neighbors[(d, side)]
         t = strips[(d, side)]
         buf = torch.empty_like(t)
         out[(d, side)] = buf
@@ -176,12 +214,18 @@ class MultiDomain:
 
     def step(self, dt: float) -> None:
         import torch
+        nd = 1 + (self.case.n > 0) + (self.case.p > 0)
         for stage in range(self.case.time_stepper):
-            for s, sim in zip(self.subs, self.sims):
-                for (d, side), peer in s.neighbors.items():
-                    dst = self._buffer(peer, d, 1 - side)
-                    _lib.check(self.L.mfc_gpu_halo_pack(sim._h, stage, d, side, ctypes.c_void_p(dst)))
-            torch.cuda.synchronize()
+            # one direction at a time: a 2-D y strip forwards the x ghost
+            # cells its subdomain has just received
+            for d in range(nd):
+                for s, sim in zip(self.subs, self.sims):
+                    for (dd, side), peer in s.neighbors.items():
+                        if dd != d:
+                            continue
+                        dst = self._buffer(peer, d, 1 - side)
+                        _lib.check(self.L.mfc_gpu_halo_pack(sim._h, stage, d, side, ctypes.c_void_p(dst)))
+                torch.cuda.synchronize()
             for sim in self.sims:
                 _lib.check(self.L.mfc_gpu_rk_stage(sim._h, stage, float(dt)))
             torch.cuda.synchronize()

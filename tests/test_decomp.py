@@ -54,7 +54,41 @@ def test_2d_grid_of_subdomains_and_halo_strips():
                 else:
                     gy = o.start[1] - 1 - k if side == 1 else o.start[1] + o.case.n + 1 + k
                     ref = q[:, 0, gy, o.start[0]:o.start[0] + o.case.m + 1]
-                    assert np.array_equal(strip[:, 0, k, :], ref)
+                    assert strip.shape[3] == o.case.m + 3  # widened by the two x ghost cells
+                    assert np.array_equal(strip[:, 0, k, 1:-1], ref)
+
+
+def test_2d_y_strips_forward_the_diagonal_cells():
+    """The first and last columns of a 2-D y strip are the sender's x ghost
+    cells: across an x processor boundary the diagonal neighbour's cells (what
+    the receiver's viscous corner gradients read), elsewhere the x boundary
+    condition's ghost value."""
+    c = cases.shock_droplet_2d(nx=128, ny=64, steps=2).replace(bc_x=(-2, -3))
+    x_cb, y_cb, _, q = preprocess.generate(c)
+    q = q + np.arange(q.size, dtype=np.float64).reshape(q.shape) * 1e-3  # distinct values everywhere
+    subs = decomp.decompose(c, x_cb, y_cb, px=2, py=2)
+    H = 3
+    for s in subs:
+        sx, sy = s.start[0], s.start[1]
+        rows = slice(sy, sy + s.case.n + 1)
+        left = q[:, 0, rows, sx - 1] if (0, 0) in s.neighbors else None
+        right = q[:, 0, rows, sx + s.case.m + 1] if (0, 1) in s.neighbors else None
+        for (d, side), peer in s.neighbors.items():
+            if d != 1:
+                continue
+            strip = decomp.halo_strip(s, q[s.window()], 1, side, H, x_ghosts=(left, right))
+            for k in range(H):
+                gy = sy + k if side == 0 else sy + s.case.n - k
+                if left is not None:
+                    assert np.array_equal(strip[:, 0, k, 0], q[:, 0, gy, sx - 1])
+                else:  # symmetry: the mirrored edge cell with the x-momentum flipped
+                    want = q[:, 0, gy, sx].copy()
+                    want[c.num_fluids] *= -1
+                    assert np.array_equal(strip[:, 0, k, 0], want)
+                if right is not None:
+                    assert np.array_equal(strip[:, 0, k, -1], q[:, 0, gy, sx + s.case.m + 1])
+                else:  # extrapolation: the edge cell
+                    assert np.array_equal(strip[:, 0, k, -1], q[:, 0, gy, sx + s.case.m])
 
 
 def _free_port():
@@ -120,6 +154,61 @@ def test_subdomains_on_one_gpu_reproduce_the_whole_domain(kind):
     assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
 
 
+def _viscous_case(kind):
+    """A viscous case and its process grid.  "dyadic" grids have cell
+    boundaries k * 2^-j, so every cell centre and centre spacing is exact."""
+    if kind.startswith("sod"):
+        c = cases.sod_1d(m=255, steps=20, dt=5e-5).replace(re_shear=(50.0, 80.0), re_bulk=(30.0, 0.0))
+        x_cb, _, _, q = preprocess.generate(c)
+        return c, x_cb, None, q, 3, 1
+    prec = kind.split("_")[-1]
+    c = cases.shock_droplet_2d(nx=128, ny=64, steps=20, precision=prec)
+    c = c.replace(re_shear=(1.0 / 1e-1, 1.0 / 2e-3), re_bulk=(0.0, 1.0 / 5e-3))
+    if "periodic" in kind:
+        c = c.replace(bc_x=(-1, -1), bc_y=(-1, -1))
+    x_cb, y_cb, _, q = preprocess.generate(c)
+    if "dyadic" in kind:  # same number of cells, spacing 2^-13 instead of 0.02/128
+        x_cb = np.arange(-1, c.m + 1, dtype=np.float64) * 2.0 ** -13
+        y_cb = np.arange(-1, c.n + 1, dtype=np.float64) * 2.0 ** -13
+    return c, x_cb, y_cb, q, int(kind[0]), int(kind[2])
+
+
+def _whole_and_split(c, x_cb, y_cb, q, px, py):
+    from microfc_gb300 import Simulation
+    assert c.viscous
+    with Simulation(c, x_cb, y_cb, q_cons=q) as sim:
+        sim.run(0, 20)
+        ref = sim.download()
+    with decomp.MultiDomain(c, x_cb, y_cb, q_cons=q, px=px, py=py) as md:
+        md.run(0, 20)
+        got = md.download()
+    return got, ref
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["2x2_dyadic_fp64", "3x2_dyadic_split", "4x1_dyadic_fp64", "sod3_fp64",
+                                  "2x2_periodic_dyadic_fp64"])
+def test_viscous_subdomains_reproduce_the_whole_domain(kind):
+    """Viscous terms across processor boundaries, including the corner cells
+    of the cross derivatives that come from the diagonal neighbours: bit for
+    bit where the cell centres are exact (dyadic grids; the 1-D Sod grid has
+    256 cells on [0, 1])."""
+    got, ref = _whole_and_split(*_viscous_case(kind))
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.gpu
+def test_viscous_subdomains_on_a_general_grid():
+    """On a general grid a subdomain builds its ghost cell centre from the
+    neighbour's width, x_cc(-1) = x_cc(0) - (dx(0) + dx(-1))/2, as the
+    reference's s_populate_grid_variables_buffers does after the width
+    exchange; the undecomposed run takes the interior centre x_cb + dx/2.
+    The two centre spacings differ in the last bit, so the viscous gradients
+    next to a processor boundary do too: the runs agree to round-off."""
+    from conftest import rel_l1
+    got, ref = _whole_and_split(*_viscous_case("4x1_fp64"))
+    err = rel_l1(got, ref)
+    assert err.max() <= 1e-10, err
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", ["fp64", "split"])
 def test_3d_subdomains_reproduce_the_whole_domain(prec):

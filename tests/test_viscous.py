@@ -81,14 +81,8 @@ def test_split_precision_viscous_error_bounded(oracle_lib):
 
 
 def test_viscous_refusals():
-    from microfc_gb300 import Simulation, decomp
+    from microfc_gb300 import Simulation
     from microfc_gb300._lib import MfcError
-    c = cases.sod_1d(m=99, steps=2)
-    x_cb, _, _, q = preprocess.generate(c)
-    s = decomp.decompose(c, x_cb, px=2)[0]
-    with Simulation(s.case, s.x_cb, q_cons=np.ascontiguousarray(q[s.window()]), check=False) as sim:
-        with pytest.raises(MfcError, match="processor boundaries"):
-            sim.set_viscosity((10.0, 10.0))
     b = cases.shock_bubble_3d(N=28, steps=2, precision="fp64")
     with Simulation(b) as sim:
         with pytest.raises(MfcError, match="1-D and 2-D"):
