@@ -180,13 +180,14 @@ __device__ __forceinline__ float rcp_approx(float x) {
 //               rescaled by b's exponent with integer operations;
 //               y = y0 + y0 (1 - b y0)                 |y b - 1| < 2^-42
 //   div_rn(a):  q0 = a y;  r0 = a - b q0 (one rounding);  q1 = q0 + r0 y,
-//               so |q1 - a/b| < ulp(q1)/2 + 2^-80 |a/b| < ulp(q1) and
-//               r1 = a - b q1 is exact.  |a/b - q1| = |r1| / |b| is then
-//               compared, with integer operations on the bit patterns,
-//               against half the spacing of doubles from q1 towards a/b;
-//               beyond it the neighbour is the rounded quotient.
+//               so |q1 - a/b| < ulp(q1)/2 + 2^-80 |a/b| < ulp(q1) and the
+//               remainder a - b q1 is exact.  It is formed in 64-bit
+//               integer arithmetic from the significands (GB300's integer
+//               pipes are idle while its FP64 pipe is the bottleneck) and
+//               compared against half the spacing of doubles from q1
+//               towards a/b; beyond it the neighbour is the rounded quotient.
 //
-// A divisor costs 2 FP64 operations, each quotient 4 (one multiply and three
+// A divisor costs 2 FP64 operations, each quotient 3 (one multiply and two
 // FMAs).  The argument holds while |a| and |b| lie in [2^-250, 2^251): then
 // every intermediate (q near 2^+-501, residuals near |b| ulp(q)) is a normal
 // double.  Anything else (zero, subnormal, huge, inf or NaN operands) takes
@@ -225,17 +226,24 @@ __device__ __forceinline__ double div_rn(double a, const DivisorF64& d) {
   const double q0 = a * d.y;
   const double r0 = fma(-d.b, q0, a);
   const double q1 = fma(r0, d.y, q0);
-  const double r1 = fma(-d.b, q1, a);
+  // The rounding test on the exact remainder, in integer arithmetic.  With
+  // the significands A, B, Q (53 bits with the implicit one), the biased
+  // exponents Ea, Eb, Eq and u = 2^(Eb+Eq-2150):
+  //   |a| - |b| |q1| = D u,   D = A 2^(Ea-Eb-Eq+1075) - B Q,
+  // and |D| < B < 2^53 because q1 is within one ulp of a/b; so D is the
+  // difference of the two products' low 64 bits.  Half the spacing of
+  // doubles from q1 towards a/b is B/2 in units u (B/4 below a power of two).
   int64_t qb = __double_as_longlong(q1);
-  const int64_t rb = __double_as_longlong(r1);
-  const int64_t rmag = rb & 0x7fffffffffffffffLL;
-  const bool up = (rb ^ ab) >= 0;  // sign(r1) == sign(a): |a/b| > |q1|
-  const bool pow2 = (qb & 0xfffffffffffffLL) == 0;
-  // half the spacing towards a/b times |b|, as a bit pattern: |b| * 2^(E(q1) - 53), one less
-  // when stepping down from a power of two
-  const int64_t sh = ((qb >> 52) & 0x7ff) - (1023 + 53) - ((!up && pow2) ? 1 : 0);
-  const int64_t tb = (__double_as_longlong(d.b) & 0x7fffffffffffffffLL) + sh * ((int64_t)1 << 52);
-  if (rmag > tb) qb += up ? 1 : -1;
+  constexpr uint64_t kM = 0xfffffffffffffULL, kI = 1ULL << 52;
+  const uint64_t bb = (uint64_t)__double_as_longlong(d.b);
+  const uint64_t A = ((uint64_t)ab & kM) | kI, B = (bb & kM) | kI, Q = ((uint64_t)qb & kM) | kI;
+  const int shift = ((int)ea - (int)((bb >> 52) & 0x7ffu) - (int)(((uint64_t)qb >> 52) & 0x7ffu) + 1075) & 63;
+  const int64_t D = (int64_t)((A << shift) - B * Q);
+  if (D > 0) {
+    if (((uint64_t)D << 1) > B) qb += 1;  // |a/b| above |q1| by more than half a step
+  } else if (((uint64_t)(-D) << (Q == kI ? 2 : 1)) > B) {
+    qb -= 1;
+  }
   return __longlong_as_double(qb);
 }
 
