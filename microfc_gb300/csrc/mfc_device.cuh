@@ -167,52 +167,63 @@ __device__ __forceinline__ float rcp_approx(float x) {
 //
 // GB300 issues two FP64 operations per SM and clock, and an IEEE division
 // costs several of them, so the WENO weights (alpha_k = d_k / b_k^2 for both
-// faces, omega_k = alpha_k / sum alpha) spend about half of the plain path's
-// FP64 issue on divisions.  The quotient must still be the correctly rounded
-// one (the plain path reproduces the CPU reference bit for bit), so this is
-// the textbook Newton-Raphson reciprocal with a Markstein-style correction
-// and an exact-residual rounding test (J.-M. Muller et al., Handbook of
-// Floating-Point Arithmetic, 2nd ed., ch. 4-5: division with an FMA, the
-// exactness of the remainder a - b*q for a faithful q, and the impossibility
-// of a quotient lying exactly halfway between two doubles):
+// faces, omega_k = alpha_k / sum alpha) would spend about half of the plain
+// path's FP64 issue on divisions.  The quotient must still be the correctly
+// rounded one (the plain path reproduces the CPU reference bit for bit).
+// Here only the divisor's reciprocal uses the FP64 pipe; each quotient is
+// formed in 64-bit integer arithmetic, on pipes that sit idle while the
+// FP64 pipe is the bottleneck (J.-M. Muller et al., Handbook of
+// Floating-Point Arithmetic, 2nd ed., ch. 4-5 and 9: Newton-Raphson
+// reciprocals, exact remainders, and the fact that a quotient of two
+// doubles never lies exactly halfway between two doubles).
 //
-//   divisor(b): y0 = rcp.approx.f32 of b's significand (|rel err| < 2^-21),
-//               rescaled by b's exponent with integer operations;
-//               y = y0 + y0 (1 - b y0)                 |y b - 1| < 2^-42
-//   div_rn(a):  q0 = a y;  r0 = a - b q0 (one rounding);  q1 = q0 + r0 y,
-//               so |q1 - a/b| < ulp(q1)/2 + 2^-80 |a/b| < ulp(q1) and the
-//               remainder a - b q1 is exact.  It is formed in 64-bit
-//               integer arithmetic from the significands (GB300's integer
-//               pipes are idle while its FP64 pipe is the bottleneck) and
-//               compared against half the spacing of doubles from q1
-//               towards a/b; beyond it the neighbour is the rounded quotient.
+//   divisor(b): significand B (53 bits with the implicit one) of |b|;
+//     r = FP32 reciprocal of B 2^-52 (rcp.approx, one FP32 Newton step);
+//     y = y0 + y0 (1 - b y0) in FP64 from it, |y b - 1| < 2^-46;
+//     R = 2^64 / (B 2^-52) (1 + e), |e| < 2^-45: y's significand aligned
+//     by y's exponent (all ones when 1/(B 2^-52) rounds to 1).
+//   div_rn(a):  significand A of |a|; As = A, or 2A when A < B, so that
+//     As / B lies in [1, 2);  Q = floor(As R / 2^64) approximates
+//     As 2^52 / B within 2^8;  D = As 2^52 - B Q is exact in 64 bits
+//     (|D| < 2^61);  dl = floor(D / B) from D's top bits and R's top 24
+//     bits, off by at most one;  Q += dl, D -= dl B leaves D / B in
+//     (-2^-12, 1 + 2^-12), so the rounded quotient is Q + (2 D > B) (a tie
+//     is impossible); a carry to 2^53 moves to the next binade.  Sign and
+//     exponent come from a's and b's fields.
 //
-// A divisor costs 2 FP64 operations, each quotient 3 (one multiply and two
-// FMAs).  The argument holds while |a| and |b| lie in [2^-250, 2^251): then
-// every intermediate (q near 2^+-501, residuals near |b| ulp(q)) is a normal
+// A divisor costs 2 FP64 operations, a quotient none.  The argument holds
+// while |a| and |b| lie in [2^-250, 2^251): the quotient is then a normal
 // double.  Anything else (zero, subnormal, huge, inf or NaN operands) takes
 // the ordinary IEEE division, except a zero numerator over an in-window
 // divisor, whose signed-zero quotient is written directly.
 constexpr uint32_t kDivExpLo = 1023u - 250u, kDivExpSpan = 501u;
+constexpr uint64_t kSigMask = 0xfffffffffffffULL, kSigOne = 1ULL << 52;
 
 static __device__ __noinline__ double div_ieee(double a, double b) { return a / b; }
 
 struct DivisorF64 {
-  double b, y;
-  bool ok;
+  double b;
+  uint64_t B, R;  // significand with the implicit one; 2^64 / (B 2^-52) in 64-bit fixed point
+  uint32_t se;    // b's sign (bit 11) and biased exponent
+  bool ok;        // b inside the window
 };
 
 __device__ __forceinline__ DivisorF64 divisor(double b) {
   const uint32_t hi = (uint32_t)__double2hiint(b), lo = (uint32_t)__double2loint(b);
   const uint32_t eb = (hi >> 20) & 0x7ffu;
-  const float f = __uint_as_float(0x3f800000u | ((hi & 0xfffffu) << 3) | (lo >> 29));  // [1, 2)
-  const uint32_t rb = __float_as_uint(rcp_approx(f));                                    // (1/2, 1]
+  // b's significand rounded to 24 bits (a carry to 2.0 is harmless)
+  const float f = __uint_as_float(((0x3f800000u | ((hi & 0xfffffu) << 3) | (lo >> 29)) + ((lo >> 28) & 1u)));
+  const float r0 = rcp_approx(f);
+  const uint32_t rb = __float_as_uint(fmaf(r0, fmaf(-f, r0, 1.0f), r0));  // (1/2, 1]
   const uint32_t ey = (rb >> 23) + (2046u - 127u) - eb;  // exponent of y0 = r * 2^-(eb - 1023)
   const double y0 = __hiloint2double((int)((hi & 0x80000000u) | (ey << 20) | ((rb & 0x7fffffu) >> 3)),
                                      (int)(rb << 29));
-  const bool ok = eb - kDivExpLo < kDivExpSpan;
-  const double e = fma(-b, y0, 1.0);
-  return {b, fma(y0, e, y0), ok};
+  const double y = fma(y0, fma(-b, y0, 1.0), y0);
+  const uint64_t yb = (uint64_t)__double_as_longlong(y);
+  const int sh = (int)(((uint32_t)(yb >> 52) & 0x7ffu) + eb) - 2034;  // 10, 11, or 12 when y rounded to 1
+  const uint64_t Y = (yb & kSigMask) | kSigOne;
+  const uint64_t B = (((uint64_t)hi << 32 | lo) & kSigMask) | kSigOne;
+  return {b, B, sh >= 12 ? ~0ULL : Y << sh, (hi >> 20) & 0xfffu, eb - kDivExpLo < kDivExpSpan};
 }
 
 __device__ __forceinline__ double div_rn(double a, const DivisorF64& d) {
@@ -223,28 +234,20 @@ __device__ __forceinline__ double div_rn(double a, const DivisorF64& d) {
       return __longlong_as_double((ab ^ __double_as_longlong(d.b)) & (int64_t)0x8000000000000000ULL);
     return div_ieee(a, d.b);
   }
-  const double q0 = a * d.y;
-  const double r0 = fma(-d.b, q0, a);
-  const double q1 = fma(r0, d.y, q0);
-  // The rounding test on the exact remainder, in integer arithmetic.  With
-  // the significands A, B, Q (53 bits with the implicit one), the biased
-  // exponents Ea, Eb, Eq and u = 2^(Eb+Eq-2150):
-  //   |a| - |b| |q1| = D u,   D = A 2^(Ea-Eb-Eq+1075) - B Q,
-  // and |D| < B < 2^53 because q1 is within one ulp of a/b; so D is the
-  // difference of the two products' low 64 bits.  Half the spacing of
-  // doubles from q1 towards a/b is B/2 in units u (B/4 below a power of two).
-  int64_t qb = __double_as_longlong(q1);
-  constexpr uint64_t kM = 0xfffffffffffffULL, kI = 1ULL << 52;
-  const uint64_t bb = (uint64_t)__double_as_longlong(d.b);
-  const uint64_t A = ((uint64_t)ab & kM) | kI, B = (bb & kM) | kI, Q = ((uint64_t)qb & kM) | kI;
-  const int shift = ((int)ea - (int)((bb >> 52) & 0x7ffu) - (int)(((uint64_t)qb >> 52) & 0x7ffu) + 1075) & 63;
-  const int64_t D = (int64_t)((A << shift) - B * Q);
-  if (D > 0) {
-    if (((uint64_t)D << 1) > B) qb += 1;  // |a/b| above |q1| by more than half a step
-  } else if (((uint64_t)(-D) << (Q == kI ? 2 : 1)) > B) {
-    qb -= 1;
-  }
-  return __longlong_as_double(qb);
+  const uint64_t A = ((uint64_t)ab & kSigMask) | kSigOne;
+  const uint32_t lt = A < d.B ? 1u : 0u;
+  const uint64_t As = A << lt;
+  uint64_t Q = __umul64hi(As, d.R);
+  const int64_t D = (int64_t)((As << 52) - d.B * Q);
+  const int64_t dl = ((D >> 32) * (int64_t)(d.R >> 40)) >> 44;
+  Q += (uint64_t)dl;
+  const int64_t D1 = D - dl * (int64_t)d.B;
+  Q += (2 * D1 > (int64_t)d.B) ? 1u : 0u;
+  const uint32_t carry = (uint32_t)(Q >> 53);  // rounded up to 2^53: the next binade
+  Q >>= carry;
+  const uint64_t eq = (uint64_t)(ea - (d.se & 0x7ffu) + 1023u - lt + carry);
+  const uint64_t sign = (uint64_t)(((uint32_t)((uint64_t)ab >> 63)) ^ (d.se >> 11)) << 63;
+  return __longlong_as_double((int64_t)(sign | (eq << 52) | (Q & kSigMask)));
 }
 
 // FP32 counterparts (split path): the division itself, under the unit's
@@ -703,7 +706,11 @@ __device__ __forceinline__ double rk_combine(int kind, double base, double in, d
     case kRkEuler: return base + dt * r;
     case kRk2Final: return (base + in + dt * r) / 2.0;
     case kRk3Mid: return (3.0 * base + in + dt * r) / 4.0;
-    case kRk3Final: return div_rn(base + 2.0 * in + 2.0 * dt * r, DivisorF64{3.0, 1.0 / 3.0, true});
+    case kRk3Final: {
+      // divisor(3.0), spelled out: significand 1.5, 2^64 / 1.5 rounded down, exponent 1024
+      constexpr DivisorF64 kThree{3.0, 0x18000000000000ULL, 0xaaaaaaaaaaaaaaaaULL, 0x400u, true};
+      return div_rn(base + 2.0 * in + 2.0 * dt * r, kThree);
+    }
     default: return r;
   }
 }
