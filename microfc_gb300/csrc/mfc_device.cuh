@@ -170,18 +170,17 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // faces, omega_k = alpha_k / sum alpha) would spend about half of the plain
 // path's FP64 issue on divisions.  The quotient must still be the correctly
 // rounded one (the plain path reproduces the CPU reference bit for bit).
-// Here only the divisor's reciprocal uses the FP64 pipe; each quotient is
-// formed in 64-bit integer arithmetic, on pipes that sit idle while the
-// FP64 pipe is the bottleneck (J.-M. Muller et al., Handbook of
+// Here the reciprocal and every quotient are formed in 64-bit integer (and
+// FP32) arithmetic, on pipes that sit idle while the FP64 pipe is the
+// bottleneck (J.-M. Muller et al., Handbook of
 // Floating-Point Arithmetic, 2nd ed., ch. 4-5 and 9: Newton-Raphson
 // reciprocals, exact remainders, and the fact that a quotient of two
 // doubles never lies exactly halfway between two doubles).
 //
 //   divisor(b): significand B (53 bits with the implicit one) of |b|;
 //     r = FP32 reciprocal of B 2^-52 (rcp.approx, one FP32 Newton step);
-//     y = y0 + y0 (1 - b y0) in FP64 from it, |y b - 1| < 2^-46;
-//     R = 2^64 / (B 2^-52) (1 + e), |e| < 2^-45: y's significand aligned
-//     by y's exponent (all ones when 1/(B 2^-52) rounds to 1).
+//     R = 2^64 / (B 2^-52) (1 + e), |e| < 2^-46, by one Newton step from r
+//     in 64-bit fixed point (all ones for B = 2^52).
 //   div_rn(a):  significand A of |a|; As = A, or 2A when A < B, so that
 //     As / B lies in [1, 2);  Q = floor(As R / 2^64) approximates
 //     As 2^52 / B within 2^8;  D = As 2^52 - B Q is exact in 64 bits
@@ -191,7 +190,7 @@ __device__ __forceinline__ float rcp_approx(float x) {
 //     is impossible); a carry to 2^53 moves to the next binade.  Sign and
 //     exponent come from a's and b's fields.
 //
-// A divisor costs 2 FP64 operations, a quotient none.  The argument holds
+// Neither a divisor nor a quotient issues an FP64 operation.  The argument holds
 // while |a| and |b| lie in [2^-250, 2^251): the quotient is then a normal
 // double.  Anything else (zero, subnormal, huge, inf or NaN operands) takes
 // the ordinary IEEE division, except a zero numerator over an in-window
@@ -211,19 +210,22 @@ struct DivisorF64 {
 __device__ __forceinline__ DivisorF64 divisor(double b) {
   const uint32_t hi = (uint32_t)__double2hiint(b), lo = (uint32_t)__double2loint(b);
   const uint32_t eb = (hi >> 20) & 0x7ffu;
-  // b's significand rounded to 24 bits (a carry to 2.0 is harmless)
+  // FP32 reciprocal of b's significand rounded to 24 bits (a carry to 2.0 is
+  // harmless), refined by one FP32 Newton step: r in [1/2, 1], |r f - 1| < 2^-23
   const float f = __uint_as_float(((0x3f800000u | ((hi & 0xfffffu) << 3) | (lo >> 29)) + ((lo >> 28) & 1u)));
   const float r0 = rcp_approx(f);
-  const uint32_t rb = __float_as_uint(fmaf(r0, fmaf(-f, r0, 1.0f), r0));  // (1/2, 1]
-  const uint32_t ey = (rb >> 23) + (2046u - 127u) - eb;  // exponent of y0 = r * 2^-(eb - 1023)
-  const double y0 = __hiloint2double((int)((hi & 0x80000000u) | (ey << 20) | ((rb & 0x7fffffu) >> 3)),
-                                     (int)(rb << 29));
-  const double y = fma(y0, fma(-b, y0, 1.0), y0);
-  const uint64_t yb = (uint64_t)__double_as_longlong(y);
-  const int sh = (int)(((uint32_t)(yb >> 52) & 0x7ffu) + eb) - 2034;  // 10, 11, or 12 when y rounded to 1
-  const uint64_t Y = (yb & kSigMask) | kSigOne;
+  const uint32_t rb = __float_as_uint(fmaf(r0, fmaf(-f, r0, 1.0f), r0));
+  // R0 = r 2^64 = m 2^(40+k) (2^64 wraps to 0, which the step below undoes);
+  // one Newton step in fixed point, R = R0 + R0 (2^116 - B R0) 2^-116, with
+  // 2^116 - B R0 = e 2^(40+k) and e = 2^(76-k) - B m, which is small and so
+  // equals minus the low 64 bits of B m
+  const uint32_t k = (rb >> 23) - 126u;
+  const uint64_t m = (rb & 0x7fffffu) | 0x800000u;
   const uint64_t B = (((uint64_t)hi << 32 | lo) & kSigMask) | kSigOne;
-  return {b, B, sh >= 12 ? ~0ULL : Y << sh, (hi >> 20) & 0xfffu, eb - kDivExpLo < kDivExpSpan};
+  const int64_t e = -(int64_t)(B * m);
+  const int64_t corr = ((int64_t)m * (e >> 14)) >> (22 - 2 * k);
+  const uint64_t R = B == kSigOne ? ~0ULL : (m << (40 + k)) + (uint64_t)corr;
+  return {b, B, R, (hi >> 20) & 0xfffu, eb - kDivExpLo < kDivExpSpan};
 }
 
 __device__ __forceinline__ double div_rn(double a, const DivisorF64& d) {
