@@ -403,8 +403,9 @@ def main():
             "peak_kind": "measured in-process (FMA chains, mfc_gpu_measure_peaks)",
             "peaks_measured": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak},
             # the peak counts an FMA as 2 flops; the bit-faithful path may fuse
-            # nothing, so each algorithmic add, mul, div or sqrt needs at least
-            # one pipe instruction: its ceiling is half the flop peak
+            # nothing, so each algorithmic add or mul needs its own FP64 pipe
+            # instruction (divisions run on the integer pipes): against that
+            # instruction ceiling, half the flop peak
             "issue_frac": ach / (peak / 2.0)}
     sim.close()
     if not args.no_modes and args.precision == "fp64":
