@@ -268,6 +268,9 @@ int mfc_gpu_ensemble_upload(mfc_gpu_ensemble* ens, int case_index, const double*
 int mfc_gpu_ensemble_download(mfc_gpu_ensemble* ens, int case_index, double* host_q);
 /* Autotuner over the compiled ensemble tile variants (see mfc_gpu_tune). */
 int mfc_gpu_ensemble_tune(mfc_gpu_ensemble* ens, int reps, int* variant_out, double* ms_out);
+/* Pins the ensemble's tile variant (the numbering of mfc_gpu_ensemble_tune);
+ * every variant gives the same bits.  Returns its tile shape. */
+int mfc_gpu_ensemble_select_variant(mfc_gpu_ensemble* ens, int variant, int* tx, int* ty, int* threads);
 /* Steps t_step_start .. t_step_stop-1 of every case; each case's last step
  * uses its dt after the p_main trim.  use_graph != 0 replays the stage
  * launches of a step from a CUDA graph.  Synchronous; MFC_ERR_STATE on NaN. */

@@ -9,6 +9,8 @@ void register_ensemble_fp32(std::vector<EnsembleEntry>& r) {
   r.push_back(ensemble_entry<2, 5, float, 32, 8, 256>());
   r.push_back(ensemble_entry<2, 5, float, 32, 32, 512>());
   r.push_back(ensemble_entry<2, 5, float, 64, 8, 256>());
+  r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, false, 4>());
+  r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, false, 5>());
 }
 
 }  // namespace mfc
@@ -19,6 +21,9 @@ void register_ensemble_gated(std::vector<EnsembleEntry>& r) {
   r.push_back(ensemble_entry<2, 5, float, 32, 16, 256, true>());
   r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, true>());
   r.push_back(ensemble_entry<2, 5, float, 32, 32, 512, true>());
+  // register-capped 16x16 tiles: four or five blocks per SM
+  r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, true, 4>());
+  r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, true, 5>());
 }
 
 }  // namespace mfc

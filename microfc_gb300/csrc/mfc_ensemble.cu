@@ -326,6 +326,22 @@ int mfc_gpu_ensemble_tune(mfc_gpu_ensemble* e, int reps, int* variant_out, doubl
   return err == cudaSuccess ? MFC_OK : mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
 }
 
+int mfc_gpu_ensemble_select_variant(mfc_gpu_ensemble* e, int variant, int* tx, int* ty, int* threads) {
+  if (!e) return mfc::report_error(MFC_ERR_INVALID, "NULL ensemble");
+  int idx = -1;
+  for (const auto& x : g_ens) {
+    if (x.nf != e->nf || x.wo != e->wo || x.prec != e->prec) continue;
+    if (++idx != variant) continue;
+    int rc = configure(e, &x);
+    if (rc) return rc;
+    if (tx) *tx = x.tx;
+    if (ty) *ty = x.ty;
+    if (threads) *threads = x.nt;
+    return MFC_OK;
+  }
+  return mfc::report_error(MFC_ERR_INVALID, "no such ensemble tile variant");
+}
+
 // Time steps t_step_start .. t_step_stop-1 for every case (each with its own
 // dt; the last step uses that case's dt after the p_main trim).  With
 // use_graph the stage launches of one step are captured once in a CUDA graph

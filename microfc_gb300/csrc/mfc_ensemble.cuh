@@ -34,8 +34,9 @@ struct EnsParams {
 };
 static_assert(sizeof(EnsParams) <= 32764, "ensemble parameters must fit the kernel parameter space");
 
+// One persistent block's walk over the work list (the body of both kernels).
 template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE>
-__global__ void __launch_bounds__(NT) ensemble_stage_kernel(const __grid_constant__ EnsParams E) {
+__device__ __forceinline__ void ensemble_walk(const EnsParams& E) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   for (int t = blockIdx.x; t < E.total_tiles; t += gridDim.x) {
     int lo = 0, hi = E.num_cases - 1;
@@ -65,6 +66,23 @@ __global__ void __launch_bounds__(NT) ensemble_stage_kernel(const __grid_constan
   }
 }
 
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE>
+__global__ void __launch_bounds__(NT) ensemble_stage_kernel(const __grid_constant__ EnsParams E) {
+  ensemble_walk<NF, WO, RT, TX, TY, NT, GATE>(E);
+}
+
+// The same with the registers capped so that MINB blocks fit on an SM.
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB>
+__global__ void __launch_bounds__(NT, MINB) ensemble_stage_kernel_mb(const __grid_constant__ EnsParams E) {
+  ensemble_walk<NF, WO, RT, TX, TY, NT, GATE>(E);
+}
+
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB>
+constexpr auto ensemble_func() {
+  if constexpr (MINB > 1) return &ensemble_stage_kernel_mb<NF, WO, RT, TX, TY, NT, GATE, MINB>;
+  else return &ensemble_stage_kernel<NF, WO, RT, TX, TY, NT, GATE>;
+}
+
 struct EnsembleEntry {
   int nf, wo, prec, tx, ty, nt;
   size_t smem, smem_shared_coef;  // dynamic shared memory: per-cell records / shared record
@@ -72,20 +90,20 @@ struct EnsembleEntry {
   cudaError_t (*launch)(const EnsParams& E, int grid, size_t smem, cudaStream_t st);
 };
 
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB = 1>
 cudaError_t ensemble_launch(const EnsParams& E, int grid, size_t smem, cudaStream_t st) {
-  ensemble_stage_kernel<NF, WO, RT, TX, TY, NT, GATE><<<grid, NT, smem, st>>>(E);
+  ensemble_func<NF, WO, RT, TX, TY, NT, GATE, MINB>()<<<grid, NT, smem, st>>>(E);
   return cudaGetLastError();
 }
 
 // prec: 0 FP64, 1 split, 2 split with the learned gate
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1>
 EnsembleEntry ensemble_entry() {
   return EnsembleEntry{NF, WO, sizeof(RT) == 8 ? 0 : (GATE ? 2 : 1), TX, TY, NT,
                        stage_smem_bytes<2, NF, WO, RT, TX, TY, NT, GATE>(),
                        stage_smem_bytes_shared_coef<2, NF, WO, RT, TX, TY, NT, GATE>(),
-                       reinterpret_cast<const void*>(&ensemble_stage_kernel<NF, WO, RT, TX, TY, NT, GATE>),
-                       &ensemble_launch<NF, WO, RT, TX, TY, NT, GATE>};
+                       reinterpret_cast<const void*>(ensemble_func<NF, WO, RT, TX, TY, NT, GATE, MINB>()),
+                       &ensemble_launch<NF, WO, RT, TX, TY, NT, GATE, MINB>};
 }
 
 void register_ensemble_fp64(std::vector<EnsembleEntry>& r);

@@ -115,6 +115,13 @@ class Ensemble:
         w = np.ascontiguousarray(params, dtype=np.float32)
         _lib.check(self.L.mfc_gpu_ensemble_set_gate(self._h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
 
+    def select_variant(self, variant: int):
+        """Pin a tile variant (mfc_gpu_ensemble_select_variant); returns (tx, ty, threads)."""
+        tx, ty, nt = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        _lib.check(self.L.mfc_gpu_ensemble_select_variant(self._h, int(variant), ctypes.byref(tx), ctypes.byref(ty),
+                                                          ctypes.byref(nt)))
+        return tx.value, ty.value, nt.value
+
     def tune(self, reps: int = 5):
         v, ms = ctypes.c_int(-1), ctypes.c_double(0)
         _lib.check(self.L.mfc_gpu_ensemble_tune(self._h, int(reps), ctypes.byref(v), ctypes.byref(ms)))

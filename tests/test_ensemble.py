@@ -54,6 +54,36 @@ def test_ensemble_autotuner_keeps_results():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["split", "gated"])
+def test_every_ensemble_variant_gives_the_same_bits(precision):
+    from microfc_gb300 import gate
+    from microfc_gb300._lib import MfcError
+    cl = _mixed(precision)
+    params = gate.load() if precision == "gated" else None
+    refs = []
+    for c in cl:
+        with Simulation(c) as sim:
+            if params is not None:
+                sim.set_gate(params)
+            sim.run(0, 6)
+            refs.append(sim.download())
+    v = 0
+    while True:
+        with Ensemble(cl) as ens:
+            if params is not None:
+                ens.set_gate(params)
+            try:
+                shape = ens.select_variant(v)
+            except MfcError:
+                break
+            ens.run(0, 6)
+            for i, ref in enumerate(refs):
+                assert np.array_equal(ens.download(i).view(np.uint64), ref.view(np.uint64)), (v, shape, i)
+        v += 1
+    assert v >= 2
+
+
+@pytest.mark.gpu
 def test_single_case_autotuner_keeps_results():
     c = cases.shock_droplet_2d(nx=128, ny=64, steps=4)
     with Simulation(c) as sim:
