@@ -59,13 +59,17 @@ inline void set_fp32_constants(DevParams& D) {
 
 // Split precision on a grid whose FP32 coefficient records are the same for
 // every cell of a direction (uniform spacing): that one record per
-// direction.  The single-case kernels receive it by value, so the
-// reconstruction takes its coefficients from the constant bank instead of
-// staging one record per cell in shared memory.  on[d] = 0: per-cell records.
-struct UniformCoef {
-  int on[3];
-  float rec[3][kCoefRec];
+// direction, each coefficient duplicated into both lanes of a packed FP32
+// pair (the reconstruction works on pairs of variables).  The kernels
+// receive it by value, so the reconstruction takes its coefficients from the
+// constant bank instead of staging per-cell records in shared memory.
+// on[d] = 0: per-cell records.
+template <int NDIR>
+struct UniformCoefT {
+  int on[NDIR];
+  unsigned long long rec[NDIR][kCoefRec];  // (c, c) pairs
 };
+using UniformCoef = UniformCoefT<3>;
 
 // Viscous parameters: fluid_pp(i)%Re(1:2) as the reference's Re_size, Re_idx
 // and Res (m_global_parameters.fpp:300-336, m_viscous.fpp:33-45), and the
@@ -372,37 +376,74 @@ __device__ __forceinline__ void cons_to_prim_split(const double (&q)[Eqs<ND, NF>
   out[Q::E] = __fdividef(d2f_bits(dE), gam);
 }
 
-// WENO5 for the split-precision path: the same stencils, smoothness
-// indicators and weights as weno_cell, with the divisions regrouped -- one
-// reciprocal of beta_k^2 shared by the left and right weights and one
-// reciprocal of sum(alpha_k) per face value.  The weights are still
-// normalised before they multiply the candidate values, so nothing grows
-// beyond the operands' range.  Mathematically identical; rounding differs.
-__device__ __forceinline__ void weno5_cell_fast(const float* __restrict__ c, const float (&v)[5], float eps, float& vL,
-                                                float& vR) {
-  const float d1 = v[4] - v[3];
-  const float d0 = v[3] - v[2];
-  const float dm1 = v[2] - v[1];
-  const float dm2 = v[1] - v[0];
-  const float b0 = fmaf(d1, fmaf(c[kBeta + 0], d1, c[kBeta + 1] * d0), fmaf(c[kBeta + 2] * d0, d0, eps));
-  const float b1 = fmaf(d0, fmaf(c[kBeta + 3], d0, c[kBeta + 4] * dm1), fmaf(c[kBeta + 5] * dm1, dm1, eps));
-  const float b2 = fmaf(dm1, fmaf(c[kBeta + 6], dm1, c[kBeta + 7] * dm2), fmaf(c[kBeta + 8] * dm2, dm2, eps));
-  const float r0 = rcp_approx(b0 * b0), r1 = rcp_approx(b1 * b1), r2 = rcp_approx(b2 * b2);
-  {
-    const float p0 = fmaf(c[kPL + 1], d0, fmaf(c[kPL + 0], d1, v[2]));
-    const float p1 = fmaf(c[kPL + 3], dm1, fmaf(c[kPL + 2], d0, v[2]));
-    const float p2 = fmaf(c[kPL + 5], dm2, fmaf(c[kPL + 4], dm1, v[2]));
-    const float a0 = c[kDL + 0] * r0, a1 = c[kDL + 1] * r1, a2 = c[kDL + 2] * r2;
-    const float is = rcp_approx(a0 + a1 + a2);
-    vL = fmaf(a2 * is, p2, fmaf(a1 * is, p1, (a0 * is) * p0));
-  }
-  {
-    const float p0 = fmaf(c[kPR + 1], d0, fmaf(c[kPR + 0], d1, v[2]));
-    const float p1 = fmaf(c[kPR + 3], dm1, fmaf(c[kPR + 2], d0, v[2]));
-    const float p2 = fmaf(c[kPR + 5], dm2, fmaf(c[kPR + 4], dm1, v[2]));
-    const float a0 = c[kDR + 0] * r0, a1 = c[kDR + 1] * r1, a2 = c[kDR + 2] * r2;
-    const float is = rcp_approx(a0 + a1 + a2);
-    vR = fmaf(a2 * is, p2, fmaf(a1 * is, p1, (a0 * is) * p0));
+// ---------------------------------------------------------------------------
+// Packed FP32 pairs for the split path: two lanes of one 64-bit register,
+// computed by one instruction (FFMA2 / FMUL2 / FADD2 on GB300).  Each lane
+// is rounded exactly as the scalar operation would round it (to nearest,
+// subnormals flushed like the split units' -ftz=true), so a pair gives the
+// bits of two scalar evaluations with half the issue slots.
+using f32x2 = unsigned long long;
+__device__ __forceinline__ f32x2 f2_pack(float lo, float hi) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f32x2 p, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(p));
+}
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.ftz.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("sub.rn.ftz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 f2_rcp(f32x2 a) {
+  float x, y;
+  f2_unpack(a, x, y);
+  return f2_pack(rcp_approx(x), rcp_approx(y));
+}
+
+// WENO5 for the split-precision path, two variables at once (one per lane):
+// the stencils, smoothness indicators and weights of weno_cell, with the
+// divisions regrouped -- one reciprocal of beta_k^2 shared by the left and
+// right weights and one reciprocal of sum(alpha_k) per face value.  The
+// weights are still normalised before they multiply the candidate values,
+// so nothing grows beyond the operands' range.  Mathematically identical to
+// weno_cell; rounding differs.  C(k) returns coefficient k of the cell's
+// record as a (c, c) pair.
+template <class Coef>
+__device__ __forceinline__ void weno5_pair_fast(const Coef& C, const f32x2 (&v)[5], f32x2 eps, f32x2& vL,
+                                                f32x2& vR) {
+  const f32x2 d1 = f2_sub(v[4], v[3]), d0 = f2_sub(v[3], v[2]), dm1 = f2_sub(v[2], v[1]), dm2 = f2_sub(v[1], v[0]);
+  const f32x2 b0 = f2_fma(d1, f2_fma(C(kBeta + 0), d1, f2_mul(C(kBeta + 1), d0)), f2_fma(f2_mul(C(kBeta + 2), d0), d0, eps));
+  const f32x2 b1 = f2_fma(d0, f2_fma(C(kBeta + 3), d0, f2_mul(C(kBeta + 4), dm1)), f2_fma(f2_mul(C(kBeta + 5), dm1), dm1, eps));
+  const f32x2 b2 = f2_fma(dm1, f2_fma(C(kBeta + 6), dm1, f2_mul(C(kBeta + 7), dm2)), f2_fma(f2_mul(C(kBeta + 8), dm2), dm2, eps));
+  const f32x2 r0 = f2_rcp(f2_mul(b0, b0)), r1 = f2_rcp(f2_mul(b1, b1)), r2 = f2_rcp(f2_mul(b2, b2));
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const int kP = side ? kPR : kPL, kD = side ? kDR : kDL;
+    const f32x2 p0 = f2_fma(C(kP + 1), d0, f2_fma(C(kP + 0), d1, v[2]));
+    const f32x2 p1 = f2_fma(C(kP + 3), dm1, f2_fma(C(kP + 2), d0, v[2]));
+    const f32x2 p2 = f2_fma(C(kP + 5), dm2, f2_fma(C(kP + 4), dm1, v[2]));
+    const f32x2 a0 = f2_mul(C(kD + 0), r0), a1 = f2_mul(C(kD + 1), r1), a2 = f2_mul(C(kD + 2), r2);
+    const f32x2 is = f2_rcp(f2_add(f2_add(a0, a1), a2));
+    const f32x2 val = f2_fma(f2_mul(a2, is), p2, f2_fma(f2_mul(a1, is), p1, f2_mul(f2_mul(a0, is), p0)));
+    if (side) vR = val;
+    else vL = val;
   }
 }
 

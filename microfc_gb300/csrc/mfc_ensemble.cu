@@ -96,7 +96,10 @@ int launch_stage(mfc_gpu_ensemble* e, int stage, int last) {
   E.stage = stage;
   E.time_stepper = e->ts;
   E.last_step = last;
-  E.U = e->U;
+  for (int d = 0; d < 2; ++d) {
+    E.U.on[d] = e->U.on[d];
+    for (int k = 0; k < mfc::kCoefRec; ++k) E.U.rec[d][k] = e->U.rec[d][k];
+  }
   for (int i = 0; i < e->num; ++i) E.c[i] = e->cases[i];
   cudaError_t err = e->entry->launch(E, e->grid, e->smem, e->stream);
   if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));

@@ -29,7 +29,7 @@ struct EnsParams {
   // split WENO5: the coefficient record every cell of every case shares when
   // all cases have uniform grids (the FP32 records of a uniform grid do not
   // depend on its spacing); all off otherwise
-  UniformCoef U;
+  UniformCoefT<2> U;
   EnsCase c[kMaxEnsemble];
 };
 static_assert(sizeof(EnsParams) <= 32764, "ensemble parameters must fit the kernel parameter space");

@@ -82,21 +82,20 @@ __device__ __forceinline__ double weno5_weight_deviation(const double* __restric
   return dev;
 }
 
-// WENO5 with the optimal linear weights d_k (the gate's "smooth" branch).
-__device__ __forceinline__ void weno5_cell_linear(const float* __restrict__ c, const float (&v)[5], float& vL,
-                                                  float& vR) {
-  const float d1 = v[4] - v[3], d0 = v[3] - v[2], dm1 = v[2] - v[1], dm2 = v[1] - v[0];
-  {
-    const float p0 = fmaf(c[kPL + 1], d0, fmaf(c[kPL + 0], d1, v[2]));
-    const float p1 = fmaf(c[kPL + 3], dm1, fmaf(c[kPL + 2], d0, v[2]));
-    const float p2 = fmaf(c[kPL + 5], dm2, fmaf(c[kPL + 4], dm1, v[2]));
-    vL = fmaf(c[kDL + 2], p2, fmaf(c[kDL + 1], p1, c[kDL + 0] * p0));
-  }
-  {
-    const float p0 = fmaf(c[kPR + 1], d0, fmaf(c[kPR + 0], d1, v[2]));
-    const float p1 = fmaf(c[kPR + 3], dm1, fmaf(c[kPR + 2], d0, v[2]));
-    const float p2 = fmaf(c[kPR + 5], dm2, fmaf(c[kPR + 4], dm1, v[2]));
-    vR = fmaf(c[kDR + 2], p2, fmaf(c[kDR + 1], p1, c[kDR + 0] * p0));
+// WENO5 with the optimal linear weights d_k (the gate's "smooth" branch),
+// two variables at once (weno5_pair_fast's packed pairs).
+template <class Coef>
+__device__ __forceinline__ void weno5_pair_linear(const Coef& C, const f32x2 (&v)[5], f32x2& vL, f32x2& vR) {
+  const f32x2 d1 = f2_sub(v[4], v[3]), d0 = f2_sub(v[3], v[2]), dm1 = f2_sub(v[2], v[1]), dm2 = f2_sub(v[1], v[0]);
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const int kP = side ? kPR : kPL, kD = side ? kDR : kDL;
+    const f32x2 p0 = f2_fma(C(kP + 1), d0, f2_fma(C(kP + 0), d1, v[2]));
+    const f32x2 p1 = f2_fma(C(kP + 3), dm1, f2_fma(C(kP + 2), d0, v[2]));
+    const f32x2 p2 = f2_fma(C(kP + 5), dm2, f2_fma(C(kP + 4), dm1, v[2]));
+    const f32x2 val = f2_fma(C(kD + 2), p2, f2_fma(C(kD + 1), p1, f2_mul(C(kD + 0), p0)));
+    if (side) vR = val;
+    else vL = val;
   }
 }
 

@@ -192,10 +192,11 @@ inline float d2f_trunc(double x) {
   return f;
 }
 
-// Split-precision WENO5 on a uniform grid: fills U.rec[d] and sets U.on[d]
-// for every direction whose cells -kCoefPad .. n-1+kCoefPad all have the same
-// FP32 coefficient record (the one the kernels would stage per cell), so
-// that the kernels may use that one record everywhere with identical results.
+// Split-precision WENO5 on a uniform grid: fills U.rec[d] (each coefficient
+// as a (c, c) pair) and sets U.on[d] for every direction whose cells
+// -kCoefPad .. n-1+kCoefPad all have the same FP32 coefficient record (the
+// one the kernels would stage per cell), so that the kernels may use that
+// one record everywhere with identical results.
 inline void uniform_records(const GridTables& t, int nd, const int* n, int weno_order, int precision,
                             UniformCoef& U) {
   U = UniformCoef{};
@@ -216,7 +217,7 @@ inline void uniform_records(const GridTables& t, int nd, const int* n, int weno_
     }
     if (!same) continue;
     U.on[d] = 1;
-    for (int k = 0; k < kCoefRec; ++k) U.rec[d][k] = rec[k];
+    for (int k = 0; k < kCoefRec; ++k) U.rec[d][k] = (unsigned long long)bits(rec[k]) << 32 | bits(rec[k]);
   }
 }
 

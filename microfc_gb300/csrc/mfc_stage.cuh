@@ -75,10 +75,15 @@ struct StageShape {
   static constexpr int TYE = (ND > 1) ? TY : 1;
   static constexpr int LX = TX + 2 * H;
   static constexpr int LY = (ND > 1) ? TY + 2 * H : 1;
-  static constexpr int NQ = S * LY * LX;  // primitive tile
+  // split WENO5 keeps the primitive variables and the WENO values in
+  // interleaved pairs (2p, 2p+1), reconstructed two at a time with packed
+  // FP32 instructions; SP counts the variables with the padding one
+  static constexpr bool PAIR = sizeof(RT) == 4 && WO == 5;
+  static constexpr int SP = PAIR ? (S + 1) / 2 * 2 : S;
+  static constexpr int NQ = SP * LY * LX;  // primitive tile
   // WENO outputs (left and right face values), x and y layouts share space
-  static constexpr int NWX = S * TYE * (TX + 2);
-  static constexpr int NWY = (ND > 1) ? S * (TY + 2) * TX : 0;
+  static constexpr int NWX = SP * TYE * (TX + 2);
+  static constexpr int NWY = (ND > 1) ? SP * (TY + 2) * TX : 0;
   static constexpr int NW = NWX > NWY ? NWX : NWY;
   // fluxes + interface velocity (+ the viscous x-momentum, y-momentum and
   // energy source fluxes)
@@ -121,11 +126,12 @@ struct GateShape {
 // tiles of many cases per persistent block).  smem_raw must hold
 // stage_smem_bytes() (or stage_smem_bytes_shared_coef() when U covers every
 // direction).
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, bool VISC = false>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, bool VISC = false,
+          class UC = UniformCoef>
 __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __restrict__ qin,
                                            const double* __restrict__ qbase, double* __restrict__ qout,
                                            const double dt, const int kind, const int x0, const int y0,
-                                           unsigned char* smem_raw, const UniformCoef* U = nullptr) {
+                                           unsigned char* smem_raw, const UC* U = nullptr) {
   static_assert(!GATE || (sizeof(RT) == 4 && WO == 5), "the learned gate runs on the split-precision WENO5 path");
   static_assert(!(GATE && VISC), "the gated kernel is inviscid");
   using Sh = StageShape<ND, NF, WO, RT, TX, TY, VISC>;
@@ -137,13 +143,26 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   constexpr bool kSplit = sizeof(RT) == 4;
   using AT = RT;  // type of the flux-divergence accumulation
 
-  RT* sq = reinterpret_cast<RT*>(smem_raw);  // [S][LY][LX] primitive
+  RT* sq = reinterpret_cast<RT*>(smem_raw);  // [S][LY][LX] primitive ([S/2][LY][LX][2] in pairs)
   RT* wl = sq + Sh::OW;                       // left-face values
   RT* wr = wl + Sh::align16(Sh::NW);          // right-face values
   RT* fl = sq + Sh::OF;                       // fluxes [S+1][...]
   // split: FP32 x coefficients [TX+2][kCoefRec], after the gate's share
   RT* scx = reinterpret_cast<RT*>(smem_raw + Sh::kMainBytes + (GATE ? GateShape<ND, TX, TY, NT>::kBytes : 0));
   RT* scy = scx + kCoefRec * Sh::NCX;         // split: FP32 y coefficients [TY+2][kCoefRec]
+  // element of variable v in the primitive tile and in the x / y WENO values
+  constexpr bool kPair = Sh::PAIR;
+  constexpr int NCX_ = TX + 2, NCY_ = TY + 2;
+  auto qi = [](int v, int ly, int lx) {
+    return kPair ? (((v >> 1) * LY + ly) * LX + lx) * 2 + (v & 1) : (v * LY + ly) * LX + lx;
+  };
+  auto wxi = [](int v, int ty, int cx) {
+    return kPair ? (((v >> 1) * TYE + ty) * NCX_ + cx) * 2 + (v & 1) : (v * TYE + ty) * NCX_ + cx;
+  };
+  auto wyi = [](int v, int cy, int tx) {
+    return kPair ? (((v >> 1) * NCY_ + cy) * TX + tx) * 2 + (v & 1) : (v * NCY_ + cy) * TX + tx;
+  };
+  (void)wyi;
 
   const int tid = threadIdx.x;
   const int nx = P.n[0], ny = P.n[1];
@@ -217,11 +236,12 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       float pr[S];
       cons_to_prim_split<ND, NF>(q, P, pr);
 #pragma unroll
-      for (int v = 0; v < S; ++v) sq[(v * LY + ly) * LX + lx] = pr[v];
+      for (int v = 0; v < S; ++v) sq[qi(v, ly, lx)] = pr[v];
+      if constexpr (Sh::SP > S) sq[qi(S, ly, lx)] = 0.f;  // the padding lane
     } else {
       cons_to_prim<ND, NF>(q, P);
 #pragma unroll
-      for (int v = 0; v < S; ++v) sq[(v * LY + ly) * LX + lx] = RT(q[v]);
+      for (int v = 0; v < S; ++v) sq[qi(v, ly, lx)] = RT(q[v]);
     }
   }
   if constexpr (Sh::NCOEF > 0) {
@@ -269,14 +289,12 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
       if (cell < G::NGX) {
         const int cx = cell % (TX + 2), ty = cell / (TX + 2);
-        const RT* row = sq + (var * LY + ((ND > 1) ? ty + H : 0)) * LX + cx + H - 1;
 #pragma unroll
-        for (int k = 0; k < 5; ++k) s[k] = row[k - 2];
+        for (int k = 0; k < 5; ++k) s[k] = sq[qi(var, (ND > 1) ? ty + H : 0, cx + H - 1 + k - 2)];
       } else if (cell < NG) {
         const int c2 = cell - G::NGX, tx = c2 % TX, cy = c2 / TX;
-        const RT* col = sq + var * LY * LX + (cy + H - 1) * LX + tx + H;
 #pragma unroll
-        for (int k = 0; k < 5; ++k) s[k] = col[(k - 2) * LX];
+        for (int k = 0; k < 5; ++k) s[k] = sq[qi(var, cy + H - 1 + k - 2, tx + H)];
       }
       float xf[5];
       gate_norm5_var(s, xf, lane < 16 ? 0 : 1);
@@ -302,45 +320,56 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   {
     constexpr int NCX = TX + 2;
     // variable v of the cell at (cx, ty); c: the cell's coefficient record
-    auto x_recon = [&](const RT* __restrict__ c, const int cx, const int ty, const int v, const bool nonlin) {
-      const RT* row = sq + (v * LY + ((ND > 1) ? ty + H : 0)) * LX + cx + H - 1;
+    auto x_recon = [&](const RT* __restrict__ c, const int cx, const int ty, const int v) {
       RT st[5];
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         const int o = k - 2;
-        st[k] = (o >= -(WO / 2) && o <= WO / 2) ? row[o] : RT(0);
+        st[k] = (o >= -(WO / 2) && o <= WO / 2) ? sq[qi(v, (ND > 1) ? ty + H : 0, cx + H - 1 + o)] : RT(0);
       }
       RT vl, vr;
-      if constexpr (GATE) {
-        if (nonlin) weno5_cell_fast(c, st, eps, vl, vr);
-        else weno5_cell_linear(c, st, vl, vr);
-      } else if constexpr (kSplit && WO == 5) {
-        weno5_cell_fast(c, st, eps, vl, vr);
-      } else {
-        weno_cell<WO, RT>(c, st, eps, vl, vr);
-      }
-      wl[(v * TYE + ty) * NCX + cx] = vl;
-      wr[(v * TYE + ty) * NCX + cx] = vr;
+      weno_cell<WO, RT>(c, st, eps, vl, vr);
+      wl[wxi(v, ty, cx)] = vl;
+      wr[wxi(v, ty, cx)] = vr;
     };
-    if constexpr (Sh::NCOEF > 0) {
-      deal_positions<TYE * NCX, S, NT>(tid, [&](const int p, const int v, const bool all) {
+    if constexpr (kPair) {
+      constexpr int NPR = Sh::SP / 2;  // variable pairs
+      const f32x2 eps2 = f2_pack(eps, eps);
+      // variable pair pr of the cell at (cx, ty); C(k): coefficient k as a (c, c) pair
+      auto x_pair = [&](const auto& C, const int cx, const int ty, const int pr, const bool nonlin) {
+        const f32x2* row = reinterpret_cast<const f32x2*>(sq) + (pr * LY + ((ND > 1) ? ty + H : 0)) * LX + cx + H - 1;
+        f32x2 st[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) st[k] = row[k - 2];
+        f32x2 vl, vr;
+        if constexpr (GATE) {
+          if (nonlin) weno5_pair_fast(C, st, eps2, vl, vr);
+          else weno5_pair_linear(C, st, vl, vr);
+        } else {
+          weno5_pair_fast(C, st, eps2, vl, vr);
+        }
+        reinterpret_cast<f32x2*>(wl)[(pr * TYE + ty) * NCX + cx] = vl;
+        reinterpret_cast<f32x2*>(wr)[(pr * TYE + ty) * NCX + cx] = vr;
+      };
+      deal_positions<TYE * NCX, NPR, NT>(tid, [&](const int p, const int v, const bool all) {
         const int cx = p % NCX, ty = p / NCX;
         bool nonlin = true;
         if constexpr (GATE) nonlin = gflag[p] != 0;
         // the shared record of a uniform grid, else the cell's staged record
-        // (reloaded per variable: keeping it live across them costs registers)
+        // (reloaded per pair: keeping it live across them costs registers)
         auto one = [&](const int w) {
           if (ux) {
-            x_recon(U->rec[0], cx, ty, w, nonlin);
+            const f32x2* rec = U->rec[0];
+            x_pair([&](int k) { return rec[k]; }, cx, ty, w, nonlin);
           } else {
             RT c[kCoefRec];
             load_coef_record(scx + cx * kCoefRec, c);
-            x_recon(c, cx, ty, w, nonlin);
+            x_pair([&](int k) { return f2_pack(c[k], c[k]); }, cx, ty, w, nonlin);
           }
         };
         if (all) {
 #pragma unroll 1
-          for (int w = 0; w < S; ++w) one(w);
+          for (int w = 0; w < NPR; ++w) one(w);
         } else {
           one(v);
         }
@@ -359,7 +388,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
 #pragma unroll
           for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
         }
-        x_recon(c, cx, ty, v, true);
+        x_recon(c, cx, ty, v);
       }
     }
   }
@@ -376,8 +405,8 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       const bool rfl = (gface == nx - 1 && P.bc_end[0] == -4);  // qR(m+1) = qL(m)
 #pragma unroll
       for (int v = 0; v < S; ++v) {
-        const RT a = wr[(v * TYE + ty) * NCX + f];
-        const RT b = wl[(v * TYE + ty) * NCX + f + 1];
+        const RT a = wr[wxi(v, ty, f)];
+        const RT b = wl[wxi(v, ty, f + 1)];
         qL[v] = lfr ? b : a;
         qR[v] = rfl ? a : b;
       }
@@ -386,7 +415,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         hllc_face<ND, NF, 0, RT, true>(qL, qR, gam_i, pi_i, F, us, vs);
         const ViscParams& V = *P.visc;
         const int ly = (ND > 1) ? ty + H : 0, lx = f + H - 1;  // the face's left cell
-        auto U = [&](int c, int x, int y) { return sq[((Q::MOM + c) * LY + y) * LX + x]; };
+        auto U = [&](int c, int x, int y) { return sq[qi(Q::MOM + c, y, x)]; };
         const auto Dx = divisor(narrow<RT>(__ldg(V.dcc[0] + min(x0 + f, nx))));  // x_cc(j+1) - x_cc(j)
 #pragma unroll
         for (int c = 0; c < ND; ++c) {
@@ -435,7 +464,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
     const AT du = AT(fl[(S * TYE + ty) * NFXr + tx + 1]) - AT(fl[(S * TYE + ty) * NFXr + tx]);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
-      const AT a = AT(sq[((Q::ADV + f) * LY + (ND > 1 ? ty + H : 0)) * LX + tx + H]);
+      const AT a = AT(sq[qi(Q::ADV + f, ND > 1 ? ty + H : 0, tx + H)]);
       rhs[k][Q::ADV + f] = mul_add(inv * a, du, rhs[k][Q::ADV + f]);
     }
     if constexpr (VISC) {  // m_rhs.fpp:591-603: momentum .. energy
@@ -449,45 +478,53 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   if constexpr (ND > 1) {
     constexpr int NCY = TY + 2;
     // variable v of the cell at (tx, cy)
-    auto y_recon = [&](const RT* __restrict__ c, const int tx, const int cy, const int v, const bool nonlin) {
-      const RT* col = sq + (v * LY + cy + H - 1) * LX + tx + H;
+    auto y_recon = [&](const RT* __restrict__ c, const int tx, const int cy, const int v) {
       RT st[5];
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
         const int o = k - 2;
-        st[k] = (o >= -(WO / 2) && o <= WO / 2) ? col[o * LX] : RT(0);
+        st[k] = (o >= -(WO / 2) && o <= WO / 2) ? sq[qi(v, cy + H - 1 + o, tx + H)] : RT(0);
       }
       RT vl, vr;
-      if constexpr (GATE) {
-        if (nonlin) weno5_cell_fast(c, st, eps, vl, vr);
-        else weno5_cell_linear(c, st, vl, vr);
-      } else if constexpr (kSplit && WO == 5) {
-        weno5_cell_fast(c, st, eps, vl, vr);
-      } else {
-        weno_cell<WO, RT>(c, st, eps, vl, vr);
-      }
-      wl[(v * NCY + cy) * TX + tx] = vl;
-      wr[(v * NCY + cy) * TX + tx] = vr;
+      weno_cell<WO, RT>(c, st, eps, vl, vr);
+      wl[wyi(v, cy, tx)] = vl;
+      wr[wyi(v, cy, tx)] = vr;
     };
-    if constexpr (Sh::NCOEF > 0) {
-      deal_positions<NCY * TX, S, NT>(tid, [&](const int p, const int v, const bool all) {
+    if constexpr (kPair) {
+      constexpr int NPR = Sh::SP / 2;
+      const f32x2 eps2 = f2_pack(eps, eps);
+      auto y_pair = [&](const auto& C, const int tx, const int cy, const int pr, const bool nonlin) {
+        const f32x2* col = reinterpret_cast<const f32x2*>(sq) + (pr * LY + cy + H - 1) * LX + tx + H;
+        f32x2 st[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) st[k] = col[(k - 2) * LX];
+        f32x2 vl, vr;
+        if constexpr (GATE) {
+          if (nonlin) weno5_pair_fast(C, st, eps2, vl, vr);
+          else weno5_pair_linear(C, st, vl, vr);
+        } else {
+          weno5_pair_fast(C, st, eps2, vl, vr);
+        }
+        reinterpret_cast<f32x2*>(wl)[(pr * NCY + cy) * TX + tx] = vl;
+        reinterpret_cast<f32x2*>(wr)[(pr * NCY + cy) * TX + tx] = vr;
+      };
+      deal_positions<NCY * TX, NPR, NT>(tid, [&](const int p, const int v, const bool all) {
         const int tx = p % TX, cy = p / TX;
         bool nonlin = true;
         if constexpr (GATE) nonlin = gflag[GateShape<ND, TX, TY, NT>::NGX + p] != 0;
-        // the shared record of a uniform grid, else the cell's staged record
-        // (reloaded per variable: keeping it live across them costs registers)
         auto one = [&](const int w) {
           if (uy) {
-            y_recon(U->rec[1], tx, cy, w, nonlin);
+            const f32x2* rec = U->rec[1];
+            y_pair([&](int k) { return rec[k]; }, tx, cy, w, nonlin);
           } else {
             RT c[kCoefRec];
             load_coef_record(scy + cy * kCoefRec, c);
-            y_recon(c, tx, cy, w, nonlin);
+            y_pair([&](int k) { return f2_pack(c[k], c[k]); }, tx, cy, w, nonlin);
           }
         };
         if (all) {
 #pragma unroll 1
-          for (int w = 0; w < S; ++w) one(w);
+          for (int w = 0; w < NPR; ++w) one(w);
         } else {
           one(v);
         }
@@ -505,7 +542,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
 #pragma unroll
           for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
         }
-        y_recon(c, tx, cy, v, true);
+        y_recon(c, tx, cy, v);
       }
     }
     __syncthreads();
@@ -520,8 +557,8 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       const bool rfl = (gface == ny - 1 && P.bc_end[1] == -4);
 #pragma unroll
       for (int v = 0; v < S; ++v) {
-        const RT a = wr[(v * NCY + f) * TX + tx];
-        const RT b = wl[(v * NCY + f + 1) * TX + tx];
+        const RT a = wr[wyi(v, f, tx)];
+        const RT b = wl[wyi(v, f + 1, tx)];
         qL[v] = lfr ? b : a;
         qR[v] = rfl ? a : b;
       }
@@ -530,7 +567,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         hllc_face<ND, NF, 1, RT, true>(qL, qR, gam_i, pi_i, F, us, vs);
         const ViscParams& V = *P.visc;
         const int ly = f + H - 1, lx = tx + H;  // the face's lower cell
-        auto U = [&](int c, int x, int y) { return sq[((Q::MOM + c) * LY + y) * LX + x]; };
+        auto U = [&](int c, int x, int y) { return sq[qi(Q::MOM + c, y, x)]; };
         const auto Dy = divisor(narrow<RT>(__ldg(V.dcc[1] + min(y0 + f, ny))));  // y_cc(k+1) - y_cc(k)
         const int gx = min(x0 + tx, nx - 1);
         const auto D0 = divisor(narrow<RT>(__ldg(V.dcc[0] + gx))), D1 = divisor(narrow<RT>(__ldg(V.dcc[0] + gx + 1)));
@@ -571,7 +608,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       const AT du = AT(fl[(S * NFYr + ty + 1) * TX + tx]) - AT(fl[(S * NFYr + ty) * TX + tx]);
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
-        const AT a = AT(sq[((Q::ADV + f) * LY + ty + H) * LX + tx + H]);
+        const AT a = AT(sq[qi(Q::ADV + f, ty + H, tx + H)]);
         rhs[k][Q::ADV + f] = mul_add(inv * a, du, rhs[k][Q::ADV + f]);
       }
       if constexpr (VISC) {  // m_rhs.fpp:639-651

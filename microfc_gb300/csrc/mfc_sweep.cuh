@@ -65,6 +65,17 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
   RT* wr = wl + Sh::NW;
   RT* fl = wr + Sh::NW;
   RT* sc = sq + Sh::OC;  // 16-byte aligned coefficient records
+  // split WENO5 keeps the variables in interleaved pairs (2p, 2p+1) of the
+  // primitive tile and the WENO values, reconstructed two at a time with
+  // packed FP32 instructions (sys_size is even in 3-D)
+  constexpr bool kPair = Sh::NCOEF > 0;
+  static_assert(!kPair || S % 2 == 0, "3-D pairs need an even number of variables");
+  auto qi = [](int v, int p, int la) {
+    return kPair ? (((v >> 1) * NP + p) * LA + la) * 2 + (v & 1) : (v * NP + p) * LA + la;
+  };
+  auto wi = [](int v, int p, int ca) {
+    return kPair ? (((v >> 1) * NP + p) * (TA + 2) + ca) * 2 + (v & 1) : (v * NP + p) * (TA + 2) + ca;
+  };
 
   const int tid = threadIdx.x;
   // block origin: blockIdx.x tiles the fastest non-sweep axis for DIR != 0
@@ -131,11 +142,11 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
       float pr[S];
       cons_to_prim_split<3, NF>(q, P, pr);
 #pragma unroll
-      for (int v = 0; v < S; ++v) sq[(v * NP + p) * LA + la] = pr[v];
+      for (int v = 0; v < S; ++v) sq[qi(v, p, la)] = pr[v];
     } else {
       cons_to_prim<3, NF>(q, P);
 #pragma unroll
-      for (int v = 0; v < S; ++v) sq[(v * NP + p) * LA + la] = RT(q[v]);
+      for (int v = 0; v < S; ++v) sq[qi(v, p, la)] = RT(q[v]);
     }
   }
   if constexpr (Sh::NCOEF > 0) {
@@ -153,35 +164,47 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
   constexpr int NCA = TA + 2;
   // variable v of cell ca of pencil p; c: the cell's coefficient record
   auto recon = [&](const RT* __restrict__ c, const int ca, const int p, const int v) {
-    const RT* line = sq + (v * NP + p) * LA + ca + H - 1;
     RT stc[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
       const int o = k - 2;
-      stc[k] = (o >= -(WO / 2) && o <= WO / 2) ? line[o] : RT(0);
+      stc[k] = (o >= -(WO / 2) && o <= WO / 2) ? sq[qi(v, p, ca + H - 1 + o)] : RT(0);
     }
     RT vl, vr;
-    if constexpr (kSplit && WO == 5) weno5_cell_fast(c, stc, eps, vl, vr);
-    else weno_cell<WO, RT>(c, stc, eps, vl, vr);
-    wl[(v * NP + p) * NCA + ca] = vl;
-    wr[(v * NP + p) * NCA + ca] = vr;
+    weno_cell<WO, RT>(c, stc, eps, vl, vr);
+    wl[wi(v, p, ca)] = vl;
+    wr[wi(v, p, ca)] = vr;
   };
-  if constexpr (Sh::NCOEF > 0) {
-    deal_positions<NP * NCA, S, NT>(tid, [&](const int q, const int v, const bool all) {
+  if constexpr (kPair) {
+    constexpr int NPR = S / 2;
+    const f32x2 eps2 = f2_pack(eps, eps);
+    // variable pair pr of cell ca of pencil p; C(k): coefficient k as a (c, c) pair
+    auto pair = [&](const auto& C, const int ca, const int p, const int pr) {
+      const f32x2* line = reinterpret_cast<const f32x2*>(sq) + (pr * NP + p) * LA + ca + H - 1;
+      f32x2 stc[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) stc[k] = line[k - 2];
+      f32x2 vl, vr;
+      weno5_pair_fast(C, stc, eps2, vl, vr);
+      reinterpret_cast<f32x2*>(wl)[(pr * NP + p) * NCA + ca] = vl;
+      reinterpret_cast<f32x2*>(wr)[(pr * NP + p) * NCA + ca] = vr;
+    };
+    deal_positions<NP * NCA, NPR, NT>(tid, [&](const int q, const int v, const bool all) {
       const int ca = q % NCA, p = q / NCA;
       // the shared record of a uniform grid, else the cell's staged record
       auto one = [&](const int w) {
         if (ua) {
-          recon(U.rec[DIR], ca, p, w);
+          const f32x2* rec = U.rec[DIR];
+          pair([&](int k) { return rec[k]; }, ca, p, w);
         } else {
           RT c[kCoefRec];
           load_coef_record(sc + ca * kCoefRec, c);
-          recon(c, ca, p, w);
+          pair([&](int k) { return f2_pack(c[k], c[k]); }, ca, p, w);
         }
       };
       if (all) {
 #pragma unroll 1
-        for (int w = 0; w < S; ++w) one(w);
+        for (int w = 0; w < NPR; ++w) one(w);
       } else {
         one(v);
       }
@@ -212,8 +235,8 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
     const bool rfl = (gface == na - 1 && P.bc_end[OA] == -4);
 #pragma unroll
     for (int v = 0; v < S; ++v) {
-      const RT a = wr[(v * NP + p) * NCA + f];
-      const RT b = wl[(v * NP + p) * NCA + f + 1];
+      const RT a = wr[wi(v, p, f)];
+      const RT b = wl[wi(v, p, f + 1)];
       qL[v] = lfr ? b : a;
       qR[v] = rfl ? a : b;
     }
@@ -249,7 +272,7 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
     const AT du = AT(fl[(S * NP + p) * NFA + ta + 1]) - AT(fl[(S * NP + p) * NFA + ta]);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
-      const AT a = AT(sq[((Q::ADV + f) * NP + p) * LA + ta + H]);
+      const AT a = AT(sq[qi(Q::ADV + f, p, ta + H)]);
       r[Q::ADV + f] = mul_add(inv * a, du, r[Q::ADV + f]);
     }
     if (DIR < 2) {

@@ -11,6 +11,7 @@ void register_stage_2d_fp32(std::vector<StageEntry>& r) {
   r.push_back(stage_entry<2, 2, 5, float, 16, 16, 256>());
   r.push_back(stage_entry<2, 2, 5, float, 64, 8, 512>());
   r.push_back(stage_entry<2, 2, 5, float, 16, 16, 256, false, 6>());
+  r.push_back(stage_entry<2, 2, 5, float, 16, 16, 256, false, 5>());
   r.push_back(stage_entry<2, 2, 5, float, 16, 8, 128>());
   r.push_back(stage_entry<2, 2, 5, float, 16, 16, 128>());
   r.push_back(stage_entry<2, 1, 5, float, 32, 16, 256>());
