@@ -758,15 +758,19 @@ __device__ __forceinline__ double rk_combine(int kind, double base, double in, d
   }
 }
 
-// The same combinations for the split-precision path: FP64 state and
-// accumulation, fused, with the division by 3 replaced by a multiplication.
-__device__ __forceinline__ double rk_combine_split(int kind, double base, double in, double dt, double r) {
+// The same combinations for the split-precision path, written as q^n plus
+// the stage's increment: (q1 - q0 + dt r)/2 for RK2, (q1 - q0 + dt r)/4 and
+// 2 (q2 - q0 + dt r)/3 for RK3.  The increment is small next to the state,
+// so it is formed in FP32 from the FP32 right-hand side and the FP64
+// difference of the registers, and the state accumulates in FP64: one or two
+// FP64 operations per value instead of two or three.
+__device__ __forceinline__ double rk_combine_split(int kind, double base, double in, float dt, float r) {
   switch (kind) {
-    case kRkEuler: return fma(dt, r, base);
-    case kRk2Final: return 0.5 * fma(dt, r, base + in);
-    case kRk3Mid: return 0.25 * fma(dt, r, fma(3.0, base, in));
-    case kRk3Final: return (1.0 / 3.0) * fma(2.0 * dt, r, fma(2.0, in, base));
-    default: return r;
+    case kRkEuler: return base + f2d_bits(dt * r);
+    case kRk2Final: return base + f2d_bits(0.5f * fmaf(dt, r, d2f_bits(in - base)));
+    case kRk3Mid: return base + f2d_bits(0.25f * fmaf(dt, r, d2f_bits(in - base)));
+    case kRk3Final: return base + f2d_bits((2.0f / 3.0f) * fmaf(dt, r, d2f_bits(in - base)));
+    default: return f2d_bits(r);
   }
 }
 

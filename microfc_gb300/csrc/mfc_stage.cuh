@@ -623,6 +623,8 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
 
   // ---- phase 6b: RK combination and store ------------------------------------
   bool bad = false;
+  const float dtf = kSplit ? __double2float_rn(dt) : 0.f;  // the split path's increments are FP32
+  (void)dtf;
   double icfl = 0.0;
 #pragma unroll
   for (int k = 0; k < CPT; ++k) {
@@ -635,15 +637,14 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
     double qn[S];
 #pragma unroll
     for (int v = 0; v < S; ++v) {
-      const double r = widen(rhs[k][v]);
       double out;
       if (kind == kRhsOnly) {
-        out = r;
+        out = widen(rhs[k][v]);
       } else {
         const double b = __ldg(qbase + o + v * P.sv);
         const double in = (kind == kRkEuler) ? b : __ldg(qin + o + v * P.sv);
-        if constexpr (kSplit) out = rk_combine_split(kind, b, in, dt, r);
-        else out = rk_combine(kind, b, in, dt, r);
+        if constexpr (kSplit) out = rk_combine_split(kind, b, in, dtf, rhs[k][v]);
+        else out = rk_combine(kind, b, in, dt, rhs[k][v]);
       }
       bad |= not_finite(out);
       qout[o + v * P.sv] = out;

@@ -252,6 +252,8 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
   AT* rhs_buf = reinterpret_cast<AT*>(P.work);
   bool bad = false;
   double icfl = 0.0;
+  const float dtf = kSplit ? __double2float_rn(dt) : 0.f;  // the split path's increments are FP32
+  (void)dtf;
   for (int it = tid; it < NP * TA; it += NT) {
     int ta, pb, pc;
     if (DIR == 0) { ta = it % TA; pb = (it / TA) % TB; pc = it / (TA * TB); }
@@ -283,15 +285,14 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
     double qn[S];
 #pragma unroll
     for (int v = 0; v < S; ++v) {
-      const double rv = widen(r[v]);
       double out;
       if (kind == kRhsOnly) {
-        out = rv;
+        out = widen(r[v]);
       } else {
         const double b = __ldg(qbase + o + v * P.sv);
         const double in = (kind == kRkEuler) ? b : __ldg(qin + o + v * P.sv);
-        if constexpr (kSplit) out = rk_combine_split(kind, b, in, dt, rv);
-        else out = rk_combine(kind, b, in, dt, rv);
+        if constexpr (kSplit) out = rk_combine_split(kind, b, in, dtf, r[v]);
+        else out = rk_combine(kind, b, in, dt, r[v]);
       }
       bad |= not_finite(out);
       qout[o + v * P.sv] = out;
