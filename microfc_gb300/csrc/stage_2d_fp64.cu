@@ -1,6 +1,7 @@
 // Instantiations of the fused stage kernel for 2-D cases, FP64 arithmetic.
 // Tile variants (TX x TY cells, NT threads) are chosen by the autotuner; the
-// first entry per configuration is the default.
+// first entry per configuration is the default (the autotuner's usual choice
+// on GB300).
 #include "mfc_launch.h"
 
 namespace mfc {
@@ -10,8 +11,8 @@ void register_stage_2d_fp64(std::vector<StageEntry>& r) {
 // of a tile take one pass each, as do its 3808 x reconstructions (7 per
 // thread), so fewer threads wait at the barriers between the phases.
 #define MFC_2D(NF, WO)                                           \
-  r.push_back(stage_entry<2, NF, WO, double, 16, 16, 256>());   \
   r.push_back(stage_entry<2, NF, WO, double, 32, 16, 512>());   \
+  r.push_back(stage_entry<2, NF, WO, double, 16, 16, 256>());   \
   r.push_back(stage_entry<2, NF, WO, double, 32, 16, 544>());
   MFC_2D(2, 5)
   MFC_2D(1, 5)
