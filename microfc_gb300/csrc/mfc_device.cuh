@@ -158,6 +158,16 @@ __device__ __forceinline__ double f2d_bits(float f) {
   return __hiloint2double((int)f2d_high_word(b), (int)lo);
 }
 
+// Programmatic dependent launch.  The single-case stage kernels are launched
+// with cudaLaunchAttributeProgrammaticStreamSerialization, so the next RK
+// stage's kernel may become resident while this one drains its last tiles:
+// griddep_wait() holds a kernel until the previous one has completed and its
+// stores are visible (everything before it may read only constant tables),
+// griddep_launch_dependents() lets the next kernel start.  Both are no-ops
+// in a kernel launched without the attribute.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Approximate FP32 reciprocal (PTX rcp.approx.ftz.f32); the split path
 // refines it where more accuracy is needed.
 __device__ __forceinline__ float rcp_approx(float x) {

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include <type_traits>
+#include <utility>
 
 #include "mfc_device.cuh"
 #include "mfc_stage.cuh"
@@ -26,6 +27,25 @@ struct StageEntry {
                         double* qout, double dt, int kind, cudaStream_t st);
   bool visc = false;  // compiled with the viscous terms
 };
+
+// Launches a stage kernel with programmatic stream serialization, so that
+// it may become resident while the previous kernel on the stream drains
+// (the kernel waits for that kernel's results with griddep_wait).
+template <class... KArgs, class... Args>
+cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                             Args&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // MINB > 1 selects the register-capped kernel (stage_kernel_mb).
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool VISC>
@@ -50,9 +70,8 @@ cudaError_t stage_launch(const DevParams& P, const UniformCoef& U, const double*
   const bool shared_coef = U.on[0] && (ND < 2 || U.on[1]);
   const size_t smem = shared_coef ? stage_smem_bytes_shared_coef<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>()
                                   : stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>();
-  stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>()<<<grid, NT, smem, st>>>(P, U, qin, qbase, qout, dt,
-                                                                                      kind);
-  return cudaGetLastError();
+  return launch_dependent(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>(), grid, dim3(NT), smem, st, P, U,
+                          qin, qbase, qout, dt, kind);
 }
 
 // prec of a registry entry: 0 FP64, 1 split, 2 split with the learned gate
@@ -94,10 +113,15 @@ struct Sweep3D {
     const dim3 g0((nx + TA0 - 1) / TA0, (ny + TB0 - 1) / TB0, (nz + TC0 - 1) / TC0);
     const dim3 g1((nx + TB1 - 1) / TB1, (ny + TA1 - 1) / TA1, nz);
     const dim3 g2((nx + TB1 - 1) / TB1, (nz + TA1 - 1) / TA1, ny);
-    sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT><<<g0, NT, K<0>::kSmemBytes, st>>>(P, U, qin, qbase, qout, dt, kind);
-    sweep_kernel<NF, WO, RT, 1, TA1, TB1, 1, NT><<<g1, NT, K<1>::kSmemBytes, st>>>(P, U, qin, qbase, qout, dt, kind);
-    sweep_kernel<NF, WO, RT, 2, TA1, TB1, 1, NT><<<g2, NT, K<2>::kSmemBytes, st>>>(P, U, qin, qbase, qout, dt, kind);
-    return cudaGetLastError();
+    cudaError_t e = launch_dependent(&sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT>, g0, dim3(NT), K<0>::kSmemBytes,
+                                     st, P, U, qin, qbase, qout, dt, kind);
+    if (e == cudaSuccess)
+      e = launch_dependent(&sweep_kernel<NF, WO, RT, 1, TA1, TB1, 1, NT>, g1, dim3(NT), K<1>::kSmemBytes, st, P, U, qin,
+                           qbase, qout, dt, kind);
+    if (e == cudaSuccess)
+      e = launch_dependent(&sweep_kernel<NF, WO, RT, 2, TA1, TB1, 1, NT>, g2, dim3(NT), K<2>::kSmemBytes, st, P, U, qin,
+                           qbase, qout, dt, kind);
+    return e;
   }
   static StageEntry entry() {
     return StageEntry{3, NF, WO, sizeof(RT) == 8 ? 0 : 1, TA0, TB1, NT, K<1>::kSmemBytes, 3, &prepare, &launch};

@@ -189,6 +189,27 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   (void)uy;
 
   // ---- phase 1: load + BCs + cons -> prim --------------------------------
+  if constexpr (Sh::NCOEF > 0) {
+    // the tile's coefficient records (constant tables: staged before the
+    // wait for the previous stage); global reads coalesced along the cells,
+    // records written per cell
+    for (int it = ux ? kCoefRec * Sh::NCX : tid; it < kCoefRec * Sh::NCX; it += NT) {
+      const int cx = it % Sh::NCX, k = it / Sh::NCX;
+      scx[cx * kCoefRec + k] =
+          k < kNumCoef ? d2f_bits(__ldg(P.coef[0] + k * P.cstride[0] + clamp_coef_index(x0 - 1 + cx, nx) + P.coff))
+                       : 0.f;
+    }
+    if constexpr (ND > 1) {
+      for (int it = uy ? kCoefRec * Sh::NCY : tid; it < kCoefRec * Sh::NCY; it += NT) {
+        const int cy = it % Sh::NCY, k = it / Sh::NCY;
+        scy[cy * kCoefRec + k] =
+            k < kNumCoef
+                ? d2f_bits(__ldg(P.coef[1] + k * P.cstride[1] + clamp_coef_index(y0 - 1 + cy, ny) + P.coff))
+                : 0.f;
+      }
+    }
+  }
+  griddep_wait();  // the state below is the previous stage's output
   for (int c = tid; c < LX * LY; c += NT) {
     const int lx = c % LX, ly = c / LX;
     const bool hx = lx < H || lx >= H + TX;
@@ -242,24 +263,6 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       cons_to_prim<ND, NF>(q, P);
 #pragma unroll
       for (int v = 0; v < S; ++v) sq[qi(v, ly, lx)] = RT(q[v]);
-    }
-  }
-  if constexpr (Sh::NCOEF > 0) {
-    // global reads coalesced along the cells, records written per cell
-    for (int it = ux ? kCoefRec * Sh::NCX : tid; it < kCoefRec * Sh::NCX; it += NT) {
-      const int cx = it % Sh::NCX, k = it / Sh::NCX;
-      scx[cx * kCoefRec + k] =
-          k < kNumCoef ? d2f_bits(__ldg(P.coef[0] + k * P.cstride[0] + clamp_coef_index(x0 - 1 + cx, nx) + P.coff))
-                       : 0.f;
-    }
-    if constexpr (ND > 1) {
-      for (int it = uy ? kCoefRec * Sh::NCY : tid; it < kCoefRec * Sh::NCY; it += NT) {
-        const int cy = it % Sh::NCY, k = it / Sh::NCY;
-        scy[cy * kCoefRec + k] =
-            k < kNumCoef
-                ? d2f_bits(__ldg(P.coef[1] + k * P.cstride[1] + clamp_coef_index(y0 - 1 + cy, ny) + P.coff))
-                : 0.f;
-      }
     }
   }
   __syncthreads();
@@ -622,6 +625,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   }
 
   // ---- phase 6b: RK combination and store ------------------------------------
+  griddep_launch_dependents();
   bool bad = false;
   const float dtf = kSplit ? __double2float_rn(dt) : 0.f;  // the split path's increments are FP32
   (void)dtf;

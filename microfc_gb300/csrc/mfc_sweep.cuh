@@ -104,6 +104,18 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
   const int64_t st[3] = {1, P.sy, P.sz};
 
   // ---- load + BCs + cons -> prim ------------------------------------------------
+  // the tile's coefficient records come from constant tables: staged before
+  // the wait for the previous kernel
+  if constexpr (Sh::NCOEF > 0) {
+    for (int it = ua ? kCoefRec * (TA + 2) : tid; it < kCoefRec * (TA + 2); it += NT) {
+      const int ca = it % (TA + 2), k = it / (TA + 2);
+      sc[ca * kCoefRec + k] =
+          k < kNumCoef
+              ? d2f_bits(__ldg(P.coef[DIR] + k * P.cstride[DIR] + clamp_coef_index(a0 - 1 + ca, na) + P.coff))
+              : 0.f;
+    }
+  }
+  griddep_wait();  // the state (and the partial RHS) below are earlier kernels' output
   // thread order: the a index fastest for the x sweep, the pencil b index
   // fastest otherwise, so that global loads are coalesced along x
   for (int it = tid; it < NP * LA; it += NT) {
@@ -147,15 +159,6 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
       cons_to_prim<3, NF>(q, P);
 #pragma unroll
       for (int v = 0; v < S; ++v) sq[qi(v, p, la)] = RT(q[v]);
-    }
-  }
-  if constexpr (Sh::NCOEF > 0) {
-    for (int it = ua ? kCoefRec * (TA + 2) : tid; it < kCoefRec * (TA + 2); it += NT) {
-      const int ca = it % (TA + 2), k = it / (TA + 2);
-      sc[ca * kCoefRec + k] =
-          k < kNumCoef
-              ? d2f_bits(__ldg(P.coef[DIR] + k * P.cstride[DIR] + clamp_coef_index(a0 - 1 + ca, na) + P.coff))
-              : 0.f;
     }
   }
   __syncthreads();
@@ -249,6 +252,7 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
   __syncthreads();
 
   // ---- flux divergence, accumulation, RK on the last sweep ---------------------------
+  griddep_launch_dependents();
   AT* rhs_buf = reinterpret_cast<AT*>(P.work);
   bool bad = false;
   double icfl = 0.0;
