@@ -49,12 +49,12 @@ __device__ __forceinline__ double widen(double x) { return x; }
 __device__ __forceinline__ double widen(float x) { return f2d_bits(x); }
 
 // Work distribution of a split WENO5 phase: NPOS positions (cells of the
-// tile's rows or columns) times S variables.  Each full pass gives a thread
-// one position with all S variables, so that the position's index
-// arithmetic, gate flag and coefficient record serve S reconstructions; the
-// NPOS % NT positions left over are dealt out per (position, variable), so
-// that no thread does more than ceil(S * NPOS / NT) reconstructions.
-// f(p, v, all): position p, all variables when all, else variable v.
+// tile's rows or columns) times S items (the variable pairs).  Each full
+// pass gives a thread one position with all S items, so that the position's
+// index arithmetic, gate flag and coefficient record serve S
+// reconstructions; the NPOS % NT positions left over are dealt out per
+// (position, item), so that no thread does more than ceil(S * NPOS / NT).
+// f(p, v, all): position p, all items when all, else item v.
 template <int NPOS, int S, int NT, class F>
 __device__ __forceinline__ void deal_positions(const int tid, F&& f) {
   constexpr int FULL = (NPOS / NT) * NT, REM = NPOS - FULL;
