@@ -282,23 +282,30 @@ int mfc_gpu_ensemble_finalize(mfc_gpu_ensemble* ens);
 int mfc_gpu_ensemble_set_gate(mfc_gpu_ensemble* ens, const float* host_params);
 
 /* ---- Initial condition on the device: the reference's pre_process patches
- * (src/pre_process/m_create_patches.fpp:47-313: line segment 1, circle 2,
- * rectangle 3; sphere 8 and cuboid 9 are their 3-D analogues), the
- * smoothed-patch blend (m_assign_patches.fpp:54-165) and prim -> cons
- * (src/common/m_variables_conversion.fpp:385-443), on the uniform grid of
- * m_grid.f90:54-70 over the given domain.  Fields mirror patch_icpp(i)%... of
- * the case file; alter_patch[j] != 0 lets the patch overwrite cells owned by
- * patch j (j = 0: no patch yet).  Writes register 0 (q_cons_ts(1)) directly:
- * no host initial condition and no file round trip.  Same operation order
- * as the CPU pre_process; only tanh (smoothed circles and spheres) may
- * differ from the host's libm in the last bit. */
+ * (src/pre_process/m_create_patches.fpp:47-534): line segment 1, circle 2,
+ * rectangle 3, sweep line 4, ellipse 5, isentropic vortex 6, 2-D analytical
+ * 7, 1-D analytical 15 and varcircle 18 (geometries 2-7 and 18 are
+ * z-independent in 3-D); sphere 8 and cuboid 9 are the 3-D analogues of 2
+ * and 3.  Then the smoothed-patch blend (m_assign_patches.fpp:54-165) and
+ * prim -> cons (src/common/m_variables_conversion.fpp:385-443), on the
+ * uniform grid of m_grid.f90:54-70 over the given domain.  Fields mirror
+ * patch_icpp(i)%... of the case file; alter_patch[j] != 0 lets the patch
+ * overwrite cells owned by patch j (j = 0: no patch yet).  Writes register 0
+ * (q_cons_ts(1)) directly: no host initial condition and no file round trip.
+ * Same operation order as the CPU pre_process; only tanh (smoothed circles,
+ * spheres, ellipses and sweep lines) and exp (the analytical patches'
+ * pressure bump) may differ from the host's libm in the last bit.  Refused:
+ * a geometry the grid's dimensionality does not take, a smooth_patch_id
+ * outside 1..num_patches on a patch that blends, an ellipse with a
+ * non-positive semi-axis, a sweep line with a zero normal. */
 #define MFC_MAX_PATCHES 10
 typedef struct mfc_patch {
-  int32_t geometry;                 /* 1, 2, 3, 8 or 9                                  */
+  int32_t geometry;                 /* 1-9, 15 or 18 (see above)                        */
   double x_centroid, y_centroid, z_centroid;
   double length_x, length_y, length_z;
   double radius;
-  int32_t smoothen;                 /* circles/spheres: tanh-smoothed volume fraction   */
+  int32_t smoothen;                 /* circles, spheres, ellipses, sweep lines: tanh    */
+                                    /* smoothed volume fraction                         */
   int32_t smooth_patch_id;          /* 1-based patch the smoothing blends into          */
   double smooth_coeff;
   int32_t alter_patch[MFC_MAX_PATCHES + 1];
@@ -306,9 +313,16 @@ typedef struct mfc_patch {
   double alpha[MFC_MAX_FLUIDS];
   double vel[3];
   double pres;
+  double normal[3];                 /* sweep line: (a, b) of a x + b y + c >= 0          */
+  double radii[3];                  /* ellipse: semi-axes along x and y                 */
+  double epsilon;                   /* varcircle: thickness of the annulus              */
 } mfc_patch;
 
-/* domain: x_beg, x_end, y_beg, y_end, z_beg, z_end (unused directions ignored). */
+/* domain: x_beg, x_end, y_beg, y_end, z_beg, z_end (unused directions
+ * ignored), the uniform grid of m_grid.f90:54-70.  domain == NULL (single
+ * case only): the context's own cell boundaries, with cell centres
+ * (x_cb(i-1) + x_cb(i))/2 and the smallest cell width as the smoothing
+ * length, as pre_process sets them on a stretched grid (m_grid.f90:72-90). */
 int mfc_gpu_generate_ic(mfc_gpu_ctx* ctx, const mfc_patch* patches, int num_patches, const double* domain);
 int mfc_gpu_ensemble_generate_ic(mfc_gpu_ensemble* ens, int case_index, const mfc_patch* patches, int num_patches,
                                  const double* domain);

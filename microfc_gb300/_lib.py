@@ -70,6 +70,9 @@ class MfcPatch(ctypes.Structure):
         ("alpha", ctypes.c_double * MFC_MAX_FLUIDS),
         ("vel", ctypes.c_double * 3),
         ("pres", ctypes.c_double),
+        ("normal", ctypes.c_double * 3),
+        ("radii", ctypes.c_double * 3),
+        ("epsilon", ctypes.c_double),
     ]
 
 

@@ -22,7 +22,9 @@ DFLT_REAL = -1e6         # m_global_parameters.fpp:37
 @dataclass
 class Patch:
     """One initial-condition patch (pre_process patch_icpp)."""
-    geometry: int                       # 1 line, 2 circle, 3 rectangle, 8 sphere, 9 cuboid
+    geometry: int                       # 1 line, 2 circle, 3 rectangle, 4 sweep line, 5 ellipse,
+                                        # 6 isentropic vortex, 7 2-D analytical, 8 sphere, 9 cuboid,
+                                        # 15 1-D analytical, 18 varcircle
     centroid: tuple = (0.0, 0.0, 0.0)
     length: tuple = (0.0, 0.0, 0.0)
     radius: float = 0.0
@@ -34,6 +36,18 @@ class Patch:
     alpha: tuple = ()
     vel: tuple = (0.0, 0.0, 0.0)
     pres: float = 0.0
+    normal: tuple = (0.0, 0.0, 0.0)     # sweep line: normal of the line, pointing into the patch
+    radii: tuple = (0.0, 0.0, 0.0)      # ellipse: semi-axes along x and y
+    epsilon: float = 0.0                # varcircle: thickness of the annulus
+
+
+def stretch_map(x: float, a: float, lo: float, hi: float) -> float:
+    """The hyperbolic stretching factor of a grid coordinate
+    (m_grid.f90:79-83), as the input check evaluates it on the domain's ends
+    (m_start_up.fpp:261-276)."""
+    import math
+    return (a + math.log(math.cosh(a * (x - lo))) + math.log(math.cosh(a * (x - hi)))
+            - 2.0 * math.log(math.cosh(0.5 * a * (hi - lo)))) / a
 
 
 @dataclass
@@ -60,6 +74,8 @@ class Case:
     re_shear: tuple = ()                # fluid_pp(i)%Re(1), shear Reynolds number (<= 0 or absent: inviscid)
     re_bulk: tuple = ()                 # fluid_pp(i)%Re(2), bulk Reynolds number
     patches: list = field(default_factory=list)
+    stretch_x: tuple = ()               # (a_x, x_a, x_b, loops_x) of a stretched x grid; () = uniform
+    stretch_y: tuple = ()               # (a_y, y_a, y_b, loops_y)
     precision: str = "fp64"             # "fp64", "split" or "gated" (split + learned WENO gate)
     name: str = "case"
 
@@ -152,6 +168,25 @@ class Case:
                 bad("Unsupported value of fluid_pp(i)%pi_inf")
         if self.precision not in ("fp64", "split", "gated"):
             bad("Unsupported value of precision mode")
+        # grid stretching, m_start_up.fpp:238-330 (pre_process)
+        for ax, st, dom, used in (("x", self.stretch_x, self.x_domain, True),
+                                  ("y", self.stretch_y, self.y_domain, self.n > 0)):
+            if not st:
+                continue
+            if not used:
+                bad(f"Unsupported choice of the combination of values for n and stretch_{ax}")
+            a, lo, hi, loops = st
+            for name, v in ((f"a_{ax}", a), (f"{ax}_a", lo), (f"{ax}_b", hi)):
+                if v == DFLT_REAL:
+                    bad(f"Unsupported choice of the combination of values for stretch_{ax} and {name}")
+            if lo >= hi:
+                bad(f"Unsupported choice of the combination of values for stretch_{ax}, {ax}_a and {ax}_b")
+            for end, v in (("beg", dom[0]), ("end", dom[1])):
+                if stretch_map(v, a, lo, hi) <= 0.0:
+                    bad(f"Unsupported choice of the combination of values for {ax}_domain%{end}, "
+                        f"stretch_{ax}, a_{ax}, {ax}_a, and {ax}_b")
+            if loops < 1:
+                bad(f"Unsupported choice for the value of loops_{ax}")
 
     # -- case-file dictionary --------------------------------------------------
     @classmethod
@@ -223,8 +258,14 @@ class Case:
                 smooth_coeff=float(pd.get("smooth_coeff", 0.0)),
                 alter_patch=alter,
                 alpha_rho=vecs("alpha_rho", nf), alpha=vecs("alpha", nf),
-                vel=vecs("vel", 3)[:3] if nd else (0.0,), pres=float(pd.get("pres", 0.0))))
+                vel=vecs("vel", 3)[:3] if nd else (0.0,), pres=float(pd.get("pres", 0.0)),
+                normal=vecs("normal", 3), radii=vecs("radii", 3), epsilon=float(pd.get("epsilon", 0.0))))
         bcy = (int(g.get("bc_y%beg", DFLT_INT)), int(g.get("bc_y%end", DFLT_INT)))
+        stretch = {}
+        for ax in ("x", "y"):
+            if g.get(f"stretch_{ax}", False) in (True, 1):
+                stretch[ax] = (float(g.get(f"a_{ax}", DFLT_REAL)), float(g.get(f"{ax}_a", DFLT_REAL)),
+                               float(g.get(f"{ax}_b", DFLT_REAL)), int(g.get(f"loops_{ax}", 1)))
         bcz = (int(g.get("bc_z%beg", DFLT_INT)), int(g.get("bc_z%end", DFLT_INT)))
         return cls(
             m=int(g["m"]), n=n, p=p,
@@ -238,6 +279,7 @@ class Case:
             weno_order=int(g.get("weno_order", 5)), weno_eps=float(g.get("weno_eps", 1e-16)),
             bc_x=(int(g.get("bc_x%beg", -3)), int(g.get("bc_x%end", -3))), bc_y=bcy, bc_z=bcz,
             gammas=tuple(gam), pi_infs=tuple(pinf), re_shear=tuple(res[0]), re_bulk=tuple(res[1]), patches=plist,
+            stretch_x=stretch.get("x", ()), stretch_y=stretch.get("y", ()),
             precision=str(g.get("gpu_precision", "fp64")), name=str(g.get("case_name", "case")))
 
     def to_namelist(self) -> str:

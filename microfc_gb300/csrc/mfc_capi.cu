@@ -380,8 +380,17 @@ int mfc_gpu_upload_state(mfc_gpu_ctx* c, const double* host_q) {
 
 int mfc_gpu_generate_ic(mfc_gpu_ctx* c, const mfc_patch* patches, int num_patches, const double* domain) {
   if (!c) return fail(MFC_ERR_INVALID, "NULL context");
-  mfc::IcTarget t{c->nd, c->prm.num_fluids, {c->n[0], c->n[1], c->n[2]}, c->sy, c->sz, c->sv,
-                  c->prm.gammas, c->prm.pi_infs, c->reg[0]};
+  mfc::IcTarget t{c->nd,
+                  c->prm.num_fluids,
+                  {c->n[0], c->n[1], c->n[2]},
+                  c->sy,
+                  c->sz,
+                  c->sv,
+                  c->prm.gammas,
+                  c->prm.pi_infs,
+                  c->reg[0],
+                  {c->cb_host[0].data(), c->nd > 1 ? c->cb_host[1].data() : nullptr,
+                   c->nd > 2 ? c->cb_host[2].data() : nullptr}};
   const std::string why = mfc::generate_ic(t, patches, num_patches, domain, c->stream, &c->launches);
   if (!why.empty()) return fail(MFC_ERR_INVALID, why);
   MFC_CUDA(cudaStreamSynchronize(c->stream));

@@ -261,7 +261,8 @@ int mfc_gpu_ensemble_generate_ic(mfc_gpu_ensemble* e, int i, const mfc_patch* pa
                                  const double* domain) {
   if (!e || i < 0 || i >= e->num) return mfc::report_error(MFC_ERR_INVALID, "bad ensemble case index");
   const mfc::EnsCase& C = e->cases[i];
-  mfc::IcTarget t{2, e->nf, {e->nx[i], e->ny[i], 1}, C.P.sy, C.P.sz, C.P.sv, C.P.gammas, C.P.pi_infs, C.reg[0]};
+  if (!domain) return mfc::report_error(MFC_ERR_INVALID, "ensemble initial conditions need a domain");
+  mfc::IcTarget t{2, e->nf, {e->nx[i], e->ny[i], 1}, C.P.sy, C.P.sz, C.P.sv, C.P.gammas, C.P.pi_infs, C.reg[0], {}};
   const std::string why = mfc::generate_ic(t, patches, num_patches, domain, e->stream, &e->launches);
   if (!why.empty()) return mfc::report_error(MFC_ERR_INVALID, why);
   cudaError_t err = cudaStreamSynchronize(e->stream);

@@ -18,9 +18,11 @@ struct IcTarget {
   const double* gammas;   // num_fluids values
   const double* pi_infs;
   double* q;              // register 0 of the case
+  const double* cb[3];    // host cell boundaries x_cb(-1:m) ... of the case, or null
 };
 
 // Launches the generator on `stream`; returns "" or the reason it refused.
+// domain == null: the grid is t.cb (any rectilinear grid, e.g. stretched).
 std::string generate_ic(const IcTarget& t, const mfc_patch* patches, int num_patches, const double* domain,
                         cudaStream_t stream, int64_t* launches);
 

@@ -78,7 +78,8 @@ class Ensemble:
     def generate_ic(self, i: int) -> None:
         """pre_process of case i on the device, straight into its state."""
         arr, dom = preprocess.device_patches(self.cases[i])
-        _lib.check(self.L.mfc_gpu_ensemble_generate_ic(self._h, int(i), arr, len(arr), _dp(dom)))
+        _lib.check(self.L.mfc_gpu_ensemble_generate_ic(self._h, int(i), arr, len(arr),
+                                                       None if dom is None else _dp(dom)))
 
     def close(self):
         if getattr(self, "_h", None):

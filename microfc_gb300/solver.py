@@ -97,7 +97,7 @@ class Simulation:
     def generate_ic(self, case: Case | None = None) -> None:
         """pre_process on the device: the case's patches straight into q_cons_ts(1)."""
         arr, dom = preprocess.device_patches(case or self.case)
-        _lib.check(self.L.mfc_gpu_generate_ic(self._h, arr, len(arr), _dp(dom)))
+        _lib.check(self.L.mfc_gpu_generate_ic(self._h, arr, len(arr), None if dom is None else _dp(dom)))
 
     # -- life cycle -----------------------------------------------------------
     def close(self) -> None:

@@ -56,6 +56,9 @@ class MfoPatch(ctypes.Structure):
         ("alpha", ctypes.c_double * MAX_FLUIDS),
         ("vel", ctypes.c_double * 3),
         ("pres", ctypes.c_double),
+        ("normal", ctypes.c_double * 3),
+        ("radii", ctypes.c_double * 3),
+        ("epsilon", ctypes.c_double),
     ]
 
 
@@ -96,7 +99,7 @@ def lib():
         L.mfo_generate_ic.restype = ctypes.c_int
         L.mfo_generate_ic.argtypes = [ctypes.POINTER(MfoParams), ctypes.POINTER(MfoPatch), ctypes.c_int,
                                       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
-                                      ctypes.c_double, ctypes.c_double, dp, dp, dp, dp]
+                                      ctypes.c_double, ctypes.c_double, dp, dp, dp, dp, dp]
         L.mfo_count_ops.restype = ctypes.c_int
         L.mfo_count_ops.argtypes = [ctypes.POINTER(MfoParams), dp, dp, dp, dp, ctypes.c_double, dp]
         _lib = L
@@ -205,14 +208,21 @@ def generate_ic(case):
             a.alpha[f] = pt.alpha[f]
         for d in range(3):
             a.vel[d] = pt.vel[d] if d < len(pt.vel) else 0.0
+            a.normal[d] = pt.normal[d] if d < len(pt.normal) else 0.0
+            a.radii[d] = pt.radii[d] if d < len(pt.radii) else 0.0
         a.pres = pt.pres
+        a.epsilon = pt.epsilon
     S = case.sys_size
     x_cb = np.zeros(case.m + 2)
     y_cb = np.zeros(case.n + 2)
     z_cb = np.zeros(case.p + 2)
     cons = np.zeros((S, case.p + 1, case.n + 1, case.m + 1))
     (xb, xe), (yb, ye), (zb, ze) = case.x_domain, case.y_domain, case.z_domain
-    rc = L.mfo_generate_ic(ctypes.byref(q), arr, P, xb, xe, yb, ye, zb, ze,
+    st = np.zeros(8)
+    for k, s in enumerate((case.stretch_x, case.stretch_y)):
+        if s:
+            st[4 * k: 4 * k + 4] = s
+    rc = L.mfo_generate_ic(ctypes.byref(q), arr, P, xb, xe, yb, ye, zb, ze, _dp(st),
                            _dp(x_cb), _dp(y_cb), _dp(z_cb), _dp(cons))
     if rc != 0:
         raise ValueError(f"oracle IC generation failed ({rc})")

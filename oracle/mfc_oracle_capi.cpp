@@ -126,11 +126,13 @@ int mfo_get_threads(void) {
 
 // ---------------------------------------------------------------------------
 // pre_process restatement: uniform grid and patches -> conservative state.
+// stretch: null, or {a_x, x_a, x_b, loops_x, a_y, y_a, y_b, loops_y} with
+// loops 0 for a uniform direction.
 int mfo_generate_ic(const mfo_params* q, const mfo_patch* patches, int num_patches, double x_beg, double x_end,
-                    double y_beg, double y_end, double z_beg, double z_end, double* x_cb, double* y_cb, double* z_cb,
-                    double* cons_out) {
-  return generate_ic(to_params(q), patches, num_patches, x_beg, x_end, y_beg, y_end, z_beg, z_end, x_cb, y_cb,
-                     z_cb, cons_out);
+                    double y_beg, double y_end, double z_beg, double z_end, const double* stretch, double* x_cb,
+                    double* y_cb, double* z_cb, double* cons_out) {
+  return generate_ic(to_params(q), patches, num_patches, x_beg, x_end, y_beg, y_end, z_beg, z_end, stretch, x_cb,
+                     y_cb, z_cb, cons_out);
 }
 
 // Operation counts of one full time step of the oracle, per interior cell.
