@@ -214,7 +214,7 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
     plain FP64 runs.  Accuracy of these modes against FP64 is asserted by
     tests/test_gpu_parity.py, tests/test_gate.py and tests/test_ensemble.py."""
     import torch
-    from microfc_gb300 import Simulation, gate
+    from microfc_gb300 import Simulation, _lib, gate
     from microfc_gb300.ensemble import Ensemble, random_droplet_cases
     out = {}
     params = gate.load() if os.path.exists(gate.WEIGHTS_FILE) else None
@@ -224,11 +224,13 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
             if p is not None:
                 s.set_gate(p)
             variant, _ = s.tune(5)
+            s.select_variant(variant)
+            tma = bool(s.variant_features(variant) & _lib.MFC_VARIANT_TMA)
             st = torch.cuda.ExternalStream(s.stream)
             t = _time_steps(s, st, flush, args.steps, args.warmup, case.dt)
             rate = case.cells * args.steps / t
             out[prec] = {"value": rate, "unit": "cell-updates/s", "ms_per_step": 1e3 * t / args.steps,
-                         "vs_plain_fp64": rate / fp64_rate, "tile_variant": variant}
+                         "vs_plain_fp64": rate / fp64_rate, "tile_variant": variant, "tma_staging": tma}
     if params is None:
         out["gated"] = {"unavailable": "no trained gate parameters (python -m microfc_gb300.gate)"}
     # config 3: the 3-D air/helium shock-bubble at 256^3, split precision,
@@ -385,7 +387,8 @@ def main():
         "config": {"workload": WORKLOAD if args.precision == "fp64" else WORKLOAD.replace("plain FP64", args.precision),
                    "cells": cells, "equations": case.sys_size, "dt": case.dt,
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}",
-                   "tile": {"variant": variant, "tx": tile[0], "ty": tile[1], "threads": tile[2]}},
+                   "tile": {"variant": variant, "tx": tile[0], "ty": tile[1], "threads": tile[2],
+                            "tma_staging": bool(sim.variant_features(variant) & _lib.MFC_VARIANT_TMA)}},
         "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes, "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,

@@ -25,11 +25,12 @@ EXPORTS = (
     "mfc_gpu_ensemble_finalize", "mfc_gpu_ensemble_set_gate", "mfc_gate_param_count", "mfc_gate_workspace_floats",
     "mfc_gpu_set_gate", "mfc_gpu_gate_samples", "mfc_gate_gradients", "mfc_gate_train_step", "mfc_gate_infer",
     "mfc_gpu_set_monitor", "mfc_gpu_icfl", "mfc_gpu_run_cfl", "mfc_gpu_generate_ic", "mfc_gpu_ensemble_generate_ic",
-    "mfc_gpu_snapshot", "mfc_gpu_snapshot_wait", "mfc_gpu_select_variant",
+    "mfc_gpu_snapshot", "mfc_gpu_snapshot_wait", "mfc_gpu_select_variant", "mfc_gpu_variant_features",
     "mfc_gpu_rk_stage", "mfc_gpu_halo_buffer", "mfc_gpu_halo_pack", "mfc_gpu_set_halo_widths",
     "mfc_gpu_set_viscosity", "mfc_gpu_set_uniform_coefficients", "mfc_gpu_ensemble_select_variant",
 )
 MFC_PREC_GATED = 2
+MFC_VARIANT_TMA = 0x1
 
 
 class MfcParams(ctypes.Structure):
@@ -130,6 +131,7 @@ def load(build_if_missing: bool = True):
     L.mfc_gpu_ensemble_upload.argtypes = [vp, ctypes.c_int, dp]
     ip = ctypes.POINTER(ctypes.c_int)
     L.mfc_gpu_select_variant.argtypes = [vp, ctypes.c_int, ip, ip, ip]
+    L.mfc_gpu_variant_features.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]
     L.mfc_gpu_rk_stage.argtypes = [vp, ctypes.c_int, ctypes.c_double]
     L.mfc_gpu_set_viscosity.argtypes = [vp, dp, dp]
     L.mfc_gpu_set_uniform_coefficients.argtypes = [vp, ctypes.c_int, ip]

@@ -63,6 +63,43 @@ const StageEntry* find_stage(int nd, int nf, int wo, int prec, bool visc) {
 }
 
 int report_error(int code, const std::string& msg) { return fail(code, msg); }
+
+bool encode_tile_map(TileMap& t, const double* base, int nx, int ny, int S, int64_t sy, int64_t sv, int box_w,
+                     int box_h) {
+  std::memset(&t, 0, sizeof(t));
+  // the driver's encoder, looked up through the runtime (no link against libcuda)
+  using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static const Encode encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return static_cast<Encode>(nullptr);
+    return reinterpret_cast<Encode>(fn);
+  }();
+  if (!encode || !base) return false;
+  // TMA rules: 16-byte aligned base and strides, boxes of at most 256 cells
+  // per dimension whose rows are a multiple of 16 bytes
+  if (reinterpret_cast<uintptr_t>(base) % 16 != 0 || (sy * 8) % 16 != 0 || (sv * 8) % 16 != 0) return false;
+  if (sy < nx || sv < sy * ny || sv * 8 >= (int64_t(1) << 40)) return false;
+  if (box_w < 1 || box_w > 256 || box_h < 1 || box_h > 256 || S > 256 || (box_w * 8) % 16 != 0) return false;
+  const cuuint64_t dims[3] = {cuuint64_t(nx), cuuint64_t(ny), cuuint64_t(S)};
+  const cuuint64_t strides[2] = {cuuint64_t(sy) * 8, cuuint64_t(sv) * 8};
+  const cuuint32_t box[3] = {cuuint32_t(box_w), cuuint32_t(box_h), cuuint32_t(S)};
+  const cuuint32_t unit[3] = {1, 1, 1};
+  const CUresult r = encode(&t.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double*>(base), dims, strides, box,
+                            unit, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    std::memset(&t, 0, sizeof(t));
+    return false;
+  }
+  t.on = 1;
+  return true;
+}
 }  // namespace mfc
 
 struct mfc_gpu_ctx {
@@ -715,6 +752,20 @@ int mfc_gpu_select_variant(mfc_gpu_ctx* c, int variant, int* tx, int* ty, int* t
     if (tx) *tx = e.tx;
     if (ty) *ty = e.ty;
     if (threads) *threads = e.nt;
+    return MFC_OK;
+  }
+  return fail(MFC_ERR_INVALID, "no such tile variant for this configuration");
+}
+
+int mfc_gpu_variant_features(mfc_gpu_ctx* c, int variant, uint32_t* features) {
+  if (!c || !features) return fail(MFC_ERR_INVALID, "NULL argument");
+  int idx = -1;
+  for (const auto& e : g_reg) {
+    if (e.nd != c->nd || e.nf != c->prm.num_fluids || e.wo != c->prm.weno_order || e.prec != c->prm.precision ||
+        e.visc != (c->visc != nullptr))
+      continue;
+    if (++idx != variant) continue;
+    *features = e.tma ? MFC_VARIANT_TMA : 0u;
     return MFC_OK;
   }
   return fail(MFC_ERR_INVALID, "no such tile variant for this configuration");

@@ -26,6 +26,7 @@ struct StageEntry {
   cudaError_t (*launch)(const DevParams& P, const UniformCoef& U, const double* qin, const double* qbase,
                         double* qout, double dt, int kind, cudaStream_t st);
   bool visc = false;  // compiled with the viscous terms
+  bool tma = false;   // interior tiles staged by a TMA bulk tensor copy
 };
 
 // Launches a stage kernel with programmatic stream serialization, so that
@@ -47,40 +48,78 @@ cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, si
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
-// MINB > 1 selects the register-capped kernel (stage_kernel_mb).
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool VISC>
+// MINB > 1 selects the register-capped kernel (stage_kernel_mb); TMA the
+// kernel that stages interior tiles with a bulk tensor copy.
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool VISC, bool TMA = false>
 constexpr auto stage_func() {
   static_assert(MINB == 1 || !VISC, "register-capped variants are inviscid");
-  if constexpr (MINB > 1) return &stage_kernel_mb<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>;
+  static_assert(!TMA || (ND == 2 && !VISC), "TMA staging is compiled for the inviscid 2-D kernel");
+  if constexpr (TMA && MINB > 1) return &stage_kernel_tma_mb<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>;
+  else if constexpr (TMA) return &stage_kernel_tma<ND, NF, WO, RT, TX, TY, NT, GATE>;
+  else if constexpr (MINB > 1) return &stage_kernel_mb<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>;
   else return &stage_kernel<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>;
 }
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false>
-cudaError_t stage_prepare() {
-  return cudaFuncSetAttribute(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>(),
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>());
+// Dynamic shared memory of a launch: without the coefficient records on a
+// uniform grid, and at least the TMA staging area of a TMA kernel.
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool VISC, bool TMA>
+constexpr size_t stage_launch_smem(bool shared_coef) {
+  size_t s = shared_coef ? stage_smem_bytes_shared_coef<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>()
+                         : stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>();
+  if constexpr (TMA) {
+    const size_t t = stage_tma_bytes<ND, NF, WO, RT, TX, TY>();
+    s = s > t ? s : t;
+  }
+  return s;
 }
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false,
+          bool TMA = false>
+cudaError_t stage_prepare() {
+  return cudaFuncSetAttribute(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA>(),
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)stage_launch_smem<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, TMA>(false));
+}
+
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false,
+          bool TMA = false>
 cudaError_t stage_launch(const DevParams& P, const UniformCoef& U, const double* qin, const double* qbase,
                          double* qout, double dt, int kind, cudaStream_t st) {
   const dim3 grid((unsigned)((P.n[0] + TX - 1) / TX), ND > 1 ? (unsigned)((P.n[1] + TY - 1) / TY) : 1u, 1u);
   // a uniform grid stages no coefficient records: launch without their share
   const bool shared_coef = U.on[0] && (ND < 2 || U.on[1]);
-  const size_t smem = shared_coef ? stage_smem_bytes_shared_coef<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>()
-                                  : stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>();
-  return launch_dependent(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>(), grid, dim3(NT), smem, st, P, U,
-                          qin, qbase, qout, dt, kind);
+  const size_t smem = stage_launch_smem<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, TMA>(shared_coef);
+  if constexpr (TMA) {
+    // the map of this launch's input register; without one (a layout the
+    // copy engine does not take) every tile takes the plain loads
+    using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
+    TileMap T{};
+    encode_tile_map(T, qin, P.n[0], P.n[1], Sh::S, P.sy, P.sv, TmaBox<TX, Sh::H>::kWidth, Sh::LY);
+    return launch_dependent(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA>(), grid, dim3(NT), smem, st,
+                            P, U, T, qin, qbase, qout, dt, kind);
+  } else {
+    return launch_dependent(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA>(), grid, dim3(NT), smem, st,
+                            P, U, qin, qbase, qout, dt, kind);
+  }
 }
 
 // prec of a registry entry: 0 FP64, 1 split, 2 split with the learned gate
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false,
+          bool TMA = false>
 StageEntry stage_entry() {
-  return StageEntry{ND, NF, WO, sizeof(RT) == 8 ? 0 : (GATE ? 2 : 1), TX, TY, NT,
-                    stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>(), 1,
-                    &stage_prepare<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>,
-                    &stage_launch<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC>, VISC};
+  return StageEntry{ND,
+                    NF,
+                    WO,
+                    sizeof(RT) == 8 ? 0 : (GATE ? 2 : 1),
+                    TX,
+                    TY,
+                    NT,
+                    stage_launch_smem<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, TMA>(false),
+                    1,
+                    &stage_prepare<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA>,
+                    &stage_launch<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA>,
+                    VISC,
+                    TMA};
 }
 
 // 3-D: three directional sweeps per stage (mfc_sweep.cuh).  The x sweep uses

@@ -19,6 +19,7 @@
 
 #include "mfc_device.cuh"
 #include "mfc_gate.cuh"
+#include "mfc_tma.cuh"
 
 namespace mfc {
 
@@ -127,11 +128,12 @@ struct GateShape {
 // stage_smem_bytes() (or stage_smem_bytes_shared_coef() when U covers every
 // direction).
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, bool VISC = false,
-          class UC = UniformCoef>
+          class UC = UniformCoef, bool TMA = false>
 __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __restrict__ qin,
                                            const double* __restrict__ qbase, double* __restrict__ qout,
                                            const double dt, const int kind, const int x0, const int y0,
-                                           unsigned char* smem_raw, const UC* U = nullptr) {
+                                           unsigned char* smem_raw, const UC* U = nullptr,
+                                           const TileMap* T = nullptr) {
   static_assert(!GATE || (sizeof(RT) == 4 && WO == 5), "the learned gate runs on the split-precision WENO5 path");
   static_assert(!(GATE && VISC), "the gated kernel is inviscid");
   using Sh = StageShape<ND, NF, WO, RT, TX, TY, VISC>;
@@ -209,50 +211,8 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       }
     }
   }
-  griddep_wait();  // the state below is the previous stage's output
-  for (int c = tid; c < LX * LY; c += NT) {
-    const int lx = c % LX, ly = c / LX;
-    const bool hx = lx < H || lx >= H + TX;
-    const bool hy = (ND > 1) && (ly < H || ly >= H + TY);
-    // corners are never read, except the four diagonal neighbours of the
-    // tile that the viscous cross derivatives use
-    if (hx && hy && !(VISC && (lx == H - 1 || lx == H + TX) && (ly == H - 1 || ly == H + TY))) continue;
-    bool fx = false, fy = false;
-    const int rx = x0 - H + lx, ry = (ND > 1) ? y0 - H + ly : 0;
-    // processor boundaries: ghost cells come from the neighbour's halo buffer
-    const int px = rx < 0 ? (P.bc_beg[0] >= 0 ? 0 : -1) : (rx >= nx && P.bc_end[0] >= 0 ? 1 : -1);
-    const int py = (ND > 1) ? (ry < 0 ? (P.bc_beg[1] >= 0 ? 0 : -1) : (ry >= ny && P.bc_end[1] >= 0 ? 1 : -1)) : -1;
-    const double* src;
-    int64_t vs = P.sv;
-    // cells of partial edge tiles beyond the first H ghosts are never stored:
-    // their depth is clamped.  y strips are nx + 2 wide (the x ghost cells
-    // -1 and nx of the neighbour's rows come first and last).
-    if (px >= 0 && py >= 0) {
-      // between two processor boundaries (the viscous corner cells): the
-      // diagonal neighbour's cell, forwarded by the y neighbour
-      const int d = min(py == 0 ? -1 - ry : ry - ny, H - 1);
-      src = P.halo[2 + py] + (int64_t)d * (nx + 2) + (px == 0 ? 0 : nx + 1);
-      vs = (int64_t)H * (nx + 2);
-    } else if (px >= 0) {
-      const int d = min(px == 0 ? -1 - rx : rx - nx, H - 1);
-      const int yy = (ND > 1) ? map_cell(ry, ny, P.bc_beg[1], P.bc_end[1], &fy) : 0;
-      src = P.halo[px] + (int64_t)yy * H + d;
-      vs = (int64_t)ny * H;
-    } else if (py >= 0) {
-      const int d = min(py == 0 ? -1 - ry : ry - ny, H - 1);
-      const int xx = map_cell(rx, nx, P.bc_beg[0], P.bc_end[0], &fx);
-      src = P.halo[2 + py] + (int64_t)d * (nx + 2) + xx + 1;
-      vs = (int64_t)H * (nx + 2);
-    } else {
-      const int gx = map_cell(rx, nx, P.bc_beg[0], P.bc_end[0], &fx);
-      const int gy = (ND > 1) ? map_cell(ry, ny, P.bc_beg[1], P.bc_end[1], &fy) : 0;
-      src = qin + gy * P.sy + gx;
-    }
-    double q[S];
-#pragma unroll
-    for (int v = 0; v < S; ++v) q[v] = __ldg(src + v * vs);
-    if (fx) q[Q::MOM] = -q[Q::MOM];
-    if (ND > 1 && fy) q[Q::MOM + 1] = -q[Q::MOM + 1];
+  // one cell of the tile: BCs already applied, cons -> prim into the tile
+  auto store_prim = [&](double (&q)[S], const int ly, const int lx) {
     if constexpr (kSplit) {
       float pr[S];
       cons_to_prim_split<ND, NF>(q, P, pr);
@@ -263,6 +223,102 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       cons_to_prim<ND, NF>(q, P);
 #pragma unroll
       for (int v = 0; v < S; ++v) sq[qi(v, ly, lx)] = RT(q[v]);
+    }
+  };
+  // corners are never read, except the four diagonal neighbours of the tile
+  // that the viscous cross derivatives use
+  auto unused_corner = [](const int lx, const int ly) {
+    const bool hx = lx < H || lx >= H + TX;
+    const bool hy = (ND > 1) && (ly < H || ly >= H + TY);
+    return hx && hy && !(VISC && (lx == H - 1 || lx == H + TX) && (ly == H - 1 || ly == H + TY));
+  };
+
+  // TMA staging: a tile whose halo lies inside the domain (no boundary
+  // condition, no processor halo) arrives in one bulk tensor copy of all
+  // variables into the WENO and flux arrays, which are free until phase 2.
+  // Split precision uses it only on a uniform grid, where no coefficient
+  // records share that space.
+  bool use_tma = false;
+  unsigned char* stg = nullptr;
+  uint32_t bar = 0;
+  using Box = TmaBox<TX, H>;
+  constexpr uint32_t kStageBytes = uint32_t(Box::kWidth) * LY * S * 8;
+  if constexpr (TMA && ND == 2 && !VISC) {
+    use_tma = T != nullptr && T->on && x0 >= H && x0 + TX + H <= nx && y0 >= H && y0 + TY + H <= ny &&
+              (!kSplit || (ux && uy));
+    if (use_tma) {
+      const uintptr_t a = reinterpret_cast<uintptr_t>(smem_raw + Sh::OW * sizeof(RT));
+      stg = reinterpret_cast<unsigned char*>((a + 127) & ~uintptr_t(127));
+      bar = smem_addr(stg + kStageBytes);
+      if (tid == 0) mbar_init(bar, 1);
+    }
+  }
+  griddep_wait();  // the state below is the previous stage's output
+  if (use_tma) {
+    volatile int* landed = reinterpret_cast<volatile int*>(stg + kStageBytes + 8);
+    if (tid == 0) {
+      mbar_arrive_expect_tx(bar, kStageBytes);
+      tma_load_3d(smem_addr(stg), &T->map, x0 - Box::kLead, y0 - H, 0, bar);
+      const bool ok = mbar_wait_bounded(bar, 0, 1000000000ull);       // 1 s
+      if (!ok) (void)mbar_wait_bounded(bar, 0, 1000000000ull);         // the copy may still be in flight
+      *landed = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (*landed == 0) {
+      if (tid == 0 && P.status) atomicOr(P.status, MFC_FLAG_TIMEOUT);
+      return;
+    }
+    (void)mbar_try_wait(bar, 0);  // completed: each thread acquires the copy's writes
+    const double* sd = reinterpret_cast<const double*>(stg);
+    for (int c = tid; c < LX * LY; c += NT) {
+      const int lx = c % LX, ly = c / LX;
+      if (unused_corner(lx, ly)) continue;
+      double q[S];
+#pragma unroll
+      for (int v = 0; v < S; ++v) q[v] = sd[(v * LY + ly) * Box::kWidth + lx + (Box::kLead - H)];
+      store_prim(q, ly, lx);
+    }
+  } else {  // plain loads, with the boundary conditions and processor halos
+    for (int c = tid; c < LX * LY; c += NT) {
+      const int lx = c % LX, ly = c / LX;
+      if (unused_corner(lx, ly)) continue;
+      bool fx = false, fy = false;
+      const int rx = x0 - H + lx, ry = (ND > 1) ? y0 - H + ly : 0;
+      // processor boundaries: ghost cells come from the neighbour's halo buffer
+      const int px = rx < 0 ? (P.bc_beg[0] >= 0 ? 0 : -1) : (rx >= nx && P.bc_end[0] >= 0 ? 1 : -1);
+      const int py = (ND > 1) ? (ry < 0 ? (P.bc_beg[1] >= 0 ? 0 : -1) : (ry >= ny && P.bc_end[1] >= 0 ? 1 : -1)) : -1;
+      const double* src;
+      int64_t vs = P.sv;
+      // cells of partial edge tiles beyond the first H ghosts are never stored:
+      // their depth is clamped.  y strips are nx + 2 wide (the x ghost cells
+      // -1 and nx of the neighbour's rows come first and last).
+      if (px >= 0 && py >= 0) {
+        // between two processor boundaries (the viscous corner cells): the
+        // diagonal neighbour's cell, forwarded by the y neighbour
+        const int d = min(py == 0 ? -1 - ry : ry - ny, H - 1);
+        src = P.halo[2 + py] + (int64_t)d * (nx + 2) + (px == 0 ? 0 : nx + 1);
+        vs = (int64_t)H * (nx + 2);
+      } else if (px >= 0) {
+        const int d = min(px == 0 ? -1 - rx : rx - nx, H - 1);
+        const int yy = (ND > 1) ? map_cell(ry, ny, P.bc_beg[1], P.bc_end[1], &fy) : 0;
+        src = P.halo[px] + (int64_t)yy * H + d;
+        vs = (int64_t)ny * H;
+      } else if (py >= 0) {
+        const int d = min(py == 0 ? -1 - ry : ry - ny, H - 1);
+        const int xx = map_cell(rx, nx, P.bc_beg[0], P.bc_end[0], &fx);
+        src = P.halo[2 + py] + (int64_t)d * (nx + 2) + xx + 1;
+        vs = (int64_t)H * (nx + 2);
+      } else {
+        const int gx = map_cell(rx, nx, P.bc_beg[0], P.bc_end[0], &fx);
+        const int gy = (ND > 1) ? map_cell(ry, ny, P.bc_beg[1], P.bc_end[1], &fy) : 0;
+        src = qin + gy * P.sy + gx;
+      }
+      double q[S];
+#pragma unroll
+      for (int v = 0; v < S; ++v) q[v] = __ldg(src + v * vs);
+      if (fx) q[Q::MOM] = -q[Q::MOM];
+      if (ND > 1 && fy) q[Q::MOM + 1] = -q[Q::MOM + 1];
+      store_prim(q, ly, lx);
     }
   }
   __syncthreads();
@@ -685,6 +741,39 @@ __global__ void __launch_bounds__(NT, MINB) stage_kernel_mb(const DevParams P, c
   extern __shared__ __align__(16) unsigned char smem_raw[];
   stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
                                                (ND > 1) ? blockIdx.y * TY : 0, smem_raw, &U);
+}
+
+// The kernel with TMA staging of interior tiles (2-D, inviscid); T maps the
+// stage input qin.  MINB > 1 caps the registers as stage_kernel_mb does.
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE>
+__global__ void __launch_bounds__(NT) stage_kernel_tma(const DevParams P, const __grid_constant__ UniformCoef U,
+                                                       const __grid_constant__ TileMap T,
+                                                       const double* __restrict__ qin,
+                                                       const double* __restrict__ qbase, double* __restrict__ qout,
+                                                       const double dt, const int kind) {
+  extern __shared__ __align__(128) unsigned char smem_tma[];
+  stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE, false, UniformCoef, true>(
+      P, qin, qbase, qout, dt, kind, blockIdx.x * TX, (ND > 1) ? blockIdx.y * TY : 0, smem_tma, &U, &T);
+}
+
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB>
+__global__ void __launch_bounds__(NT, MINB) stage_kernel_tma_mb(const DevParams P, const __grid_constant__ UniformCoef U,
+                                                                const __grid_constant__ TileMap T,
+                                                                const double* __restrict__ qin,
+                                                                const double* __restrict__ qbase,
+                                                                double* __restrict__ qout, const double dt,
+                                                                const int kind) {
+  extern __shared__ __align__(128) unsigned char smem_tma[];
+  stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE, false, UniformCoef, true>(
+      P, qin, qbase, qout, dt, kind, blockIdx.x * TX, (ND > 1) ? blockIdx.y * TY : 0, smem_tma, &U, &T);
+}
+
+// Shared memory a TMA-staged tile needs beyond the primitive tile: the box
+// of all variables (128-byte aligned), its mbarrier and a flag.
+template <int ND, int NF, int WO, class RT, int TX, int TY>
+constexpr size_t stage_tma_bytes() {
+  using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
+  return sizeof(RT) * size_t(Sh::OW) + 128 + size_t(TmaBox<TX, Sh::H>::kWidth) * Sh::LY * Sh::S * 8 + 16;
 }
 
 // Shared memory of one stage-kernel block (with the gate's share when on).

@@ -201,6 +201,12 @@ class Simulation:
                                                  ctypes.byref(nt)))
         return tx.value, ty.value, nt.value
 
+    def variant_features(self, variant: int) -> int:
+        """MFC_VARIANT_* bits of a tile variant (mfc_gpu_variant_features)."""
+        f = ctypes.c_uint32(0)
+        _lib.check(self.L.mfc_gpu_variant_features(self._h, int(variant), ctypes.byref(f)))
+        return f.value
+
     def set_monitor(self, on: bool = True) -> None:
         """Fused ICFL monitor (the reference's run-time information)."""
         _lib.check(self.L.mfc_gpu_set_monitor(self._h, int(bool(on))))

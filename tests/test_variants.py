@@ -1,9 +1,9 @@
 """Every compiled tile variant the autotuner can pick gives the same bits: the
 per-cell arithmetic does not depend on the tile shape, so a tuned run must
 equal the default one (and, for FP64, the CPU oracle) exactly.  Ragged grids
-exercise partial edge tiles.  (The FP32 units are compiled with FMA
-contraction, so a variant whose register cap made the compiler fuse
-differently would fail here; one such 16x8 variant was dropped.)"""
+exercise partial edge tiles.  (Every unit is compiled without FMA
+contraction and the FP32 path writes its FMAs explicitly, so no register
+cap can make two variants fuse differently.)"""
 import numpy as np
 import pytest
 
@@ -76,3 +76,44 @@ def test_uniform_coefficient_record_matches_per_cell_records(kind):
             sim.run(0, 6)
             outs.append(sim.download())
     assert np.array_equal(outs[0].view(np.uint64), outs[1].view(np.uint64))
+
+
+@pytest.mark.parametrize("prec", ["fp64", "split", "gated"])
+@pytest.mark.parametrize("uniform", [True, False], ids=["uniform", "records"])
+def test_tma_staged_variants_match_plain_loads(prec, uniform):
+    """Variants that stage interior tiles with one TMA bulk tensor copy give
+    the bits of the first plain-load variant, no bounded wait gives up, and
+    split precision with per-cell coefficient records (whose shared memory
+    the staging area would overlap) takes the plain loads."""
+    from microfc_gb300 import Simulation
+    from microfc_gb300._lib import MFC_FLAG_TIMEOUT, MFC_VARIANT_TMA, MfcError
+    if prec == "fp64" and not uniform:
+        pytest.skip("the FP64 kernel stages no coefficient records")
+    c = cases.shock_droplet_2d(nx=160, ny=96, steps=4, precision=prec)
+    params = gate.load() if prec == "gated" else None
+    x, y, z, q = preprocess.generate(c)
+    ref, staged_out = None, []
+    v = 0
+    while True:
+        with Simulation(c, x, y, z, q_cons=q) as sim:
+            if params is not None:
+                sim.set_gate(params)
+            if not uniform:
+                sim.set_uniform_coefficients(False)
+            try:
+                shape = sim.select_variant(v)
+            except MfcError:
+                break
+            staged = bool(sim.variant_features(v) & MFC_VARIANT_TMA)
+            if staged or ref is None:
+                sim.run(0, 4)
+                out = sim.download()
+                assert not sim.status() & MFC_FLAG_TIMEOUT
+                if staged:
+                    staged_out.append((shape, out))
+                else:
+                    ref = out
+        v += 1
+    assert ref is not None and staged_out
+    for shape, out in staged_out:
+        assert np.array_equal(out.view(np.uint64), ref.view(np.uint64)), shape
