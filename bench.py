@@ -242,11 +242,14 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
     for prec3, n3 in (("split", 10), ("fp64", 2)):
         with Simulation(c3.replace(precision=prec3), ic="device") as s:
             v3[prec3], _ = s.tune(2)
+            s.select_variant(v3[prec3])
+            if prec3 == "split":
+                tma3 = bool(s.variant_features(v3[prec3]) & _lib.MFC_VARIANT_TMA)
             st = torch.cuda.ExternalStream(s.stream)
             r3[prec3] = c3.cells * n3 / _time_steps(s, st, flush, n3, 2, c3.dt)
     out["split_3d"] = {"workload": "3-D air/helium shock-bubble 256^3, 2 fluids, WENO5-JS + HLLC + TVD-RK3",
                        "value": r3["split"], "unit": "cell-updates/s", "steps": 10, "tile_variant": v3["split"],
-                       "plain_fp64": r3["fp64"], "vs_plain_fp64": r3["split"] / r3["fp64"]}
+                       "tma_staging": tma3, "plain_fp64": r3["fp64"], "vs_plain_fp64": r3["split"] / r3["fp64"]}
     # config 5: 64 cases, nx in {128,256,384,512}, ny = nx/2, seed 0
     prec = "gated" if params is not None else "split"
     cl = random_droplet_cases(count=64, seed=0, steps=500, precision=prec)

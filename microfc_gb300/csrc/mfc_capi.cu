@@ -64,41 +64,79 @@ const StageEntry* find_stage(int nd, int nf, int wo, int prec, bool visc) {
 
 int report_error(int code, const std::string& msg) { return fail(code, msg); }
 
-bool encode_tile_map(TileMap& t, const double* base, int nx, int ny, int S, int64_t sy, int64_t sv, int box_w,
-                     int box_h) {
-  std::memset(&t, 0, sizeof(t));
-  // the driver's encoder, looked up through the runtime (no link against libcuda)
-  using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-  static const Encode encode = [] {
+namespace {
+// the driver's encoder, looked up through the runtime (no link against libcuda)
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiled tiled_encoder() {
+  static const EncodeTiled encode = [] {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q{};
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
             cudaSuccess ||
         q != cudaDriverEntryPointSuccess)
-      return static_cast<Encode>(nullptr);
-    return reinterpret_cast<Encode>(fn);
+      return static_cast<EncodeTiled>(nullptr);
+    return reinterpret_cast<EncodeTiled>(fn);
   }();
-  if (!encode || !base) return false;
-  // TMA rules: 16-byte aligned base and strides, boxes of at most 256 cells
-  // per dimension whose rows are a multiple of 16 bytes
-  if (reinterpret_cast<uintptr_t>(base) % 16 != 0 || (sy * 8) % 16 != 0 || (sv * 8) % 16 != 0) return false;
-  if (sy < nx || sv < sy * ny || sv * 8 >= (int64_t(1) << 40)) return false;
-  if (box_w < 1 || box_w > 256 || box_h < 1 || box_h > 256 || S > 256 || (box_w * 8) % 16 != 0) return false;
-  const cuuint64_t dims[3] = {cuuint64_t(nx), cuuint64_t(ny), cuuint64_t(S)};
-  const cuuint64_t strides[2] = {cuuint64_t(sy) * 8, cuuint64_t(sv) * 8};
-  const cuuint32_t box[3] = {cuuint32_t(box_w), cuuint32_t(box_h), cuuint32_t(S)};
-  const cuuint32_t unit[3] = {1, 1, 1};
-  const CUresult r = encode(&t.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double*>(base), dims, strides, box,
-                            unit, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return encode;
+}
+
+// FP64 tensor of `rank` dimensions (x first, the variable last); strides in
+// elements for dimensions 1.. .  TMA rules: 16-byte aligned base and
+// strides, boxes of at most 256 cells per dimension whose rows are a
+// multiple of 16 bytes.
+bool encode_fp64(TileMap& t, const double* base, int rank, const int64_t* dims, const int64_t* strides,
+                 const int* box) {
+  std::memset(&t, 0, sizeof(t));
+  const EncodeTiled encode = tiled_encoder();
+  if (!encode || !base || reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
+  cuuint64_t gd[5], gs[4];
+  cuuint32_t bd[5], unit[5];
+  for (int d = 0; d < rank; ++d) {
+    if (dims[d] < 1 || box[d] < 1 || box[d] > 256) return false;
+    gd[d] = cuuint64_t(dims[d]);
+    bd[d] = cuuint32_t(box[d]);
+    unit[d] = 1;
+    if (d > 0) {
+      if ((strides[d - 1] * 8) % 16 != 0 || strides[d - 1] * 8 >= (int64_t(1) << 40)) return false;
+      gs[d - 1] = cuuint64_t(strides[d - 1]) * 8;
+    }
+  }
+  if ((box[0] * 8) % 16 != 0) return false;
+  const CUresult r =
+      encode(&t.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, cuuint32_t(rank), const_cast<double*>(base), gd, gs, bd, unit,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     std::memset(&t, 0, sizeof(t));
     return false;
   }
   t.on = 1;
   return true;
+}
+}  // namespace
+
+bool encode_tile_map(TileMap& t, const double* base, int nx, int ny, int S, int64_t sy, int64_t sv, int box_w,
+                     int box_h) {
+  if (sy < nx || sv < sy * ny) {
+    std::memset(&t, 0, sizeof(t));
+    return false;
+  }
+  const int64_t dims[3] = {nx, ny, S}, strides[2] = {sy, sv};
+  const int box[3] = {box_w, box_h, S};
+  return encode_fp64(t, base, 3, dims, strides, box);
+}
+
+bool encode_tile_map_3d(TileMap& t, const double* base, int nx, int ny, int nz, int S, int64_t sy, int64_t sz,
+                        int64_t sv, int bx, int by, int bz) {
+  if (sy < nx || sz < sy * ny || sv < sz * nz) {
+    std::memset(&t, 0, sizeof(t));
+    return false;
+  }
+  const int64_t dims[4] = {nx, ny, nz, S}, strides[3] = {sy, sz, sv};
+  const int box[4] = {bx, by, bz, S};
+  return encode_fp64(t, base, 4, dims, strides, box);
 }
 }  // namespace mfc
 

@@ -124,21 +124,22 @@ StageEntry stage_entry() {
 
 // 3-D: three directional sweeps per stage (mfc_sweep.cuh).  The x sweep uses
 // TA0 x TB0 x TC0 tiles (x along the sweep); the y and z sweeps use
-// TA1 x TB1 x 1 tiles with x across the pencils.
-template <int NF, int WO, class RT, int TA0, int TB0, int TC0, int TA1, int TB1, int NT>
+// TA1 x TB1 x 1 tiles with x across the pencils.  TMA: tiles whose sweep
+// halo lies inside the domain arrive by one bulk tensor copy.
+template <int NF, int WO, class RT, int TA0, int TB0, int TC0, int TA1, int TB1, int NT, bool TMA = false>
 struct Sweep3D {
   template <int DIR>
   using K = std::conditional_t<DIR == 0, SweepShape<NF, WO, RT, 0, TA0, TB0, TC0>,
                                SweepShape<NF, WO, RT, DIR, TA1, TB1, 1>>;
+  template <int DIR>
+  static constexpr auto func() {
+    if constexpr (DIR == 0) return &sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT, TMA>;
+    else return &sweep_kernel<NF, WO, RT, DIR, TA1, TB1, 1, NT, TMA>;
+  }
 
   template <int DIR>
   static cudaError_t prep() {
-    if constexpr (DIR == 0)
-      return cudaFuncSetAttribute(sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K<0>::kSmemBytes);
-    else
-      return cudaFuncSetAttribute(sweep_kernel<NF, WO, RT, DIR, TA1, TB1, 1, NT>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K<DIR>::kSmemBytes);
+    return cudaFuncSetAttribute(func<DIR>(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K<DIR>::kSmemBytes);
   }
   static cudaError_t prepare() {
     cudaError_t e = prep<0>();
@@ -146,24 +147,35 @@ struct Sweep3D {
     if (e == cudaSuccess) e = prep<2>();
     return e;
   }
+  // the map of the stage input for the sweep's box (none: plain loads)
+  template <int DIR>
+  static TileMap tile_map(const DevParams& P, const double* qin) {
+    TileMap T{};
+    if constexpr (TMA && K<DIR>::kTmaFits)
+      encode_tile_map_3d(T, qin, P.n[0], P.n[1], P.n[2], K<DIR>::S, P.sy, P.sz, P.sv, K<DIR>::BX, K<DIR>::BY,
+                         K<DIR>::BZ);
+    return T;
+  }
   static cudaError_t launch(const DevParams& P, const UniformCoef& U, const double* qin, const double* qbase,
                             double* qout, double dt, int kind, cudaStream_t st) {
     const unsigned nx = P.n[0], ny = P.n[1], nz = P.n[2];
     const dim3 g0((nx + TA0 - 1) / TA0, (ny + TB0 - 1) / TB0, (nz + TC0 - 1) / TC0);
     const dim3 g1((nx + TB1 - 1) / TB1, (ny + TA1 - 1) / TA1, nz);
     const dim3 g2((nx + TB1 - 1) / TB1, (nz + TA1 - 1) / TA1, ny);
-    cudaError_t e = launch_dependent(&sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT>, g0, dim3(NT), K<0>::kSmemBytes,
-                                     st, P, U, qin, qbase, qout, dt, kind);
+    const TileMap T0 = tile_map<0>(P, qin), T1 = tile_map<1>(P, qin), T2 = tile_map<2>(P, qin);
+    cudaError_t e =
+        launch_dependent(func<0>(), g0, dim3(NT), K<0>::kSmemBytes, st, P, U, T0, qin, qbase, qout, dt, kind);
     if (e == cudaSuccess)
-      e = launch_dependent(&sweep_kernel<NF, WO, RT, 1, TA1, TB1, 1, NT>, g1, dim3(NT), K<1>::kSmemBytes, st, P, U, qin,
-                           qbase, qout, dt, kind);
+      e = launch_dependent(func<1>(), g1, dim3(NT), K<1>::kSmemBytes, st, P, U, T1, qin, qbase, qout, dt, kind);
     if (e == cudaSuccess)
-      e = launch_dependent(&sweep_kernel<NF, WO, RT, 2, TA1, TB1, 1, NT>, g2, dim3(NT), K<2>::kSmemBytes, st, P, U, qin,
-                           qbase, qout, dt, kind);
+      e = launch_dependent(func<2>(), g2, dim3(NT), K<2>::kSmemBytes, st, P, U, T2, qin, qbase, qout, dt, kind);
     return e;
   }
   static StageEntry entry() {
-    return StageEntry{3, NF, WO, sizeof(RT) == 8 ? 0 : 1, TA0, TB1, NT, K<1>::kSmemBytes, 3, &prepare, &launch};
+    static_assert(!TMA || (K<0>::kTmaFits && K<1>::kTmaFits && K<2>::kTmaFits),
+                  "the TMA box of every sweep must fit its WENO and flux arrays");
+    return StageEntry{3, NF, WO, sizeof(RT) == 8 ? 0 : 1, TA0, TB1, NT, K<1>::kSmemBytes, 3, &prepare, &launch,
+                      false, TMA};
   }
 };
 

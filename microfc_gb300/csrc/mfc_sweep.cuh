@@ -36,6 +36,14 @@ struct SweepShape {
   static constexpr int align16(int n) { return (n * int(sizeof(RT)) + 15) / 16 * 16 / int(sizeof(RT)); }
   static constexpr int OC = align16(NQ + 2 * NW + NFL);
   static constexpr size_t kSmemBytes = sizeof(RT) * (size_t(OC) + size_t(NCOEF));
+  // TMA staging box of the tile (x, y, z extents; all S variables), in the
+  // WENO and flux arrays: DIR 0 starts x on an even cell
+  static constexpr int BX = DIR == 0 ? TmaBox<TA, H>::kWidth : TB;
+  static constexpr int BY = DIR == 0 ? TB : (DIR == 1 ? LA : TC);
+  static constexpr int BZ = DIR == 0 ? TC : (DIR == 1 ? TC : LA);
+  static constexpr uint32_t kStageBytes = uint32_t(BX) * BY * BZ * S * 8;
+  static constexpr bool kTmaFits = (BX * 8) % 16 == 0 && BX <= 256 && BY <= 256 && BZ <= 256 &&
+                                   size_t(kStageBytes) + 128 + 16 <= sizeof(RT) * size_t(OC - NQ);
 };
 
 // Pencil p of a block and position a along the sweep -> global (x, y, z).
@@ -48,10 +56,13 @@ __device__ __forceinline__ void sweep_coords(int a, int b, int c, int& x, int& y
   else { x = b; y = c; z = a; }
 }
 
-template <int NF, int WO, class RT, int DIR, int TA, int TB, int TC, int NT>
+// TMA: a tile whose sweep halo lies inside the domain arrives by one bulk
+// tensor copy (T maps the stage input qin; T.on = 0: plain loads only).
+template <int NF, int WO, class RT, int DIR, int TA, int TB, int TC, int NT, bool TMA = false>
 __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __grid_constant__ UniformCoef U,
-                                                   const double* __restrict__ qin, const double* __restrict__ qbase,
-                                                   double* __restrict__ qout, const double dt, const int kind) {
+                                                   const __grid_constant__ TileMap T, const double* __restrict__ qin,
+                                                   const double* __restrict__ qbase, double* __restrict__ qout,
+                                                   const double dt, const int kind) {
   using Sh = SweepShape<NF, WO, RT, DIR, TA, TB, TC>;
   using Q = Eqs<3, NF>;
   constexpr int S = Sh::S, H = Sh::H, LA = Sh::LA, NP = Sh::NP;
@@ -115,41 +126,8 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
               : 0.f;
     }
   }
-  griddep_wait();  // the state (and the partial RHS) below are earlier kernels' output
-  // thread order: the a index fastest for the x sweep, the pencil b index
-  // fastest otherwise, so that global loads are coalesced along x
-  for (int it = tid; it < NP * LA; it += NT) {
-    int la, pb, pc;
-    if (DIR == 0) { la = it % LA; pb = (it / LA) % TB; pc = it / (LA * TB); }
-    else { pb = it % TB; la = (it / TB) % LA; pc = it / (TB * LA); }
-    bool fa = false, dummy = false;
-    const int ra = a0 - H + la;
-    // processor boundary along the sweep: the ghost cell comes from the
-    // neighbour's halo buffer (x: [S][nz][ny][H], y: [S][nz][H][nx],
-    // z: [S][H][ny][nx]; depth 0 next to the boundary)
-    const int side = ra < 0 ? (P.bc_beg[OA] >= 0 ? 0 : -1) : (ra >= na && P.bc_end[OA] >= 0 ? 1 : -1);
-    const int gb = map_cell(b0 + pb, nb, P.bc_beg[OB], P.bc_end[OB], &dummy);
-    const int gc = map_cell(c0 + pc, nc, P.bc_beg[OC], P.bc_end[OC], &dummy);
-    const double* src;
-    int64_t vs = P.sv;
-    if (side >= 0) {
-      const int d = min(side == 0 ? -1 - ra : ra - na, H - 1);  // deeper cells of partial tiles are never stored
-      int x, y, z;
-      sweep_coords<DIR>(d, gb, gc, x, y, z);
-      const int nx = P.n[0], ny = P.n[1], nz = P.n[2];
-      const double* h = P.halo[2 * DIR + side];
-      if (DIR == 0) { src = h + ((int64_t)z * ny + y) * H + d; vs = (int64_t)nz * ny * H; }
-      else if (DIR == 1) { src = h + ((int64_t)z * H + d) * nx + x; vs = (int64_t)nz * H * nx; }
-      else { src = h + ((int64_t)d * ny + y) * nx + x; vs = (int64_t)H * ny * nx; }
-    } else {
-      const int ga = map_cell(ra, na, P.bc_beg[OA], P.bc_end[OA], &fa);
-      src = qin + ga * st[OA] + gb * st[OB] + gc * st[OC];
-    }
-    double q[S];
-#pragma unroll
-    for (int v = 0; v < S; ++v) q[v] = __ldg(src + v * vs);
-    if (fa) q[Q::MOM + DIR] = -q[Q::MOM + DIR];
-    const int p = pc * TB + pb;
+  // one cell: BCs applied, cons -> prim into the tile
+  auto store_prim = [&](double (&q)[S], const int p, const int la) {
     if constexpr (kSplit) {
       float pr[S];
       cons_to_prim_split<3, NF>(q, P, pr);
@@ -159,6 +137,88 @@ __global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __gr
       cons_to_prim<3, NF>(q, P);
 #pragma unroll
       for (int v = 0; v < S; ++v) sq[qi(v, p, la)] = RT(q[v]);
+    }
+  };
+  bool use_tma = false;
+  unsigned char* stg = nullptr;
+  uint32_t bar = 0;
+  if constexpr (TMA && Sh::kTmaFits) {
+    use_tma = T.on && a0 >= H && a0 + TA + H <= na && b0 + TB <= nb && c0 + TC <= nc;
+    if (use_tma) {
+      const uintptr_t a = reinterpret_cast<uintptr_t>(wl);
+      stg = reinterpret_cast<unsigned char*>((a + 127) & ~uintptr_t(127));
+      bar = smem_addr(stg + Sh::kStageBytes);
+      if (tid == 0) mbar_init(bar, 1);
+    }
+  }
+  griddep_wait();  // the state (and the partial RHS) below are earlier kernels' output
+  if (use_tma) {
+    volatile int* landed = reinterpret_cast<volatile int*>(stg + Sh::kStageBytes + 8);
+    if (tid == 0) {
+      mbar_arrive_expect_tx(bar, Sh::kStageBytes);
+      if (DIR == 0) tma_load_4d(smem_addr(stg), &T.map, a0 - TmaBox<TA, H>::kLead, b0, c0, 0, bar);
+      else if (DIR == 1) tma_load_4d(smem_addr(stg), &T.map, b0, a0 - H, c0, 0, bar);
+      else tma_load_4d(smem_addr(stg), &T.map, b0, c0, a0 - H, 0, bar);
+      const bool ok = mbar_wait_bounded(bar, 0, 1000000000ull);  // 1 s
+      if (!ok) (void)mbar_wait_bounded(bar, 0, 1000000000ull);    // the copy may still be in flight
+      *landed = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (*landed == 0) {
+      if (tid == 0 && P.status) atomicOr(P.status, MFC_FLAG_TIMEOUT);
+      return;
+    }
+    (void)mbar_try_wait(bar, 0);  // completed: each thread acquires the copy's writes
+    const double* sd = reinterpret_cast<const double*>(stg);
+    for (int it = tid; it < NP * LA; it += NT) {
+      int la, pb, pc;
+      if (DIR == 0) { la = it % LA; pb = (it / LA) % TB; pc = it / (LA * TB); }
+      else { pb = it % TB; la = (it / TB) % LA; pc = it / (TB * LA); }
+      // box element (x, y, z) of variable v: ((v * BZ + z) * BY + y) * BX + x
+      int bx, by, bz;
+      if (DIR == 0) { bx = la + TmaBox<TA, H>::kLead - H; by = pb; bz = pc; }
+      else if (DIR == 1) { bx = pb; by = la; bz = pc; }
+      else { bx = pb; by = pc; bz = la; }
+      double q[S];
+#pragma unroll
+      for (int v = 0; v < S; ++v) q[v] = sd[((v * Sh::BZ + bz) * Sh::BY + by) * Sh::BX + bx];
+      store_prim(q, pc * TB + pb, la);
+    }
+  } else {  // plain loads, with the boundary conditions and processor halos
+    // thread order: the a index fastest for the x sweep, the pencil b index
+    // fastest otherwise, so that global loads are coalesced along x
+    for (int it = tid; it < NP * LA; it += NT) {
+      int la, pb, pc;
+      if (DIR == 0) { la = it % LA; pb = (it / LA) % TB; pc = it / (LA * TB); }
+      else { pb = it % TB; la = (it / TB) % LA; pc = it / (TB * LA); }
+      bool fa = false, dummy = false;
+      const int ra = a0 - H + la;
+      // processor boundary along the sweep: the ghost cell comes from the
+      // neighbour's halo buffer (x: [S][nz][ny][H], y: [S][nz][H][nx],
+      // z: [S][H][ny][nx]; depth 0 next to the boundary)
+      const int side = ra < 0 ? (P.bc_beg[OA] >= 0 ? 0 : -1) : (ra >= na && P.bc_end[OA] >= 0 ? 1 : -1);
+      const int gb = map_cell(b0 + pb, nb, P.bc_beg[OB], P.bc_end[OB], &dummy);
+      const int gc = map_cell(c0 + pc, nc, P.bc_beg[OC], P.bc_end[OC], &dummy);
+      const double* src;
+      int64_t vs = P.sv;
+      if (side >= 0) {
+        const int d = min(side == 0 ? -1 - ra : ra - na, H - 1);  // deeper cells of partial tiles are never stored
+        int x, y, z;
+        sweep_coords<DIR>(d, gb, gc, x, y, z);
+        const int nx = P.n[0], ny = P.n[1], nz = P.n[2];
+        const double* h = P.halo[2 * DIR + side];
+        if (DIR == 0) { src = h + ((int64_t)z * ny + y) * H + d; vs = (int64_t)nz * ny * H; }
+        else if (DIR == 1) { src = h + ((int64_t)z * H + d) * nx + x; vs = (int64_t)nz * H * nx; }
+        else { src = h + ((int64_t)d * ny + y) * nx + x; vs = (int64_t)H * ny * nx; }
+      } else {
+        const int ga = map_cell(ra, na, P.bc_beg[OA], P.bc_end[OA], &fa);
+        src = qin + ga * st[OA] + gb * st[OB] + gc * st[OC];
+      }
+      double q[S];
+#pragma unroll
+      for (int v = 0; v < S; ++v) q[v] = __ldg(src + v * vs);
+      if (fa) q[Q::MOM + DIR] = -q[Q::MOM + DIR];
+      store_prim(q, pc * TB + pb, la);
     }
   }
   __syncthreads();

@@ -80,6 +80,16 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
+// 4-D tiled copy global -> shared, completing on `bar`.
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, int w,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(bar)
+      : "memory");
+}
+
 // Bounded wait of one thread for phase `parity` of `bar`: false once
 // `limit_ns` nanoseconds of the global timer have passed, so a copy that
 // never lands ends the wait instead of hanging the block.
@@ -97,5 +107,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
 // the driver entry point is unavailable.
 bool encode_tile_map(TileMap& t, const double* base, int nx, int ny, int S, int64_t sy, int64_t sv, int box_w,
                      int box_h);
+
+// The same for a 3-D register [S][nz][ny][sy] (plane stride sz) as a 4-D
+// tensor (x, y, z, variable) with a box of bx x by x bz x S cells.
+bool encode_tile_map_3d(TileMap& t, const double* base, int nx, int ny, int nz, int S, int64_t sy, int64_t sz,
+                        int64_t sv, int bx, int by, int bz);
 
 }  // namespace mfc

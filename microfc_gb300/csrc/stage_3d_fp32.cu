@@ -4,7 +4,10 @@
 namespace mfc {
 
 void register_stage_3d_fp32(std::vector<StageEntry>& r) {
-  r.push_back(Sweep3D<2, 5, float, 32, 4, 2, 16, 16, 256>::entry());  // default: fastest at 256^3
+  // default: fastest at 256^3, tiles staged by one TMA bulk tensor copy
+  r.push_back(Sweep3D<2, 5, float, 32, 4, 2, 16, 16, 256, true>::entry());
+  r.push_back(Sweep3D<2, 5, float, 32, 4, 2, 16, 16, 256>::entry());
+  r.push_back(Sweep3D<2, 5, float, 32, 8, 1, 16, 16, 256, true>::entry());
   r.push_back(Sweep3D<2, 5, float, 32, 4, 2, 16, 32, 256>::entry());
   r.push_back(Sweep3D<2, 5, float, 32, 8, 1, 16, 16, 256>::entry());
   r.push_back(Sweep3D<2, 5, float, 32, 4, 2, 32, 8, 256>::entry());

@@ -78,7 +78,7 @@ def test_uniform_coefficient_record_matches_per_cell_records(kind):
     assert np.array_equal(outs[0].view(np.uint64), outs[1].view(np.uint64))
 
 
-@pytest.mark.parametrize("prec", ["fp64", "split", "gated"])
+@pytest.mark.parametrize("prec", ["fp64", "split", "gated", "3d_fp64", "3d_split"])
 @pytest.mark.parametrize("uniform", [True, False], ids=["uniform", "records"])
 def test_tma_staged_variants_match_plain_loads(prec, uniform):
     """Variants that stage interior tiles with one TMA bulk tensor copy give
@@ -87,9 +87,14 @@ def test_tma_staged_variants_match_plain_loads(prec, uniform):
     the staging area would overlap) takes the plain loads."""
     from microfc_gb300 import Simulation
     from microfc_gb300._lib import MFC_FLAG_TIMEOUT, MFC_VARIANT_TMA, MfcError
-    if prec == "fp64" and not uniform:
-        pytest.skip("the FP64 kernel stages no coefficient records")
-    c = cases.shock_droplet_2d(nx=160, ny=96, steps=4, precision=prec)
+    if prec.endswith("fp64") and not uniform:
+        pytest.skip("the FP64 kernels stage no coefficient records")
+    if prec.startswith("3d"):
+        # interior tiles in every sweep: x tiles of 32 cells, y and z of 16
+        c = cases.shock_bubble_3d(N=40, steps=4, precision=prec[3:])
+        c = c.replace(m=71, dt=c.dt / 2)
+    else:
+        c = cases.shock_droplet_2d(nx=160, ny=96, steps=4, precision=prec)
     params = gate.load() if prec == "gated" else None
     x, y, z, q = preprocess.generate(c)
     ref, staged_out = None, []
