@@ -11,6 +11,8 @@ void register_ensemble_fp32(std::vector<EnsembleEntry>& r) {
   r.push_back(ensemble_entry<2, 5, float, 64, 8, 256>());
   r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, false, 4>());
   r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, false, 5>());
+  // interior tiles staged by one TMA bulk tensor copy
+  r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, false, 5, true>());
 }
 
 }  // namespace mfc
@@ -24,6 +26,9 @@ void register_ensemble_gated(std::vector<EnsembleEntry>& r) {
   // register-capped 16x16 tiles: four or five blocks per SM
   r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, true, 4>());
   r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, true, 5>());
+  // interior tiles staged by one TMA bulk tensor copy (four blocks per SM:
+  // the five-block cap spills the TMA kernel's registers)
+  r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, true, 4, true>());
 }
 
 }  // namespace mfc

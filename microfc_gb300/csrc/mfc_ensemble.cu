@@ -62,6 +62,7 @@ struct mfc_gpu_ensemble {
   mfc::UniformCoef U{};  // the shared coefficient record of all cases (split WENO5, uniform grids)
   int64_t launches = 0;
   mfc::EnsParams* ep = nullptr;  // host staging of the kernel parameters
+  mfc::TileMap* maps = nullptr;  // device: TMA maps [register][case] of a TMA tile variant
 };
 
 namespace {
@@ -86,6 +87,20 @@ int configure(mfc_gpu_ensemble* e, const mfc::EnsembleEntry* en) {
   e->grid = std::min(base, bps * sms);
   e->smem = smem;
   e->entry = en;
+  if (en->tma && e->maps) {
+    // the maps of this variant's box, in stream order after any launch of
+    // the previous variant that reads them
+    std::vector<mfc::TileMap> maps(3 * (size_t)e->num);
+    for (int r = 0; r < 3; ++r)
+      for (int i = 0; i < e->num; ++i) {
+        const mfc::EnsCase& C = e->cases[i];
+        mfc::encode_tile_map(maps[(size_t)r * e->num + i], C.reg[r], e->nx[i], e->ny[i], 2 * e->nf + 3, C.P.sy,
+                             C.P.sv, en->box_w, en->box_h);
+      }
+    err = cudaMemcpyAsync(e->maps, maps.data(), sizeof(mfc::TileMap) * maps.size(), cudaMemcpyHostToDevice,
+                          e->stream);
+    if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+  }
   return MFC_OK;
 }
 
@@ -96,6 +111,7 @@ int launch_stage(mfc_gpu_ensemble* e, int stage, int last) {
   E.stage = stage;
   E.time_stepper = e->ts;
   E.last_step = last;
+  E.maps = e->entry->tma ? e->maps : nullptr;
   for (int d = 0; d < 2; ++d) {
     E.U.on[d] = e->U.on[d];
     for (int k = 0; k < mfc::kCoefRec; ++k) E.U.rec[d][k] = e->U.rec[d][k];
@@ -214,6 +230,7 @@ int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_ca
       (err = cudaMalloc(&e->state, sizeof(double) * state_elems)) != cudaSuccess ||
       (err = cudaMalloc(&e->tables, sizeof(double) * table_elems)) != cudaSuccess ||
       (err = cudaMalloc(&e->status, sizeof(uint32_t))) != cudaSuccess ||
+      (err = cudaMalloc(&e->maps, sizeof(mfc::TileMap) * 3 * (size_t)num_cases)) != cudaSuccess ||
       (c0.precision == MFC_PREC_GATED && (err = cudaMalloc(&e->gate_w, mfc::kGateBufferBytes)) != cudaSuccess))
     return cleanup(mfc::report_error(MFC_ERR_NOMEM, cudaGetErrorString(err)));
   cudaMemsetAsync(e->state, 0, sizeof(double) * state_elems, e->stream);
@@ -415,6 +432,7 @@ int mfc_gpu_ensemble_finalize(mfc_gpu_ensemble* e) {
   cudaFree(e->tables);
   cudaFree(e->status);
   cudaFree(e->gate_w);
+  cudaFree(e->maps);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e->ep;
   delete e;

@@ -26,6 +26,9 @@ struct EnsCase {
 
 struct EnsParams {
   int num_cases, total_tiles, stage, time_stepper, last_step;
+  // TMA maps of every case's registers, [register][case] (device memory),
+  // for the tile variant launched; null: plain loads
+  const TileMap* maps;
   // split WENO5: the coefficient record every cell of every case shares when
   // all cases have uniform grids (the FP32 records of a uniform grid do not
   // depend on its spacing); all off otherwise
@@ -35,9 +38,18 @@ struct EnsParams {
 static_assert(sizeof(EnsParams) <= 32764, "ensemble parameters must fit the kernel parameter space");
 
 // One persistent block's walk over the work list (the body of both kernels).
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE>
+// TMA: interior tiles arrive by one bulk tensor copy; the block initialises
+// its mbarrier once and alternates its phase per copied tile.
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool TMA>
 __device__ __forceinline__ void ensemble_walk(const EnsParams& E) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t parity = 0;
+  if constexpr (TMA) {
+    if (E.maps != nullptr && threadIdx.x == 0)
+      mbar_init(smem_addr(tma_staging<2, NF, WO, RT, TX, TY>(smem_raw) + tma_stage_bytes<2, NF, WO, RT, TX, TY>()),
+                1);
+    __syncthreads();
+  }
   for (int t = blockIdx.x; t < E.total_tiles; t += gridDim.x) {
     int lo = 0, hi = E.num_cases - 1;
     while (lo < hi) {
@@ -50,37 +62,38 @@ __device__ __forceinline__ void ensemble_walk(const EnsParams& E) {
     const int x0 = (lt % C.tiles_x) * TX, y0 = (lt / C.tiles_x) * TY;
     const double* in;
     double* out;
-    int kind;
+    int kind, reg;
     if (E.stage == 0) {
-      in = C.reg[0], out = C.reg[1], kind = kRkEuler;
+      in = C.reg[0], out = C.reg[1], kind = kRkEuler, reg = 0;
     } else if (E.time_stepper == 2) {
-      in = C.reg[1], out = C.reg[0], kind = kRk2Final;
+      in = C.reg[1], out = C.reg[0], kind = kRk2Final, reg = 1;
     } else if (E.stage == 1) {
-      in = C.reg[1], out = C.reg[2], kind = kRk3Mid;
+      in = C.reg[1], out = C.reg[2], kind = kRk3Mid, reg = 1;
     } else {
-      in = C.reg[2], out = C.reg[0], kind = kRk3Final;
+      in = C.reg[2], out = C.reg[0], kind = kRk3Final, reg = 2;
     }
-    stage_tile<2, NF, WO, RT, TX, TY, NT, GATE>(C.P, in, C.reg[0], out, E.last_step ? C.dt_last : C.dt, kind, x0,
-                                                y0, smem_raw, &E.U);
+    const TileMap* T = (TMA && E.maps != nullptr) ? E.maps + reg * E.num_cases + lo : nullptr;
+    stage_tile<2, NF, WO, RT, TX, TY, NT, GATE, false, UniformCoefT<2>, TMA>(
+        C.P, in, C.reg[0], out, E.last_step ? C.dt_last : C.dt, kind, x0, y0, smem_raw, &E.U, T, &parity);
     __syncthreads();  // the next tile reuses the shared memory
   }
 }
 
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool TMA>
 __global__ void __launch_bounds__(NT) ensemble_stage_kernel(const __grid_constant__ EnsParams E) {
-  ensemble_walk<NF, WO, RT, TX, TY, NT, GATE>(E);
+  ensemble_walk<NF, WO, RT, TX, TY, NT, GATE, TMA>(E);
 }
 
 // The same with the registers capped so that MINB blocks fit on an SM.
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool TMA>
 __global__ void __launch_bounds__(NT, MINB) ensemble_stage_kernel_mb(const __grid_constant__ EnsParams E) {
-  ensemble_walk<NF, WO, RT, TX, TY, NT, GATE>(E);
+  ensemble_walk<NF, WO, RT, TX, TY, NT, GATE, TMA>(E);
 }
 
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool TMA>
 constexpr auto ensemble_func() {
-  if constexpr (MINB > 1) return &ensemble_stage_kernel_mb<NF, WO, RT, TX, TY, NT, GATE, MINB>;
-  else return &ensemble_stage_kernel<NF, WO, RT, TX, TY, NT, GATE>;
+  if constexpr (MINB > 1) return &ensemble_stage_kernel_mb<NF, WO, RT, TX, TY, NT, GATE, MINB, TMA>;
+  else return &ensemble_stage_kernel<NF, WO, RT, TX, TY, NT, GATE, TMA>;
 }
 
 struct EnsembleEntry {
@@ -88,22 +101,45 @@ struct EnsembleEntry {
   size_t smem, smem_shared_coef;  // dynamic shared memory: per-cell records / shared record
   const void* func;
   cudaError_t (*launch)(const EnsParams& E, int grid, size_t smem, cudaStream_t st);
+  bool tma;    // interior tiles staged by TMA (needs EnsParams::maps)
+  int box_w;   // x extent of the TMA box (cells), box_h rows
+  int box_h;
 };
 
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB = 1>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB = 1, bool TMA = false>
 cudaError_t ensemble_launch(const EnsParams& E, int grid, size_t smem, cudaStream_t st) {
-  ensemble_func<NF, WO, RT, TX, TY, NT, GATE, MINB>()<<<grid, NT, smem, st>>>(E);
+  ensemble_func<NF, WO, RT, TX, TY, NT, GATE, MINB, TMA>()<<<grid, NT, smem, st>>>(E);
   return cudaGetLastError();
 }
 
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool TMA>
+constexpr size_t ensemble_smem(bool shared_coef) {
+  size_t s = shared_coef ? stage_smem_bytes_shared_coef<2, NF, WO, RT, TX, TY, NT, GATE>()
+                         : stage_smem_bytes<2, NF, WO, RT, TX, TY, NT, GATE>();
+  if constexpr (TMA) {
+    const size_t t = stage_tma_bytes<2, NF, WO, RT, TX, TY>();
+    s = s > t ? s : t;
+  }
+  return s;
+}
+
 // prec: 0 FP64, 1 split, 2 split with the learned gate
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool TMA = false>
 EnsembleEntry ensemble_entry() {
-  return EnsembleEntry{NF, WO, sizeof(RT) == 8 ? 0 : (GATE ? 2 : 1), TX, TY, NT,
-                       stage_smem_bytes<2, NF, WO, RT, TX, TY, NT, GATE>(),
-                       stage_smem_bytes_shared_coef<2, NF, WO, RT, TX, TY, NT, GATE>(),
-                       reinterpret_cast<const void*>(ensemble_func<NF, WO, RT, TX, TY, NT, GATE, MINB>()),
-                       &ensemble_launch<NF, WO, RT, TX, TY, NT, GATE, MINB>};
+  using Sh = StageShape<2, NF, WO, RT, TX, TY>;
+  return EnsembleEntry{NF,
+                       WO,
+                       sizeof(RT) == 8 ? 0 : (GATE ? 2 : 1),
+                       TX,
+                       TY,
+                       NT,
+                       ensemble_smem<NF, WO, RT, TX, TY, NT, GATE, TMA>(false),
+                       ensemble_smem<NF, WO, RT, TX, TY, NT, GATE, TMA>(true),
+                       reinterpret_cast<const void*>(ensemble_func<NF, WO, RT, TX, TY, NT, GATE, MINB, TMA>()),
+                       &ensemble_launch<NF, WO, RT, TX, TY, NT, GATE, MINB, TMA>,
+                       TMA,
+                       TmaBox<TX, Sh::H>::kWidth,
+                       Sh::LY};
 }
 
 void register_ensemble_fp64(std::vector<EnsembleEntry>& r);

@@ -122,6 +122,20 @@ struct GateShape {
   static constexpr size_t kBytes = ((NGX + NGY + 15) / 16) * 16;
 };
 
+// The TMA staging area of a stage tile (2-D): after the primitive tile,
+// 128-byte aligned, the box of all variables, then its mbarrier and a flag.
+template <int ND, int NF, int WO, class RT, int TX, int TY>
+__device__ __forceinline__ unsigned char* tma_staging(unsigned char* smem_raw) {
+  using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
+  const uintptr_t a = reinterpret_cast<uintptr_t>(smem_raw + Sh::OW * sizeof(RT));
+  return reinterpret_cast<unsigned char*>((a + 127) & ~uintptr_t(127));
+}
+template <int ND, int NF, int WO, class RT, int TX, int TY>
+constexpr uint32_t tma_stage_bytes() {
+  using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
+  return uint32_t(TmaBox<TX, Sh::H>::kWidth) * Sh::LY * Sh::S * 8;
+}
+
 // One tile of one RK stage; the tile's first cell is (x0, y0).  Used by the
 // single-case kernel (one tile per block) and by the ensemble kernel (many
 // tiles of many cases per persistent block).  smem_raw must hold
@@ -133,7 +147,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
                                            const double* __restrict__ qbase, double* __restrict__ qout,
                                            const double dt, const int kind, const int x0, const int y0,
                                            unsigned char* smem_raw, const UC* U = nullptr,
-                                           const TileMap* T = nullptr) {
+                                           const TileMap* T = nullptr, uint32_t* tma_parity = nullptr) {
   static_assert(!GATE || (sizeof(RT) == 4 && WO == 5), "the learned gate runs on the split-precision WENO5 path");
   static_assert(!(GATE && VISC), "the gated kernel is inviscid");
   using Sh = StageShape<ND, NF, WO, RT, TX, TY, VISC>;
@@ -242,25 +256,33 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   unsigned char* stg = nullptr;
   uint32_t bar = 0;
   using Box = TmaBox<TX, H>;
-  constexpr uint32_t kStageBytes = uint32_t(Box::kWidth) * LY * S * 8;
+  constexpr uint32_t kStageBytes = tma_stage_bytes<ND, NF, WO, RT, TX, TY>();
   if constexpr (TMA && ND == 2 && !VISC) {
     use_tma = T != nullptr && T->on && x0 >= H && x0 + TX + H <= nx && y0 >= H && y0 + TY + H <= ny &&
               (!kSplit || (ux && uy));
     if (use_tma) {
-      const uintptr_t a = reinterpret_cast<uintptr_t>(smem_raw + Sh::OW * sizeof(RT));
-      stg = reinterpret_cast<unsigned char*>((a + 127) & ~uintptr_t(127));
+      stg = tma_staging<ND, NF, WO, RT, TX, TY>(smem_raw);
       bar = smem_addr(stg + kStageBytes);
-      if (tid == 0) mbar_init(bar, 1);
+      // one tile per block: a fresh barrier; a block walking many tiles
+      // (tma_parity given) initialised it once and alternates its phase
+      if (tid == 0 && tma_parity == nullptr) mbar_init(bar, 1);
     }
   }
   griddep_wait();  // the state below is the previous stage's output
   if (use_tma) {
+    const uint32_t par = tma_parity ? *tma_parity : 0u;
     volatile int* landed = reinterpret_cast<volatile int*>(stg + kStageBytes + 8);
     if (tid == 0) {
+      // a walking block: its reads of this memory for the previous tile come
+      // first, and its maps live in global memory
+      if (tma_parity) {
+        fence_proxy_async_smem();
+        tensormap_acquire(&T->map);
+      }
       mbar_arrive_expect_tx(bar, kStageBytes);
       tma_load_3d(smem_addr(stg), &T->map, x0 - Box::kLead, y0 - H, 0, bar);
-      const bool ok = mbar_wait_bounded(bar, 0, 1000000000ull);       // 1 s
-      if (!ok) (void)mbar_wait_bounded(bar, 0, 1000000000ull);         // the copy may still be in flight
+      const bool ok = mbar_wait_bounded(bar, par, 1000000000ull);  // 1 s
+      if (!ok) (void)mbar_wait_bounded(bar, par, 1000000000ull);    // the copy may still be in flight
       *landed = ok ? 1 : 0;
     }
     __syncthreads();
@@ -268,7 +290,8 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       if (tid == 0 && P.status) atomicOr(P.status, MFC_FLAG_TIMEOUT);
       return;
     }
-    (void)mbar_try_wait(bar, 0);  // completed: each thread acquires the copy's writes
+    (void)mbar_try_wait(bar, par);  // completed: each thread acquires the copy's writes
+    if (tma_parity) *tma_parity ^= 1u;
     const double* sd = reinterpret_cast<const double*>(stg);
     for (int c = tid; c < LX * LY; c += NT) {
       const int lx = c % LX, ly = c / LX;
