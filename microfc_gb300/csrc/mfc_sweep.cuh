@@ -58,8 +58,10 @@ __device__ __forceinline__ void sweep_coords(int a, int b, int c, int& x, int& y
 
 // TMA: a tile whose sweep halo lies inside the domain arrives by one bulk
 // tensor copy (T maps the stage input qin; T.on = 0: plain loads only).
-template <int NF, int WO, class RT, int DIR, int TA, int TB, int TC, int NT, bool TMA = false>
-__global__ void __launch_bounds__(NT) sweep_kernel(const DevParams P, const __grid_constant__ UniformCoef U,
+// MINB > 0 caps the registers so that MINB blocks fit on an SM; MINB = 0
+// leaves the minimum unspecified (ptxas allocates as without the bound).
+template <int NF, int WO, class RT, int DIR, int TA, int TB, int TC, int NT, bool TMA = false, int MINB = 0>
+__global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, const __grid_constant__ UniformCoef U,
                                                    const __grid_constant__ TileMap T, const double* __restrict__ qin,
                                                    const double* __restrict__ qbase, double* __restrict__ qout,
                                                    const double dt, const int kind) {
