@@ -11,7 +11,8 @@ pressure recovery alone would flag nearly every cell); the inputs come
 from the split path's FP32 primitives, as the gated kernel sees them.  Smooth
 cells then use the
 optimal linear weights d_k; plain WENO everywhere stays the fallback
-(precision "split") and the judge (FP64, precision "fp64").
+(precision "split") and the measure of the gated form's error (FP64,
+precision "fp64").
 
 Training data are states the solver itself generates: seeded runs of the
 2-D shock-droplet case (Mach uniform in [1.2, 2.5], droplet radius uniform
