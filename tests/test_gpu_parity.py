@@ -166,6 +166,32 @@ def test_stretched_grid_matches_oracle(oracle_lib, prec):
         assert np.all(np.isfinite(got)) and err[dens_alpha].max() <= TOL_SPLIT, err
 
 
+def test_pre_process_stretched_grid_runs_like_the_oracle(oracle_lib):
+    """A case file's stretch_x/stretch_y (m_grid.f90:72-90): the device
+    initial condition on the context's stretched cell boundaries, then 10
+    plain FP64 steps, against the oracle on the host pre_process's grid and
+    state."""
+    import dataclasses
+    case = cases.shock_droplet_2d(nx=96, ny=64, steps=10).replace(
+        stretch_x=(12.0, 0.006, 0.010, 1), stretch_y=(12.0, 0.004, 0.006, 1))
+    # the map stretches the domain to about [0, 0.04] x [0, 0.018]: the
+    # background patch covers it
+    bg = dataclasses.replace(case.patches[0], centroid=(0.025, 0.0125, 0.0), length=(0.05, 0.025, 0.0))
+    case = case.replace(patches=[bg] + list(case.patches[1:]), dt=1.8e-8)  # CFL 0.3 on the finest cells
+    case.check()
+    x_cb, y_cb, _, q = preprocess.generate(case)
+    ref, _ = _oracle_run(oracle_lib, case, x_cb, y_cb, q, 10)
+    with Simulation(case, ic="device") as sim:
+        q_dev = sim.download()
+        scale = np.abs(q).reshape(q.shape[0], -1).max(axis=1)[:, None, None, None]
+        assert np.all(np.abs(q_dev - q) <= 2e-15 * scale)  # tanh of the smoothed droplet
+    with Simulation(case, x_cb, y_cb, q_cons=q) as sim:
+        sim.run(0, 10)
+        assert sim.status() == 0
+        got = sim.download()
+    _check(case, got, ref, TOL_FP64)
+
+
 def _bubble(nx, ny, nz, steps, **kw):
     c = cases.shock_bubble_3d(N=max(nx, ny, nz), steps=steps, precision="fp64")
     c = c.replace(m=nx - 1, n=ny - 1, p=nz - 1, **kw)
