@@ -229,8 +229,8 @@ int mfc_gpu_tune(mfc_gpu_ctx* ctx, int reps, int* variant_out, double* ms_out);
 int mfc_gpu_select_variant(mfc_gpu_ctx* ctx, int variant, int* tx, int* ty, int* threads);
 /* Features of tile variant `variant` of the context's configuration, as
  * MFC_VARIANT_* bits in *features; MFC_ERR_INVALID past the last variant. */
-#define MFC_VARIANT_TMA 0x1u /* interior tiles arrive by one TMA bulk tensor copy (2-D; on a
-                                uniform grid in split precision)                             */
+#define MFC_VARIANT_TMA 0x1u /* interior tiles arrive by one TMA bulk tensor copy (2-D and
+                                3-D inviscid kernels)                                       */
 int mfc_gpu_variant_features(mfc_gpu_ctx* ctx, int variant, uint32_t* features);
 
 /* ---- Learned WENO gate (no reference counterpart).  A 10-32-32-1 MLP on a

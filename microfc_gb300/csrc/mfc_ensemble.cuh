@@ -114,13 +114,7 @@ cudaError_t ensemble_launch(const EnsParams& E, int grid, size_t smem, cudaStrea
 
 template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool TMA>
 constexpr size_t ensemble_smem(bool shared_coef) {
-  size_t s = shared_coef ? stage_smem_bytes_shared_coef<2, NF, WO, RT, TX, TY, NT, GATE>()
-                         : stage_smem_bytes<2, NF, WO, RT, TX, TY, NT, GATE>();
-  if constexpr (TMA) {
-    const size_t t = stage_tma_bytes<2, NF, WO, RT, TX, TY>();
-    s = s > t ? s : t;
-  }
-  return s;
+  return stage_smem_total<2, NF, WO, RT, TX, TY, NT, GATE, false, TMA>(shared_coef);
 }
 
 // prec: 0 FP64, 1 split, 2 split with the learned gate

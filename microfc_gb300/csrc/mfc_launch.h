@@ -61,16 +61,10 @@ constexpr auto stage_func() {
 }
 
 // Dynamic shared memory of a launch: without the coefficient records on a
-// uniform grid, and at least the TMA staging area of a TMA kernel.
+// uniform grid; a TMA kernel's records sit past its staging area.
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool VISC, bool TMA>
 constexpr size_t stage_launch_smem(bool shared_coef) {
-  size_t s = shared_coef ? stage_smem_bytes_shared_coef<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>()
-                         : stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>();
-  if constexpr (TMA) {
-    const size_t t = stage_tma_bytes<ND, NF, WO, RT, TX, TY>();
-    s = s > t ? s : t;
-  }
-  return s;
+  return stage_smem_total<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, TMA>(shared_coef);
 }
 
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false,

@@ -136,10 +136,34 @@ constexpr uint32_t tma_stage_bytes() {
   return uint32_t(TmaBox<TX, Sh::H>::kWidth) * Sh::LY * Sh::S * 8;
 }
 
+// Offset of the split path's coefficient records in a block's shared
+// memory: after the main arrays and the gate's flags, and after the TMA
+// staging area (worst-case alignment) of a TMA kernel, so that records
+// staged before the copy lands are not overwritten.
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool VISC, bool TMA>
+constexpr size_t stage_coef_offset() {
+  using Sh = StageShape<ND, NF, WO, RT, TX, TY, VISC>;
+  size_t o = Sh::kMainBytes + (GATE ? GateShape<ND, TX, TY, NT>::kBytes : 0);
+  if constexpr (TMA) {
+    const size_t t =
+        (sizeof(RT) * size_t(Sh::OW) + 128 + tma_stage_bytes<ND, NF, WO, RT, TX, TY>() + 16 + 15) / 16 * 16;
+    o = o > t ? o : t;
+  }
+  return o;
+}
+
+// Dynamic shared memory of one block: without the coefficient records when
+// the grid is uniform (every direction reads the shared record).
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool VISC, bool TMA>
+constexpr size_t stage_smem_total(bool shared_coef) {
+  return stage_coef_offset<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, TMA>() +
+         (shared_coef ? 0 : StageShape<ND, NF, WO, RT, TX, TY, VISC>::kCoefBytes);
+}
+
 // One tile of one RK stage; the tile's first cell is (x0, y0).  Used by the
 // single-case kernel (one tile per block) and by the ensemble kernel (many
 // tiles of many cases per persistent block).  smem_raw must hold
-// stage_smem_bytes() (or stage_smem_bytes_shared_coef() when U covers every
+// stage_smem_total() (of shared_coef = true when U covers every
 // direction).
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, bool VISC = false,
           class UC = UniformCoef, bool TMA = false>
@@ -164,7 +188,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   RT* wr = wl + Sh::align16(Sh::NW);          // right-face values
   RT* fl = sq + Sh::OF;                       // fluxes [S+1][...]
   // split: FP32 x coefficients [TX+2][kCoefRec], after the gate's share
-  RT* scx = reinterpret_cast<RT*>(smem_raw + Sh::kMainBytes + (GATE ? GateShape<ND, TX, TY, NT>::kBytes : 0));
+  RT* scx = reinterpret_cast<RT*>(smem_raw + stage_coef_offset<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, TMA>());
   RT* scy = scx + kCoefRec * Sh::NCX;         // split: FP32 y coefficients [TY+2][kCoefRec]
   // element of variable v in the primitive tile and in the x / y WENO values
   constexpr bool kPair = Sh::PAIR;
@@ -249,17 +273,15 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
 
   // TMA staging: a tile whose halo lies inside the domain (no boundary
   // condition, no processor halo) arrives in one bulk tensor copy of all
-  // variables into the WENO and flux arrays, which are free until phase 2.
-  // Split precision uses it only on a uniform grid, where no coefficient
-  // records share that space.
+  // variables into the WENO and flux arrays, which are free until phase 2
+  // (the coefficient records sit past the staging area).
   bool use_tma = false;
   unsigned char* stg = nullptr;
   uint32_t bar = 0;
   using Box = TmaBox<TX, H>;
   constexpr uint32_t kStageBytes = tma_stage_bytes<ND, NF, WO, RT, TX, TY>();
   if constexpr (TMA && ND == 2 && !VISC) {
-    use_tma = T != nullptr && T->on && x0 >= H && x0 + TX + H <= nx && y0 >= H && y0 + TY + H <= ny &&
-              (!kSplit || (ux && uy));
+    use_tma = T != nullptr && T->on && x0 >= H && x0 + TX + H <= nx && y0 >= H && y0 + TY + H <= ny;
     if (use_tma) {
       stg = tma_staging<ND, NF, WO, RT, TX, TY>(smem_raw);
       bar = smem_addr(stg + kStageBytes);
@@ -789,28 +811,6 @@ __global__ void __launch_bounds__(NT, MINB) stage_kernel_tma_mb(const DevParams 
   extern __shared__ __align__(128) unsigned char smem_tma[];
   stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE, false, UniformCoef, true>(
       P, qin, qbase, qout, dt, kind, blockIdx.x * TX, (ND > 1) ? blockIdx.y * TY : 0, smem_tma, &U, &T);
-}
-
-// Shared memory a TMA-staged tile needs beyond the primitive tile: the box
-// of all variables (128-byte aligned), its mbarrier and a flag.
-template <int ND, int NF, int WO, class RT, int TX, int TY>
-constexpr size_t stage_tma_bytes() {
-  using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
-  return sizeof(RT) * size_t(Sh::OW) + 128 + size_t(TmaBox<TX, Sh::H>::kWidth) * Sh::LY * Sh::S * 8 + 16;
-}
-
-// Shared memory of one stage-kernel block (with the gate's share when on).
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool VISC = false>
-constexpr size_t stage_smem_bytes() {
-  return StageShape<ND, NF, WO, RT, TX, TY, VISC>::kSmemBytes + (GATE ? GateShape<ND, TX, TY, NT>::kBytes : 0);
-}
-
-// The same without the coefficient records, for launches on a uniform grid
-// (every direction reads the shared record).
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool VISC = false>
-constexpr size_t stage_smem_bytes_shared_coef() {
-  return stage_smem_bytes<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>() -
-         StageShape<ND, NF, WO, RT, TX, TY, VISC>::kCoefBytes;
 }
 
 }  // namespace mfc

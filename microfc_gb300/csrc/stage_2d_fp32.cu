@@ -6,7 +6,7 @@ namespace mfc {
 
 void register_stage_2d_fp32(std::vector<StageEntry>& r) {
   // the first entry is the default: the autotuner's usual choice on GB300,
-  // interior tiles staged by one TMA bulk tensor copy (on a uniform grid)
+  // interior tiles staged by one TMA bulk tensor copy
   r.push_back(stage_entry<2, 2, 5, float, 16, 16, 256, false, 5, false, true>());
   r.push_back(stage_entry<2, 2, 5, float, 16, 16, 256, false, 5>());
   r.push_back(stage_entry<2, 2, 5, float, 32, 16, 256>());

@@ -82,9 +82,9 @@ def test_uniform_coefficient_record_matches_per_cell_records(kind):
 @pytest.mark.parametrize("uniform", [True, False], ids=["uniform", "records"])
 def test_tma_staged_variants_match_plain_loads(prec, uniform):
     """Variants that stage interior tiles with one TMA bulk tensor copy give
-    the bits of the first plain-load variant, no bounded wait gives up, and
-    split precision with per-cell coefficient records (whose shared memory
-    the staging area would overlap) takes the plain loads."""
+    the bits of the first plain-load variant and no bounded wait gives up,
+    with the shared coefficient record of a uniform grid and with per-cell
+    records (staged beside the copy's landing area)."""
     from microfc_gb300 import Simulation
     from microfc_gb300._lib import MFC_FLAG_TIMEOUT, MFC_VARIANT_TMA, MfcError
     if prec.endswith("fp64") and not uniform:
