@@ -263,3 +263,13 @@ def test_device_initial_condition_rejects_bad_patches():
     with Simulation(case) as sim:
         with pytest.raises(MfcError, match="geometry"):
             sim.generate_ic(bad)
+    # 2-D: the device refuses what the host pre_process refuses
+    g2 = _gallery_case()
+    with Simulation(g2) as sim:
+        for patch, msg in ((Patch(geometry=5, centroid=(0.5, 0.2, 0), radii=(0.1, 0.0, 0)), "semi-axes"),
+                           (Patch(geometry=4, centroid=(0.5, 0.2, 0)), "normal is zero"),
+                           (Patch(geometry=9, centroid=(0.5, 0.2, 0), length=(0.1, 0.1, 0.1)), "geometry")):
+            p = Patch(**{**patch.__dict__, "alter_patch": (1,), "alpha_rho": (1.0, 0.0), "alpha": (1.0, 0.0)})
+            with pytest.raises(MfcError, match=msg):
+                sim.generate_ic(g2.replace(patches=[g2.patches[0], p]))
+        sim.generate_ic(g2)  # the context still takes a valid set
