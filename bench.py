@@ -257,6 +257,7 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
         if params is not None:
             ens.set_gate(params)
         variant, _ = ens.tune(reps=3)
+        ens_tma = bool(ens.variant_features(variant) & _lib.MFC_VARIANT_TMA)
         ens.run(0, 3, use_graph=True)  # warm-up (advances the state; timing only)
         torch.cuda.synchronize()
         nsteps = 20
@@ -282,7 +283,8 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
     seq_rate = sum(c.cells for c in cl) / seq_time
     out["ensemble"] = {"cases": len(cl), "cells": int(sum(c.cells for c in cl)), "precision": prec,
                        "value": ens_rate, "unit": "cell-updates/s", "steps": nsteps, "graph": True,
-                       "tile_variant": variant, "timing": "CUDA events on the ensemble stream around 20 graph-replayed steps",
+                       "tile_variant": variant, "tma_staging": ens_tma,
+                       "timing": "CUDA events on the ensemble stream around 20 graph-replayed steps",
                        "sequential_plain_fp64": seq_rate, "vs_sequential_plain_fp64": ens_rate / seq_rate}
     return out
 

@@ -276,6 +276,9 @@ int mfc_gpu_ensemble_tune(mfc_gpu_ensemble* ens, int reps, int* variant_out, dou
 /* Pins the ensemble's tile variant (the numbering of mfc_gpu_ensemble_tune);
  * every variant gives the same bits.  Returns its tile shape. */
 int mfc_gpu_ensemble_select_variant(mfc_gpu_ensemble* ens, int variant, int* tx, int* ty, int* threads);
+/* MFC_VARIANT_* bits of ensemble tile variant `variant` (see
+ * mfc_gpu_variant_features). */
+int mfc_gpu_ensemble_variant_features(mfc_gpu_ensemble* ens, int variant, uint32_t* features);
 /* Steps t_step_start .. t_step_stop-1 of every case; each case's last step
  * uses its dt after the p_main trim.  use_graph != 0 replays the stage
  * launches of a step from a CUDA graph.  Synchronous; MFC_ERR_STATE on NaN. */

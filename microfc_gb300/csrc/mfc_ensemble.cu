@@ -363,6 +363,18 @@ int mfc_gpu_ensemble_select_variant(mfc_gpu_ensemble* e, int variant, int* tx, i
   return mfc::report_error(MFC_ERR_INVALID, "no such ensemble tile variant");
 }
 
+int mfc_gpu_ensemble_variant_features(mfc_gpu_ensemble* e, int variant, uint32_t* features) {
+  if (!e || !features) return mfc::report_error(MFC_ERR_INVALID, "NULL argument");
+  int idx = -1;
+  for (const auto& x : g_ens) {
+    if (x.nf != e->nf || x.wo != e->wo || x.prec != e->prec) continue;
+    if (++idx != variant) continue;
+    *features = x.tma ? MFC_VARIANT_TMA : 0u;
+    return MFC_OK;
+  }
+  return mfc::report_error(MFC_ERR_INVALID, "no such ensemble tile variant");
+}
+
 // Time steps t_step_start .. t_step_stop-1 for every case (each with its own
 // dt; the last step uses that case's dt after the p_main trim).  With
 // use_graph the stage launches of one step are captured once in a CUDA graph

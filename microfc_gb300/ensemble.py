@@ -123,6 +123,12 @@ class Ensemble:
                                                           ctypes.byref(nt)))
         return tx.value, ty.value, nt.value
 
+    def variant_features(self, variant: int) -> int:
+        """MFC_VARIANT_* bits of a tile variant (mfc_gpu_ensemble_variant_features)."""
+        f = ctypes.c_uint32(0)
+        _lib.check(self.L.mfc_gpu_ensemble_variant_features(self._h, int(variant), ctypes.byref(f)))
+        return f.value
+
     def tune(self, reps: int = 5):
         v, ms = ctypes.c_int(-1), ctypes.c_double(0)
         _lib.check(self.L.mfc_gpu_ensemble_tune(self._h, int(reps), ctypes.byref(v), ctypes.byref(ms)))

@@ -67,7 +67,8 @@ def test_every_ensemble_variant_gives_the_same_bits(precision):
                 sim.set_gate(params)
             sim.run(0, 6)
             refs.append(sim.download())
-    v = 0
+    from microfc_gb300._lib import MFC_VARIANT_TMA
+    v, tma = 0, 0
     while True:
         with Ensemble(cl) as ens:
             if params is not None:
@@ -76,11 +77,12 @@ def test_every_ensemble_variant_gives_the_same_bits(precision):
                 shape = ens.select_variant(v)
             except MfcError:
                 break
+            tma += bool(ens.variant_features(v) & MFC_VARIANT_TMA)
             ens.run(0, 6)
             for i, ref in enumerate(refs):
                 assert np.array_equal(ens.download(i).view(np.uint64), ref.view(np.uint64)), (v, shape, i)
         v += 1
-    assert v >= 2
+    assert v >= 2 and tma >= 1  # the TMA-staged variants are among them
 
 
 @pytest.mark.gpu
