@@ -442,13 +442,15 @@ int mfc_gpu_download(mfc_gpu_ctx* c, int var, double* host_sf, int64_t ld_y, int
   return MFC_OK;
 }
 
+// The whole state in one strided copy: every row of every variable is n[0]
+// values, rows follow each other every n[0] values on the host and every
+// sy (= the padded pitch) in the register, across variables too (sv = sy *
+// rows per variable).
 int mfc_gpu_upload_state(mfc_gpu_ctx* c, const double* host_q) {
   if (!c || !host_q) return fail(MFC_ERR_INVALID, "NULL argument");
-  const int64_t cells = (int64_t)c->n[0] * c->n[1] * c->n[2];
-  for (int v = 0; v < c->S; ++v) {
-    int rc = copy_var(c, c->reg[0], v, host_q + v * cells, nullptr, c->n[0], (int64_t)c->n[0] * c->n[1]);
-    if (rc) return rc;
-  }
+  const size_t rows = (size_t)c->S * c->n[1] * c->n[2];
+  MFC_CUDA(cudaMemcpy2DAsync(c->reg[0], (size_t)c->sy * 8, host_q, (size_t)c->n[0] * 8, (size_t)c->n[0] * 8, rows,
+                             cudaMemcpyHostToDevice, c->stream));
   MFC_CUDA(cudaStreamSynchronize(c->stream));
   return MFC_OK;
 }
@@ -474,11 +476,9 @@ int mfc_gpu_generate_ic(mfc_gpu_ctx* c, const mfc_patch* patches, int num_patche
 
 int mfc_gpu_download_state(mfc_gpu_ctx* c, double* host_q) {
   if (!c || !host_q) return fail(MFC_ERR_INVALID, "NULL argument");
-  const int64_t cells = (int64_t)c->n[0] * c->n[1] * c->n[2];
-  for (int v = 0; v < c->S; ++v) {
-    int rc = copy_var(c, c->reg[0], v, nullptr, host_q + v * cells, c->n[0], (int64_t)c->n[0] * c->n[1]);
-    if (rc) return rc;
-  }
+  const size_t rows = (size_t)c->S * c->n[1] * c->n[2];
+  MFC_CUDA(cudaMemcpy2DAsync(host_q, (size_t)c->n[0] * 8, c->reg[0], (size_t)c->sy * 8, (size_t)c->n[0] * 8, rows,
+                             cudaMemcpyDeviceToHost, c->stream));
   MFC_CUDA(cudaStreamSynchronize(c->stream));
   return MFC_OK;
 }
