@@ -345,8 +345,10 @@ int mfc_gpu_ensemble_generate_ic(mfc_gpu_ensemble* ens, int case_index, const mf
  * q_in (state at t^n) and q_out (state at t^{n+1}) are distinct device
  * arrays [S][p+1][n+1][ld_y], x fastest.  Limits: S*(n+1)*(p+1)*ld_y <=
  * 7*2^20 doubles and at most 4096 cells per direction; larger cases return
- * MFC_ERR_INVALID.  Synchronous with respect to `stream` (a cudaStream_t,
- * NULL = legacy default stream); returns MFC_ERR_STATE if a NaN was written.
+ * MFC_ERR_INVALID, and so does MFC_PREC_GATED (the gate's parameters live
+ * in a context).  Synchronous with respect to `stream` (a cudaStream_t,
+ * NULL = legacy default stream); returns MFC_ERR_STATE if a NaN was written
+ * or a TMA staging wait timed out (q_out is then incomplete).
  * All calls share the array: calls that overlap on the GPU race.  The first
  * call on a device looks up the array's address with that device current;
  * make it before any stream capture. */

@@ -722,6 +722,7 @@ int mfc_gpu_run(mfc_gpu_ctx* c, int t_step_start, int t_step_stop, double* dt_in
   int rc = mfc_gpu_status(c, &flags, 0);
   if (rc) return rc;
   if (flags & MFC_FLAG_NAN) return fail(MFC_ERR_STATE, "NaN or Inf in the conservative state");
+  if (flags & MFC_FLAG_TIMEOUT) return fail(MFC_ERR_STATE, "a TMA staging wait timed out; the state is incomplete");
   if (c->monitor_on) {  // m_data_output.fpp:296-306
     double icfl = 0.0;
     if ((rc = mfc_gpu_icfl(c, &icfl, 0))) return rc;

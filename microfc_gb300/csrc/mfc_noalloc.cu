@@ -42,8 +42,12 @@ namespace {
 
 constexpr int64_t kNoAllocMaxRegElems = int64_t(7) << 20;
 constexpr int kNoAllocMaxCells = 4096;
+// per direction: 1/dx of the cells, the cell-centre spacings (cells + 1) and
+// the coefficient rows (cells + 2 * kCoefPad each), as build_grid_tables
+// lays them out
 constexpr int64_t kNoAllocTableElems =
-    3 * (int64_t(kNoAllocMaxCells) + int64_t(mfc::kNumCoef) * (kNoAllocMaxCells + 2 * mfc::kCoefPad));
+    3 * (int64_t(kNoAllocMaxCells) + (int64_t(kNoAllocMaxCells) + 1) +
+         int64_t(mfc::kNumCoef) * (kNoAllocMaxCells + 2 * mfc::kCoefPad));
 constexpr int64_t kNoAllocStatusOffset = kNoAllocMaxRegElems + kNoAllocTableElems;
 constexpr int64_t kNoAllocScratchElems = kNoAllocStatusOffset + 32;  // + one 256-byte slot for the status word
 
@@ -83,6 +87,9 @@ extern "C" int mfc_gpu_tvd_rk_noalloc(const mfc_params* p, const double* q_in, d
   if (p->p > 0)
     return mfc::report_error(MFC_ERR_INVALID, "mfc_gpu_tvd_rk_noalloc handles 1-D and 2-D cases; 3-D cases need "
                                               "the RHS work buffer that mfc_gpu_init allocates");
+  if (p->precision == MFC_PREC_GATED)
+    return mfc::report_error(MFC_ERR_INVALID, "mfc_gpu_tvd_rk_noalloc takes MFC_PREC_FP64 or MFC_PREC_SPLIT; the "
+                                              "learned gate needs the parameters that mfc_gpu_set_gate uploads");
   if (!q_in || !q_out) return mfc::report_error(MFC_ERR_INVALID, "q_in and q_out must be device arrays");
   if (q_in == q_out) return mfc::report_error(MFC_ERR_INVALID, "q_in and q_out must be different arrays");
   const int nd = 1 + (p->n > 0) + (p->p > 0);
@@ -105,6 +112,8 @@ extern "C" int mfc_gpu_tvd_rk_noalloc(const mfc_params* p, const double* q_in, d
   mfc::GridTables gt;
   const std::string gwhy = mfc::build_grid_tables(p, nd, n, b, gt);
   if (!gwhy.empty()) return mfc::report_error(MFC_ERR_INVALID, gwhy);
+  if ((int64_t)gt.host.size() > kNoAllocTableElems)
+    return mfc::report_error(MFC_ERR_INVALID, "mfc_gpu_tvd_rk_noalloc: the grid tables exceed their fixed scratch");
 
   DeviceGuard guard;
   cudaError_t e = cudaGetDevice(&guard.prev);
@@ -172,5 +181,7 @@ extern "C" int mfc_gpu_tvd_rk_noalloc(const mfc_params* p, const double* q_in, d
       (e = cudaStreamSynchronize(st)) != cudaSuccess)
     return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(e));
   if (flags & MFC_FLAG_NAN) return mfc::report_error(MFC_ERR_STATE, "NaN or Inf in the conservative state");
+  if (flags & MFC_FLAG_TIMEOUT)
+    return mfc::report_error(MFC_ERR_STATE, "a TMA staging wait timed out; tiles of q_out were not written");
   return MFC_OK;
 }

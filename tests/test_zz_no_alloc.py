@@ -10,8 +10,9 @@ intermediate RK register and grid tables in a fixed file-scope device array
 
 The GPU test checks it against the regular entry point (mfc_gpu_init +
 mfc_gpu_tvd_rk) on two calls in a row, at the tolerance of the other parity
-tests (relative L1 <= 1e-10 per field; the FP64 path is bit-faithful, so the
-results are expected to be identical).  This file is collected last so a run
+tests (relative L1 <= 1e-10 per field; both the FP64 and the split path give
+the same bits for any row pitch and tile variant, so the results are
+expected to be identical), in FP64 and split precision.  This file is collected last so a run
 that stops at the first failure has already run every other test.
 """
 import ctypes
@@ -25,7 +26,7 @@ from microfc_gb300 import Simulation, _lib, cases, preprocess
 TOL = 1e-10
 
 
-def _params(case, x_cb, y_cb):
+def _params(case, x_cb, y_cb, precision=None):
     P = _lib.MfcParams()
     P.m, P.n, P.p = case.m, case.n, case.p
     P.num_fluids = case.num_fluids
@@ -41,25 +42,33 @@ def _params(case, x_cb, y_cb):
     P.x_cb = x_cb.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     if y_cb is not None:
         P.y_cb = y_cb.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-    P.precision = _lib.MFC_PREC_FP64
+    P.precision = _lib.MFC_PREC_FP64 if precision is None else precision
     P.device = 0
     return P
 
 
+FP64, SPLIT = _lib.MFC_PREC_FP64, _lib.MFC_PREC_SPLIT
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("builder", [
-    lambda: cases.shock_droplet_2d(nx=96, ny=64, steps=2),
-    lambda: cases.sod_1d(m=299, steps=2, dt=1e-4),
-    lambda: cases.shock_droplet_2d(nx=64, ny=40, steps=2).replace(time_stepper=2, bc_x=(-2, -4)),
-])
-def test_noalloc_step_matches_regular_entry_point_twice_in_a_row(builder):
+@pytest.mark.parametrize("builder,precision,pad", [
+    (lambda: cases.shock_droplet_2d(nx=96, ny=64, steps=2), FP64, 3),
+    (lambda: cases.sod_1d(m=299, steps=2, dt=1e-4), FP64, 3),
+    (lambda: cases.shock_droplet_2d(nx=64, ny=40, steps=2).replace(time_stepper=2, bc_x=(-2, -4)), FP64, 3),
+    # split precision: an odd row pitch (no tensor map; plain tile loads) and
+    # an even one (interior tiles staged by the TMA copy over the caller's array)
+    (lambda: cases.shock_droplet_2d(nx=96, ny=64, steps=2), SPLIT, 3),
+    (lambda: cases.shock_droplet_2d(nx=96, ny=64, steps=2), SPLIT, 4),
+    (lambda: cases.sod_1d(m=299, steps=2, dt=1e-4), SPLIT, 3),
+], ids=["droplet-fp64", "sod-fp64", "droplet-rk2-fp64", "droplet-split-odd", "droplet-split-even", "sod-split"])
+def test_noalloc_step_matches_regular_entry_point_twice_in_a_row(builder, precision, pad):
     import torch
 
     case = builder()
     x_cb, y_cb, _, q0 = preprocess.generate(case)
     L = _lib.load()
-    P = _params(case, x_cb, y_cb)
-    ld_y = case.m + 1 + 3  # a row pitch other than the regular path's
+    P = _params(case, x_cb, y_cb, precision)
+    ld_y = case.m + 1 + pad  # a row pitch other than the regular path's
     shape = (case.sys_size, case.p + 1, case.n + 1, ld_y)
     host = np.zeros(shape)
     host[..., : case.m + 1] = q0
@@ -79,7 +88,8 @@ def test_noalloc_step_matches_regular_entry_point_twice_in_a_row(builder):
     assert rc == 0, L.mfc_gpu_last_error().decode()
     two = a.cpu().numpy()[..., : case.m + 1].copy()
 
-    with Simulation(case, x_cb, y_cb, q_cons=q0) as sim:
+    regular = case.replace(precision="fp64" if precision == FP64 else "split")
+    with Simulation(regular, x_cb, y_cb, q_cons=q0) as sim:
         sim.tvd_rk(0)
         ref1 = sim.download()
         sim.tvd_rk(1)
@@ -110,3 +120,16 @@ def test_noalloc_rejects_cases_beyond_its_scratch():
     assert "4096 cells" in L.mfc_gpu_last_error().decode()
     rc = L.mfc_gpu_tvd_rk_noalloc(ctypes.byref(P), fake_in, fake_in, 64, 1e-9, None)
     assert rc == _lib.MFC_ERR_INVALID
+
+
+def test_noalloc_refuses_the_gated_precision_before_any_device_call():
+    """The gate's parameters live in a context, so the no-allocation step has
+    none to give the gated kernel: it must refuse the precision up front
+    (the fake device pointers below are never dereferenced)."""
+    L = _lib.load()
+    case = cases.shock_droplet_2d(nx=64, ny=32, steps=2, dt=1e-9)
+    x_cb, y_cb, _, _ = preprocess.generate(case)
+    P = _params(case, x_cb, y_cb, _lib.MFC_PREC_GATED)
+    rc = L.mfc_gpu_tvd_rk_noalloc(ctypes.byref(P), ctypes.c_void_p(0x1000), ctypes.c_void_p(0x2000), 64, 1e-9, None)
+    assert rc == _lib.MFC_ERR_INVALID
+    assert "gate" in L.mfc_gpu_last_error().decode()
