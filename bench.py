@@ -10,13 +10,17 @@ interior cells x steps / seconds.
 * e2e     -- the same through the public API with host buffers: every step
              uploads the state from pinned host memory, advances one step and
              downloads the state (all inside the timed region).
-* roofline     -- HBM roofline of the stage kernel (algorithmic 448 B per
-                  cell-update) against the measured copy bandwidth.
-* compute_roofline -- the bound that actually limits this path: algorithmic
-                  flops per cell-update (counted by the oracle) x rate vs the
-                  FP64 (or, split precision, FP32) FMA peak measured in-process.
-* cpu_baseline -- the oracle (C++ restatement of the reference's CPU code,
-                  OpenMP over the host cores) on a 1024 x 64 strip.
+* roofline     -- the slower-of roofline of the stage kernel: algorithmic
+                  flops per launch (counted by the oracle) / the launch's
+                  CUDA-event duration against the FP64 (split precision:
+                  FP32) FMA peak measured in-process, with the HBM figure
+                  (algorithmic 448 B per cell-update against the measured
+                  copy bandwidth) beside it; "bound" names whichever of the
+                  two the kernel is closer to.
+* cpu_baseline -- the oracle (C++ restatement of the reference's CPU code)
+                  built with the reference's Release flags (-O3, -march /
+                  -mcpu=native, default FMA contraction), OpenMP over the host
+                  cores, on the full 1024 x 512 grid.
 
 ``--impl reference`` times that CPU implementation alone and prints the
 reference arm's line.  Under torchrun (N > 1) every rank runs an independent
@@ -136,38 +140,41 @@ def replica_rate(seconds: float, units_per_rank: int, ws: int, device: str = "cu
     return ws * units_per_rank / seconds, seconds
 
 
-def cpu_baseline(steps: int = 2, ny: int = 64):
-    """The oracle on a 1024 x ny strip of the workload, all host cores."""
+CPU_FLAGS = "g++ -O3 -march/-mcpu=native, default FMA contraction (the reference's Release flags), OpenMP"
+
+
+def _cpu_oracle():
+    """The oracle's Release-flag build on the full workload, all host cores."""
     import oracle
     from microfc_gb300 import cases, preprocess
-    full = cases.shock_droplet_2d(nx=NX, ny=NY)
-    case = cases.shock_droplet_2d(nx=NX, ny=ny, dt=full.dt)
+    case = cases.shock_droplet_2d(nx=NX, ny=NY)
     x_cb, y_cb, _, q = preprocess.generate(case)
-    o = oracle.Oracle(case, x_cb, y_cb, threads=os.cpu_count() or 1)
+    o = oracle.Oracle(case, x_cb, y_cb, threads=os.cpu_count() or 1, build="native")
     o.set_state(q)
+    return o, case, oracle.lib("native").mfo_get_threads()
+
+
+def cpu_baseline(min_seconds: float = 10.0, max_steps: int = 400):
+    """Full RK3 steps of the 1024 x 512 workload on the host cores until
+    min_seconds of CPU work have run (at least 3 steps)."""
+    o, case, cores = _cpu_oracle()
     o.tvd_rk(case.dt)  # warm-up
-    t0 = time.perf_counter()
-    for _ in range(steps):
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps and (steps < 3 or time.perf_counter() - t0 < min_seconds):
         o.tvd_rk(case.dt)
+        steps += 1
     t = time.perf_counter() - t0
-    cores = oracle.lib().mfo_get_threads()
     return {"value": case.cells * steps / t, "unit": "cell-updates/s", "cores": cores, "kind": "port",
-            "sample": f"{steps} full RK3 time steps of the workload's physics on a {NX}x{ny} strip "
-                      f"(C++ restatement of the reference's CPU code, OpenMP over {cores} threads)"}
+            "flags": CPU_FLAGS, "same_config": True,
+            "sample": f"{steps} full RK3 time steps of the {NX}x{NY} workload (C++ restatement of the "
+                      f"reference's CPU code, OpenMP over {cores} threads)"}
 
 
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
-    import oracle
-    from microfc_gb300 import cases, preprocess
-    ny = 64
-    full = cases.shock_droplet_2d(nx=NX, ny=NY)
-    case = cases.shock_droplet_2d(nx=NX, ny=ny, dt=full.dt)
-    x_cb, y_cb, _, q = preprocess.generate(case)
-    o = oracle.Oracle(case, x_cb, y_cb, threads=os.cpu_count() or 1)
-    o.set_state(q)
+    o, case, cores = _cpu_oracle()
     for _ in range(args.warmup):
         o.tvd_rk(case.dt)
     t0 = time.perf_counter()
@@ -175,15 +182,17 @@ def run_reference(args):
         o.tvd_rk(case.dt)
     t = time.perf_counter() - t0
     v = case.cells * args.steps / t
-    cores = oracle.lib().mfo_get_threads()
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps * (NY / ny),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample": f"{NX}x{ny} strip per step", "l2": "n/a (CPU)"},
-        "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} RK3 steps on a {NX}x{ny} strip of the workload; the reference "
-                                   "(Fortran) cannot be built here, so its C++ restatement (the oracle) runs"},
+        "config": {"workload": WORKLOAD, "cells": case.cells, "sample": f"the full {NX}x{NY} grid every step",
+                   "l2": "n/a (CPU)", "flags": CPU_FLAGS},
+        "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": cores, "kind": "port", "flags": CPU_FLAGS,
+                         "same_config": True,
+                         "sample": f"{args.steps} RK3 steps of the full {NX}x{NY} workload; the reference "
+                                   "(Fortran + Fypp) cannot be built here, so its C++ restatement (the oracle) "
+                                   "runs, built with the reference's Release flags"},
         "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -233,10 +242,30 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
                          "vs_plain_fp64": rate / fp64_rate, "tile_variant": variant, "tma_staging": tma}
     if params is None:
         out["gated"] = {"unavailable": "no trained gate parameters (python -m microfc_gb300.gate)"}
+    # config 4's grid: the droplet at 2048 x 1024 (7 equations, 117 MB per
+    # register), gated against split and plain FP64 on the same case; the
+    # device initial condition avoids a host pre_process of 2 M cells
+    from microfc_gb300 import cases
+    c4 = cases.shock_droplet_2d(nx=2048, ny=1024)
+    r4, v4 = {}, {}
+    for prec4, n4 in (("fp64", 4), ("split", 20)) + ((("gated", 20),) if params is not None else ()):
+        with Simulation(c4.replace(precision=prec4), ic="device") as s:
+            if prec4 == "gated":
+                s.set_gate(params)
+            v4[prec4], _ = s.tune(3)
+            s.select_variant(v4[prec4])
+            st = torch.cuda.ExternalStream(s.stream)
+            r4[prec4] = c4.cells * n4 / _time_steps(s, st, flush, n4, 3, c4.dt)
+    out["config4_2048x1024"] = {
+        "workload": "2D shock-droplet 2048x1024, 2 fluids, WENO5-JS + HLLC + TVD-RK3",
+        "unit": "cell-updates/s", "plain_fp64": r4["fp64"], "split": r4["split"],
+        "tile_variants": v4, "timing": "CUDA events per step on the library's stream, L2 flushed between steps"}
+    if "gated" in r4:
+        out["config4_2048x1024"].update(gated=r4["gated"], gated_vs_plain_fp64=r4["gated"] / r4["fp64"],
+                                        gated_vs_split=r4["gated"] / r4["split"])
     # config 3: the 3-D air/helium shock-bubble at 256^3, split precision,
     # against plain FP64 on the same case (states of 1 GB per register: no
     # L2 reuse between steps)
-    from microfc_gb300 import cases
     c3 = cases.shock_bubble_3d(N=256, steps=500, precision="split")
     r3, v3 = {}, {}
     for prec3, n3 in (("split", 10), ("fp64", 2)):
@@ -379,10 +408,13 @@ def main():
 
     # ---- rooflines ---------------------------------------------------------------------
     hbm, peak_kind = _peaks()
-    per_launch_s = t_total / launches
+    per_launch_s = t_total / launches  # every timed launch is the stage kernel
     achieved = BYTES_PER_CELL_UPDATE * cells / 3 / per_launch_s / 1e9
     traffic = _profile_value("stage_kernel_fp64_droplet_1024x512.md", "dram_bytes_per_launch")
     flops = _profile_value("flop_count_droplet_1024x512.md", "algorithmic_flops_per_cell_update")
+    hbm_roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": traffic, "bytes_per_cell_update": BYTES_PER_CELL_UPDATE,
+                "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"}
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -396,25 +428,32 @@ def main():
                             "tma_staging": bool(sim.variant_features(variant) & _lib.MFC_VARIANT_TMA)}},
         "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes, "steps": e2e_steps},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
-                     if peak_kind == "measured" else "fallback"},
+        "roofline": hbm_roof,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
     if flops:
+        # algorithmic flops of one launch (a third of a cell-update per cell)
+        # over the launch's average CUDA-event duration
         peak = fp64_peak if args.precision == "fp64" else fp32_peak
-        ach = flops * value / ws / 1e12
-        line["compute_roofline"] = {
+        ach = flops * cells / 3 / per_launch_s / 1e12
+        compute = {
             "bound": "fp64" if args.precision == "fp64" else "fp32", "achieved": ach, "peak": peak,
-            "unit": "TFLOP/s", "frac": ach / peak, "flops_per_cell_update": flops,
-            "peak_kind": "measured in-process (FMA chains, mfc_gpu_measure_peaks)",
-            "peaks_measured": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak},
+            "unit": "TFLOP/s", "frac": ach / peak, "traffic": traffic, "flops_per_cell_update": flops,
+            "peak_kind": "measured in-process (FMA chains, mfc_gpu_measure_peaks; MEASURED_PEAKS.json has no "
+                         "FP64/FP32 entry)",
+            "peaks_measured": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak}}
+        if args.precision == "fp64":
             # the peak counts an FMA as 2 flops; the bit-faithful path may fuse
             # nothing, so each algorithmic add or mul needs its own FP64 pipe
-            # instruction (divisions run on the integer pipes): against that
-            # instruction ceiling, half the flop peak
-            "issue_frac": ach / (peak / 2.0)}
+            # instruction (divisions run on the integer pipes): its ceiling is
+            # half the flop peak
+            compute["no_fma_ceiling_frac"] = ach / (peak / 2.0)
+        # the slower-of roofline: the bound the kernel is closer to
+        if compute["frac"] >= hbm_roof["frac"]:
+            line["roofline"] = dict(compute, hbm=hbm_roof)
+        else:
+            line["roofline"] = dict(hbm_roof, compute=compute)
     sim.close()
     if not args.no_modes and args.precision == "fp64":
         line["modes"] = other_modes(args, case, x_cb, y_cb, q0, flush, value / ws)

@@ -18,8 +18,13 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "libmfc_oracle.so")
+# the same sources built with the reference's Release flags (-O3, -march /
+# -mcpu=native, default FMA contraction): the timed CPU baseline, and the
+# stand-in for a default-flag CPU build of the reference
+_LIB_NATIVE_PATH = os.path.join(_HERE, "libmfc_oracle_native.so")
+_PATHS = {"exact": _LIB_PATH, "native": _LIB_NATIVE_PATH}
 _lock = threading.Lock()
-_lib = None
+_libs = {}
 
 MAX_FLUIDS = 4
 MAX_PATCHES = 10
@@ -63,26 +68,27 @@ class MfoPatch(ctypes.Structure):
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (g++ only; a few seconds)."""
+    """Compile both oracle builds with their Makefile (g++ only; seconds)."""
     with _lock:
-        if force or not os.path.exists(_LIB_PATH) or _stale():
+        if force or any(not os.path.exists(p) or _stale(p) for p in _PATHS.values()):
             subprocess.run(["make", "-s", "-C", _HERE, "-j4"], check=True)
     return _LIB_PATH
 
 
-def _stale() -> bool:
-    t = os.path.getmtime(_LIB_PATH)
+def _stale(path: str) -> bool:
+    t = os.path.getmtime(path)
     for f in os.listdir(_HERE):
-        if f.endswith((".cpp", ".hpp")) and os.path.getmtime(os.path.join(_HERE, f)) > t:
+        if f.endswith((".cpp", ".hpp", "Makefile")) and os.path.getmtime(os.path.join(_HERE, f)) > t:
             return True
     return False
 
 
-def lib():
-    global _lib
-    if _lib is None:
+def lib(variant: str = "exact"):
+    """The oracle library: "exact" (no FMA contraction; the parity oracle) or
+    "native" (the reference's Release flags)."""
+    if variant not in _libs:
         build()
-        L = ctypes.CDLL(_LIB_PATH)
+        L = ctypes.CDLL(_PATHS[variant])
         dp = ctypes.POINTER(ctypes.c_double)
         L.mfo_create.restype = ctypes.c_void_p
         L.mfo_create.argtypes = [ctypes.POINTER(MfoParams), dp, dp, dp]
@@ -100,10 +106,12 @@ def lib():
         L.mfo_generate_ic.argtypes = [ctypes.POINTER(MfoParams), ctypes.POINTER(MfoPatch), ctypes.c_int,
                                       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double, ctypes.c_double, dp, dp, dp, dp, dp]
+        L.mfo_weno.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, dp, dp]
+        L.mfo_riemann.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp, dp]
         L.mfo_count_ops.restype = ctypes.c_int
         L.mfo_count_ops.argtypes = [ctypes.POINTER(MfoParams), dp, dp, dp, dp, ctypes.c_double, dp]
-        _lib = L
-    return _lib
+        _libs[variant] = L
+    return _libs[variant]
 
 
 def _dp(a):
@@ -136,8 +144,9 @@ def params_from_case(case) -> MfoParams:
 class Oracle:
     """The oracle solver for one case (state of shape [S, p+1, n+1, m+1])."""
 
-    def __init__(self, case, x_cb, y_cb=None, z_cb=None, threads: int = 0):
-        L = lib()
+    def __init__(self, case, x_cb, y_cb=None, z_cb=None, threads: int = 0, build: str = "exact"):
+        self._L = L = lib(build)
+        self.build = build
         if threads:
             L.mfo_set_threads(int(threads))
         self.case = case
@@ -152,37 +161,61 @@ class Oracle:
 
     def close(self):
         if getattr(self, "_h", None):
-            lib().mfo_destroy(self._h)
+            self._L.mfo_destroy(self._h)
             self._h = None
 
     __del__ = close
 
     def set_state(self, q, reg: int = 0):
         a = np.ascontiguousarray(q, dtype=np.float64).reshape(self.shape)
-        lib().mfo_set_state(self._h, reg, _dp(a))
+        self._L.mfo_set_state(self._h, reg, _dp(a))
 
     def get_state(self, reg: int = 0):
         a = np.empty(self.shape, dtype=np.float64)
-        lib().mfo_get_state(self._h, reg, _dp(a))
+        self._L.mfo_get_state(self._h, reg, _dp(a))
         return a
 
     def compute_rhs(self, reg: int = 0):
         rhs = np.empty(self.shape, dtype=np.float64)
         prim = np.empty(self.shape, dtype=np.float64)
-        lib().mfo_compute_rhs(self._h, reg, _dp(rhs), _dp(prim))
+        self._L.mfo_compute_rhs(self._h, reg, _dp(rhs), _dp(prim))
         return rhs, prim
 
+    def face_shape(self, dir: int, faces: bool = False):
+        """[S, p+1, n+1, m+1] with the extent along dir widened to the face
+        window: cells -1 .. s+1 (faces=False) or faces -1/2 .. s+1/2."""
+        shape = list(self.shape)
+        shape[3 - dir] += 1 if faces else 2
+        return tuple(shape)
+
+    def weno(self, dir: int, reg: int = 0):
+        """s_weno of register reg along dir over the face window: (vL, vR)."""
+        shape = self.face_shape(dir)
+        vl, vr = np.empty(shape), np.empty(shape)
+        self._L.mfo_weno(self._h, reg, dir, _dp(vl), _dp(vr))
+        return vl, vr
+
+    def riemann(self, dir: int, qL_rs, qR_rs):
+        """s_hllc_riemann_solver along dir: (flux [S, ...], flux_src [...])."""
+        shape = self.face_shape(dir)
+        a = np.ascontiguousarray(qL_rs, dtype=np.float64).reshape(shape)
+        b = np.ascontiguousarray(qR_rs, dtype=np.float64).reshape(shape)
+        fshape = self.face_shape(dir, faces=True)
+        flux, src = np.empty(fshape), np.empty(fshape[1:])
+        self._L.mfo_riemann(self._h, dir, _dp(a), _dp(b), _dp(flux), _dp(src))
+        return flux, src
+
     def tvd_rk(self, dt: float, last_step: bool = False):
-        lib().mfo_tvd_rk(self._h, float(dt), int(bool(last_step)))
+        self._L.mfo_tvd_rk(self._h, float(dt), int(bool(last_step)))
 
     def run(self, t_step_start: int, t_step_stop: int, dt: float) -> float:
-        return lib().mfo_run(self._h, int(t_step_start), int(t_step_stop), float(dt))
+        return self._L.mfo_run(self._h, int(t_step_start), int(t_step_stop), float(dt))
 
     def count_ops(self, state, dt: float):
         """Operation counts per interior cell for one full time step."""
         a = np.ascontiguousarray(state, dtype=np.float64).reshape(self.shape)
         out = np.zeros(5, dtype=np.float64)
-        lib().mfo_count_ops(ctypes.byref(self._q), *(_dp(c) for c in self._cb), _dp(a), float(dt), _dp(out))
+        self._L.mfo_count_ops(ctypes.byref(self._q), *(_dp(c) for c in self._cb), _dp(a), float(dt), _dp(out))
         return dict(zip(("add", "mul", "div", "sqrt", "cmp"), out.tolist()))
 
 
