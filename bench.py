@@ -222,6 +222,7 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
     plain FP64, and the 64-case ensemble of config 5 against 64 sequential
     plain FP64 runs.  Accuracy of these modes against FP64 is asserted by
     tests/test_gpu_parity.py, tests/test_gate.py and tests/test_ensemble.py."""
+    import numpy as np
     import torch
     from microfc_gb300 import Simulation, _lib, gate
     from microfc_gb300.ensemble import Ensemble, random_droplet_cases
@@ -242,6 +243,30 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
                          "vs_plain_fp64": rate / fp64_rate, "tile_variant": variant, "tma_staging": tma}
     if params is None:
         out["gated"] = {"unavailable": "no trained gate parameters (python -m microfc_gb300.gate)"}
+    # the opt-in contracted FP64 variant: rate, its FP64 roofline fraction,
+    # and its distance from the plain (bit-faithful) path after 100 steps
+    flops = _profile_value("flop_count_droplet_1024x512.md", "algorithmic_flops_per_cell_update")
+    fp64_peak, _ = _lib.measure_peaks(torch.cuda.current_device())
+    with Simulation(case.replace(precision="fp64_fma"), x_cb, y_cb, q_cons=q0) as s:
+        variant, _ = s.tune(5)
+        s.select_variant(variant)
+        st = torch.cuda.ExternalStream(s.stream)
+        t = _time_steps(s, st, flush, args.steps, args.warmup, case.dt)
+        rate = case.cells * args.steps / t
+        s.upload(q0)
+        s.run(0, 100)
+        q_fma = s.download()
+    with Simulation(case, x_cb, y_cb, q_cons=q0) as s:
+        s.run(0, 100)
+        q_plain = s.download()
+    a, b = q_fma.reshape(q_fma.shape[0], -1), q_plain.reshape(q_plain.shape[0], -1)
+    l1 = (np.abs(a - b).sum(axis=1) / np.abs(b).sum(axis=1)).tolist()
+    out["fp64_fma"] = {"value": rate, "unit": "cell-updates/s", "ms_per_step": 1e3 * t / args.steps,
+                       "vs_plain_fp64": rate / fp64_rate, "tile_variant": variant,
+                       "roofline": {"bound": "fp64", "achieved": flops * rate / 1e12 if flops else None,
+                                    "peak": fp64_peak, "unit": "TFLOP/s",
+                                    "frac": flops * rate / 1e12 / fp64_peak if flops else None},
+                       "rel_l1_vs_plain_fp64_100_steps": l1}
     # config 4's grid: the droplet at 2048 x 1024 (7 equations, 117 MB per
     # register), gated against split and plain FP64 on the same case; the
     # device initial condition avoids a host pre_process of 2 M cells

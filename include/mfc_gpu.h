@@ -17,6 +17,8 @@
  *   mfc_gpu_upload/download the "!$acc update device/host(q_cons_ts(1))" transfers
  *                           (src/simulation/p_main.fpp:191-193, 295-296)
  *   mfc_gpu_compute_rhs     s_compute_rhs (src/simulation/m_rhs.fpp:405-679)
+ *   mfc_gpu_weno            s_weno (src/simulation/m_weno.fpp:365-542)
+ *   mfc_gpu_riemann         s_hllc_riemann_solver (src/simulation/m_riemann_solvers.fpp:71-351)
  *   mfc_gpu_tvd_rk          s_1st/2nd/3rd_order_tvd_rk (m_time_steppers.fpp:129, 197, 271)
  *   mfc_gpu_run             the time-stepping loop of p_main (p_main.fpp:196-318)
  *   mfc_gpu_status          the NaN scan of p_main.fpp:295-305 (as a device flag)
@@ -57,6 +59,8 @@ extern "C" {
 #define MFC_PREC_FP64 0  /* plain FP64 everywhere (parity path)                       */
 #define MFC_PREC_SPLIT 1 /* FP32 WENO/HLLC; FP64 state, RK update, pressure recovery   */
 #define MFC_PREC_GATED 2 /* MFC_PREC_SPLIT + the learned WENO gate (2-D, WENO5)         */
+#define MFC_PREC_FP64_FMA 3 /* opt-in: FP64 with multiply-add contraction (2-D, WENO5);  */
+                            /* faster, no longer bit-identical to the parity oracle      */
 
 /*
  * Case parameters: the solver-relevant subset of the reference's &user_inputs
@@ -81,7 +85,7 @@ typedef struct mfc_params {
   const double* x_cb;       /* host, m+2 values                                           */
   const double* y_cb;       /* host, n+2 values, or NULL when n == 0                      */
   const double* z_cb;       /* host, p+2 values, or NULL when p == 0                      */
-  int32_t precision;        /* MFC_PREC_FP64 or MFC_PREC_SPLIT                            */
+  int32_t precision;        /* MFC_PREC_FP64, _SPLIT, _GATED or _FP64_FMA                  */
   int32_t device;           /* CUDA device ordinal (the reference binds local_rank % ndev) */
 } mfc_params;
 
@@ -117,6 +121,37 @@ int mfc_gpu_download_state(mfc_gpu_ctx* ctx, double* host_q);
  * NULL), both [S][p+1][n+1][m+1].  Uses the unfused sweep kernels; intended
  * for verification and for hosts that run their own time integrator. */
 int mfc_gpu_compute_rhs(mfc_gpu_ctx* ctx, double* rhs_out, double* prim_out);
+
+/* The two halves of a directional sweep, one call each, for hosts that call
+ * s_weno or s_hllc_riemann_solver on their own (a host with its own flux
+ * assembly, a verification harness that wants the face states).  Plain FP64
+ * (MFC_PREC_FP64 contexts without processor boundaries), the arithmetic of
+ * the fused kernels.  Face window of direction dir (0 = x, 1 = y, 2 = z; s =
+ * m, n or p along dir): the cells j = -1 .. s+1 along dir and the interior
+ * cells across it, host arrays [S][e2][e1][e0] (x fastest) with e_dir = s+3
+ * (cell j at index j+1) and the other extents m+1, n+1, p+1.
+ *
+ * Drop-in for s_weno(v_vf, vL_x, vL_y, vR_x, vR_y, weno_dir, is1, is2)
+ * (src/simulation/m_weno.fpp:365-542) as s_reconstruct_cell_boundary_values
+ * calls it (m_rhs.fpp:920-952), on the primitive variables of register 0
+ * with the case's boundary conditions in the ghost cells (m_rhs.fpp:434-447):
+ * vL / vR receive the left-face (x_{j-1/2}) and right-face (x_{j+1/2}) values
+ * over the face window, the part of the reference's is1 x is2 window that the
+ * Riemann solver reads. */
+int mfc_gpu_weno(mfc_gpu_ctx* ctx, int dir, double* vL, double* vR);
+
+/* Drop-in for s_hllc_riemann_solver (src/simulation/m_riemann_solvers.fpp:
+ * 71-351, inviscid contexts) with its Riemann-state buffers of bc -4
+ * (:444-619).  qL_rs / qR_rs are its qL_prim_rs / qR_prim_rs over the face
+ * window: the state left of face j+1/2 is qL_rs(j), the state right of it
+ * qR_rs(j+1).  s_compute_rhs passes the right-face WENO values as qL_prim_rs
+ * and the left-face values as qR_prim_rs (m_rhs.fpp:545-556): qL_rs = vR and
+ * qR_rs = vL of mfc_gpu_weno.  Outputs for the faces j+1/2, j = -1 .. s
+ * (index j+1, extent s+2 along dir): flux [S][...] (flux_vf) and flux_src
+ * [...] = flux_src_vf(advxb), the interface velocity vel_src(dir) of the
+ * alpha*div(u) source (:314-325). */
+int mfc_gpu_riemann(mfc_gpu_ctx* ctx, int dir, const double* qL_rs, const double* qR_rs, double* flux,
+                    double* flux_src);
 
 /* Drop-in for s_{1,2,3}_order_tvd_rk(t_step, time_avg): one full time step of
  * register 0 with time step dt, as fused stage kernels (one launch per RK
@@ -173,6 +208,22 @@ int mfc_gpu_status(mfc_gpu_ctx* ctx, uint32_t* flags, int clear);
  * 2-D contexts, with or without processor boundaries; all-zero Reynolds
  * numbers switch back to the inviscid kernels.  Call before stepping. */
 int mfc_gpu_set_viscosity(mfc_gpu_ctx* ctx, const double* re_shear, const double* re_bulk);
+
+/* Variables the WENO reconstruction works on (no reference counterpart: the
+ * reference reconstructs the primitive variables, m_weno.fpp:470-536).
+ * MFC_RECON_CHARACTERISTIC projects each cell's stencil on the
+ * characteristic fields of the quasi-linear primitive system along the sweep
+ * direction, frozen at the cell's own state -- alpha_i rho_i - kappa_i p
+ * (kappa_i = alpha_i rho_i / (rho c^2)), p -/+ rho c u_n, the tangential
+ * velocities and the volume fractions, with the mixture sound speed
+ * c^2 = ((Gamma + 1) p + Pi) / (Gamma rho) of the HLLC solver -- reconstructs
+ * them with the same WENO weights and maps both face values back.  Plain
+ * FP64 contexts, 1-D and 2-D, WENO3 or WENO5, inviscid, without processor
+ * boundaries (WENO1 reconstructs nothing and keeps the primitive kernel).
+ * Call before stepping; MFC_RECON_PRIMITIVE switches back. */
+#define MFC_RECON_PRIMITIVE 0
+#define MFC_RECON_CHARACTERISTIC 1
+int mfc_gpu_set_reconstruction(mfc_gpu_ctx* ctx, int variables);
 
 /* Split and gated WENO5 on a uniform grid (no reference counterpart): when
  * every cell of a direction has the same FP32 coefficient record, the

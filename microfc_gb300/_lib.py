@@ -17,7 +17,7 @@ MFC_PREC_FP64, MFC_PREC_SPLIT = 0, 1
 EXPORTS = (
     "mfc_gpu_abi_version", "mfc_gpu_last_error", "mfc_gpu_init", "mfc_gpu_sys_size",
     "mfc_gpu_upload", "mfc_gpu_download", "mfc_gpu_upload_state", "mfc_gpu_download_state",
-    "mfc_gpu_compute_rhs", "mfc_gpu_tvd_rk", "mfc_gpu_run", "mfc_gpu_status", "mfc_gpu_stream",
+    "mfc_gpu_compute_rhs", "mfc_gpu_weno", "mfc_gpu_riemann", "mfc_gpu_set_reconstruction", "mfc_gpu_tvd_rk", "mfc_gpu_run", "mfc_gpu_status", "mfc_gpu_stream",
     "mfc_gpu_launch_count", "mfc_gpu_finalize", "mfc_gpu_measure_peaks", "mfc_gpu_tvd_rk_noalloc",
     "mfc_gpu_selftest_div",
     "mfc_gpu_tune", "mfc_gpu_ensemble_init", "mfc_gpu_ensemble_upload", "mfc_gpu_ensemble_download",
@@ -30,6 +30,8 @@ EXPORTS = (
     "mfc_gpu_set_viscosity", "mfc_gpu_set_uniform_coefficients", "mfc_gpu_ensemble_select_variant", "mfc_gpu_ensemble_variant_features",
 )
 MFC_PREC_GATED = 2
+MFC_PREC_FP64_FMA = 3
+MFC_RECON_PRIMITIVE, MFC_RECON_CHARACTERISTIC = 0, 1
 MFC_VARIANT_TMA = 0x1
 
 
@@ -114,6 +116,9 @@ def load(build_if_missing: bool = True):
     L.mfc_gpu_upload_state.argtypes = [vp, dp]
     L.mfc_gpu_download_state.argtypes = [vp, dp]
     L.mfc_gpu_compute_rhs.argtypes = [vp, dp, dp]
+    L.mfc_gpu_weno.argtypes = [vp, ctypes.c_int, dp, dp]
+    L.mfc_gpu_set_reconstruction.argtypes = [vp, ctypes.c_int]
+    L.mfc_gpu_riemann.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
     L.mfc_gpu_tvd_rk.argtypes = [vp, ctypes.c_double, ctypes.c_int]
     L.mfc_gpu_run.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp]
     L.mfc_gpu_status.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32), ctypes.c_int]

@@ -34,6 +34,9 @@ def unit_flags(src: str) -> list[str]:
     paths of one kernel could round the same cell differently."""
     if src.endswith("_fp32.cu"):
         return ["-prec-div=false", "-prec-sqrt=false", "-ftz=true", "-fmad=false"]
+    if src.endswith("_fp64fma.cu"):
+        # the opt-in contracted FP64 variant (MFC_PREC_FP64_FMA)
+        return ["-fmad=true"]
     return ["-fmad=false"]
 
 

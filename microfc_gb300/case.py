@@ -76,7 +76,12 @@ class Case:
     patches: list = field(default_factory=list)
     stretch_x: tuple = ()               # (a_x, x_a, x_b, loops_x) of a stretched x grid; () = uniform
     stretch_y: tuple = ()               # (a_y, y_a, y_b, loops_y)
-    precision: str = "fp64"             # "fp64", "split" or "gated" (split + learned WENO gate)
+    precision: str = "fp64"             # "fp64", "split", "gated" (split + learned WENO gate) or
+                                        # "fp64_fma" (FP64 with multiply-add contraction, 2-D WENO5)
+    # WENO of the characteristic fields instead of the primitive variables
+    # (case key "char_decomp"; no counterpart in the reference, which
+    # reconstructs primitive variables): FP64 1-D and 2-D, WENO3/5
+    char_decomp: bool = False
     name: str = "case"
 
     # index layout, m_global_parameters.fpp:302-310
@@ -166,8 +171,10 @@ class Case:
                 bad("Unsupported value of fluid_pp(i)%gamma")
             if pi < 0:
                 bad("Unsupported value of fluid_pp(i)%pi_inf")
-        if self.precision not in ("fp64", "split", "gated"):
+        if self.precision not in ("fp64", "split", "gated", "fp64_fma"):
             bad("Unsupported value of precision mode")
+        if self.char_decomp and (self.precision != "fp64" or self.p > 0 or self.viscous or self.weno_order == 1):
+            bad("char_decomp needs plain FP64, an inviscid 1-D or 2-D case and WENO3 or WENO5")
         # grid stretching, m_start_up.fpp:238-330 (pre_process)
         for ax, st, dom, used in (("x", self.stretch_x, self.x_domain, True),
                                   ("y", self.stretch_y, self.y_domain, self.n > 0)):
@@ -280,7 +287,8 @@ class Case:
             bc_x=(int(g.get("bc_x%beg", -3)), int(g.get("bc_x%end", -3))), bc_y=bcy, bc_z=bcz,
             gammas=tuple(gam), pi_infs=tuple(pinf), re_shear=tuple(res[0]), re_bulk=tuple(res[1]), patches=plist,
             stretch_x=stretch.get("x", ()), stretch_y=stretch.get("y", ()),
-            precision=str(g.get("gpu_precision", "fp64")), name=str(g.get("case_name", "case")))
+            precision=str(g.get("gpu_precision", "fp64")), name=str(g.get("case_name", "case")),
+            char_decomp=str(g.get("char_decomp", "F")).strip().upper() in ("T", "TRUE", ".TRUE.", "1"))
 
     def to_namelist(self) -> str:
         """The &user_inputs namelist of the reference's simulation.inp."""

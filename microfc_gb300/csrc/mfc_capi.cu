@@ -44,21 +44,23 @@ void build_registry() {
     mfc::register_stage_1d_fp64(g_reg);
     mfc::register_stage_1d_fp32(g_reg);
     mfc::register_stage_2d_fp64(g_reg);
+    mfc::register_stage_2d_fp64fma(g_reg);
     mfc::register_stage_2d_fp32(g_reg);
     mfc::register_stage_3d_fp64(g_reg);
     mfc::register_stage_3d_fp32(g_reg);
     mfc::register_stage_visc_fp64(g_reg);
     mfc::register_stage_visc_fp32(g_reg);
+    mfc::register_stage_char_fp64(g_reg);
   });
 }
 
 }  // namespace
 
 namespace mfc {
-const StageEntry* find_stage(int nd, int nf, int wo, int prec, bool visc) {
+const StageEntry* find_stage(int nd, int nf, int wo, int prec, bool visc, bool chr) {
   build_registry();
   for (const auto& e : g_reg)
-    if (e.nd == nd && e.nf == nf && e.wo == wo && e.prec == prec && e.visc == visc) return &e;
+    if (e.nd == nd && e.nf == nf && e.wo == wo && e.prec == prec && e.visc == visc && e.chr == chr) return &e;
   return nullptr;
 }
 
@@ -150,6 +152,7 @@ struct mfc_gpu_ctx {
   double* rhs = nullptr;
   double* work = nullptr;       // 3-D: partial RHS between the directional sweeps
   void* gate_w = nullptr;       // MFC_PREC_GATED: FP16 gate parameters
+  uint8_t* gate_flags = nullptr;  // MFC_PREC_GATED: a step's first-stage gate decisions
   bool gate_ready = false;
   unsigned long long* monitor = nullptr;  // max ICFL of the monitored steps (double bits)
   bool monitor_on = false;
@@ -171,6 +174,7 @@ struct mfc_gpu_ctx {
   std::vector<double> cb_host[3];      // the cell boundaries passed at init
   std::vector<double> ghost_w[3][2];   // neighbour widths of processor boundaries
   mfc::ViscParams* visc = nullptr;     // device copy (viscous cases)
+  bool chr = false;                    // WENO of the characteristic fields
   size_t off_dcc[3] = {0, 0, 0};       // spacing tables inside `tables`
   mfc::DevParams dev{};
   mfc::UniformCoef ucoef{};        // uniform grids: the split kernels' shared coefficient records
@@ -179,6 +183,25 @@ struct mfc_gpu_ctx {
   const mfc::StageEntry* stage = nullptr;
   int64_t launches = 0;
 };
+
+namespace mfc {
+bool ctx_view(mfc_gpu_ctx* c, CtxView& v) {
+  if (!c) return false;
+  v.dev = &c->dev;
+  v.q0 = c->reg[0];
+  v.stream = c->stream;
+  v.nd = c->nd;
+  v.nf = c->prm.num_fluids;
+  v.wo = c->prm.weno_order;
+  v.S = c->S;
+  v.prec = c->prm.precision;
+  for (int d = 0; d < 3; ++d) v.n[d] = c->n[d];
+  v.visc = c->visc != nullptr;
+  v.has_proc = c->has_proc;
+  v.launches = &c->launches;
+  return true;
+}
+}  // namespace mfc
 
 namespace {
 
@@ -344,6 +367,9 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if (p->precision == MFC_PREC_GATED && (e = cudaMalloc(&c->gate_w, mfc::kGateBufferBytes)) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
+  if (p->precision == MFC_PREC_GATED &&
+      (e = cudaMalloc(&c->gate_flags, mfc::gate_flag_bytes(c->n[0], c->n[1]))) != cudaSuccess)
+    return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if (c->nd == 3 && (e = cudaMalloc(&c->work, sizeof(double) * c->reg_elems)) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if ((e = cudaMalloc(&c->monitor, sizeof(unsigned long long))) != cudaSuccess)
@@ -415,7 +441,8 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
   c->ucoef = c->ucoef_found;
   D.coff = mfc::kCoefPad;
   D.status = c->status;
-  D.work = c->work;
+  D.work = c->work;  // shares its slot with gate_flags: set the one in use
+  if (c->gate_flags) D.gate_flags = c->gate_flags;
   D.gate_w = c->gate_w;
 
   if ((e = c->stage->prepare()) != cudaSuccess) return cleanup(fail(MFC_ERR_CUDA, cudaGetErrorString(e)));
@@ -638,6 +665,7 @@ int mfc_gpu_set_viscosity(mfc_gpu_ctx* c, const double* re_shear, const double* 
     return MFC_OK;
   }
   if (c->nd > 2) return fail(MFC_ERR_INVALID, "viscous terms are built for 1-D and 2-D cases");
+  if (c->chr) return fail(MFC_ERR_INVALID, "the characteristic-field reconstruction is inviscid");
   const mfc::StageEntry* e = mfc::find_stage(c->nd, nf, c->prm.weno_order, c->prm.precision, true);
   if (!e) return fail(MFC_ERR_INVALID, "no viscous kernel compiled for this fluid count / WENO order / precision");
   for (int d = 0; d < c->nd; ++d) V.dcc[d] = c->tables + c->off_dcc[d];
@@ -646,6 +674,25 @@ int mfc_gpu_set_viscosity(mfc_gpu_ctx* c, const double* re_shear, const double* 
   MFC_CUDA(cudaMemcpy(c->visc, &V, sizeof(V), cudaMemcpyHostToDevice));
   if (e->prepare() != cudaSuccess) return fail(MFC_ERR_CUDA, "viscous kernel does not fit on this device");
   c->dev.visc = c->visc;
+  c->stage = e;
+  return MFC_OK;
+}
+
+int mfc_gpu_set_reconstruction(mfc_gpu_ctx* c, int variables) {
+  if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  if (variables != MFC_RECON_PRIMITIVE && variables != MFC_RECON_CHARACTERISTIC)
+    return fail(MFC_ERR_INVALID, "variables must be MFC_RECON_PRIMITIVE or MFC_RECON_CHARACTERISTIC");
+  const bool chr = variables == MFC_RECON_CHARACTERISTIC && c->prm.weno_order > 1;
+  if (chr && c->visc) return fail(MFC_ERR_INVALID, "the characteristic-field reconstruction is inviscid");
+  if (chr && c->has_proc)
+    return fail(MFC_ERR_INVALID, "the characteristic-field reconstruction is built without processor boundaries");
+  const mfc::StageEntry* e =
+      mfc::find_stage(c->nd, c->prm.num_fluids, c->prm.weno_order, c->prm.precision, c->visc != nullptr, chr);
+  if (!e)
+    return fail(MFC_ERR_INVALID, "no characteristic-field kernel compiled for this configuration (FP64, 1-D or "
+                                 "2-D, WENO3 or WENO5)");
+  MFC_CUDA(e->prepare());
+  c->chr = chr;
   c->stage = e;
   return MFC_OK;
 }
@@ -746,7 +793,7 @@ int mfc_gpu_tune(mfc_gpu_ctx* c, int reps, int* variant_out, double* ms_out) {
   MFC_CUDA(cudaEventCreate(&b));
   for (const auto& e : g_reg) {
     if (e.nd != c->nd || e.nf != c->prm.num_fluids || e.wo != c->prm.weno_order || e.prec != c->prm.precision ||
-        e.visc != (c->visc != nullptr))
+        e.visc != (c->visc != nullptr) || e.chr != c->chr)
       continue;
     ++idx;
     if (e.prepare() != cudaSuccess) continue;
@@ -783,7 +830,7 @@ int mfc_gpu_select_variant(mfc_gpu_ctx* c, int variant, int* tx, int* ty, int* t
   int idx = -1;
   for (const auto& e : g_reg) {
     if (e.nd != c->nd || e.nf != c->prm.num_fluids || e.wo != c->prm.weno_order || e.prec != c->prm.precision ||
-        e.visc != (c->visc != nullptr))
+        e.visc != (c->visc != nullptr) || e.chr != c->chr)
       continue;
     if (++idx != variant) continue;
     if (e.prepare() != cudaSuccess) return fail(MFC_ERR_CUDA, "tile variant does not fit on this device");
@@ -801,7 +848,7 @@ int mfc_gpu_variant_features(mfc_gpu_ctx* c, int variant, uint32_t* features) {
   int idx = -1;
   for (const auto& e : g_reg) {
     if (e.nd != c->nd || e.nf != c->prm.num_fluids || e.wo != c->prm.weno_order || e.prec != c->prm.precision ||
-        e.visc != (c->visc != nullptr))
+        e.visc != (c->visc != nullptr) || e.chr != c->chr)
       continue;
     if (++idx != variant) continue;
     *features = e.tma ? MFC_VARIANT_TMA : 0u;
@@ -894,6 +941,7 @@ int mfc_gpu_finalize(mfc_gpu_ctx* c) {
   cudaFree(c->status);
   cudaFree(c->work);
   cudaFree(c->gate_w);
+  cudaFree(c->gate_flags);
   cudaFree(c->monitor);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;

@@ -34,7 +34,18 @@ struct DevParams {
                            // cells i = -kCoefPad .. n-1+kCoefPad, coff = kCoefPad
   int coff, cstride[3];
   uint32_t* status;
-  void* work;  // 3-D: partial RHS between the directional sweeps ([S][z][y][x], RT)
+  // The two never coexist (the gate runs on 2-D cases only), so they share
+  // one slot: the ensemble's 96 parameter blocks must fit the kernel
+  // parameter space.
+  union {
+    // 3-D: partial RHS between the directional sweeps ([S][z][y][x], RT)
+    void* work;
+    // learned WENO gate: the decisions of a time step's first stage, one
+    // byte per reconstructed cell and direction, reused by its later stages
+    // (NULL: every stage runs the network).  x plane [ny][nx + 2] (cells x =
+    // -1 .. nx), then y plane [ny + 2][nx] (cells y = -1 .. ny).
+    uint8_t* gate_flags;
+  };
   const void* gate_w;  // learned WENO gate: FP16 MLP parameters (mfc_gate.cuh layout)
   unsigned long long* monitor;  // set on a step's last stage: max ICFL of the new state (double bits)
   // processor boundaries (bc >= 0): device table of 6 halo buffers, [2*dir + side]
@@ -46,6 +57,11 @@ struct DevParams {
   const double* const* halo;
   const struct ViscParams* visc;  // viscous cases: Reynolds numbers and spacing tables (NULL: inviscid)
 };
+
+// Bytes of the stored gate decisions of an nx x ny case (DevParams::gate_flags).
+inline size_t gate_flag_bytes(int nx, int ny) {
+  return (size_t)ny * (size_t)(nx + 2) + (size_t)(ny + 2) * (size_t)nx;
+}
 
 // Rounds the EOS and WENO constants to FP32 once on the host (the split
 // path's reconstruction and Riemann solve read them as floats).

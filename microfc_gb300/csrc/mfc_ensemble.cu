@@ -54,6 +54,7 @@ struct mfc_gpu_ensemble {
   double* tables = nullptr;
   uint32_t* status = nullptr;
   void* gate_w = nullptr;  // MFC_PREC_GATED: FP16 gate parameters
+  uint8_t* gate_flags = nullptr;  // MFC_PREC_GATED: every case's first-stage gate decisions
   bool gate_ready = false;
   cudaStream_t stream = nullptr;
   const mfc::EnsembleEntry* entry = nullptr;
@@ -233,6 +234,11 @@ int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_ca
       (err = cudaMalloc(&e->maps, sizeof(mfc::TileMap) * 3 * (size_t)num_cases)) != cudaSuccess ||
       (c0.precision == MFC_PREC_GATED && (err = cudaMalloc(&e->gate_w, mfc::kGateBufferBytes)) != cudaSuccess))
     return cleanup(mfc::report_error(MFC_ERR_NOMEM, cudaGetErrorString(err)));
+  size_t flag_bytes = 0;
+  for (int i = 0; i < num_cases; ++i) flag_bytes += mfc::gate_flag_bytes(e->nx[i], e->ny[i]);
+  if (c0.precision == MFC_PREC_GATED && (err = cudaMalloc(&e->gate_flags, flag_bytes)) != cudaSuccess)
+    return cleanup(mfc::report_error(MFC_ERR_NOMEM, cudaGetErrorString(err)));
+  size_t flag_off = 0;
   cudaMemsetAsync(e->state, 0, sizeof(double) * state_elems, e->stream);
   cudaMemsetAsync(e->status, 0, sizeof(uint32_t), e->stream);
   for (int i = 0; i < num_cases; ++i) {
@@ -249,6 +255,8 @@ int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_ca
     }
     C.P.status = e->status;
     C.P.gate_w = e->gate_w;
+    C.P.gate_flags = e->gate_flags ? e->gate_flags + flag_off : nullptr;
+    flag_off += mfc::gate_flag_bytes(e->nx[i], e->ny[i]);
     C.dt = e->dt[i];
     C.dt_last = e->dt[i];
   }
@@ -444,6 +452,7 @@ int mfc_gpu_ensemble_finalize(mfc_gpu_ensemble* e) {
   cudaFree(e->tables);
   cudaFree(e->status);
   cudaFree(e->gate_w);
+  cudaFree(e->gate_flags);
   cudaFree(e->maps);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e->ep;

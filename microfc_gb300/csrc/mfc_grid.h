@@ -200,7 +200,7 @@ inline float d2f_trunc(double x) {
 inline void uniform_records(const GridTables& t, int nd, const int* n, int weno_order, int precision,
                             UniformCoef& U) {
   U = UniformCoef{};
-  if (precision == MFC_PREC_FP64 || weno_order != 5) return;
+  if (precision == MFC_PREC_FP64 || precision == MFC_PREC_FP64_FMA || weno_order != 5) return;
   for (int d = 0; d < nd; ++d) {
     const int cells = n[d] + 2 * kCoefPad;
     auto bits = [](float f) {
@@ -255,8 +255,11 @@ inline std::string validate_params(const mfc_params* p, bool allow_processor = f
   if (p->n > 0 && !p->y_cb) return "y_cb is NULL";
   if (p->p > 0 && !p->z_cb) return "z_cb is NULL";
   if (p->p > 0 && p->p + 1 < stcls) return "Unsupported combination of values of p and weno_order";
-  if (p->precision != MFC_PREC_FP64 && p->precision != MFC_PREC_SPLIT && p->precision != MFC_PREC_GATED)
+  if (p->precision != MFC_PREC_FP64 && p->precision != MFC_PREC_SPLIT && p->precision != MFC_PREC_GATED &&
+      p->precision != MFC_PREC_FP64_FMA)
     return "Unsupported precision";
+  if (p->precision == MFC_PREC_FP64_FMA && (p->n == 0 || p->p > 0 || p->weno_order != 5))
+    return "The contracted FP64 variant is compiled for 2-D WENO5 cases";
   if (p->precision == MFC_PREC_GATED && (p->n == 0 || p->p > 0 || p->weno_order != 5))
     return "The learned gate runs on 2-D WENO5 cases";
   return "";

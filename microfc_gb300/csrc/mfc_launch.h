@@ -11,6 +11,7 @@
 #include <type_traits>
 #include <utility>
 
+#include "../../include/mfc_gpu.h"
 #include "mfc_device.cuh"
 #include "mfc_stage.cuh"
 #include "mfc_sweep.cuh"
@@ -18,7 +19,7 @@
 namespace mfc {
 
 struct StageEntry {
-  int nd, nf, wo, prec;  // prec: 0 = FP64, 1 = split (FP32 WENO/HLLC)
+  int nd, nf, wo, prec;  // prec: an MFC_PREC_* value
   int tx, ty, nt;
   size_t smem;
   int kernels;  // kernel launches per RK stage (1 in 1-D/2-D, 3 sweeps in 3-D)
@@ -27,6 +28,7 @@ struct StageEntry {
                         double* qout, double dt, int kind, cudaStream_t st);
   bool visc = false;  // compiled with the viscous terms
   bool tma = false;   // interior tiles staged by a TMA bulk tensor copy
+  bool chr = false;   // WENO of the characteristic fields (MFC_RECON_CHARACTERISTIC)
 };
 
 // Launches a stage kernel with programmatic stream serialization, so that
@@ -49,15 +51,18 @@ cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, si
 }
 
 // MINB > 1 selects the register-capped kernel (stage_kernel_mb); TMA the
-// kernel that stages interior tiles with a bulk tensor copy.
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool VISC, bool TMA = false>
+// kernel that stages interior tiles with a bulk tensor copy; FMA the
+// instantiations compiled with multiply-add contraction (MFC_PREC_FP64_FMA).
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool VISC, bool TMA = false,
+          bool FMA = false, bool CHAR = false>
 constexpr auto stage_func() {
   static_assert(MINB == 1 || !VISC, "register-capped variants are inviscid");
   static_assert(!TMA || (ND == 2 && !VISC), "TMA staging is compiled for the inviscid 2-D kernel");
-  if constexpr (TMA && MINB > 1) return &stage_kernel_tma_mb<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>;
-  else if constexpr (TMA) return &stage_kernel_tma<ND, NF, WO, RT, TX, TY, NT, GATE>;
-  else if constexpr (MINB > 1) return &stage_kernel_mb<ND, NF, WO, RT, TX, TY, NT, GATE, MINB>;
-  else return &stage_kernel<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>;
+  static_assert(!CHAR || (!TMA && MINB == 1), "characteristic-field WENO uses the plain stage kernel");
+  if constexpr (TMA && MINB > 1) return &stage_kernel_tma_mb<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, FMA>;
+  else if constexpr (TMA) return &stage_kernel_tma<ND, NF, WO, RT, TX, TY, NT, GATE, FMA>;
+  else if constexpr (MINB > 1) return &stage_kernel_mb<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, FMA>;
+  else return &stage_kernel<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, FMA, CHAR>;
 }
 
 // Dynamic shared memory of a launch: without the coefficient records on a
@@ -68,15 +73,15 @@ constexpr size_t stage_launch_smem(bool shared_coef) {
 }
 
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false,
-          bool TMA = false>
+          bool TMA = false, bool FMA = false, bool CHAR = false>
 cudaError_t stage_prepare() {
-  return cudaFuncSetAttribute(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA>(),
+  return cudaFuncSetAttribute(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA, FMA, CHAR>(),
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)stage_launch_smem<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, TMA>(false));
 }
 
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false,
-          bool TMA = false>
+          bool TMA = false, bool FMA = false, bool CHAR = false>
 cudaError_t stage_launch(const DevParams& P, const UniformCoef& U, const double* qin, const double* qbase,
                          double* qout, double dt, int kind, cudaStream_t st) {
   const dim3 grid((unsigned)((P.n[0] + TX - 1) / TX), ND > 1 ? (unsigned)((P.n[1] + TY - 1) / TY) : 1u, 1u);
@@ -89,31 +94,34 @@ cudaError_t stage_launch(const DevParams& P, const UniformCoef& U, const double*
     using Sh = StageShape<ND, NF, WO, RT, TX, TY>;
     TileMap T{};
     encode_tile_map(T, qin, P.n[0], P.n[1], Sh::S, P.sy, P.sv, TmaBox<TX, Sh::H>::kWidth, Sh::LY);
-    return launch_dependent(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA>(), grid, dim3(NT), smem, st,
-                            P, U, T, qin, qbase, qout, dt, kind);
+    return launch_dependent(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA, FMA, CHAR>(), grid, dim3(NT), smem,
+                            st, P, U, T, qin, qbase, qout, dt, kind);
   } else {
-    return launch_dependent(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA>(), grid, dim3(NT), smem, st,
-                            P, U, qin, qbase, qout, dt, kind);
+    return launch_dependent(stage_func<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA, FMA, CHAR>(), grid, dim3(NT), smem,
+                            st, P, U, qin, qbase, qout, dt, kind);
   }
 }
 
-// prec of a registry entry: 0 FP64, 1 split, 2 split with the learned gate
+// prec of a registry entry: 0 FP64, 1 split, 2 split with the learned gate,
+// 3 FP64 with multiply-add contraction
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool VISC = false,
-          bool TMA = false>
+          bool TMA = false, bool FMA = false, bool CHAR = false>
 StageEntry stage_entry() {
+  static_assert(!FMA || sizeof(RT) == 8, "the contracted variant is FP64");
   return StageEntry{ND,
                     NF,
                     WO,
-                    sizeof(RT) == 8 ? 0 : (GATE ? 2 : 1),
+                    FMA ? 3 : sizeof(RT) == 8 ? 0 : (GATE ? 2 : 1),
                     TX,
                     TY,
                     NT,
                     stage_launch_smem<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, TMA>(false),
                     1,
-                    &stage_prepare<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA>,
-                    &stage_launch<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA>,
+                    &stage_prepare<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA, FMA, CHAR>,
+                    &stage_launch<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, VISC, TMA, FMA, CHAR>,
                     VISC,
-                    TMA};
+                    TMA,
+                    CHAR};
 }
 
 // 3-D: three directional sweeps per stage (mfc_sweep.cuh).  The x sweep uses
@@ -177,8 +185,21 @@ struct Sweep3D {
   }
 };
 
+// What the standalone entry points of other translation units need from a
+// context (mfc_gpu_ctx is private to mfc_capi.cu).
+struct CtxView {
+  const DevParams* dev = nullptr;  // the context's kernel parameters
+  const double* q0 = nullptr;      // register 0 (q_cons_ts(1))
+  cudaStream_t stream = nullptr;
+  int nd = 0, nf = 0, wo = 0, S = 0, prec = 0;
+  int n[3] = {1, 1, 1};
+  bool visc = false, has_proc = false;
+  int64_t* launches = nullptr;     // the context's launch counter
+};
+bool ctx_view(mfc_gpu_ctx* c, CtxView& v);
+
 // The default (first registered) launcher of a configuration, or nullptr.
-const StageEntry* find_stage(int nd, int nf, int wo, int prec, bool visc = false);
+const StageEntry* find_stage(int nd, int nf, int wo, int prec, bool visc = false, bool chr = false);
 
 // Records msg as the calling thread's mfc_gpu_last_error() and returns code.
 int report_error(int code, const std::string& msg);
@@ -193,10 +214,12 @@ int gate_upload(const float* host_params, void* dev_half, cudaStream_t st);
 void register_stage_1d_fp64(std::vector<StageEntry>& r);
 void register_stage_1d_fp32(std::vector<StageEntry>& r);
 void register_stage_2d_fp64(std::vector<StageEntry>& r);
+void register_stage_2d_fp64fma(std::vector<StageEntry>& r);
 void register_stage_2d_fp32(std::vector<StageEntry>& r);
 void register_stage_3d_fp64(std::vector<StageEntry>& r);
 void register_stage_3d_fp32(std::vector<StageEntry>& r);
 void register_stage_visc_fp64(std::vector<StageEntry>& r);
 void register_stage_visc_fp32(std::vector<StageEntry>& r);
+void register_stage_char_fp64(std::vector<StageEntry>& r);
 
 }  // namespace mfc

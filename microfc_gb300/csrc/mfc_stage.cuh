@@ -160,13 +160,89 @@ constexpr size_t stage_smem_total(bool shared_coef) {
          (shared_coef ? 0 : StageShape<ND, NF, WO, RT, TX, TY, VISC>::kCoefBytes);
 }
 
+// WENO of the characteristic fields at one position (FP64): the stencil of
+// the position's cell, at(v, o) = primitive variable v at offset o along DIR,
+// is projected on the characteristic fields of the quasi-linear primitive
+// system frozen at the cell's own state; each field is reconstructed with
+// the cell's coefficients; the face values are mapped back to primitive
+// variables into L(v) / R(v).  The fields (no counterpart in the
+// reference, which reconstructs the primitive variables) in the slots of
+// the primitive variables:
+//   partial density i: alpha_i rho_i - kappa_i p,  kappa_i = alpha_i rho_i / (rho c^2)
+//   normal momentum:   p - rho c u_n   (the u_n - c wave)
+//   energy:            p + rho c u_n   (the u_n + c wave)
+//   tangential velocities and volume fractions unchanged,
+// with rho = max(sum alpha_i rho_i, 1e-16), Gamma = sum alpha_i Gamma_i,
+// Pi = sum alpha_i Pi_i and c^2 = max(((Gamma + 1) p + Pi) / (Gamma rho),
+// 1e-16), the mixture sound speed of the HLLC solver.  Back:
+// p = (w+ + w-) 0.5, u_n = (w+ - w-) / (2 rho c), alpha_i rho_i = w_i + kappa_i p.
+// The oracle (Solver::weno with char_decomp) evaluates the same expressions
+// in the same order.
+template <int ND, int NF, int WO, int DIR, class At, class OutL, class OutR>
+__device__ __forceinline__ void char_weno_position(const double (&c)[kCoefRec], const At& at, const double eps,
+                                                   const DevParams& P, const OutL& L, const OutR& R) {
+  using Q = Eqs<ND, NF>;
+  constexpr int S = Q::S, UN = Q::MOM + DIR;
+  double rho = 0.0, gam = 0.0, pinf = 0.0;
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    rho = rho + at(f, 0);
+    gam = gam + at(Q::ADV + f, 0) * P.gammas[f];
+    pinf = pinf + at(Q::ADV + f, 0) * P.pi_infs[f];
+  }
+  rho = fmax(rho, 1e-16);
+  const double c2 = fmax(div_rn((gam + 1.0) * at(Q::E, 0) + pinf, divisor(gam * rho)), 1e-16);
+  const double rc = rho * sqrt(c2);
+  const DivisorF64 Dk = divisor(rho * c2);
+  double kap[NF];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) kap[f] = div_rn(at(f, 0), Dk);
+#pragma unroll 1
+  for (int v = 0; v < S; ++v) {
+    double st[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const int o = k - 2;
+      if (o < -(WO / 2) || o > WO / 2) {
+        st[k] = 0.0;
+      } else if (v < NF) {
+        double kv = kap[0];
+#pragma unroll
+        for (int f = 1; f < NF; ++f) kv = v == f ? kap[f] : kv;
+        st[k] = at(v, o) - kv * at(Q::E, o);
+      } else if (v == UN) {
+        st[k] = at(Q::E, o) - rc * at(UN, o);
+      } else if (v == Q::E) {
+        st[k] = at(Q::E, o) + rc * at(UN, o);
+      } else {
+        st[k] = at(v, o);
+      }
+    }
+    double vl, vr;
+    weno_cell<WO, double>(c, st, eps, vl, vr);
+    L(v) = vl;
+    R(v) = vr;
+  }
+  const DivisorF64 D2 = divisor(2.0 * rc);
+  auto back = [&](const auto& O) {
+    const double wm = O(UN), wp = O(Q::E);
+    const double pr = (wp + wm) * 0.5;
+    O(Q::E) = pr;
+    O(UN) = div_rn(wp - wm, D2);
+#pragma unroll
+    for (int f = 0; f < NF; ++f) O(f) = O(f) + kap[f] * pr;
+  };
+  back(L);
+  back(R);
+}
+
 // One tile of one RK stage; the tile's first cell is (x0, y0).  Used by the
 // single-case kernel (one tile per block) and by the ensemble kernel (many
 // tiles of many cases per persistent block).  smem_raw must hold
 // stage_smem_total() (of shared_coef = true when U covers every
 // direction).
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, bool VISC = false,
-          class UC = UniformCoef, bool TMA = false>
+          class UC = UniformCoef, bool TMA = false, bool CHAR = false>
 __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __restrict__ qin,
                                            const double* __restrict__ qbase, double* __restrict__ qout,
                                            const double dt, const int kind, const int x0, const int y0,
@@ -174,6 +250,8 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
                                            const TileMap* T = nullptr, uint32_t* tma_parity = nullptr) {
   static_assert(!GATE || (sizeof(RT) == 4 && WO == 5), "the learned gate runs on the split-precision WENO5 path");
   static_assert(!(GATE && VISC), "the gated kernel is inviscid");
+  static_assert(!CHAR || (sizeof(RT) == 8 && WO > 1 && !VISC && !GATE && ND < 3),
+                "characteristic-field WENO is compiled for the inviscid FP64 1-D/2-D WENO3/5 kernel");
   using Sh = StageShape<ND, NF, WO, RT, TX, TY, VISC>;
   using Q = Eqs<ND, NF>;
   constexpr int S = Sh::S, H = Sh::H, LX = Sh::LX, LY = Sh::LY, TYE = Sh::TYE;
@@ -369,52 +447,95 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   __syncthreads();
 
   // ---- learned gate: one flag per (cell, direction), tensor-core MLP -------
+  // The first stage of a time step (and an RHS evaluation) runs the network
+  // on every reconstructed position of the tile; with P.gate_flags it also
+  // stores the decisions, and the step's later stages read them back instead
+  // of running the network again: the gate judges each cell once per time
+  // step, on the state at t^n.  Every stored position (including the ghost
+  // positions x = -1, nx and y = -1, ny next to the domain) is written by
+  // exactly one tile.
   const uint8_t* gflag = nullptr;
   if constexpr (GATE) {
     using G = GateShape<ND, TX, TY, NT>;
-    static_assert(G::kScratchBytes <= 2 * sizeof(RT) * size_t(Sh::align16(Sh::NW)),
-                  "the gate's scratch must fit the WENO value arrays");
-    unsigned char* scratch = reinterpret_cast<unsigned char*>(wl);
-    __half* gin = reinterpret_cast<__half*>(scratch);
-    uint32_t* frag = reinterpret_cast<uint32_t*>(scratch + G::kFragOff);
+    constexpr int NG = G::NGX + G::NGY;
     uint8_t* flags = smem_raw + Sh::kMainBytes;
-    const int warp = tid >> 5, lane = tid & 31;
-    const uint32_t* gsrc =
-        reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(P.gate_w) + kGateFragOffset);
-    for (int i = tid; i < kGateFragWords * 8; i += NT)
-      reinterpret_cast<uint4*>(frag)[i] = __ldg(reinterpret_cast<const uint4*>(gsrc) + i);
-    __syncthreads();
-    const GateFragsSmem F{frag + 4 * lane};
-    __half* my = gin + warp * 256;
-    constexpr int NG = G::NGX + G::NGY, NCH = (NG + 15) / 16;
-    for (int ch = warp; ch < NCH; ch += NT / 32) {
-      const int cell = ch * 16 + (lane & 15);
-      const int var = lane < 16 ? Q::ADV : Q::E;  // alpha_1 | pressure
-      float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-      if (cell < G::NGX) {
-        const int cx = cell % (TX + 2), ty = cell / (TX + 2);
-#pragma unroll
-        for (int k = 0; k < 5; ++k) s[k] = sq[qi(var, (ND > 1) ? ty + H : 0, cx + H - 1 + k - 2)];
-      } else if (cell < NG) {
-        const int c2 = cell - G::NGX, tx = c2 % TX, cy = c2 / TX;
-#pragma unroll
-        for (int k = 0; k < 5; ++k) s[k] = sq[qi(var, cy + H - 1 + k - 2, tx + H)];
+    // position p of the tile: its slot in the stored planes (false: beyond
+    // the planes, a cell of a partial edge tile whose results are not kept)
+    // and whether this tile is the one that stores it
+    auto flag_slot = [&](const int p, int64_t& slot, bool& owner) {
+      if (p < G::NGX) {
+        const int cx = p % (TX + 2), ty = p / (TX + 2);
+        const int gx = x0 - 1 + cx, gy = y0 + ty;
+        slot = (int64_t)gy * (nx + 2) + (gx + 1);
+        owner = (cx >= 1 && cx <= TX) || gx == -1 || gx == nx;
+        return gx >= -1 && gx <= nx && gy < ny;
       }
-      float xf[5];
-      gate_norm5_var(s, xf, lane < 16 ? 0 : 1);
-      // columns 0..7 (alpha_1) or 8..15 (pressure) of the cell's row: five
-      // features and three zeros, one 16-byte store
-      const uint4 half8 = make_uint4(pack_h2(xf[0], xf[1]), pack_h2(xf[2], xf[3]), pack_h2(xf[4], 0.f), 0u);
-      reinterpret_cast<uint4*>(my + (lane & 15) * 16)[lane >> 4] = half8;
-      __syncwarp();
-      float lo, hi;
-      gate_mlp16(my, F, lo, hi);
-      if ((lane & 3) == 0) {
-        const int c_lo = ch * 16 + (lane >> 2), c_hi = c_lo + 8;
-        if (c_lo < NG) flags[c_lo] = lo > 0.f;
-        if (c_hi < NG) flags[c_hi] = hi > 0.f;
+      const int p2 = p - G::NGX, tx = p2 % TX, cy = p2 / TX;
+      const int gx = x0 + tx, gy = y0 - 1 + cy;
+      slot = (int64_t)ny * (nx + 2) + (int64_t)(gy + 1) * nx + gx;
+      owner = (cy >= 1 && cy <= TY) || gy == -1 || gy == ny;
+      return gx < nx && gy >= -1 && gy <= ny;
+    };
+    if (P.gate_flags != nullptr && kind != kRkEuler && kind != kRhsOnly) {
+      // a later stage of the step: the first stage's decisions
+      for (int p = tid; p < NG; p += NT) {
+        int64_t slot;
+        bool owner;
+        flags[p] = flag_slot(p, slot, owner) ? __ldg(P.gate_flags + slot) : uint8_t(1);
       }
-      __syncwarp();
+    } else {
+      static_assert(G::kScratchBytes <= 2 * sizeof(RT) * size_t(Sh::align16(Sh::NW)),
+                    "the gate's scratch must fit the WENO value arrays");
+      unsigned char* scratch = reinterpret_cast<unsigned char*>(wl);
+      __half* gin = reinterpret_cast<__half*>(scratch);
+      uint32_t* frag = reinterpret_cast<uint32_t*>(scratch + G::kFragOff);
+      const int warp = tid >> 5, lane = tid & 31;
+      const uint32_t* gsrc =
+          reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(P.gate_w) + kGateFragOffset);
+      for (int i = tid; i < kGateFragWords * 8; i += NT)
+        reinterpret_cast<uint4*>(frag)[i] = __ldg(reinterpret_cast<const uint4*>(gsrc) + i);
+      __syncthreads();
+      const GateFragsSmem F{frag + 4 * lane};
+      __half* my = gin + warp * 256;
+      constexpr int NCH = (NG + 15) / 16;
+      for (int ch = warp; ch < NCH; ch += NT / 32) {
+        const int cell = ch * 16 + (lane & 15);
+        const int var = lane < 16 ? Q::ADV : Q::E;  // alpha_1 | pressure
+        float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        if (cell < G::NGX) {
+          const int cx = cell % (TX + 2), ty = cell / (TX + 2);
+#pragma unroll
+          for (int k = 0; k < 5; ++k) s[k] = sq[qi(var, (ND > 1) ? ty + H : 0, cx + H - 1 + k - 2)];
+        } else if (cell < NG) {
+          const int c2 = cell - G::NGX, tx = c2 % TX, cy = c2 / TX;
+#pragma unroll
+          for (int k = 0; k < 5; ++k) s[k] = sq[qi(var, cy + H - 1 + k - 2, tx + H)];
+        }
+        float xf[5];
+        gate_norm5_var(s, xf, lane < 16 ? 0 : 1);
+        // columns 0..7 (alpha_1) or 8..15 (pressure) of the cell's row: five
+        // features and three zeros, one 16-byte store
+        const uint4 half8 = make_uint4(pack_h2(xf[0], xf[1]), pack_h2(xf[2], xf[3]), pack_h2(xf[4], 0.f), 0u);
+        reinterpret_cast<uint4*>(my + (lane & 15) * 16)[lane >> 4] = half8;
+        __syncwarp();
+        float lo, hi;
+        gate_mlp16(my, F, lo, hi);
+        if ((lane & 3) == 0) {
+          const int c_lo = ch * 16 + (lane >> 2), c_hi = c_lo + 8;
+          if (c_lo < NG) flags[c_lo] = lo > 0.f;
+          if (c_hi < NG) flags[c_hi] = hi > 0.f;
+        }
+        __syncwarp();
+      }
+      __syncthreads();
+      if (P.gate_flags != nullptr && kind == kRkEuler) {
+        // the first stage stores the decisions of the positions it owns
+        for (int p = tid; p < NG; p += NT) {
+          int64_t slot;
+          bool owner;
+          if (flag_slot(p, slot, owner) && owner) P.gate_flags[slot] = flags[p];
+        }
+      }
     }
     gflag = flags;
     __syncthreads();
@@ -478,6 +599,21 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
           one(v);
         }
       });
+    } else if constexpr (CHAR) {
+      // characteristic fields: one thread per position, all variables
+      const double* cf = P.coef[0];
+      const int cs = P.cstride[0];
+      for (int it = tid; it < TYE * NCX; it += NT) {
+        const int cx = it % NCX, ty = it / NCX;
+        RT c[kCoefRec];
+        const int gi = clamp_coef_index(x0 - 1 + cx, nx) + P.coff;
+#pragma unroll
+        for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
+        const int ly = (ND > 1) ? ty + H : 0, lx = cx + H - 1;
+        char_weno_position<ND, NF, WO, 0>(
+            c, [&](int v, int o) { return sq[qi(v, ly, lx + o)]; }, eps, P,
+            [&](int v) -> RT& { return wl[wxi(v, ty, cx)]; }, [&](int v) -> RT& { return wr[wxi(v, ty, cx)]; });
+      }
     } else {
       // FP64 (and split WENO1/3): coefficients per reconstruction from global memory
       const double* cf = P.coef[0];
@@ -633,6 +769,20 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
           one(v);
         }
       });
+    } else if constexpr (CHAR) {
+      const double* cf = P.coef[1];
+      const int cs = P.cstride[1];
+      for (int it = tid; it < NCY * TX; it += NT) {
+        const int tx = it % TX, cy = it / TX;
+        RT c[kCoefRec];
+        const int gi = clamp_coef_index(y0 - 1 + cy, ny) + P.coff;
+#pragma unroll
+        for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
+        const int ly = cy + H - 1, lx = tx + H;
+        char_weno_position<ND, NF, WO, 1>(
+            c, [&](int v, int o) { return sq[qi(v, ly + o, lx)]; }, eps, P,
+            [&](int v) -> RT& { return wl[wyi(v, cy, tx)]; }, [&](int v) -> RT& { return wr[wyi(v, cy, tx)]; });
+      }
     } else {
       const double* cf = P.coef[1];
       const int cs = P.cstride[1];
@@ -767,17 +917,22 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   if (P.monitor) monitor_max(P.monitor, icfl);
 }
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, bool VISC = false>
+// FMA tags the instantiations of the translation unit compiled with
+// multiply-add contraction (-fmad=true), so that their host-side symbols
+// differ from the bit-faithful ones; the kernel body does not use it.
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, bool VISC = false,
+          bool FMA = false, bool CHAR = false>
 __global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const __grid_constant__ UniformCoef U,
                                                    const double* __restrict__ qin, const double* __restrict__ qbase,
                                                    double* __restrict__ qout, const double dt, const int kind) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
+  stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, UniformCoef, false, CHAR>(P, qin, qbase, qout, dt, kind,
+                                                                               blockIdx.x * TX,
                                                      (ND > 1) ? blockIdx.y * TY : 0, smem_raw, &U);
 }
 
 // The same kernel with its registers capped so that MINB blocks fit on an SM.
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool FMA = false>
 __global__ void __launch_bounds__(NT, MINB) stage_kernel_mb(const DevParams P, const __grid_constant__ UniformCoef U,
                                                             const double* __restrict__ qin,
                                                             const double* __restrict__ qbase,
@@ -790,7 +945,7 @@ __global__ void __launch_bounds__(NT, MINB) stage_kernel_mb(const DevParams P, c
 
 // The kernel with TMA staging of interior tiles (2-D, inviscid); T maps the
 // stage input qin.  MINB > 1 caps the registers as stage_kernel_mb does.
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool FMA = false>
 __global__ void __launch_bounds__(NT) stage_kernel_tma(const DevParams P, const __grid_constant__ UniformCoef U,
                                                        const __grid_constant__ TileMap T,
                                                        const double* __restrict__ qin,
@@ -801,7 +956,7 @@ __global__ void __launch_bounds__(NT) stage_kernel_tma(const DevParams P, const 
       P, qin, qbase, qout, dt, kind, blockIdx.x * TX, (ND > 1) ? blockIdx.y * TY : 0, smem_tma, &U, &T);
 }
 
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool FMA = false>
 __global__ void __launch_bounds__(NT, MINB) stage_kernel_tma_mb(const DevParams P, const __grid_constant__ UniformCoef U,
                                                                 const __grid_constant__ TileMap T,
                                                                 const double* __restrict__ qin,

@@ -8,6 +8,8 @@ s_initialize_*_module                  ``Simulation(case, ...)`` -> mfc_gpu_init
 !$acc update device(q_cons_ts(1))      ``Simulation.upload``    -> mfc_gpu_upload_state
 !$acc update host(q_cons_ts(1))        ``Simulation.download``  -> mfc_gpu_download_state
 s_compute_rhs (m_rhs.fpp:405)          ``Simulation.s_compute_rhs``
+s_weno (m_weno.fpp:365)                ``Simulation.s_weno``    -> mfc_gpu_weno
+s_hllc_riemann_solver                  ``Simulation.s_hllc_riemann_solver`` -> mfc_gpu_riemann
 s_1st/2nd/3rd_order_tvd_rk             ``Simulation.s_1st_order_tvd_rk`` ...
 p_main time loop (p_main.fpp:196-318)  ``Simulation.run``       -> mfc_gpu_run
 s_finalize_*_module                    ``Simulation.close``     -> mfc_gpu_finalize
@@ -49,7 +51,7 @@ def make_params(case: Case, x_cb, y_cb=None, z_cb=None, device: int = 0):
     P.y_cb = _dp(cb[1]) if cb[1] is not None else None
     P.z_cb = _dp(cb[2]) if cb[2] is not None else None
     P.precision = {"fp64": _lib.MFC_PREC_FP64, "split": _lib.MFC_PREC_SPLIT,
-                   "gated": _lib.MFC_PREC_GATED}[case.precision]
+                   "gated": _lib.MFC_PREC_GATED, "fp64_fma": _lib.MFC_PREC_FP64_FMA}[case.precision]
     P.device = device
     return P, cb
 
@@ -89,6 +91,8 @@ class Simulation:
         self.dt = case.dt
         if case.viscous:
             self.set_viscosity(case.re_shear, case.re_bulk)
+        if case.char_decomp:
+            self.set_reconstruction("characteristic")
         if on_device:
             self.generate_ic()
         else:
@@ -154,6 +158,35 @@ class Simulation:
         _lib.check(self.L.mfc_gpu_compute_rhs(self._h, _dp(rhs), _dp(prim)))
         return rhs, prim
 
+    def face_shape(self, direction: int, faces: bool = False) -> tuple:
+        """Shape of the face window of a direction: [S, p+1, n+1, m+1] with
+        the extent along it widened to the cells -1 .. s+1 (faces=False) or
+        the faces -1/2 .. s+1/2 (faces=True)."""
+        shape = list(self.case.shape)
+        shape[3 - direction] += 1 if faces else 2
+        return tuple(shape)
+
+    def s_weno(self, direction: int):
+        """s_weno of the current state along a direction over the face window:
+        (vL, vR), the left- and right-face values of every cell."""
+        shape = self.face_shape(direction)
+        vl, vr = np.empty(shape), np.empty(shape)
+        _lib.check(self.L.mfc_gpu_weno(self._h, int(direction), _dp(vl), _dp(vr)))
+        return vl, vr
+
+    def s_hllc_riemann_solver(self, direction: int, qL_rs, qR_rs):
+        """s_hllc_riemann_solver along a direction: qL_rs(j) is the state left
+        of face j+1/2, qR_rs(j+1) the state right of it (s_compute_rhs passes
+        vR and vL of s_weno).  Returns (flux [S, ...], flux_src [...]) over the
+        faces -1/2 .. s+1/2."""
+        shape = self.face_shape(direction)
+        a = np.ascontiguousarray(qL_rs, dtype=np.float64).reshape(shape)
+        b = np.ascontiguousarray(qR_rs, dtype=np.float64).reshape(shape)
+        fshape = self.face_shape(direction, faces=True)
+        flux, src = np.empty(fshape), np.empty(fshape[1:])
+        _lib.check(self.L.mfc_gpu_riemann(self._h, int(direction), _dp(a), _dp(b), _dp(flux), _dp(src)))
+        return flux, src
+
     def tvd_rk(self, t_step: int, dt: float | None = None) -> None:
         """One call of the configured s_*_order_tvd_rk (asynchronous)."""
         last = int(t_step == self.case.t_step_stop)
@@ -185,6 +218,12 @@ class Simulation:
         a[:len(re_shear)] = re_shear
         b[:len(re_bulk)] = re_bulk
         _lib.check(self.L.mfc_gpu_set_viscosity(self._h, _dp(a), _dp(b)))
+
+    def set_reconstruction(self, variables: str = "primitive") -> None:
+        """WENO of the "primitive" variables (the reference's choice) or of
+        the "characteristic" fields (mfc_gpu_set_reconstruction)."""
+        code = {"primitive": _lib.MFC_RECON_PRIMITIVE, "characteristic": _lib.MFC_RECON_CHARACTERISTIC}[variables]
+        _lib.check(self.L.mfc_gpu_set_reconstruction(self._h, code))
 
     def set_uniform_coefficients(self, enable: bool = True) -> int:
         """Split/gated WENO5 on a uniform grid reads one shared coefficient

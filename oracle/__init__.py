@@ -44,6 +44,7 @@ class MfoParams(ctypes.Structure):
         ("pi_infs", ctypes.c_double * MAX_FLUIDS),
         ("re_shear", ctypes.c_double * MAX_FLUIDS),
         ("re_bulk", ctypes.c_double * MAX_FLUIDS),
+        ("char_decomp", ctypes.c_int),
     ]
 
 
@@ -138,6 +139,7 @@ def params_from_case(case) -> MfoParams:
         q.re_shear[i] = r
     for i, r in enumerate(getattr(case, "re_bulk", ())):
         q.re_bulk[i] = r
+    q.char_decomp = int(bool(getattr(case, "char_decomp", False)))
     return q
 
 

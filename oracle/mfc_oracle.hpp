@@ -58,6 +58,7 @@ struct Params {
   double gammas[kMaxFluids] = {0};   // fluid_pp(i)%gamma  = 1/(gamma_i - 1)
   double pi_infs[kMaxFluids] = {0};  // fluid_pp(i)%pi_inf = gamma_i pi_inf_i/(gamma_i - 1)
   double re[2][kMaxFluids] = {};     // fluid_pp(i)%Re(1:2), shear and bulk; <= 0: none
+  bool char_decomp = false;          // characteristic-field WENO (see weno(); not in the reference)
 
   int num_dims() const { return 1 + (n > 0) + (p > 0); }
   int weno_polyn() const { return (weno_order - 1) / 2; }
@@ -421,9 +422,78 @@ struct Solver {
         }
   }
 
+  // WENO1/3/5 of one stencil, m_weno.fpp:391-536: at(o) is the value at
+  // offset o from the cell, cf the cell's coefficients; the left-face
+  // (x_{j-1/2}) and right-face (x_{j+1/2}) values.
+  template <class At, class Coef>
+  void weno_stencil(const At& at, const Coef& cf, R eps, R& outL, R& outR) const {
+    if (P.weno_order == 1) {
+      outL = at(0);
+      outR = at(0);
+      return;
+    }
+    if (P.weno_order == 3) {
+      R dvd0 = at(1) - at(0);
+      R dvdm1 = at(0) - at(-1);
+      R poly0 = at(0) + cf.polyL[0][0] * dvd0;
+      R poly1 = at(0) + cf.polyL[1][0] * dvdm1;
+      R beta0 = cf.beta[0][0] * dvd0 * dvd0 + eps;
+      R beta1 = cf.beta[1][0] * dvdm1 * dvdm1 + eps;
+      R a0 = cf.dL[0] / (beta0 * beta0), a1 = cf.dL[1] / (beta1 * beta1);
+      R sa = a0 + a1;
+      R w0 = a0 / sa, w1 = a1 / sa;
+      outL = w0 * poly0 + w1 * poly1;
+      poly0 = at(0) + cf.polyR[0][0] * dvd0;
+      poly1 = at(0) + cf.polyR[1][0] * dvdm1;
+      a0 = cf.dR[0] / (beta0 * beta0); a1 = cf.dR[1] / (beta1 * beta1);
+      sa = a0 + a1;
+      w0 = a0 / sa; w1 = a1 / sa;
+      outR = w0 * poly0 + w1 * poly1;
+      return;
+    }
+    R dvd1 = at(2) - at(1);
+    R dvd0 = at(1) - at(0);
+    R dvdm1 = at(0) - at(-1);
+    R dvdm2 = at(-1) - at(-2);
+    R poly[3], beta[3], alpha[3], omega[3];
+    poly[0] = at(0) + cf.polyL[0][0] * dvd1 + cf.polyL[0][1] * dvd0;
+    poly[1] = at(0) + cf.polyL[1][0] * dvd0 + cf.polyL[1][1] * dvdm1;
+    poly[2] = at(0) + cf.polyL[2][0] * dvdm1 + cf.polyL[2][1] * dvdm2;
+    beta[0] = cf.beta[0][0] * dvd1 * dvd1 + cf.beta[0][1] * dvd1 * dvd0 + cf.beta[0][2] * dvd0 * dvd0 + eps;
+    beta[1] = cf.beta[1][0] * dvd0 * dvd0 + cf.beta[1][1] * dvd0 * dvdm1 + cf.beta[1][2] * dvdm1 * dvdm1 + eps;
+    beta[2] = cf.beta[2][0] * dvdm1 * dvdm1 + cf.beta[2][1] * dvdm1 * dvdm2 + cf.beta[2][2] * dvdm2 * dvdm2 + eps;
+    for (int l = 0; l < 3; ++l) alpha[l] = cf.dL[l] / (beta[l] * beta[l]);
+    R sa = alpha[0] + alpha[1] + alpha[2];
+    for (int l = 0; l < 3; ++l) omega[l] = alpha[l] / sa;
+    outL = omega[0] * poly[0] + omega[1] * poly[1] + omega[2] * poly[2];
+    poly[0] = at(0) + cf.polyR[0][0] * dvd1 + cf.polyR[0][1] * dvd0;
+    poly[1] = at(0) + cf.polyR[1][0] * dvd0 + cf.polyR[1][1] * dvdm1;
+    poly[2] = at(0) + cf.polyR[2][0] * dvdm1 + cf.polyR[2][1] * dvdm2;
+    for (int l = 0; l < 3; ++l) alpha[l] = cf.dR[l] / (beta[l] * beta[l]);
+    sa = alpha[0] + alpha[1] + alpha[2];
+    for (int l = 0; l < 3; ++l) omega[l] = alpha[l] / sa;
+    outR = omega[0] * poly[0] + omega[1] * poly[1] + omega[2] * poly[2];
+  }
+
   // WENO reconstruction along direction dir, m_weno.fpp:391-536.
   // is1 = [-b+polyn, s+b-polyn] along dir; all other directions over their
   // full range (incl. ghosts), as in s_reconstruct_cell_boundary_values.
+  //
+  // P.char_decomp (no counterpart in the reference, which reconstructs the
+  // primitive variables only): the stencil of cell j is first projected on
+  // the characteristic fields of the quasi-linear primitive system along dir,
+  // frozen at cell j's own state,
+  //   slot f (partial density i):   alpha_i rho_i - kappa_i p,  kappa_i = alpha_i rho_i / (rho c^2)
+  //   slot momx + dir:              p - rho c u_n   (the u_n - c wave)
+  //   slot E:                       p + rho c u_n   (the u_n + c wave)
+  //   tangential velocities, volume fractions: unchanged,
+  // with rho = max(sum alpha_i rho_i, sgm_eps), Gamma = sum alpha_i Gamma_i,
+  // Pi = sum alpha_i Pi_i and c^2 = max(((Gamma + 1) p + Pi) / (Gamma rho),
+  // sgm_eps) (the mixture sound speed of m_riemann_solvers.fpp:220-223);
+  // each field is reconstructed with the same weights, then both face values
+  // are mapped back: p = (w_+ + w_-) 0.5, u_n = (w_+ - w_-) / (2 rho c),
+  // alpha_i rho_i = w_i + kappa_i p.  WENO1 reconstructs nothing, so it
+  // keeps the primitive path.
   void weno(int dir) {
     const int polyn = P.weno_polyn();
     Axis<R>& a = ax[dir];
@@ -435,61 +505,49 @@ struct Solver {
     if (dir == 0) { ib_ = jb; ie_ = je; }
     if (dir == 1) { jb_ = jb; je_ = je; }
     if (dir == 2) { kb_ = jb; ke_ = je; }
+    const bool chr = P.char_decomp && P.weno_order > 1;
+    const int nf = P.num_fluids, un = P.mom_beg() - 1 + dir, E = P.E_idx() - 1, ab = P.adv_beg() - 1;
 #pragma omp parallel for collapse(2) schedule(static)
     for (int k = kb_; k <= ke_; ++k)
       for (int j = jb_; j <= je_; ++j)
         for (int i = ib_; i <= ie_; ++i) {
           const int c = dir == 0 ? i : dir == 1 ? j : k;
+          const auto& cf = a.C(c);
+          if (!chr) {
+            for (int v = 0; v < S; ++v) {
+              const Field<R>& q = qp[v];
+              auto at = [&](int o) { return q(i + o * di, j + o * dj, k + o * dk); };
+              weno_stencil(at, cf, eps, vL[v](i, j, k), vR[v](i, j, k));
+            }
+            continue;
+          }
+          R rho = R(0), gam = R(0), pinf = R(0), kap[kMaxFluids];
+          for (int f = 0; f < nf; ++f) {
+            rho = rho + qp[f](i, j, k);
+            gam = gam + qp[ab + f](i, j, k) * R(P.gammas[f]);
+            pinf = pinf + qp[ab + f](i, j, k) * R(P.pi_infs[f]);
+          }
+          rho = std::max(rho, R(kSgmEps));
+          const R c2 = std::max(((gam + R(1)) * qp[E](i, j, k) + pinf) / (gam * rho), R(kSgmEps));
+          const R rc = rho * sqrt(c2);
+          for (int f = 0; f < nf; ++f) kap[f] = qp[f](i, j, k) / (rho * c2);
           for (int v = 0; v < S; ++v) {
-            const Field<R>& q = qp[v];
-            auto at = [&](int o) { return q(i + o * di, j + o * dj, k + o * dk); };
-            if (P.weno_order == 1) {
-              vL[v](i, j, k) = at(0);
-              vR[v](i, j, k) = at(0);
-              continue;
-            }
-            const auto& cf = a.C(c);
-            if (P.weno_order == 3) {
-              R dvd0 = at(1) - at(0);
-              R dvdm1 = at(0) - at(-1);
-              R poly0 = at(0) + cf.polyL[0][0] * dvd0;
-              R poly1 = at(0) + cf.polyL[1][0] * dvdm1;
-              R beta0 = cf.beta[0][0] * dvd0 * dvd0 + eps;
-              R beta1 = cf.beta[1][0] * dvdm1 * dvdm1 + eps;
-              R a0 = cf.dL[0] / (beta0 * beta0), a1 = cf.dL[1] / (beta1 * beta1);
-              R sa = a0 + a1;
-              R w0 = a0 / sa, w1 = a1 / sa;
-              vL[v](i, j, k) = w0 * poly0 + w1 * poly1;
-              poly0 = at(0) + cf.polyR[0][0] * dvd0;
-              poly1 = at(0) + cf.polyR[1][0] * dvdm1;
-              a0 = cf.dR[0] / (beta0 * beta0); a1 = cf.dR[1] / (beta1 * beta1);
-              sa = a0 + a1;
-              w0 = a0 / sa; w1 = a1 / sa;
-              vR[v](i, j, k) = w0 * poly0 + w1 * poly1;
-              continue;
-            }
-            R dvd1 = at(2) - at(1);
-            R dvd0 = at(1) - at(0);
-            R dvdm1 = at(0) - at(-1);
-            R dvdm2 = at(-1) - at(-2);
-            R poly[3], beta[3], alpha[3], omega[3];
-            poly[0] = at(0) + cf.polyL[0][0] * dvd1 + cf.polyL[0][1] * dvd0;
-            poly[1] = at(0) + cf.polyL[1][0] * dvd0 + cf.polyL[1][1] * dvdm1;
-            poly[2] = at(0) + cf.polyL[2][0] * dvdm1 + cf.polyL[2][1] * dvdm2;
-            beta[0] = cf.beta[0][0] * dvd1 * dvd1 + cf.beta[0][1] * dvd1 * dvd0 + cf.beta[0][2] * dvd0 * dvd0 + eps;
-            beta[1] = cf.beta[1][0] * dvd0 * dvd0 + cf.beta[1][1] * dvd0 * dvdm1 + cf.beta[1][2] * dvdm1 * dvdm1 + eps;
-            beta[2] = cf.beta[2][0] * dvdm1 * dvdm1 + cf.beta[2][1] * dvdm1 * dvdm2 + cf.beta[2][2] * dvdm2 * dvdm2 + eps;
-            for (int l = 0; l < 3; ++l) alpha[l] = cf.dL[l] / (beta[l] * beta[l]);
-            R sa = alpha[0] + alpha[1] + alpha[2];
-            for (int l = 0; l < 3; ++l) omega[l] = alpha[l] / sa;
-            vL[v](i, j, k) = omega[0] * poly[0] + omega[1] * poly[1] + omega[2] * poly[2];
-            poly[0] = at(0) + cf.polyR[0][0] * dvd1 + cf.polyR[0][1] * dvd0;
-            poly[1] = at(0) + cf.polyR[1][0] * dvd0 + cf.polyR[1][1] * dvdm1;
-            poly[2] = at(0) + cf.polyR[2][0] * dvdm1 + cf.polyR[2][1] * dvdm2;
-            for (int l = 0; l < 3; ++l) alpha[l] = cf.dR[l] / (beta[l] * beta[l]);
-            sa = alpha[0] + alpha[1] + alpha[2];
-            for (int l = 0; l < 3; ++l) omega[l] = alpha[l] / sa;
-            vR[v](i, j, k) = omega[0] * poly[0] + omega[1] * poly[1] + omega[2] * poly[2];
+            auto at = [&](int o) {
+              const int ii = i + o * di, jj = j + o * dj, kk = k + o * dk;
+              if (v < nf) return qp[v](ii, jj, kk) - kap[v] * qp[E](ii, jj, kk);
+              if (v == un) return qp[E](ii, jj, kk) - rc * qp[un](ii, jj, kk);
+              if (v == E) return qp[E](ii, jj, kk) + rc * qp[un](ii, jj, kk);
+              return qp[v](ii, jj, kk);
+            };
+            weno_stencil(at, cf, eps, vL[v](i, j, k), vR[v](i, j, k));
+          }
+          for (auto* w : {&vL, &vR}) {
+            std::vector<Field<R>>& o = *w;
+            const R wm = o[un](i, j, k), wp = o[E](i, j, k);
+            const R pr = (wp + wm) * R(0.5);
+            o[E](i, j, k) = pr;
+            o[un](i, j, k) = (wp - wm) / (R(2) * rc);
+            for (int f = 0; f < nf; ++f) o[f](i, j, k) = o[f](i, j, k) + kap[f] * pr;
           }
         }
   }

@@ -31,6 +31,7 @@ struct mfo_params {
   double pi_infs[kMaxFluids];
   double re_shear[kMaxFluids];  // fluid_pp(i)%Re(1); <= 0: inviscid
   double re_bulk[kMaxFluids];   // fluid_pp(i)%Re(2)
+  int char_decomp;              // 1: WENO of the characteristic fields (Solver::weno)
 };
 
 static Params to_params(const mfo_params* q) {
@@ -45,6 +46,7 @@ static Params to_params(const mfo_params* q) {
   P.bc_z_beg = q->bc_z_beg; P.bc_z_end = q->bc_z_end;
   for (int i = 0; i < kMaxFluids; ++i) { P.gammas[i] = q->gammas[i]; P.pi_infs[i] = q->pi_infs[i]; }
   for (int i = 0; i < kMaxFluids; ++i) { P.re[0][i] = q->re_shear[i]; P.re[1][i] = q->re_bulk[i]; }
+  P.char_decomp = q->char_decomp != 0;
   return P;
 }
 
@@ -106,6 +108,75 @@ void mfo_tvd_rk(void* h, double dt, int last_step) {
 // The p_main.fpp time loop; returns the trimmed dt of the last step.
 double mfo_run(void* h, int t_step_start, int t_step_stop, double dt) {
   return static_cast<Solver<double>*>(h)->run(t_step_start, t_step_stop, dt);
+}
+
+// The face window of direction dir that the Riemann solver reads: cells
+// j = -1 .. s+1 along dir (s = m, n or p), interior cells across it.  Arrays
+// are [S][e2][e1][e0] with e_dir = s_dir + 3 (cell j at index j + 1) and
+// e_other = s_other + 1.
+static void face_window(const Params& P, int dir, int (&lo)[3], int (&hi)[3]) {
+  const int ss[3] = {P.m, P.n, P.p};
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = 0;
+    hi[d] = ss[d];
+  }
+  lo[dir] = -1;
+  hi[dir] = ss[dir] + 1;
+}
+
+// s_weno along direction dir (m_weno.fpp:365-542, as
+// s_reconstruct_cell_boundary_values calls it, m_rhs.fpp:920-952) of the
+// primitive variables of register reg after s_populate_conservative_
+// variables_buffers and cons -> prim (m_rhs.fpp:434-447).  vL/vR: left-face
+// (x_{j-1/2}) and right-face (x_{j+1/2}) values over the face window.
+void mfo_weno(void* h, int reg, int dir, double* vL_out, double* vR_out) {
+  auto* s = static_cast<Solver<double>*>(h);
+  for (int v = 0; v < s->S; ++v) s->qp[v].d = s->q_cons_ts[reg][v].d;
+  s->populate_buffers();
+  s->cons_to_prim();
+  s->weno(dir);
+  int lo[3], hi[3];
+  face_window(s->P, dir, lo, hi);
+  long c = 0;
+  for (int v = 0; v < s->S; ++v)
+    for (int k = lo[2]; k <= hi[2]; ++k)
+      for (int j = lo[1]; j <= hi[1]; ++j)
+        for (int i = lo[0]; i <= hi[0]; ++i, ++c) {
+          vL_out[c] = s->vL[v](i, j, k);
+          vR_out[c] = s->vR[v](i, j, k);
+        }
+}
+
+// s_hllc_riemann_solver along direction dir (m_riemann_solvers.fpp:71-351)
+// with the Riemann-state buffers of bc -4 (:444-619).  qL_rs / qR_rs are the
+// reference's qL_prim_rs / qR_prim_rs over the face window: the state left
+// of face j+1/2 is qL_rs(j), the state right of it qR_rs(j+1).  (s_compute_rhs
+// passes the right-face WENO values as qL_prim_rs and the left-face values
+// as qR_prim_rs, m_rhs.fpp:545-556.)  Outputs for faces j = -1 .. s_dir
+// (face j+1/2 at index j + 1): flux [S][...] with extent s_dir + 2 along dir,
+// and flux_src(advxb) = vel_src(dir) (m_riemann_solvers.fpp:314-325).
+void mfo_riemann(void* h, int dir, const double* qL_rs, const double* qR_rs, double* flux_out, double* src_out) {
+  auto* s = static_cast<Solver<double>*>(h);
+  int lo[3], hi[3];
+  face_window(s->P, dir, lo, hi);
+  long c = 0;
+  for (int v = 0; v < s->S; ++v)
+    for (int k = lo[2]; k <= hi[2]; ++k)
+      for (int j = lo[1]; j <= hi[1]; ++j)
+        for (int i = lo[0]; i <= hi[0]; ++i, ++c) {
+          s->vR[v](i, j, k) = qL_rs[c];  // the solver reads its left state from vR
+          s->vL[v](i, j, k) = qR_rs[c];
+        }
+  s->hllc(dir);
+  hi[dir] -= 1;  // faces -1/2 .. s+1/2
+  c = 0;
+  for (int v = 0; v <= s->S; ++v)
+    for (int k = lo[2]; k <= hi[2]; ++k)
+      for (int j = lo[1]; j <= hi[1]; ++j)
+        for (int i = lo[0]; i <= hi[0]; ++i) {
+          if (v < s->S) flux_out[c++] = s->flux[v](i, j, k);
+          else *src_out++ = s->fsrc(i, j, k);
+        }
 }
 
 void mfo_set_threads(int nthreads) {

@@ -125,3 +125,56 @@ def test_training_learns_and_the_gate_gains_over_the_method_without_it():
     print(f"rel L1 vs FP64: split {e_split:.3e} gated {e_gated:.3e} all-linear {e_lin:.3e}")
     assert e_gated <= 1e-3
     assert e_lin > 3 * e_gated
+
+
+@pytest.mark.gpu
+@pytest.mark.slow
+def test_config4_gated_against_plain_fp64_and_ungated_split():
+    """Config 4 at its stated size: the droplet at 2048 x 1024 for 2000 steps.
+    The gated form must stay within density / volume-fraction L1 <= 1e-3 of
+    plain FP64 WENO everywhere (the fallback and the judge; the FP64 GPU path
+    is the oracle bit for bit) and run at >= 2x its cell-updates/s.  Beside
+    it, the method without the network: plain split WENO everywhere (its
+    accuracy and speed are printed with the gated form's), and linear
+    weights everywhere over a shorter run (the network's accuracy gain)."""
+    import torch
+    from microfc_gb300 import Simulation, cases, gate
+
+    params = gate.load()
+    case = cases.shock_droplet_2d(nx=2048, ny=1024, steps=2000)
+
+    def run(precision, p=None, steps=2000):
+        with Simulation(case.replace(precision=precision), ic="device") as sim:
+            if p is not None:
+                sim.set_gate(p)
+            sim.tune(3)
+            st = torch.cuda.ExternalStream(sim.stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(st)
+            sim.run(0, steps)
+            e1.record(st)
+            torch.cuda.synchronize()
+            rate = case.cells * steps / (e0.elapsed_time(e1) / 1e3)
+            assert sim.status() == 0
+            return sim.download(), rate
+
+    ref, r_fp64 = run("fp64")
+    split, r_split = run("split")
+    gated, r_gated = run("gated", params)
+    cols = [0, 1, case.adv_idx, case.adv_idx + 1]
+    e_split = rel_l1(split, ref)[cols].max()
+    e_gated = rel_l1(gated, ref)[cols].max()
+    print(f"2048x1024 x 2000 steps: cell-updates/s fp64 {r_fp64:.3e} split {r_split:.3e} gated {r_gated:.3e} "
+          f"(gated/fp64 {r_gated / r_fp64:.1f}x, gated/split {r_gated / r_split:.2f}); "
+          f"max density/alpha rel L1 split {e_split:.2e} gated {e_gated:.2e}")
+    assert e_gated <= 1e-3
+    assert r_gated >= 2.0 * r_fp64
+    # the network's gain over linear weights everywhere, on the first 200 steps
+    short_ref, _ = run("fp64", steps=200)
+    short_gated, _ = run("gated", params, steps=200)
+    short_lin, _ = run("gated", gate.all_linear_params(), steps=200)
+    e_g = rel_l1(short_gated, short_ref)[cols].max()
+    e_l = rel_l1(short_lin, short_ref)[cols].max() if np.isfinite(short_lin).all() else np.inf
+    print(f"200 steps: max density/alpha rel L1 gated {e_g:.2e} all-linear {e_l:.2e}")
+    assert e_l > 3 * e_g

@@ -21,11 +21,11 @@ def _run(oracle_lib, case, steps=None):
     return x_cb, y_cb, q, o.get_state()
 
 
-def _sod_error(oracle_lib, m):
+def _sod_error(oracle_lib, m, char_decomp=False):
     t_end = 0.1
     dt = 2e-4 * 400 / (m + 1)
     steps = int(round(t_end / dt))
-    case = cases.sod_1d(m=m, steps=steps, dt=dt)
+    case = cases.sod_1d(m=m, steps=steps, dt=dt).replace(char_decomp=char_decomp)
     x_cb, _, _, q = _run(oracle_lib, case)
     prim = preprocess.to_primitive(case, q)
     rho = q[0, 0, 0] + q[1, 0, 0]
@@ -42,6 +42,41 @@ def test_sod_matches_exact_solution_and_converges(oracle_lib):
     # shock-capturing schemes converge at first order in L1 across discontinuities
     assert e400[0] < 2e-3 and e400[1] < 1.5e-3 and e400[2] < 4e-3, e400
     assert e400[0] < 0.75 * e200[0] and e400[1] < 0.75 * e200[1], (e200, e400)
+
+
+def test_characteristic_weno_matches_exact_sod_solution_and_converges(oracle_lib):
+    """WENO of the characteristic fields (no reference counterpart): the same
+    known answer as the primitive reconstruction, at least as close to it."""
+    e200 = _sod_error(oracle_lib, 199, char_decomp=True)
+    e400 = _sod_error(oracle_lib, 399, char_decomp=True)
+    prim = _sod_error(oracle_lib, 399)
+    assert e400[0] < 2e-3 and e400[1] < 1.5e-3 and e400[2] < 4e-3, e400
+    assert e400[0] < 0.75 * e200[0] and e400[1] < 0.75 * e200[1], (e200, e400)
+    assert e400[0] <= 1.1 * prim[0] and e400[1] <= 1.1 * prim[1], (e400, prim)
+
+
+def _moving_interface(**kw):
+    gw, piw = cases.stiffened(6.12, 3.43e8)
+    ga, pia = cases.stiffened(1.4)
+    left = Patch(geometry=1, centroid=(0.25, 0, 0), length=(0.5, 0, 0), alpha_rho=(1000.0 * 0.999, 1.2 * 1e-3),
+                 alpha=(0.999, 1e-3), vel=(50.0, 0, 0), pres=1e5)
+    right = Patch(geometry=1, centroid=(0.75, 0, 0), length=(0.5, 0, 0), alpha_rho=(1000.0 * 1e-3, 1.2 * 0.999),
+                  alpha=(1e-3, 0.999), vel=(50.0, 0, 0), pres=1e5)
+    return Case(m=99, x_domain=(0.0, 1.0), dt=1e-5, t_step_stop=50, t_step_save=50, num_fluids=2,
+                time_stepper=3, weno_order=5, weno_eps=1e-16, bc_x=(-3, -3), gammas=(gw, ga),
+                pi_infs=(piw, pia), patches=[left, right], **kw)
+
+
+def test_characteristic_weno_keeps_a_material_interface_in_equilibrium(oracle_lib):
+    """A water/air interface moving with uniform p and u stays in equilibrium
+    with the characteristic projection too, although its fields mix p, u and
+    the partial densities."""
+    case = _moving_interface(char_decomp=True)
+    _, _, _, q = _run(oracle_lib, case)
+    prim = preprocess.to_primitive(case, q)
+    assert np.isfinite(q).all()
+    assert np.abs(prim[case.mom_idx] / 50.0 - 1.0).max() < 1e-9
+    assert np.abs(prim[case.E_idx] / 1e5 - 1.0).max() < 1e-6
 
 
 def _smooth_case(m, weno_order, steps, dt):
