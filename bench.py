@@ -267,6 +267,16 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
                                     "peak": fp64_peak, "unit": "TFLOP/s",
                                     "frac": flops * rate / 1e12 / fp64_peak if flops else None},
                        "rel_l1_vs_plain_fp64_100_steps": l1}
+    # WENO of the characteristic fields (FP64, bit-identical to the oracle's
+    # restatement): its rate on the same workload
+    with Simulation(case.replace(char_decomp=True), x_cb, y_cb, q_cons=q0) as s:
+        variant, _ = s.tune(5)
+        s.select_variant(variant)
+        st = torch.cuda.ExternalStream(s.stream)
+        t = _time_steps(s, st, flush, args.steps, args.warmup, case.dt)
+        rate = case.cells * args.steps / t
+    out["fp64_characteristic"] = {"value": rate, "unit": "cell-updates/s", "ms_per_step": 1e3 * t / args.steps,
+                                  "vs_plain_fp64": rate / fp64_rate, "tile_variant": variant}
     # config 4's grid: the droplet at 2048 x 1024 (7 equations, 117 MB per
     # register), gated against split and plain FP64 on the same case; the
     # device initial condition avoids a host pre_process of 2 M cells
@@ -349,7 +359,7 @@ def main():
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "split", "gated"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "split", "gated", "fp64_fma"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--nx", type=int, default=NX, help="cells in x (profiling runs; the benchmark is 1024)")
     ap.add_argument("--ny", type=int, default=NY, help="cells in y (profiling runs; the benchmark is 512)")
@@ -443,8 +453,9 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64 state / f32 WENO+HLLC"
-        + (" + learned gate" if args.precision == "gated" else ""),
+        "vs_baseline": None,
+        "dtype": {"fp64": "f64", "fp64_fma": "f64 (multiply-add contraction)", "split": "f64 state / f32 WENO+HLLC",
+                  "gated": "f64 state / f32 WENO+HLLC + learned gate"}[args.precision],
         "data": "synthetic (reference-style case inputs, generated in-process)",
         "config": {"workload": WORKLOAD if args.precision == "fp64" else WORKLOAD.replace("plain FP64", args.precision),
                    "cells": cells, "equations": case.sys_size, "dt": case.dt,
@@ -460,10 +471,11 @@ def main():
     if flops:
         # algorithmic flops of one launch (a third of a cell-update per cell)
         # over the launch's average CUDA-event duration
-        peak = fp64_peak if args.precision == "fp64" else fp32_peak
+        fp64_bound = args.precision in ("fp64", "fp64_fma")
+        peak = fp64_peak if fp64_bound else fp32_peak
         ach = flops * cells / 3 / per_launch_s / 1e12
         compute = {
-            "bound": "fp64" if args.precision == "fp64" else "fp32", "achieved": ach, "peak": peak,
+            "bound": "fp64" if fp64_bound else "fp32", "achieved": ach, "peak": peak,
             "unit": "TFLOP/s", "frac": ach / peak, "traffic": traffic, "flops_per_cell_update": flops,
             "peak_kind": "measured in-process (FMA chains, mfc_gpu_measure_peaks; MEASURED_PEAKS.json has no "
                          "FP64/FP32 entry)",

@@ -154,6 +154,34 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
     }
   }
   griddep_wait();  // the state (and the partial RHS) below are earlier kernels' output
+  if constexpr (DIR > 0) {
+    // The operands of the block's last phase that the tile load does not
+    // bring in: the partial RHS (y and z sweeps) and, on the z sweep, the RK
+    // registers.  Every 128-byte line of the block's rows (TB cells along x
+    // per variable and row; rows start 128-byte aligned) is prefetched into
+    // L2 while the tile is reconstructed: at 256^3 a register is 1 GB and
+    // none of them stays in L2 between the sweeps.
+    const int arrays = DIR == 1 || kind == kRhsOnly ? 1 : (kind == kRkEuler ? 2 : 3);
+    constexpr int kLinesD = (TB * 8 + 127) / 128, kLinesA = (TB * int(sizeof(AT)) + 127) / 128;
+    constexpr int kLines = kLinesD > kLinesA ? kLinesD : kLinesA;
+    const int nrow = S * TA * TC;
+    const AT* rb = reinterpret_cast<const AT*>(P.work);
+    for (int it = tid; it < arrays * nrow * kLines; it += NT) {
+      const int line = it % kLines, r = it / kLines;
+      const int arr = r / nrow, l = r - arr * nrow;
+      const int v = l % S, ta = (l / S) % TA, pc = l / (S * TA);
+      const int per_line = arr == 0 ? 128 / int(sizeof(AT)) : 16;  // elements of a 128-byte line
+      const int gb = b0 + line * per_line;
+      const int ga = a0 + ta, gc = c0 + pc;
+      if (ga >= na || gc >= nc || gb >= nb || line >= (arr == 0 ? kLinesA : kLinesD)) continue;
+      int x, y, z;
+      sweep_coords<DIR>(ga, gb, gc, x, y, z);
+      const int64_t o = z * P.sz + y * P.sy + x + v * P.sv;
+      const void* ptr = arr == 0 ? static_cast<const void*>(rb + o)
+                                 : arr == 1 ? static_cast<const void*>(qbase + o) : static_cast<const void*>(qin + o);
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
+    }
+  }
   if (use_tma) {
     volatile int* landed = reinterpret_cast<volatile int*>(stg + Sh::kStageBytes + 8);
     if (tid == 0) {

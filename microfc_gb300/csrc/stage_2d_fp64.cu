@@ -18,6 +18,7 @@ void register_stage_2d_fp64(std::vector<StageEntry>& r) {
   MFC_2D(1, 5)
 #undef MFC_2D
   // interior tiles staged by one TMA bulk tensor copy
+  r.push_back(stage_entry<2, 2, 5, double, 32, 16, 544, false, 1, false, true>());
   r.push_back(stage_entry<2, 2, 5, double, 32, 16, 512, false, 1, false, true>());
   r.push_back(stage_entry<2, 2, 5, double, 16, 16, 256, false, 1, false, true>());
   r.push_back(stage_entry<2, 2, 3, double, 16, 16, 256>());
