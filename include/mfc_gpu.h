@@ -272,7 +272,8 @@ int mfc_gpu_finalize(mfc_gpu_ctx* ctx);
 /* No counterpart in the reference (which tunes nothing).  Autotuner: times a
  * few first-stage launches of every compiled tile variant of the context's
  * configuration (the state is not advanced), keeps the fastest and returns
- * its index and per-launch time in milliseconds. */
+ * its index and per-launch time in milliseconds.  A variant that stages its
+ * tiles by TMA (MFC_VARIANT_TMA) wins a tie within 1 %. */
 int mfc_gpu_tune(mfc_gpu_ctx* ctx, int reps, int* variant_out, double* ms_out);
 /* Pins tile variant `variant` (the numbering mfc_gpu_tune reports) and
  * returns its tile shape and threads per block; MFC_ERR_INVALID past the
@@ -397,7 +398,7 @@ int mfc_gpu_ensemble_generate_ic(mfc_gpu_ensemble* ens, int case_index, const mf
  * arrays [S][p+1][n+1][ld_y], x fastest.  Limits: S*(n+1)*(p+1)*ld_y <=
  * 7*2^20 doubles and at most 4096 cells per direction; larger cases return
  * MFC_ERR_INVALID, and so does MFC_PREC_GATED (the gate's parameters live
- * in a context).  Synchronous with respect to `stream` (a cudaStream_t,
+ * in a context; MFC_PREC_FP64, _SPLIT and _FP64_FMA are taken).  Synchronous with respect to `stream` (a cudaStream_t,
  * NULL = legacy default stream); returns MFC_ERR_STATE if a NaN was written
  * or a TMA staging wait timed out (q_out is then incomplete).
  * All calls share the array: calls that overlap on the GPU race.  The first

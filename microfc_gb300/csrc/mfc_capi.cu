@@ -788,6 +788,12 @@ int mfc_gpu_tune(mfc_gpu_ctx* c, int reps, int* variant_out, double* ms_out) {
   const mfc::StageEntry* best = nullptr;
   int idx = -1, best_idx = -1;
   float best_ms = 0.f;
+  struct Timed {
+    const mfc::StageEntry* e;
+    int idx;
+    float ms;
+  };
+  std::vector<Timed> timed;
   cudaEvent_t a, b;
   MFC_CUDA(cudaEventCreate(&a));
   MFC_CUDA(cudaEventCreate(&b));
@@ -813,9 +819,19 @@ int mfc_gpu_tune(mfc_gpu_ctx* c, int reps, int* variant_out, double* ms_out) {
       best_ms = ms;
       best_idx = idx;
     }
+    timed.push_back({&e, idx, ms});
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
+  // a variant that stages its tiles by TMA wins a tie (within 1 %): the copy
+  // engine takes the tile loads off the warps at no cost in time
+  if (best && !best->tma)
+    for (const auto& t : timed)
+      if (t.e->tma && t.ms <= best_ms * 1.01f && (!best->tma || t.ms < best_ms)) {
+        best = t.e;
+        best_ms = t.ms;
+        best_idx = t.idx;
+      }
   MFC_CUDA(cudaMemcpyAsync(c->status, &saved, sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
   MFC_CUDA(cudaStreamSynchronize(c->stream));
   if (!best) return fail(MFC_ERR_CUDA, "no tile variant could be timed");

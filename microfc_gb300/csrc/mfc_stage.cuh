@@ -369,6 +369,17 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
     }
   }
   griddep_wait();  // the state below is the previous stage's output
+  if (kind != kRkEuler && kind != kRhsOnly) {
+    // the RK base register's rows of the tile, read only by the last phase:
+    // every 128-byte line prefetched into L2 while the tile is worked on
+    constexpr int kLines = (TX * 8 + 127) / 128;
+    for (int it = tid; it < S * TYE * kLines; it += NT) {
+      const int line = it % kLines, r = it / kLines, ty = r % TYE, v = r / TYE;
+      const int gx = x0 + line * 16, gy = (ND > 1) ? y0 + ty : 0;
+      if (gx >= nx || gy >= ny) continue;
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(qbase + gy * P.sy + gx + v * P.sv));
+    }
+  }
   if (use_tma) {
     const uint32_t par = tma_parity ? *tma_parity : 0u;
     volatile int* landed = reinterpret_cast<volatile int*>(stg + kStageBytes + 8);

@@ -206,6 +206,11 @@ class MultiDomain:
     def __exit__(self, *exc):
         self.close()
 
+    def set_gate(self, params) -> None:
+        """Learned-gate parameters of every subdomain (gated cases)."""
+        for sim in self.sims:
+            sim.set_gate(params)
+
     def _buffer(self, rank: int, d: int, side: int) -> int:
         p = ctypes.c_void_p()
         n = ctypes.c_int64()

@@ -132,23 +132,35 @@ def test_rank_to_rank_exchange_over_gloo():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["sod", "sod_periodic", "droplet_2x2", "droplet_split_4x1"])
+@pytest.mark.parametrize("kind", ["sod", "sod_periodic", "droplet_2x2", "droplet_split_4x1", "droplet_gated_2x2",
+                                  "droplet_gated_periodic_3x2"])
 def test_subdomains_on_one_gpu_reproduce_the_whole_domain(kind):
-    from microfc_gb300 import Simulation
+    """Gated cases included: the decisions a step's first stage stores at
+    the ghost positions beside a processor boundary come from the halo, so
+    the later stages read what the undecomposed run reads there."""
+    from microfc_gb300 import Simulation, gate
+    params = None
     if kind.startswith("sod"):
         c = cases.sod_1d(m=199, steps=20, dt=2e-4)
         if kind == "sod_periodic":
             c = c.replace(bc_x=(-1, -1))
         px, py = 3, 1
     else:
-        prec = "split" if "split" in kind else "fp64"
+        prec = "split" if "split" in kind else "gated" if "gated" in kind else "fp64"
         c = cases.shock_droplet_2d(nx=128, ny=64, steps=20, precision=prec)
-        px, py = (2, 2) if "2x2" in kind else (4, 1)
+        if "periodic" in kind:
+            c = c.replace(bc_x=(-1, -1), bc_y=(-1, -1))
+        px, py = (2, 2) if "2x2" in kind else (3, 2) if "3x2" in kind else (4, 1)
+        params = gate.load() if prec == "gated" else None
     x_cb, y_cb, _, q = preprocess.generate(c)
     with Simulation(c, x_cb, y_cb, q_cons=q) as sim:
+        if params is not None:
+            sim.set_gate(params)
         sim.run(0, 20)
         ref = sim.download()
     with decomp.MultiDomain(c, x_cb, y_cb, q_cons=q, px=px, py=py) as md:
+        if params is not None:
+            md.set_gate(params)
         md.run(0, 20)
         got = md.download()
     assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))

@@ -47,7 +47,8 @@ def _params(case, x_cb, y_cb, precision=None):
     return P
 
 
-FP64, SPLIT = _lib.MFC_PREC_FP64, _lib.MFC_PREC_SPLIT
+FP64, SPLIT, FP64_FMA = _lib.MFC_PREC_FP64, _lib.MFC_PREC_SPLIT, _lib.MFC_PREC_FP64_FMA
+PREC_NAMES = {FP64: "fp64", SPLIT: "split", FP64_FMA: "fp64_fma"}
 
 
 @pytest.mark.gpu
@@ -60,7 +61,10 @@ FP64, SPLIT = _lib.MFC_PREC_FP64, _lib.MFC_PREC_SPLIT
     (lambda: cases.shock_droplet_2d(nx=96, ny=64, steps=2), SPLIT, 3),
     (lambda: cases.shock_droplet_2d(nx=96, ny=64, steps=2), SPLIT, 4),
     (lambda: cases.sod_1d(m=299, steps=2, dt=1e-4), SPLIT, 3),
-], ids=["droplet-fp64", "sod-fp64", "droplet-rk2-fp64", "droplet-split-odd", "droplet-split-even", "sod-split"])
+    # the opt-in contracted FP64 kernels (2-D WENO5)
+    (lambda: cases.shock_droplet_2d(nx=96, ny=64, steps=2), FP64_FMA, 3),
+], ids=["droplet-fp64", "sod-fp64", "droplet-rk2-fp64", "droplet-split-odd", "droplet-split-even", "sod-split",
+        "droplet-fp64-fma"])
 def test_noalloc_step_matches_regular_entry_point_twice_in_a_row(builder, precision, pad):
     import torch
 
@@ -88,7 +92,7 @@ def test_noalloc_step_matches_regular_entry_point_twice_in_a_row(builder, precis
     assert rc == 0, L.mfc_gpu_last_error().decode()
     two = a.cpu().numpy()[..., : case.m + 1].copy()
 
-    regular = case.replace(precision="fp64" if precision == FP64 else "split")
+    regular = case.replace(precision=PREC_NAMES[precision])
     with Simulation(regular, x_cb, y_cb, q_cons=q0) as sim:
         sim.tvd_rk(0)
         ref1 = sim.download()
