@@ -366,6 +366,9 @@ def main():
     ap.add_argument("--no-modes", action="store_true", help="skip the split/gated/ensemble figures")
     ap.add_argument("--variant", type=int, default=None,
                     help="pin this tile variant instead of running the autotuner (profiling runs)")
+    ap.add_argument("--case", default="droplet2d", choices=["droplet2d", "bubble3d"],
+                    help="profiling runs only: bubble3d is the 3-D shock-bubble at --nx^3 cells (the benchmark "
+                         "workload is droplet2d); no modes, no compute roofline")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -383,9 +386,16 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     fp64_peak, fp32_peak = _lib.measure_peaks(local)
-    case = cases.shock_droplet_2d(nx=args.nx, ny=args.ny, precision=args.precision)
-    x_cb, y_cb, _, q0 = preprocess.generate(case)
-    sim = Simulation(case, x_cb, y_cb, q_cons=q0, device=local)
+    if args.case == "bubble3d":
+        case = cases.shock_bubble_3d(N=args.nx if args.nx != NX else 256, precision=args.precision)
+        sim = Simulation(case, ic="device", device=local)
+        q0 = sim.download()
+        x_cb = y_cb = None
+        args.no_modes = True
+    else:
+        case = cases.shock_droplet_2d(nx=args.nx, ny=args.ny, precision=args.precision)
+        x_cb, y_cb, _, q0 = preprocess.generate(case)
+        sim = Simulation(case, x_cb, y_cb, q_cons=q0, device=local)
     if args.precision == "gated":
         from microfc_gb300 import gate
         sim.set_gate(gate.load())
@@ -443,12 +453,15 @@ def main():
 
     # ---- rooflines ---------------------------------------------------------------------
     hbm, peak_kind = _peaks()
-    per_launch_s = t_total / launches  # every timed launch is the stage kernel
-    achieved = BYTES_PER_CELL_UPDATE * cells / 3 / per_launch_s / 1e9
+    per_launch_s = t_total / launches  # every timed launch is the stage kernel (2-D)
+    bytes_per_update = 64 * case.sys_size  # 448 B for the benchmark's 2-D workload
+    # algorithmic bytes of the timed steps over their time (in 2-D: one
+    # launch's bytes over the launch's average duration)
+    achieved = bytes_per_update * cells * args.steps / t_total / 1e9
     traffic = _profile_value("stage_kernel_fp64_droplet_1024x512.md", "dram_bytes_per_launch")
     flops = _profile_value("flop_count_droplet_1024x512.md", "algorithmic_flops_per_cell_update")
     hbm_roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": traffic, "bytes_per_cell_update": BYTES_PER_CELL_UPDATE,
+                "traffic": traffic, "bytes_per_cell_update": bytes_per_update,
                 "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"}
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
@@ -457,7 +470,8 @@ def main():
         "dtype": {"fp64": "f64", "fp64_fma": "f64 (multiply-add contraction)", "split": "f64 state / f32 WENO+HLLC",
                   "gated": "f64 state / f32 WENO+HLLC + learned gate"}[args.precision],
         "data": "synthetic (reference-style case inputs, generated in-process)",
-        "config": {"workload": WORKLOAD if args.precision == "fp64" else WORKLOAD.replace("plain FP64", args.precision),
+        "config": {"workload": (WORKLOAD if args.precision == "fp64" else WORKLOAD.replace("plain FP64", args.precision))
+                   if args.case == "droplet2d" else f"3-D shock-bubble {case.m + 1}^3 (profiling run), {args.precision}",
                    "cells": cells, "equations": case.sys_size, "dt": case.dt,
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}",
                    "tile": {"variant": variant, "tx": tile[0], "ty": tile[1], "threads": tile[2],
@@ -468,7 +482,7 @@ def main():
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
-    if flops:
+    if flops and args.case == "droplet2d":
         # algorithmic flops of one launch (a third of a cell-update per cell)
         # over the launch's average CUDA-event duration
         fp64_bound = args.precision in ("fp64", "fp64_fma")
