@@ -527,6 +527,44 @@ __device__ __forceinline__ void weno_cell(const RT* __restrict__ c, const RT (&v
   }
 }
 
+// One face value of weno_cell (SIDE 0: left face x_{j-1/2}, 1: right face
+// x_{j+1/2}), for a cell whose other face value nobody reads: the smoothness
+// indicators, divisors and the chosen side are the same operations as in
+// weno_cell, so the value has the same bits.
+template <int WO, int SIDE, class RT>
+__device__ __forceinline__ RT weno_cell_side(const RT* __restrict__ c, const RT (&v)[5], RT eps) {
+  constexpr int kP = SIDE ? kPR : kPL, kD = SIDE ? kDR : kDL;
+  if constexpr (WO == 1) {
+    return v[2];
+  } else if constexpr (WO == 3) {
+    const RT d0 = v[3] - v[2];
+    const RT dm1 = v[2] - v[1];
+    const RT b0 = c[kBeta + 0] * d0 * d0 + eps;
+    const RT b1 = c[kBeta + 3] * dm1 * dm1 + eps;
+    const RT p0 = v[2] + c[kP + 0] * d0;
+    const RT p1 = v[2] + c[kP + 2] * dm1;
+    const auto D0 = divisor(b0 * b0), D1 = divisor(b1 * b1);
+    const RT a0 = div_rn(c[kD + 0], D0), a1 = div_rn(c[kD + 1], D1);
+    const auto S = divisor(a0 + a1);
+    return div_rn(a0, S) * p0 + div_rn(a1, S) * p1;
+  } else {
+    const RT d1 = v[4] - v[3];
+    const RT d0 = v[3] - v[2];
+    const RT dm1 = v[2] - v[1];
+    const RT dm2 = v[1] - v[0];
+    const RT b0 = c[kBeta + 0] * d1 * d1 + c[kBeta + 1] * d1 * d0 + c[kBeta + 2] * d0 * d0 + eps;
+    const RT b1 = c[kBeta + 3] * d0 * d0 + c[kBeta + 4] * d0 * dm1 + c[kBeta + 5] * dm1 * dm1 + eps;
+    const RT b2 = c[kBeta + 6] * dm1 * dm1 + c[kBeta + 7] * dm1 * dm2 + c[kBeta + 8] * dm2 * dm2 + eps;
+    const auto D0 = divisor(b0 * b0), D1 = divisor(b1 * b1), D2 = divisor(b2 * b2);
+    const RT p0 = v[2] + c[kP + 0] * d1 + c[kP + 1] * d0;
+    const RT p1 = v[2] + c[kP + 2] * d0 + c[kP + 3] * dm1;
+    const RT p2 = v[2] + c[kP + 4] * dm1 + c[kP + 5] * dm2;
+    const RT a0 = div_rn(c[kD + 0], D0), a1 = div_rn(c[kD + 1], D1), a2 = div_rn(c[kD + 2], D2);
+    const auto S = divisor(a0 + a1 + a2);
+    return div_rn(a0, S) * p0 + div_rn(a1, S) * p1 + div_rn(a2, S) * p2;
+  }
+}
+
 // HLLC flux across one face, m_riemann_solvers.fpp:132-327, for sweep
 // direction DIR.  qL/qR are the primitive states left and right of the face
 // (the reference's vR(j) and vL(j+1), after its argument swap at

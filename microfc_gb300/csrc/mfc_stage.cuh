@@ -625,8 +625,43 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
             c, [&](int v, int o) { return sq[qi(v, ly, lx + o)]; }, eps, P,
             [&](int v) -> RT& { return wl[wxi(v, ty, cx)]; }, [&](int v) -> RT& { return wr[wxi(v, ty, cx)]; });
       }
+    } else if constexpr (sizeof(RT) == 8 && WO > 1) {
+      // FP64: positions cx = 1 .. TX feed two faces each; the tile-edge
+      // positions feed one -- cell x0 - 1 only its right-face value (the left
+      // state of face x0 - 1/2), cell x0 + TX only its left-face value -- so
+      // only that value is formed there (weno_cell_side, the same bits).  The
+      // edge items go to the threads that have one interior item fewer.
+      const double* cf = P.coef[0];
+      const int cs = P.cstride[0];
+      auto coef = [&](const int cx, RT (&c)[kCoefRec]) {
+        const int gi = clamp_coef_index(x0 - 1 + cx, nx) + P.coff;
+#pragma unroll
+        for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
+      };
+      constexpr int NI = S * TYE * TX, NE = S * TYE * 2;
+      for (int it = tid; it < NI; it += NT) {
+        const int cx = 1 + it % TX, r = it / TX;
+        const int ty = r % TYE, v = r / TYE;
+        RT c[kCoefRec];
+        coef(cx, c);
+        x_recon(c, cx, ty, v);
+      }
+      for (int it = (tid + NT - NI % NT) % NT; it < NE; it += NT) {
+        const int side = it / (S * TYE), r = it % (S * TYE);
+        const int ty = r % TYE, v = r / TYE, cx = side ? NCX - 1 : 0;
+        RT c[kCoefRec];
+        coef(cx, c);
+        RT st[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          const int o = k - 2;
+          st[k] = (o >= -(WO / 2) && o <= WO / 2) ? sq[qi(v, (ND > 1) ? ty + H : 0, cx + H - 1 + o)] : RT(0);
+        }
+        if (side) wl[wxi(v, ty, cx)] = weno_cell_side<WO, 0, RT>(c, st, eps);
+        else wr[wxi(v, ty, cx)] = weno_cell_side<WO, 1, RT>(c, st, eps);
+      }
     } else {
-      // FP64 (and split WENO1/3): coefficients per reconstruction from global memory
+      // split WENO1/3 (and FP64 WENO1): coefficients per reconstruction from global memory
       const double* cf = P.coef[0];
       const int cs = P.cstride[0];
       for (int it = tid; it < S * TYE * NCX; it += NT) {
@@ -793,6 +828,38 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         char_weno_position<ND, NF, WO, 1>(
             c, [&](int v, int o) { return sq[qi(v, ly + o, lx)]; }, eps, P,
             [&](int v) -> RT& { return wl[wyi(v, cy, tx)]; }, [&](int v) -> RT& { return wr[wyi(v, cy, tx)]; });
+      }
+    } else if constexpr (sizeof(RT) == 8 && WO > 1) {
+      // FP64: rows cy = 1 .. TY feed two faces each; row y0 - 1 only its
+      // upper-face value, row y0 + TY only its lower-face value (as in x)
+      const double* cf = P.coef[1];
+      const int cs = P.cstride[1];
+      auto coef = [&](const int cy, RT (&c)[kCoefRec]) {
+        const int gi = clamp_coef_index(y0 - 1 + cy, ny) + P.coff;
+#pragma unroll
+        for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
+      };
+      constexpr int NI = S * TY * TX, NE = S * 2 * TX;
+      for (int it = tid; it < NI; it += NT) {
+        const int tx = it % TX, r = it / TX;
+        const int cy = 1 + r % TY, v = r / TY;
+        RT c[kCoefRec];
+        coef(cy, c);
+        y_recon(c, tx, cy, v);
+      }
+      for (int it = (tid + NT - NI % NT) % NT; it < NE; it += NT) {
+        const int side = it / (S * TX), r = it % (S * TX);
+        const int tx = r % TX, v = r / TX, cy = side ? NCY - 1 : 0;
+        RT c[kCoefRec];
+        coef(cy, c);
+        RT st[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          const int o = k - 2;
+          st[k] = (o >= -(WO / 2) && o <= WO / 2) ? sq[qi(v, cy + H - 1 + o, tx + H)] : RT(0);
+        }
+        if (side) wl[wyi(v, cy, tx)] = weno_cell_side<WO, 0, RT>(c, st, eps);
+        else wr[wyi(v, cy, tx)] = weno_cell_side<WO, 1, RT>(c, st, eps);
       }
     } else {
       const double* cf = P.coef[1];
