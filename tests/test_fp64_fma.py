@@ -58,6 +58,12 @@ def test_contracted_variant_full_size_against_both_oracle_builds(oracle_lib):
         o = oracle_lib.Oracle(case, x_cb, y_cb, build=build)
         o.set_state(q)
         o.run(0, 100, case.dt)
-        err = rel_l1(got, o.get_state())
+        ref = o.get_state()
+        err = rel_l1(got, ref)
         print(f"contracted FP64 vs {build} oracle, per-field rel L1:", dict(zip(_names(case), err.tolist())))
         assert err[others].max() <= TOL_FP64, (build, err)
+        # the round-off field against the momentum's scale
+        mom_y = case.mom_idx + 1
+        dv = np.abs(got[mom_y] - ref[mom_y]).sum() / np.abs(ref[case.mom_idx]).sum()
+        print(f"  sum|d(rho v)| / sum|rho u| = {dv:.3e}")
+        assert dv <= TOL_FP64
