@@ -218,8 +218,9 @@ int mfc_gpu_set_viscosity(mfc_gpu_ctx* ctx, const double* re_shear, const double
  * velocities and the volume fractions, with the mixture sound speed
  * c^2 = ((Gamma + 1) p + Pi) / (Gamma rho) of the HLLC solver -- reconstructs
  * them with the same WENO weights and maps both face values back.  Plain
- * FP64 contexts, 1-D and 2-D, WENO3 or WENO5, inviscid, without processor
- * boundaries (WENO1 reconstructs nothing and keeps the primitive kernel).
+ * FP64 contexts, 1-D, 2-D (fused kernel) and 3-D (directional sweeps),
+ * WENO3 or WENO5, inviscid, without processor boundaries (WENO1
+ * reconstructs nothing and keeps the primitive kernel).
  * Call before stepping; MFC_RECON_PRIMITIVE switches back. */
 #define MFC_RECON_PRIMITIVE 0
 #define MFC_RECON_CHARACTERISTIC 1
@@ -338,6 +339,13 @@ int mfc_gpu_ensemble_run(mfc_gpu_ensemble* ens, int t_step_start, int t_step_sto
 void* mfc_gpu_ensemble_stream(mfc_gpu_ensemble* ens);
 int64_t mfc_gpu_ensemble_launch_count(const mfc_gpu_ensemble* ens);
 int mfc_gpu_ensemble_finalize(mfc_gpu_ensemble* ens);
+/* Viscous terms for every case of an ensemble (see mfc_gpu_set_viscosity):
+ * re_shear[i * num_fluids + f] / re_bulk[...] are case i's fluid_pp(f+1)%Re(1)
+ * / %Re(2) (NULL or values <= 0: none).  One kernel advances all cases, so
+ * every case must be viscous or none (MFC_ERR_INVALID otherwise); all-zero
+ * Reynolds numbers switch back to the inviscid kernels.  FP64 and split
+ * precision (the gated ensemble is inviscid).  Call before stepping. */
+int mfc_gpu_ensemble_set_viscosity(mfc_gpu_ensemble* ens, const double* re_shear, const double* re_bulk);
 /* Gate parameters for a MFC_PREC_GATED ensemble (see mfc_gpu_set_gate). */
 int mfc_gpu_ensemble_set_gate(mfc_gpu_ensemble* ens, const float* host_params);
 

@@ -22,7 +22,7 @@ EXPORTS = (
     "mfc_gpu_selftest_div",
     "mfc_gpu_tune", "mfc_gpu_ensemble_init", "mfc_gpu_ensemble_upload", "mfc_gpu_ensemble_download",
     "mfc_gpu_ensemble_tune", "mfc_gpu_ensemble_run", "mfc_gpu_ensemble_stream", "mfc_gpu_ensemble_launch_count",
-    "mfc_gpu_ensemble_finalize", "mfc_gpu_ensemble_set_gate", "mfc_gate_param_count", "mfc_gate_workspace_floats",
+    "mfc_gpu_ensemble_finalize", "mfc_gpu_ensemble_set_gate", "mfc_gpu_ensemble_set_viscosity", "mfc_gate_param_count", "mfc_gate_workspace_floats",
     "mfc_gpu_set_gate", "mfc_gpu_gate_samples", "mfc_gate_gradients", "mfc_gate_train_step", "mfc_gate_infer",
     "mfc_gpu_set_monitor", "mfc_gpu_icfl", "mfc_gpu_run_cfl", "mfc_gpu_generate_ic", "mfc_gpu_ensemble_generate_ic",
     "mfc_gpu_snapshot", "mfc_gpu_snapshot_wait", "mfc_gpu_select_variant", "mfc_gpu_variant_features",
@@ -160,6 +160,7 @@ def load(build_if_missing: bool = True):
     L.mfc_gpu_ensemble_finalize.argtypes = [vp]
     fp = ctypes.POINTER(ctypes.c_float)
     L.mfc_gpu_ensemble_set_gate.argtypes = [vp, fp]
+    L.mfc_gpu_ensemble_set_viscosity.argtypes = [vp, dp, dp]
     L.mfc_gate_param_count.restype = ctypes.c_int
     L.mfc_gate_workspace_floats.argtypes = [ctypes.c_int]
     L.mfc_gpu_set_gate.argtypes = [vp, fp]

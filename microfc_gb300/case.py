@@ -80,7 +80,7 @@ class Case:
                                         # "fp64_fma" (FP64 with multiply-add contraction, 2-D WENO5)
     # WENO of the characteristic fields instead of the primitive variables
     # (case key "char_decomp"; no counterpart in the reference, which
-    # reconstructs primitive variables): FP64 1-D and 2-D, WENO3/5
+    # reconstructs primitive variables): FP64, 1-D to 3-D, WENO3/5
     char_decomp: bool = False
     name: str = "case"
 
@@ -173,8 +173,8 @@ class Case:
                 bad("Unsupported value of fluid_pp(i)%pi_inf")
         if self.precision not in ("fp64", "split", "gated", "fp64_fma"):
             bad("Unsupported value of precision mode")
-        if self.char_decomp and (self.precision != "fp64" or self.p > 0 or self.viscous or self.weno_order == 1):
-            bad("char_decomp needs plain FP64, an inviscid 1-D or 2-D case and WENO3 or WENO5")
+        if self.char_decomp and (self.precision != "fp64" or self.viscous or self.weno_order == 1):
+            bad("char_decomp needs plain FP64, an inviscid case and WENO3 or WENO5")
         # grid stretching, m_start_up.fpp:238-330 (pre_process)
         for ax, st, dom, used in (("x", self.stretch_x, self.x_domain, True),
                                   ("y", self.stretch_y, self.y_domain, self.n > 0)):

@@ -13,6 +13,9 @@ void register_ensemble_fp32(std::vector<EnsembleEntry>& r) {
   r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, false, 5>());
   // interior tiles staged by one TMA bulk tensor copy
   r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, false, 5, true>());
+  // with the viscous terms (mfc_gpu_ensemble_set_viscosity)
+  r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, false, 1, false, true>());
+  r.push_back(ensemble_entry<2, 5, float, 32, 16, 256, false, 1, false, true>());
 }
 
 }  // namespace mfc

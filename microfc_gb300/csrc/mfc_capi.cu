@@ -689,8 +689,8 @@ int mfc_gpu_set_reconstruction(mfc_gpu_ctx* c, int variables) {
   const mfc::StageEntry* e =
       mfc::find_stage(c->nd, c->prm.num_fluids, c->prm.weno_order, c->prm.precision, c->visc != nullptr, chr);
   if (!e)
-    return fail(MFC_ERR_INVALID, "no characteristic-field kernel compiled for this configuration (FP64, 1-D or "
-                                 "2-D, WENO3 or WENO5)");
+    return fail(MFC_ERR_INVALID, "no characteristic-field kernel compiled for this configuration (FP64, WENO3 "
+                                 "or WENO5)");
   MFC_CUDA(e->prepare());
   c->chr = chr;
   c->stage = e;

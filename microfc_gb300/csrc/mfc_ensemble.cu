@@ -8,6 +8,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <array>
 #include <vector>
 
 #include "../../include/mfc_gpu.h"
@@ -64,6 +65,9 @@ struct mfc_gpu_ensemble {
   int64_t launches = 0;
   mfc::EnsParams* ep = nullptr;  // host staging of the kernel parameters
   mfc::TileMap* maps = nullptr;  // device: TMA maps [register][case] of a TMA tile variant
+  mfc::ViscParams* visc = nullptr;  // device: per-case viscosity parameters (viscous ensembles)
+  bool viscous = false;
+  std::vector<std::array<const double*, 2>> dcc;  // per case: cell-centre spacing tables (device)
 };
 
 namespace {
@@ -159,7 +163,7 @@ int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_ca
   build_ens_registry();
   const mfc::EnsembleEntry* en = nullptr;
   for (const auto& x : g_ens)
-    if (x.nf == c0.num_fluids && x.wo == c0.weno_order && x.prec == c0.precision) { en = &x; break; }
+    if (x.nf == c0.num_fluids && x.wo == c0.weno_order && x.prec == c0.precision && !x.visc) { en = &x; break; }
   if (!en) return mfc::report_error(MFC_ERR_INVALID, "no ensemble kernel compiled for this configuration");
   cudaError_t err = cudaSetDevice(c0.device);
   if (err != cudaSuccess) return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
@@ -175,6 +179,7 @@ int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_ca
   e->nx.resize(num_cases);
   e->ny.resize(num_cases);
   e->dt.assign(dts, dts + num_cases);
+  e->dcc.resize(num_cases);
   e->ep = new mfc::EnsParams();
   auto cleanup = [&](int code) {
     mfc_gpu_ensemble_finalize(e);
@@ -249,6 +254,7 @@ int mfc_gpu_ensemble_init(const mfc_params* cases, const double* dts, int num_ca
     if ((err = cudaMemcpyAsync(tb, gts[i].host.data(), sizeof(double) * gts[i].host.size(), cudaMemcpyHostToDevice,
                                e->stream)) != cudaSuccess)
       return cleanup(mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err)));
+    e->dcc[i] = {tb + gts[i].off_dcc[0], tb + gts[i].off_dcc[1]};
     for (int d = 0; d < 2; ++d) {
       C.P.inv_d[d] = tb + gts[i].off_inv[d];
       C.P.coef[d] = tb + gts[i].off_coef[d];
@@ -332,7 +338,7 @@ int mfc_gpu_ensemble_tune(mfc_gpu_ensemble* e, int reps, int* variant_out, doubl
   cudaEventCreate(&a);
   cudaEventCreate(&b);
   for (const auto& x : g_ens) {
-    if (x.nf != e->nf || x.wo != e->wo || x.prec != e->prec) continue;
+    if (x.nf != e->nf || x.wo != e->wo || x.prec != e->prec || x.visc != e->viscous) continue;
     ++idx;
     if (configure(e, &x) != MFC_OK) continue;
     if (launch_stage(e, 0, 0) != MFC_OK) continue;  // warm-up
@@ -374,7 +380,7 @@ int mfc_gpu_ensemble_select_variant(mfc_gpu_ensemble* e, int variant, int* tx, i
   if (!e) return mfc::report_error(MFC_ERR_INVALID, "NULL ensemble");
   int idx = -1;
   for (const auto& x : g_ens) {
-    if (x.nf != e->nf || x.wo != e->wo || x.prec != e->prec) continue;
+    if (x.nf != e->nf || x.wo != e->wo || x.prec != e->prec || x.visc != e->viscous) continue;
     if (++idx != variant) continue;
     int rc = configure(e, &x);
     if (rc) return rc;
@@ -390,7 +396,7 @@ int mfc_gpu_ensemble_variant_features(mfc_gpu_ensemble* e, int variant, uint32_t
   if (!e || !features) return mfc::report_error(MFC_ERR_INVALID, "NULL argument");
   int idx = -1;
   for (const auto& x : g_ens) {
-    if (x.nf != e->nf || x.wo != e->wo || x.prec != e->prec) continue;
+    if (x.nf != e->nf || x.wo != e->wo || x.prec != e->prec || x.visc != e->viscous) continue;
     if (++idx != variant) continue;
     *features = x.tma ? MFC_VARIANT_TMA : 0u;
     return MFC_OK;
@@ -447,6 +453,53 @@ int mfc_gpu_ensemble_run(mfc_gpu_ensemble* e, int t_step_start, int t_step_stop,
   return MFC_OK;
 }
 
+int mfc_gpu_ensemble_set_viscosity(mfc_gpu_ensemble* e, const double* re_shear, const double* re_bulk) {
+  if (!e) return mfc::report_error(MFC_ERR_INVALID, "NULL ensemble");
+  if (e->gate_w) return mfc::report_error(MFC_ERR_INVALID, "the gated ensemble kernels are inviscid");
+  const int nf = e->nf;
+  std::vector<mfc::ViscParams> V((size_t)e->num);
+  int viscous_cases = 0;
+  for (int i = 0; i < e->num; ++i) {
+    mfc::ViscParams& v = V[(size_t)i];
+    v = mfc::ViscParams{};
+    for (int f = 0; f < nf; ++f) {
+      v.res[0][f] = re_shear ? re_shear[(size_t)i * nf + f] : 0.0;
+      v.res[1][f] = re_bulk ? re_bulk[(size_t)i * nf + f] : 0.0;
+    }
+    for (int r = 0; r < 2; ++r)
+      for (int f = 0; f < nf; ++f)
+        if (v.res[r][f] > 0.0) v.re_idx[r][v.re_size[r]++] = f;
+    v.dcc[0] = e->dcc[(size_t)i][0];
+    v.dcc[1] = e->dcc[(size_t)i][1];
+    viscous_cases += (v.re_size[0] > 0 || v.re_size[1] > 0);
+  }
+  if (viscous_cases != 0 && viscous_cases != e->num)
+    return mfc::report_error(MFC_ERR_INVALID, "an ensemble is viscous in every case or in none (one kernel "
+                                              "advances all cases)");
+  const bool viscous = viscous_cases > 0;
+  const mfc::EnsembleEntry* en = nullptr;
+  for (const auto& x : g_ens)
+    if (x.nf == e->nf && x.wo == e->wo && x.prec == e->prec && x.visc == viscous) {
+      en = &x;
+      break;
+    }
+  if (!en) return mfc::report_error(MFC_ERR_INVALID, "no viscous ensemble kernel compiled for this configuration");
+  cudaError_t err = cudaSuccess;
+  if (viscous) {
+    if (!e->visc && (err = cudaMalloc(&e->visc, sizeof(mfc::ViscParams) * (size_t)e->num)) != cudaSuccess)
+      return mfc::report_error(MFC_ERR_NOMEM, cudaGetErrorString(err));
+    if ((err = cudaMemcpyAsync(e->visc, V.data(), sizeof(mfc::ViscParams) * V.size(), cudaMemcpyHostToDevice,
+                               e->stream)) != cudaSuccess)
+      return mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+  }
+  for (int i = 0; i < e->num; ++i) e->cases[(size_t)i].P.visc = viscous ? e->visc + i : nullptr;
+  e->viscous = viscous;
+  int rc = configure(e, en);
+  if (rc) return rc;
+  err = cudaStreamSynchronize(e->stream);
+  return err == cudaSuccess ? MFC_OK : mfc::report_error(MFC_ERR_CUDA, cudaGetErrorString(err));
+}
+
 int mfc_gpu_ensemble_set_gate(mfc_gpu_ensemble* e, const float* host_params) {
   if (!e || !host_params) return mfc::report_error(MFC_ERR_INVALID, "NULL argument");
   if (!e->gate_w) return mfc::report_error(MFC_ERR_INVALID, "the ensemble was not created with MFC_PREC_GATED");
@@ -468,6 +521,7 @@ int mfc_gpu_ensemble_finalize(mfc_gpu_ensemble* e) {
   cudaFree(e->status);
   cudaFree(e->gate_w);
   cudaFree(e->gate_flags);
+  cudaFree(e->visc);
   cudaFree(e->maps);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e->ep;

@@ -40,8 +40,10 @@ static_assert(sizeof(EnsParams) <= 32764, "ensemble parameters must fit the kern
 // One persistent block's walk over the work list (the body of both kernels).
 // TMA: interior tiles arrive by one bulk tensor copy; the block initialises
 // its mbarrier once and alternates its phase per copied tile.
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool TMA>
+// VISC: every case carries its viscosity parameters (DevParams::visc).
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool TMA, bool VISC = false>
 __device__ __forceinline__ void ensemble_walk(const EnsParams& E) {
+  static_assert(!VISC || (!GATE && !TMA), "the viscous ensemble kernels are ungated and load their tiles plainly");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t parity = 0;
   if constexpr (TMA) {
@@ -73,15 +75,15 @@ __device__ __forceinline__ void ensemble_walk(const EnsParams& E) {
       in = C.reg[2], out = C.reg[0], kind = kRk3Final, reg = 2;
     }
     const TileMap* T = (TMA && E.maps != nullptr) ? E.maps + reg * E.num_cases + lo : nullptr;
-    stage_tile<2, NF, WO, RT, TX, TY, NT, GATE, false, UniformCoefT<2>, TMA>(
+    stage_tile<2, NF, WO, RT, TX, TY, NT, GATE, VISC, UniformCoefT<2>, TMA>(
         C.P, in, C.reg[0], out, E.last_step ? C.dt_last : C.dt, kind, x0, y0, smem_raw, &E.U, T, &parity);
     __syncthreads();  // the next tile reuses the shared memory
   }
 }
 
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool TMA>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool TMA, bool VISC = false>
 __global__ void __launch_bounds__(NT) ensemble_stage_kernel(const __grid_constant__ EnsParams E) {
-  ensemble_walk<NF, WO, RT, TX, TY, NT, GATE, TMA>(E);
+  ensemble_walk<NF, WO, RT, TX, TY, NT, GATE, TMA, VISC>(E);
 }
 
 // The same with the registers capped so that MINB blocks fit on an SM.
@@ -90,10 +92,11 @@ __global__ void __launch_bounds__(NT, MINB) ensemble_stage_kernel_mb(const __gri
   ensemble_walk<NF, WO, RT, TX, TY, NT, GATE, TMA>(E);
 }
 
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool TMA>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool TMA, bool VISC = false>
 constexpr auto ensemble_func() {
+  static_assert(!VISC || MINB == 1, "register-capped ensemble variants are inviscid");
   if constexpr (MINB > 1) return &ensemble_stage_kernel_mb<NF, WO, RT, TX, TY, NT, GATE, MINB, TMA>;
-  else return &ensemble_stage_kernel<NF, WO, RT, TX, TY, NT, GATE, TMA>;
+  else return &ensemble_stage_kernel<NF, WO, RT, TX, TY, NT, GATE, TMA, VISC>;
 }
 
 struct EnsembleEntry {
@@ -104,21 +107,24 @@ struct EnsembleEntry {
   bool tma;    // interior tiles staged by TMA (needs EnsParams::maps)
   int box_w;   // x extent of the TMA box (cells), box_h rows
   int box_h;
+  bool visc;   // compiled with the viscous terms
 };
 
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB = 1, bool TMA = false>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB = 1, bool TMA = false,
+          bool VISC = false>
 cudaError_t ensemble_launch(const EnsParams& E, int grid, size_t smem, cudaStream_t st) {
-  ensemble_func<NF, WO, RT, TX, TY, NT, GATE, MINB, TMA>()<<<grid, NT, smem, st>>>(E);
+  ensemble_func<NF, WO, RT, TX, TY, NT, GATE, MINB, TMA, VISC>()<<<grid, NT, smem, st>>>(E);
   return cudaGetLastError();
 }
 
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool TMA>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool TMA, bool VISC = false>
 constexpr size_t ensemble_smem(bool shared_coef) {
-  return stage_smem_total<2, NF, WO, RT, TX, TY, NT, GATE, false, TMA>(shared_coef);
+  return stage_smem_total<2, NF, WO, RT, TX, TY, NT, GATE, VISC, TMA>(shared_coef);
 }
 
 // prec: 0 FP64, 1 split, 2 split with the learned gate
-template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool TMA = false>
+template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE = false, int MINB = 1, bool TMA = false,
+          bool VISC = false>
 EnsembleEntry ensemble_entry() {
   using Sh = StageShape<2, NF, WO, RT, TX, TY>;
   return EnsembleEntry{NF,
@@ -127,13 +133,14 @@ EnsembleEntry ensemble_entry() {
                        TX,
                        TY,
                        NT,
-                       ensemble_smem<NF, WO, RT, TX, TY, NT, GATE, TMA>(false),
-                       ensemble_smem<NF, WO, RT, TX, TY, NT, GATE, TMA>(true),
-                       reinterpret_cast<const void*>(ensemble_func<NF, WO, RT, TX, TY, NT, GATE, MINB, TMA>()),
-                       &ensemble_launch<NF, WO, RT, TX, TY, NT, GATE, MINB, TMA>,
+                       ensemble_smem<NF, WO, RT, TX, TY, NT, GATE, TMA, VISC>(false),
+                       ensemble_smem<NF, WO, RT, TX, TY, NT, GATE, TMA, VISC>(true),
+                       reinterpret_cast<const void*>(ensemble_func<NF, WO, RT, TX, TY, NT, GATE, MINB, TMA, VISC>()),
+                       &ensemble_launch<NF, WO, RT, TX, TY, NT, GATE, MINB, TMA, VISC>,
                        TMA,
                        TmaBox<TX, Sh::H>::kWidth,
-                       Sh::LY};
+                       Sh::LY,
+                       VISC};
 }
 
 void register_ensemble_fp64(std::vector<EnsembleEntry>& r);

@@ -131,16 +131,16 @@ StageEntry stage_entry() {
 // MINB2 > 0 caps the registers of the z sweep (which also does the RK
 // combination) so that MINB2 of its blocks fit on an SM.
 template <int NF, int WO, class RT, int TA0, int TB0, int TC0, int TA1, int TB1, int NT, bool TMA = false,
-          int MINB2 = 0>
+          int MINB2 = 0, bool CHAR = false>
 struct Sweep3D {
   template <int DIR>
   using K = std::conditional_t<DIR == 0, SweepShape<NF, WO, RT, 0, TA0, TB0, TC0>,
                                SweepShape<NF, WO, RT, DIR, TA1, TB1, 1>>;
   template <int DIR>
   static constexpr auto func() {
-    if constexpr (DIR == 0) return &sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT, TMA>;
-    else if constexpr (DIR == 2) return &sweep_kernel<NF, WO, RT, 2, TA1, TB1, 1, NT, TMA, MINB2>;
-    else return &sweep_kernel<NF, WO, RT, DIR, TA1, TB1, 1, NT, TMA>;
+    if constexpr (DIR == 0) return &sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT, TMA, 0, CHAR>;
+    else if constexpr (DIR == 2) return &sweep_kernel<NF, WO, RT, 2, TA1, TB1, 1, NT, TMA, MINB2, CHAR>;
+    else return &sweep_kernel<NF, WO, RT, DIR, TA1, TB1, 1, NT, TMA, 0, CHAR>;
   }
 
   template <int DIR>
@@ -181,7 +181,7 @@ struct Sweep3D {
     static_assert(!TMA || (K<0>::kTmaFits && K<1>::kTmaFits && K<2>::kTmaFits),
                   "the TMA box of every sweep must fit its WENO and flux arrays");
     return StageEntry{3, NF, WO, sizeof(RT) == 8 ? 0 : 1, TA0, TB1, NT, K<1>::kSmemBytes, 3, &prepare, &launch,
-                      false, TMA};
+                      false, TMA, CHAR};
   }
 };
 

@@ -60,7 +60,9 @@ __device__ __forceinline__ void sweep_coords(int a, int b, int c, int& x, int& y
 // tensor copy (T maps the stage input qin; T.on = 0: plain loads only).
 // MINB > 0 caps the registers so that MINB blocks fit on an SM; MINB = 0
 // leaves the minimum unspecified (ptxas allocates as without the bound).
-template <int NF, int WO, class RT, int DIR, int TA, int TB, int TC, int NT, bool TMA = false, int MINB = 0>
+// CHAR: WENO of the characteristic fields (char_weno_position, FP64).
+template <int NF, int WO, class RT, int DIR, int TA, int TB, int TC, int NT, bool TMA = false, int MINB = 0,
+          bool CHAR = false>
 __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, const __grid_constant__ UniformCoef U,
                                                    const __grid_constant__ TileMap T, const double* __restrict__ qin,
                                                    const double* __restrict__ qbase, double* __restrict__ qout,
@@ -302,6 +304,19 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
         one(v);
       }
     });
+  } else if constexpr (CHAR) {
+    static_assert(sizeof(RT) == 8 && WO > 1, "characteristic-field WENO is compiled for FP64 WENO3/5");
+    // one thread per position, all variables
+    for (int it = tid; it < NP * NCA; it += NT) {
+      const int ca = it % NCA, p = it / NCA;
+      double c[kCoefRec];
+      const int gi = clamp_coef_index(a0 - 1 + ca, na) + P.coff;
+#pragma unroll
+      for (int k = 0; k < kNumCoef; ++k) c[k] = __ldg(P.coef[DIR] + k * P.cstride[DIR] + gi);
+      char_weno_position<3, NF, WO, DIR>(
+          c, [&](int v, int o) { return sq[qi(v, p, ca + H - 1 + o)]; }, eps, P,
+          [&](int v) -> RT& { return wl[wi(v, p, ca)]; }, [&](int v) -> RT& { return wr[wi(v, p, ca)]; });
+    }
   } else {
     for (int it = tid; it < S * NP * NCA; it += NT) {
       const int ca = it % NCA;

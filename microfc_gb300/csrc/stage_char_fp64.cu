@@ -1,6 +1,7 @@
 // Instantiations of the fused stage kernel that reconstructs the
 // characteristic fields instead of the primitive variables (FP64, inviscid,
-// WENO3/5, 1-D and 2-D; mfc_gpu_set_reconstruction).  The first entry per
+// WENO3/5; the fused kernel in 1-D and 2-D, the directional sweeps in 3-D;
+// mfc_gpu_set_reconstruction).  The first entry per
 // configuration is the default.
 #include "mfc_launch.h"
 
@@ -19,6 +20,10 @@ void register_stage_char_fp64(std::vector<StageEntry>& r) {
   MFC_CHAR(1, 2, 3, 128, 1, 128)
   MFC_CHAR(1, 1, 3, 128, 1, 128)
 #undef MFC_CHAR
+  // 3-D: the directional sweeps
+  r.push_back(Sweep3D<2, 5, double, 32, 4, 2, 16, 16, 256, false, 0, true>::entry());
+  r.push_back(Sweep3D<1, 5, double, 32, 4, 2, 16, 16, 256, false, 0, true>::entry());
+  r.push_back(Sweep3D<2, 3, double, 32, 4, 2, 16, 16, 256, false, 0, true>::entry());
 }
 
 }  // namespace mfc

@@ -50,8 +50,6 @@ class Ensemble:
         on_device = states is None and ic == "device"
         for i, c in enumerate(self.cases):
             c.check()
-            if c.viscous:
-                raise ValueError("the ensemble kernels are inviscid")
             if on_device:
                 x_cb, y_cb, _ = preprocess.grid(c)
                 q = None
@@ -69,6 +67,8 @@ class Ensemble:
         h = ctypes.c_void_p()
         _lib.check(self.L.mfc_gpu_ensemble_init(params, _dp(dts), len(self.cases), ctypes.byref(h)))
         self._h = h
+        if any(c.viscous for c in self.cases):
+            self.set_viscosity([c.re_shear for c in self.cases], [c.re_bulk for c in self.cases])
         for i, q in enumerate(qs):
             if on_device:
                 self.generate_ic(i)
@@ -110,6 +110,21 @@ class Ensemble:
         a = np.empty(self.cases[i].shape)
         _lib.check(self.L.mfc_gpu_ensemble_download(self._h, int(i), _dp(a)))
         return a
+
+    def set_viscosity(self, re_shear, re_bulk) -> None:
+        """fluid_pp(f)%Re(1:2) of every case (one sequence of num_fluids
+        values per case; mfc_gpu_ensemble_set_viscosity).  Every case must be
+        viscous, or none."""
+        nf = self.cases[0].num_fluids
+
+        def table(rows):
+            a = np.zeros((len(self.cases), nf))
+            for i, r in enumerate(rows):
+                a[i, :len(r)] = r
+            return a
+
+        a, b = table(re_shear), table(re_bulk)
+        _lib.check(self.L.mfc_gpu_ensemble_set_viscosity(self._h, _dp(a), _dp(b)))
 
     def set_gate(self, params) -> None:
         """Parameters of the learned gate (precision "gated")."""

@@ -157,7 +157,7 @@ class Oracle:
                     for a in (x_cb, y_cb, z_cb)]
         self._h = L.mfo_create(ctypes.byref(self._q), *(_dp(a) for a in self._cb))
         if not self._h:
-            raise MemoryError("oracle allocation failed")
+            raise ValueError("oracle creation failed (missing cell boundaries of a used direction, or no memory)")
         self.S = L.mfo_sys_size(self._h)
         self.shape = (self.S, case.p + 1, case.n + 1, case.m + 1)
 

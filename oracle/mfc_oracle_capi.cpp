@@ -51,6 +51,8 @@ static Params to_params(const mfo_params* q) {
 }
 
 void* mfo_create(const mfo_params* q, const double* x_cb, const double* y_cb, const double* z_cb) {
+  // every used direction needs its cell boundaries
+  if (!q || !x_cb || (q->n > 0 && !y_cb) || (q->p > 0 && !z_cb)) return nullptr;
   auto* s = new (std::nothrow) Solver<double>();
   if (!s) return nullptr;
   s->init(to_params(q), x_cb, y_cb, z_cb);

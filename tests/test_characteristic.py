@@ -20,6 +20,9 @@ CASES = {
     "droplet": lambda: cases.shock_droplet_2d(nx=96, ny=64, steps=40),
     "droplet-bc-mix": lambda: cases.shock_droplet_2d(nx=64, ny=48, steps=30).replace(bc_x=(-2, -4), bc_y=(-1, -1)),
     "droplet-weno3": lambda: cases.shock_droplet_2d(nx=64, ny=48, steps=30).replace(weno_order=3),
+    "bubble3d": lambda: cases.shock_bubble_3d(N=32, steps=10, precision="fp64"),
+    "bubble3d-bc-mix": lambda: cases.shock_bubble_3d(N=28, steps=8, precision="fp64").replace(
+        bc_y=(-2, -4), bc_z=(-1, -1)),
 }
 
 
@@ -27,12 +30,12 @@ CASES = {
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_characteristic_weno_matches_the_oracle_bitwise(oracle_lib, name):
     case = CASES[name]().replace(char_decomp=True)
-    x_cb, y_cb, _, q = preprocess.generate(case)
-    o = oracle_lib.Oracle(case, x_cb, y_cb)
+    x_cb, y_cb, z_cb, q = preprocess.generate(case)
+    o = oracle_lib.Oracle(case, x_cb, y_cb, z_cb)
     o.set_state(q)
     dref = o.run(0, case.t_step_stop, case.dt)
     ref = o.get_state()
-    with Simulation(case, x_cb, y_cb, q_cons=q) as sim:
+    with Simulation(case, x_cb, y_cb, z_cb, q_cons=q) as sim:
         dgot = sim.run(0, case.t_step_stop)
         assert sim.status() == 0
         got = sim.download()
@@ -41,7 +44,7 @@ def test_characteristic_weno_matches_the_oracle_bitwise(oracle_lib, name):
     assert rel_l1(got, ref).max() <= 1e-10
     assert np.count_nonzero(got != ref) == 0, f"{np.count_nonzero(got != ref)} values differ"
     # and it is a different reconstruction from the primitive one
-    o2 = oracle_lib.Oracle(case.replace(char_decomp=False), x_cb, y_cb)
+    o2 = oracle_lib.Oracle(case.replace(char_decomp=False), x_cb, y_cb, z_cb)
     o2.set_state(q)
     o2.run(0, case.t_step_stop, case.dt)
     assert np.count_nonzero(o2.get_state() != ref) > 0
@@ -90,6 +93,7 @@ def test_characteristic_refusals():
 
 
 def test_case_check_refuses_unsupported_characteristic_configurations():
+    cases.shock_bubble_3d(N=32, steps=2, precision="fp64").replace(char_decomp=True).check()  # 3-D is taken
     with pytest.raises(ValueError):
         cases.shock_droplet_2d(nx=64, ny=32, steps=2, precision="split").replace(char_decomp=True).check()
     with pytest.raises(ValueError):

@@ -120,3 +120,35 @@ def test_ensemble_rejects_mixed_configurations_before_touching_a_device():
     rc = L.mfc_gpu_ensemble_init(arr, dts.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 2, ctypes.byref(h))
     assert rc == _lib.MFC_ERR_INVALID and not h.value
     assert "must share" in L.mfc_gpu_last_error().decode()
+
+
+def _viscous_mixed(precision):
+    re = dict(re_shear=(1.0 / 1e-1, 1.0 / 2e-3), re_bulk=(0.0, 1.0 / 5e-3))
+    return [c.replace(**re) for c in _mixed(precision)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_viscous_ensemble_matches_single_case_runs(precision):
+    """Viscous cases (mfc_gpu_ensemble_set_viscosity) get the bits of their
+    own viscous Simulation, with graph replay and after autotuning."""
+    cl = _viscous_mixed(precision)
+    with Ensemble(cl) as ens:
+        ens.tune(reps=2)
+        ens.run(0, 6, use_graph=True)
+        got = [ens.download(i) for i in range(len(cl))]
+    for c, g in zip(cl, got):
+        ref = _single(c, 6)
+        assert np.isfinite(g).all()
+        assert np.array_equal(g, ref), c.name
+    # and the viscous terms acted: the inviscid run differs
+    inv = _single(_mixed(precision)[0], 6)
+    assert not np.array_equal(got[0], inv)
+
+
+@pytest.mark.gpu
+def test_ensemble_refuses_a_mix_of_viscous_and_inviscid_cases():
+    cl = _mixed("fp64")
+    cl[1] = cl[1].replace(re_shear=(10.0, 10.0))
+    with pytest.raises(_lib.MfcError):
+        Ensemble(cl)
