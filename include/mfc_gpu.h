@@ -343,8 +343,8 @@ int mfc_gpu_ensemble_finalize(mfc_gpu_ensemble* ens);
  * re_shear[i * num_fluids + f] / re_bulk[...] are case i's fluid_pp(f+1)%Re(1)
  * / %Re(2) (NULL or values <= 0: none).  One kernel advances all cases, so
  * every case must be viscous or none (MFC_ERR_INVALID otherwise); all-zero
- * Reynolds numbers switch back to the inviscid kernels.  FP64 and split
- * precision (the gated ensemble is inviscid).  Call before stepping. */
+ * Reynolds numbers switch back to the inviscid kernels.  FP64, split and
+ * gated precision.  Call before stepping. */
 int mfc_gpu_ensemble_set_viscosity(mfc_gpu_ensemble* ens, const double* re_shear, const double* re_bulk);
 /* Gate parameters for a MFC_PREC_GATED ensemble (see mfc_gpu_set_gate). */
 int mfc_gpu_ensemble_set_gate(mfc_gpu_ensemble* ens, const float* host_params);

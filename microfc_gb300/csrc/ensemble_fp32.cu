@@ -32,6 +32,8 @@ void register_ensemble_gated(std::vector<EnsembleEntry>& r) {
   // interior tiles staged by one TMA bulk tensor copy (four blocks per SM:
   // the five-block cap spills the TMA kernel's registers)
   r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, true, 4, true>());
+  // with the viscous terms (mfc_gpu_ensemble_set_viscosity)
+  r.push_back(ensemble_entry<2, 5, float, 16, 16, 256, true, 1, false, true>());
 }
 
 }  // namespace mfc

@@ -455,7 +455,6 @@ int mfc_gpu_ensemble_run(mfc_gpu_ensemble* e, int t_step_start, int t_step_stop,
 
 int mfc_gpu_ensemble_set_viscosity(mfc_gpu_ensemble* e, const double* re_shear, const double* re_bulk) {
   if (!e) return mfc::report_error(MFC_ERR_INVALID, "NULL ensemble");
-  if (e->gate_w) return mfc::report_error(MFC_ERR_INVALID, "the gated ensemble kernels are inviscid");
   const int nf = e->nf;
   std::vector<mfc::ViscParams> V((size_t)e->num);
   int viscous_cases = 0;

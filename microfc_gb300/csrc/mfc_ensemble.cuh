@@ -43,7 +43,7 @@ static_assert(sizeof(EnsParams) <= 32764, "ensemble parameters must fit the kern
 // VISC: every case carries its viscosity parameters (DevParams::visc).
 template <int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool TMA, bool VISC = false>
 __device__ __forceinline__ void ensemble_walk(const EnsParams& E) {
-  static_assert(!VISC || (!GATE && !TMA), "the viscous ensemble kernels are ungated and load their tiles plainly");
+  static_assert(!VISC || !TMA, "the viscous ensemble kernels load their tiles plainly");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t parity = 0;
   if constexpr (TMA) {

@@ -249,7 +249,6 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
                                            unsigned char* smem_raw, const UC* U = nullptr,
                                            const TileMap* T = nullptr, uint32_t* tma_parity = nullptr) {
   static_assert(!GATE || (sizeof(RT) == 4 && WO == 5), "the learned gate runs on the split-precision WENO5 path");
-  static_assert(!(GATE && VISC), "the gated kernel is inviscid");
   static_assert(!CHAR || (sizeof(RT) == 8 && WO > 1 && !VISC && !GATE && ND < 3),
                 "characteristic-field WENO is compiled for the inviscid FP64 1-D/2-D WENO3/5 kernel");
   using Sh = StageShape<ND, NF, WO, RT, TX, TY, VISC>;

@@ -128,21 +128,33 @@ def _viscous_mixed(precision):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp64", "split"])
+@pytest.mark.parametrize("precision", ["fp64", "split", "gated"])
 def test_viscous_ensemble_matches_single_case_runs(precision):
     """Viscous cases (mfc_gpu_ensemble_set_viscosity) get the bits of their
     own viscous Simulation, with graph replay and after autotuning."""
+    from microfc_gb300 import gate
+    params = gate.load() if precision == "gated" else None
+
+    def single(c):
+        with Simulation(c) as sim:
+            if params is not None:
+                sim.set_gate(params)
+            sim.run(0, 6)
+            return sim.download()
+
     cl = _viscous_mixed(precision)
     with Ensemble(cl) as ens:
+        if params is not None:
+            ens.set_gate(params)
         ens.tune(reps=2)
         ens.run(0, 6, use_graph=True)
         got = [ens.download(i) for i in range(len(cl))]
     for c, g in zip(cl, got):
-        ref = _single(c, 6)
+        ref = single(c)
         assert np.isfinite(g).all()
         assert np.array_equal(g, ref), c.name
     # and the viscous terms acted: the inviscid run differs
-    inv = _single(_mixed(precision)[0], 6)
+    inv = single(_mixed(precision)[0])
     assert not np.array_equal(got[0], inv)
 
 

@@ -80,6 +80,29 @@ def test_split_precision_viscous_error_bounded(oracle_lib):
     assert err[[0, 1, c.adv_idx, c.adv_idx + 1]].max() <= 1e-3, err
 
 
+def test_gated_viscous_error_bounded_and_the_viscous_terms_act(oracle_lib):
+    """The learned gate with the viscous terms: within the gated form's bar
+    (density and volume-fraction L1 <= 1e-3) of the FP64 oracle, and
+    different from the inviscid gated run."""
+    from microfc_gb300 import Simulation, gate
+    params = gate.load()
+    c = _viscous_droplet(precision="gated")
+    x_cb, y_cb, _, q = preprocess.generate(c)
+    out = {}
+    for name, case in (("viscous", c), ("inviscid", c.replace(re_shear=(), re_bulk=()))):
+        with Simulation(case, x_cb, y_cb, q_cons=q) as sim:
+            sim.set_gate(params)
+            sim.run(0, c.t_step_stop)
+            assert sim.status() == 0
+            out[name] = sim.download()
+    o = oracle_lib.Oracle(c.replace(precision="fp64"), x_cb, y_cb)
+    o.set_state(q)
+    o.run(0, c.t_step_stop, c.dt)
+    err = rel_l1(out["viscous"], o.get_state())
+    assert err[[0, 1, c.adv_idx, c.adv_idx + 1]].max() <= 1e-3, err
+    assert rel_l1(out["viscous"], out["inviscid"])[c.mom_idx] > 1e-8
+
+
 def test_viscous_refusals():
     from microfc_gb300 import Simulation
     from microfc_gb300._lib import MfcError
