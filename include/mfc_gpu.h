@@ -137,7 +137,8 @@ int mfc_gpu_compute_rhs(mfc_gpu_ctx* ctx, double* rhs_out, double* prim_out);
  * with the case's boundary conditions in the ghost cells (m_rhs.fpp:434-447):
  * vL / vR receive the left-face (x_{j-1/2}) and right-face (x_{j+1/2}) values
  * over the face window, the part of the reference's is1 x is2 window that the
- * Riemann solver reads. */
+ * Riemann solver reads.  Synchronous; both entry points allocate their
+ * device buffers for the call (host arrays in and out). */
 int mfc_gpu_weno(mfc_gpu_ctx* ctx, int dir, double* vL, double* vR);
 
 /* Drop-in for s_hllc_riemann_solver (src/simulation/m_riemann_solvers.fpp:
@@ -344,7 +345,8 @@ int mfc_gpu_ensemble_finalize(mfc_gpu_ensemble* ens);
  * / %Re(2) (NULL or values <= 0: none).  One kernel advances all cases, so
  * every case must be viscous or none (MFC_ERR_INVALID otherwise); all-zero
  * Reynolds numbers switch back to the inviscid kernels.  FP64, split and
- * gated precision.  Call before stepping. */
+ * gated precision.  Call before stepping and before mfc_gpu_ensemble_tune
+ * (it selects the first compiled viscous variant). */
 int mfc_gpu_ensemble_set_viscosity(mfc_gpu_ensemble* ens, const double* re_shear, const double* re_bulk);
 /* Gate parameters for a MFC_PREC_GATED ensemble (see mfc_gpu_set_gate). */
 int mfc_gpu_ensemble_set_gate(mfc_gpu_ensemble* ens, const float* host_params);
