@@ -84,15 +84,16 @@ EncodeTiled tiled_encoder() {
   return encode;
 }
 
-// FP64 tensor of `rank` dimensions (x first, the variable last); strides in
-// elements for dimensions 1.. .  TMA rules: 16-byte aligned base and
-// strides, boxes of at most 256 cells per dimension whose rows are a
-// multiple of 16 bytes.
-bool encode_fp64(TileMap& t, const double* base, int rank, const int64_t* dims, const int64_t* strides,
-                 const int* box) {
+// FP64 (elem_bytes 8) or FP32 (4) tensor of `rank` dimensions (x first, the
+// variable last); strides in elements for dimensions 1.. .  TMA rules:
+// 16-byte aligned base and strides, boxes of at most 256 cells per
+// dimension whose rows are a multiple of 16 bytes.
+bool encode_tensor(TileMap& t, const void* base, int elem_bytes, int rank, const int64_t* dims,
+                   const int64_t* strides, const int* box) {
   std::memset(&t, 0, sizeof(t));
   const EncodeTiled encode = tiled_encoder();
-  if (!encode || !base || reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
+  if (!encode || !base || reinterpret_cast<uintptr_t>(base) % 16 != 0 || (elem_bytes != 8 && elem_bytes != 4))
+    return false;
   cuuint64_t gd[5], gs[4];
   cuuint32_t bd[5], unit[5];
   for (int d = 0; d < rank; ++d) {
@@ -101,15 +102,15 @@ bool encode_fp64(TileMap& t, const double* base, int rank, const int64_t* dims, 
     bd[d] = cuuint32_t(box[d]);
     unit[d] = 1;
     if (d > 0) {
-      if ((strides[d - 1] * 8) % 16 != 0 || strides[d - 1] * 8 >= (int64_t(1) << 40)) return false;
-      gs[d - 1] = cuuint64_t(strides[d - 1]) * 8;
+      if ((strides[d - 1] * elem_bytes) % 16 != 0 || strides[d - 1] * elem_bytes >= (int64_t(1) << 40)) return false;
+      gs[d - 1] = cuuint64_t(strides[d - 1]) * elem_bytes;
     }
   }
-  if ((box[0] * 8) % 16 != 0) return false;
+  if ((box[0] * elem_bytes) % 16 != 0) return false;
   const CUresult r =
-      encode(&t.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, cuuint32_t(rank), const_cast<double*>(base), gd, gs, bd, unit,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      encode(&t.map, elem_bytes == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+             cuuint32_t(rank), const_cast<void*>(base), gd, gs, bd, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     std::memset(&t, 0, sizeof(t));
     return false;
@@ -127,18 +128,18 @@ bool encode_tile_map(TileMap& t, const double* base, int nx, int ny, int S, int6
   }
   const int64_t dims[3] = {nx, ny, S}, strides[2] = {sy, sv};
   const int box[3] = {box_w, box_h, S};
-  return encode_fp64(t, base, 3, dims, strides, box);
+  return encode_tensor(t, base, 8, 3, dims, strides, box);
 }
 
-bool encode_tile_map_3d(TileMap& t, const double* base, int nx, int ny, int nz, int S, int64_t sy, int64_t sz,
-                        int64_t sv, int bx, int by, int bz) {
+bool encode_tile_map_3d(TileMap& t, const void* base, int elem_bytes, int nx, int ny, int nz, int S, int64_t sy,
+                        int64_t sz, int64_t sv, int bx, int by, int bz) {
   if (sy < nx || sz < sy * ny || sv < sz * nz) {
     std::memset(&t, 0, sizeof(t));
     return false;
   }
   const int64_t dims[4] = {nx, ny, nz, S}, strides[3] = {sy, sz, sv};
   const int box[4] = {bx, by, bz, S};
-  return encode_fp64(t, base, 4, dims, strides, box);
+  return encode_tensor(t, base, elem_bytes, 4, dims, strides, box);
 }
 }  // namespace mfc
 
@@ -150,7 +151,7 @@ struct mfc_gpu_ctx {
   double* state = nullptr;      // 3 registers
   double* reg[3] = {nullptr, nullptr, nullptr};
   double* rhs = nullptr;
-  double* work = nullptr;       // 3-D: partial RHS between the directional sweeps
+  double* work = nullptr;       // 3-D: partial RHS between the directional sweeps, then the primitives
   void* gate_w = nullptr;       // MFC_PREC_GATED: FP16 gate parameters
   uint8_t* gate_flags = nullptr;  // MFC_PREC_GATED: a step's first-stage gate decisions
   bool gate_ready = false;
@@ -370,7 +371,9 @@ int mfc_gpu_init(const mfc_params* p, mfc_gpu_ctx** out) {
   if (p->precision == MFC_PREC_GATED &&
       (e = cudaMalloc(&c->gate_flags, mfc::gate_flag_bytes(c->n[0], c->n[1]))) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
-  if (c->nd == 3 && (e = cudaMalloc(&c->work, sizeof(double) * c->reg_elems)) != cudaSuccess)
+  // 3-D: the partial RHS, then the primitives the x sweep stores (S x sv
+  // values each, in the reconstruction type: FP64 at most)
+  if (c->nd == 3 && (e = cudaMalloc(&c->work, sizeof(double) * c->reg_elems * 2)) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));
   if ((e = cudaMalloc(&c->monitor, sizeof(unsigned long long))) != cudaSuccess)
     return cleanup(fail(MFC_ERR_NOMEM, cudaGetErrorString(e)));

@@ -38,7 +38,9 @@ struct DevParams {
   // one slot: the ensemble's 96 parameter blocks must fit the kernel
   // parameter space.
   union {
-    // 3-D: partial RHS between the directional sweeps ([S][z][y][x], RT)
+    // 3-D: partial RHS between the directional sweeps ([S][z][y][x], RT),
+    // then the primitives of the stage input that the x sweep stores (same
+    // layout, RT)
     void* work;
     // learned WENO gate: the decisions of a time step's first stage, one
     // byte per reconstructed cell and direction, reused by its later stages

@@ -153,13 +153,19 @@ struct Sweep3D {
     if (e == cudaSuccess) e = prep<2>();
     return e;
   }
-  // the map of the stage input for the sweep's box (none: plain loads)
+  // the map of the sweep's box (none: plain loads): the stage input for the
+  // x sweep, the primitives the x sweep stores (the work buffer's second
+  // segment, reconstruction type) for the y and z sweeps
   template <int DIR>
   static TileMap tile_map(const DevParams& P, const double* qin) {
     TileMap T{};
-    if constexpr (TMA && K<DIR>::kTmaFits)
-      encode_tile_map_3d(T, qin, P.n[0], P.n[1], P.n[2], K<DIR>::S, P.sy, P.sz, P.sv, K<DIR>::BX, K<DIR>::BY,
-                         K<DIR>::BZ);
+    if constexpr (TMA && K<DIR>::kTmaFits) {
+      constexpr int S = K<DIR>::S;
+      const void* base = DIR == 0 ? static_cast<const void*>(qin)
+                                  : static_cast<const void*>(static_cast<const RT*>(P.work) + int64_t(S) * P.sv);
+      encode_tile_map_3d(T, base, K<DIR>::kStageElem, P.n[0], P.n[1], P.n[2], S, P.sy, P.sz, P.sv, K<DIR>::BX,
+                         K<DIR>::BY, K<DIR>::BZ);
+    }
     return T;
   }
   static cudaError_t launch(const DevParams& P, const UniformCoef& U, const double* qin, const double* qbase,

@@ -14,12 +14,30 @@
 // cells that border the block's faces, solves TA+1 Riemann problems per
 // pencil and forms the flux divergence.  The partial RHS lives in a global
 // buffer (FP64, or FP32 on the split path) between the sweeps.
+//
+// The x sweep also stores the primitive variables of the cells it owns (the
+// work buffer's second segment, [S][z][y][x] in the reconstruction type),
+// and the y and z sweeps read them instead of converting the state again:
+// the conversion's FP64 operations (E - Pi, and the divisions of the plain
+// path) run once per cell and stage instead of three times, and the split
+// path's y and z sweeps load 4-byte instead of 8-byte values.  The stored
+// values are the bits the conversion gives, and a reflected ghost cell's
+// normal velocity is the stored one negated, which is what converting the
+// reflected momentum gives (the conversion is odd in the momentum), so the
+// result is unchanged bit for bit.  Ghost cells of processor boundaries come
+// from the halo buffers as conservative values and are converted as before.
 #pragma once
 
 #include "mfc_device.cuh"
 #include "mfc_stage.cuh"
 
 namespace mfc {
+
+// A stage kind as a type (the sweep's last phase is compiled once per kind).
+template <int K>
+struct KindC {
+  static constexpr int value = K;
+};
 
 template <int NF, int WO, class RT, int DIR, int TA, int TB, int TC>
 struct SweepShape {
@@ -41,8 +59,10 @@ struct SweepShape {
   static constexpr int BX = DIR == 0 ? TmaBox<TA, H>::kWidth : TB;
   static constexpr int BY = DIR == 0 ? TB : (DIR == 1 ? LA : TC);
   static constexpr int BZ = DIR == 0 ? TC : (DIR == 1 ? TC : LA);
-  static constexpr uint32_t kStageBytes = uint32_t(BX) * BY * BZ * S * 8;
-  static constexpr bool kTmaFits = (BX * 8) % 16 == 0 && BX <= 256 && BY <= 256 && BZ <= 256 &&
+  // the x sweep stages the FP64 state, the y and z sweeps the stored primitives
+  static constexpr int kStageElem = DIR == 0 ? 8 : int(sizeof(RT));
+  static constexpr uint32_t kStageBytes = uint32_t(BX) * BY * BZ * S * kStageElem;
+  static constexpr bool kTmaFits = (BX * kStageElem) % 16 == 0 && BX <= 256 && BY <= 256 && BZ <= 256 &&
                                    size_t(kStageBytes) + 128 + 16 <= sizeof(RT) * size_t(OC - NQ);
 };
 
@@ -57,7 +77,8 @@ __device__ __forceinline__ void sweep_coords(int a, int b, int c, int& x, int& y
 }
 
 // TMA: a tile whose sweep halo lies inside the domain arrives by one bulk
-// tensor copy (T maps the stage input qin; T.on = 0: plain loads only).
+// tensor copy (T maps the stage input qin on the x sweep and the stored
+// primitives on the y and z sweeps; T.on = 0: plain loads only).
 // MINB > 0 caps the registers so that MINB blocks fit on an SM; MINB = 0
 // leaves the minimum unspecified (ptxas allocates as without the bound).
 // CHAR: WENO of the characteristic fields (char_weno_position, FP64).
@@ -130,18 +151,33 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
               : 0.f;
     }
   }
-  // one cell: BCs applied, cons -> prim into the tile
-  auto store_prim = [&](double (&q)[S], const int p, const int la) {
+  // the primitives of the stage input: written by the x sweep for the cells
+  // it owns, read by the y and z sweeps
+  RT* const gprim = reinterpret_cast<RT*>(P.work) + int64_t(S) * P.sv;
+  // one cell: BCs applied, cons -> prim into the tile; the x sweep also
+  // stores the cells of its own tile (la = H .. H+TA-1 inside the domain;
+  // own: the cell's offset, or -1)
+  auto store_prim = [&](double (&q)[S], const int p, const int la, const int64_t own) {
+    RT pr[S];
     if constexpr (kSplit) {
-      float pr[S];
       cons_to_prim_split<3, NF>(q, P, pr);
-#pragma unroll
-      for (int v = 0; v < S; ++v) sq[qi(v, p, la)] = pr[v];
     } else {
       cons_to_prim<3, NF>(q, P);
 #pragma unroll
-      for (int v = 0; v < S; ++v) sq[qi(v, p, la)] = RT(q[v]);
+      for (int v = 0; v < S; ++v) pr[v] = q[v];
     }
+#pragma unroll
+    for (int v = 0; v < S; ++v) sq[qi(v, p, la)] = pr[v];
+    if (DIR == 0 && own >= 0) {
+#pragma unroll
+      for (int v = 0; v < S; ++v) gprim[own + v * P.sv] = pr[v];
+    }
+  };
+  // x sweep: the offset of tile cell (la, pb, pc) when the block owns it
+  auto owned = [&](const int la, const int pb, const int pc) -> int64_t {
+    const int ga = a0 - H + la, gb = b0 + pb, gc = c0 + pc;
+    if (la < H || la >= H + TA || ga >= na || gb >= nb || gc >= nc) return -1;
+    return int64_t(gc) * P.sz + int64_t(gb) * P.sy + ga;
   };
   bool use_tma = false;
   unsigned char* stg = nullptr;
@@ -201,7 +237,6 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
       return;
     }
     (void)mbar_try_wait(bar, 0);  // completed: each thread acquires the copy's writes
-    const double* sd = reinterpret_cast<const double*>(stg);
     for (int it = tid; it < NP * LA; it += NT) {
       int la, pb, pc;
       if (DIR == 0) { la = it % LA; pb = (it / LA) % TB; pc = it / (LA * TB); }
@@ -211,10 +246,17 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
       if (DIR == 0) { bx = la + TmaBox<TA, H>::kLead - H; by = pb; bz = pc; }
       else if (DIR == 1) { bx = pb; by = la; bz = pc; }
       else { bx = pb; by = pc; bz = la; }
-      double q[S];
+      if constexpr (DIR == 0) {
+        const double* sd = reinterpret_cast<const double*>(stg);
+        double q[S];
 #pragma unroll
-      for (int v = 0; v < S; ++v) q[v] = sd[((v * Sh::BZ + bz) * Sh::BY + by) * Sh::BX + bx];
-      store_prim(q, pc * TB + pb, la);
+        for (int v = 0; v < S; ++v) q[v] = sd[((v * Sh::BZ + bz) * Sh::BY + by) * Sh::BX + bx];
+        store_prim(q, pc * TB + pb, la, owned(la, pb, pc));
+      } else {
+        const RT* sd = reinterpret_cast<const RT*>(stg);
+#pragma unroll
+        for (int v = 0; v < S; ++v) sq[qi(v, pc * TB + pb, la)] = sd[((v * Sh::BZ + bz) * Sh::BY + by) * Sh::BX + bx];
+      }
     }
   } else {  // plain loads, with the boundary conditions and processor halos
     // thread order: the a index fastest for the x sweep, the pencil b index
@@ -244,13 +286,22 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
         else { src = h + ((int64_t)d * ny + y) * nx + x; vs = (int64_t)H * ny * nx; }
       } else {
         const int ga = map_cell(ra, na, P.bc_beg[OA], P.bc_end[OA], &fa);
-        src = qin + ga * st[OA] + gb * st[OB] + gc * st[OC];
+        const int64_t o = ga * st[OA] + gb * st[OB] + gc * st[OC];
+        if constexpr (DIR > 0) {
+          // the stored primitives; a reflected cell's normal velocity negated
+          const int p = pc * TB + pb;
+#pragma unroll
+          for (int v = 0; v < S; ++v) sq[qi(v, p, la)] = __ldg(gprim + o + v * P.sv);
+          if (fa) sq[qi(Q::MOM + DIR, p, la)] = -sq[qi(Q::MOM + DIR, p, la)];
+          continue;
+        }
+        src = qin + o;
       }
       double q[S];
 #pragma unroll
       for (int v = 0; v < S; ++v) q[v] = __ldg(src + v * vs);
       if (fa) q[Q::MOM + DIR] = -q[Q::MOM + DIR];
-      store_prim(q, pc * TB + pb, la);
+      store_prim(q, pc * TB + pb, la, DIR == 0 ? owned(la, pb, pc) : -1);
     }
   }
   __syncthreads();
@@ -363,6 +414,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
   double icfl = 0.0;
   const float dtf = kSplit ? __double2float_rn(dt) : 0.f;  // the split path's increments are FP32
   (void)dtf;
+  // KIND: the stage's combination as a compile-time constant, so that the z
+  // sweep chooses it once per block rather than once per cell and variable
+  auto finish = [&](auto kind_c) {
+  constexpr int KIND = decltype(kind_c)::value;
   for (int it = tid; it < NP * TA; it += NT) {
     int ta, pb, pc;
     if (DIR == 0) { ta = it % TA; pb = (it / TA) % TB; pc = it / (TA * TB); }
@@ -386,31 +441,55 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
       const AT a = AT(sq[qi(Q::ADV + f, p, ta + H)]);
       r[Q::ADV + f] = mul_add(inv * a, du, r[Q::ADV + f]);
     }
-    if (DIR < 2) {
+    if constexpr (DIR < 2) {
 #pragma unroll
       for (int v = 0; v < S; ++v) rhs_buf[o + v * P.sv] = r[v];
       continue;
     }
-    double qn[S];
 #pragma unroll
     for (int v = 0; v < S; ++v) {
       double out;
-      if (kind == kRhsOnly) {
+      if constexpr (KIND == kRhsOnly) {
         out = widen(r[v]);
       } else {
         const double b = __ldg(qbase + o + v * P.sv);
-        const double in = (kind == kRkEuler) ? b : __ldg(qin + o + v * P.sv);
-        if constexpr (kSplit) out = rk_combine_split(kind, b, in, dtf, r[v]);
-        else out = rk_combine(kind, b, in, dt, r[v]);
+        double in = b;
+        if constexpr (KIND != kRkEuler) in = __ldg(qin + o + v * P.sv);
+        if constexpr (kSplit) out = rk_combine_split(KIND, b, in, dtf, r[v]);
+        else out = rk_combine(KIND, b, in, dt, r[v]);
       }
       bad |= not_finite(out);
       qout[o + v * P.sv] = out;
-      qn[v] = out;
     }
-    if (P.monitor) {
+  }
+  // the stability monitor (the last stage of a monitored step) reads the
+  // new state back: this thread's own stores, from L1
+  if (DIR == 2 && P.monitor) {
+    for (int it = tid; it < NP * TA; it += NT) {
+      const int pb = it % TB, ta = (it / TB) % TA, pc = it / (TB * TA);
+      const int ga = a0 + ta, gb = b0 + pb, gc = c0 + pc;
+      if (ga >= na || gb >= nb || gc >= nc) continue;
+      int x, y, z;
+      sweep_coords<DIR>(ga, gb, gc, x, y, z);
+      const int64_t o = z * P.sz + y * P.sy + x;
+      double qn[S];
+#pragma unroll
+      for (int v = 0; v < S; ++v) qn[v] = qout[o + v * P.sv];
       const double inv[3] = {__ldg(P.inv_d[0] + x), __ldg(P.inv_d[1] + y), __ldg(P.inv_d[2] + z)};
       const double c = cell_icfl<3, NF>(qn, P, dt, inv);
       if (!(c <= icfl)) icfl = c;  // keeps NaN
+    }
+  }
+  };
+  if constexpr (DIR < 2) {
+    finish(KindC<kRhsOnly>{});  // the x and y sweeps store the partial RHS whatever the kind
+  } else {
+    switch (kind) {
+      case kRkEuler: finish(KindC<kRkEuler>{}); break;
+      case kRk2Final: finish(KindC<kRk2Final>{}); break;
+      case kRk3Mid: finish(KindC<kRk3Mid>{}); break;
+      case kRk3Final: finish(KindC<kRk3Final>{}); break;
+      default: finish(KindC<kRhsOnly>{}); break;
     }
   }
   if (bad && P.status) atomicOr(P.status, 1u);

@@ -121,9 +121,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
 bool encode_tile_map(TileMap& t, const double* base, int nx, int ny, int S, int64_t sy, int64_t sv, int box_w,
                      int box_h);
 
-// The same for a 3-D register [S][nz][ny][sy] (plane stride sz) as a 4-D
-// tensor (x, y, z, variable) with a box of bx x by x bz x S cells.
-bool encode_tile_map_3d(TileMap& t, const double* base, int nx, int ny, int nz, int S, int64_t sy, int64_t sz,
-                        int64_t sv, int bx, int by, int bz);
+// The same for a 3-D array [S][nz][ny][sy] (plane stride sz) of FP64
+// (elem_bytes 8) or FP32 (4) values as a 4-D tensor (x, y, z, variable) with
+// a box of bx x by x bz x S cells.
+bool encode_tile_map_3d(TileMap& t, const void* base, int elem_bytes, int nx, int ny, int nz, int S, int64_t sy,
+                        int64_t sz, int64_t sv, int bx, int by, int bz);
 
 }  // namespace mfc
