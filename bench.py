@@ -458,20 +458,29 @@ def main():
     # algorithmic bytes of the timed steps over their time (in 2-D: one
     # launch's bytes over the launch's average duration)
     achieved = bytes_per_update * cells * args.steps / t_total / 1e9
-    traffic = _profile_value("stage_kernel_fp64_droplet_1024x512.md", "dram_bytes_per_launch")
+    # the headline configuration, or a profiling run that names its own workload
+    headline = args.case == "droplet2d" and args.precision == "fp64" and (args.nx, args.ny) == (NX, NY)
+    prec_label = "plain FP64" if args.precision == "fp64" else args.precision
+    if args.case == "droplet2d":
+        workload = WORKLOAD if (args.nx, args.ny) == (NX, NY) else WORKLOAD.replace(f"{NX}x{NY}", f"{args.nx}x{args.ny}")
+        workload = workload.replace("plain FP64", prec_label)
+    else:
+        workload = f"3-D shock-bubble {case.m + 1}^3, 2 fluids, WENO5-JS + HLLC + TVD-RK3, {prec_label} (profiling run)"
+    metric = METRIC if headline else f"cell-updates/s ({workload})"
+    # DRAM bytes per launch measured by ncu for the headline kernel only
+    traffic = _profile_value("stage_kernel_fp64_droplet_1024x512.md", "dram_bytes_per_launch") if headline else None
     flops = _profile_value("flop_count_droplet_1024x512.md", "algorithmic_flops_per_cell_update")
     hbm_roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "traffic": traffic, "bytes_per_cell_update": bytes_per_update,
                 "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"}
     line = {
-        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+        "metric": metric, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
         "dtype": {"fp64": "f64", "fp64_fma": "f64 (multiply-add contraction)", "split": "f64 state / f32 WENO+HLLC",
                   "gated": "f64 state / f32 WENO+HLLC + learned gate"}[args.precision],
         "data": "synthetic (reference-style case inputs, generated in-process)",
-        "config": {"workload": (WORKLOAD if args.precision == "fp64" else WORKLOAD.replace("plain FP64", args.precision))
-                   if args.case == "droplet2d" else f"3-D shock-bubble {case.m + 1}^3 (profiling run), {args.precision}",
+        "config": {"workload": workload,
                    "cells": cells, "equations": case.sys_size, "dt": case.dt,
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}",
                    "tile": {"variant": variant, "tx": tile[0], "ty": tile[1], "threads": tile[2],
