@@ -417,69 +417,69 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
   // KIND: the stage's combination as a compile-time constant, so that the z
   // sweep chooses it once per block rather than once per cell and variable
   auto finish = [&](auto kind_c) {
-  constexpr int KIND = decltype(kind_c)::value;
-  for (int it = tid; it < NP * TA; it += NT) {
-    int ta, pb, pc;
-    if (DIR == 0) { ta = it % TA; pb = (it / TA) % TB; pc = it / (TA * TB); }
-    else { pb = it % TB; ta = (it / TB) % TA; pc = it / (TB * TA); }
-    const int ga = a0 + ta, gb = b0 + pb, gc = c0 + pc;
-    if (ga >= na || gb >= nb || gc >= nc) continue;
-    const int p = pc * TB + pb;
-    int x, y, z;
-    sweep_coords<DIR>(ga, gb, gc, x, y, z);
-    const int64_t o = z * P.sz + y * P.sy + x;
-    const AT inv = narrow<AT>(__ldg(P.inv_d[DIR] + ga));
-    AT r[S];
-#pragma unroll
-    for (int v = 0; v < S; ++v) {
-      const AT diff = AT(fl[(v * NP + p) * NFA + ta]) - AT(fl[(v * NP + p) * NFA + ta + 1]);
-      r[v] = (DIR == 0) ? inv * diff : mul_add(inv, diff, rhs_buf[o + v * P.sv]);
-    }
-    const AT du = AT(fl[(S * NP + p) * NFA + ta + 1]) - AT(fl[(S * NP + p) * NFA + ta]);
-#pragma unroll
-    for (int f = 0; f < NF; ++f) {
-      const AT a = AT(sq[qi(Q::ADV + f, p, ta + H)]);
-      r[Q::ADV + f] = mul_add(inv * a, du, r[Q::ADV + f]);
-    }
-    if constexpr (DIR < 2) {
-#pragma unroll
-      for (int v = 0; v < S; ++v) rhs_buf[o + v * P.sv] = r[v];
-      continue;
-    }
-#pragma unroll
-    for (int v = 0; v < S; ++v) {
-      double out;
-      if constexpr (KIND == kRhsOnly) {
-        out = widen(r[v]);
-      } else {
-        const double b = __ldg(qbase + o + v * P.sv);
-        double in = b;
-        if constexpr (KIND != kRkEuler) in = __ldg(qin + o + v * P.sv);
-        if constexpr (kSplit) out = rk_combine_split(KIND, b, in, dtf, r[v]);
-        else out = rk_combine(KIND, b, in, dt, r[v]);
-      }
-      bad |= not_finite(out);
-      qout[o + v * P.sv] = out;
-    }
-  }
-  // the stability monitor (the last stage of a monitored step) reads the
-  // new state back: this thread's own stores, from L1
-  if (DIR == 2 && P.monitor) {
+    constexpr int KIND = decltype(kind_c)::value;
     for (int it = tid; it < NP * TA; it += NT) {
-      const int pb = it % TB, ta = (it / TB) % TA, pc = it / (TB * TA);
+      int ta, pb, pc;
+      if (DIR == 0) { ta = it % TA; pb = (it / TA) % TB; pc = it / (TA * TB); }
+      else { pb = it % TB; ta = (it / TB) % TA; pc = it / (TB * TA); }
       const int ga = a0 + ta, gb = b0 + pb, gc = c0 + pc;
       if (ga >= na || gb >= nb || gc >= nc) continue;
+      const int p = pc * TB + pb;
       int x, y, z;
       sweep_coords<DIR>(ga, gb, gc, x, y, z);
       const int64_t o = z * P.sz + y * P.sy + x;
-      double qn[S];
+      const AT inv = narrow<AT>(__ldg(P.inv_d[DIR] + ga));
+      AT r[S];
 #pragma unroll
-      for (int v = 0; v < S; ++v) qn[v] = qout[o + v * P.sv];
-      const double inv[3] = {__ldg(P.inv_d[0] + x), __ldg(P.inv_d[1] + y), __ldg(P.inv_d[2] + z)};
-      const double c = cell_icfl<3, NF>(qn, P, dt, inv);
-      if (!(c <= icfl)) icfl = c;  // keeps NaN
+      for (int v = 0; v < S; ++v) {
+        const AT diff = AT(fl[(v * NP + p) * NFA + ta]) - AT(fl[(v * NP + p) * NFA + ta + 1]);
+        r[v] = (DIR == 0) ? inv * diff : mul_add(inv, diff, rhs_buf[o + v * P.sv]);
+      }
+      const AT du = AT(fl[(S * NP + p) * NFA + ta + 1]) - AT(fl[(S * NP + p) * NFA + ta]);
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        const AT a = AT(sq[qi(Q::ADV + f, p, ta + H)]);
+        r[Q::ADV + f] = mul_add(inv * a, du, r[Q::ADV + f]);
+      }
+      if constexpr (DIR < 2) {
+#pragma unroll
+        for (int v = 0; v < S; ++v) rhs_buf[o + v * P.sv] = r[v];
+        continue;
+      }
+#pragma unroll
+      for (int v = 0; v < S; ++v) {
+        double out;
+        if constexpr (KIND == kRhsOnly) {
+          out = widen(r[v]);
+        } else {
+          const double b = __ldg(qbase + o + v * P.sv);
+          double in = b;
+          if constexpr (KIND != kRkEuler) in = __ldg(qin + o + v * P.sv);
+          if constexpr (kSplit) out = rk_combine_split(KIND, b, in, dtf, r[v]);
+          else out = rk_combine(KIND, b, in, dt, r[v]);
+        }
+        bad |= not_finite(out);
+        qout[o + v * P.sv] = out;
+      }
     }
-  }
+    // the stability monitor (the last stage of a monitored step) reads the
+    // new state back: this thread's own stores, from L1
+    if (DIR == 2 && P.monitor) {
+      for (int it = tid; it < NP * TA; it += NT) {
+        const int pb = it % TB, ta = (it / TB) % TA, pc = it / (TB * TA);
+        const int ga = a0 + ta, gb = b0 + pb, gc = c0 + pc;
+        if (ga >= na || gb >= nb || gc >= nc) continue;
+        int x, y, z;
+        sweep_coords<DIR>(ga, gb, gc, x, y, z);
+        const int64_t o = z * P.sz + y * P.sy + x;
+        double qn[S];
+#pragma unroll
+        for (int v = 0; v < S; ++v) qn[v] = qout[o + v * P.sv];
+        const double inv[3] = {__ldg(P.inv_d[0] + x), __ldg(P.inv_d[1] + y), __ldg(P.inv_d[2] + z)};
+        const double c = cell_icfl<3, NF>(qn, P, dt, inv);
+        if (!(c <= icfl)) icfl = c;  // keeps NaN
+      }
+    }
   };
   if constexpr (DIR < 2) {
     finish(KindC<kRhsOnly>{});  // the x and y sweeps store the partial RHS whatever the kind
