@@ -97,8 +97,9 @@ int mfc_gpu_abi_version(void);
 /* Last error message of the calling thread (never NULL). */
 const char* mfc_gpu_last_error(void);
 
-/* Allocates the device state (3 RK registers + rhs + grid tables) and
- * uploads the grid.  Replaces s_initialize_*_module. */
+/* Allocates the device state (3 RK registers + rhs + grid tables; 3-D cases
+ * also a work area of 2 registers for the directional sweeps) and uploads
+ * the grid.  Replaces s_initialize_*_module. */
 int mfc_gpu_init(const mfc_params* params, mfc_gpu_ctx** ctx_out);
 
 /* Number of equations (sys_size = 2*num_fluids + num_dims + 1). */
