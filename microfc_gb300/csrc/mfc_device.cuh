@@ -810,6 +810,13 @@ enum RkKind : int {
   kRhsOnly = 4,   // store rhs itself (s_compute_rhs)
 };
 
+// A stage kind as a type: the kernels' last phase is compiled once per kind
+// and chosen once per block.
+template <int K>
+struct KindC {
+  static constexpr int value = K;
+};
+
 __device__ __forceinline__ double rk_combine(int kind, double base, double in, double dt, double r) {
   switch (kind) {
     case kRkEuler: return base + dt * r;

@@ -958,31 +958,55 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   const float dtf = kSplit ? __double2float_rn(dt) : 0.f;  // the split path's increments are FP32
   (void)dtf;
   double icfl = 0.0;
+  // KIND: the stage's combination as a compile-time constant, chosen once
+  // per block rather than once per cell and variable
+  auto finish = [&](auto kind_c) {
+    constexpr int KIND = decltype(kind_c)::value;
 #pragma unroll
-  for (int k = 0; k < CPT; ++k) {
-    const int e = tid + k * NT;
-    if (e >= TX * TYE) break;
-    const int tx = e % TX, ty = e / TX;
-    const int gx = x0 + tx, gy = y0 + ty;
-    if (gx >= nx || (ND > 1 && gy >= ny)) continue;
-    const int64_t o = gy * P.sy + gx;
-    double qn[S];
+    for (int k = 0; k < CPT; ++k) {
+      const int e = tid + k * NT;
+      if (e >= TX * TYE) break;
+      const int tx = e % TX, ty = e / TX;
+      const int gx = x0 + tx, gy = y0 + ty;
+      if (gx >= nx || (ND > 1 && gy >= ny)) continue;
+      const int64_t o = gy * P.sy + gx;
 #pragma unroll
-    for (int v = 0; v < S; ++v) {
-      double out;
-      if (kind == kRhsOnly) {
-        out = widen(rhs[k][v]);
-      } else {
-        const double b = __ldg(qbase + o + v * P.sv);
-        const double in = (kind == kRkEuler) ? b : __ldg(qin + o + v * P.sv);
-        if constexpr (kSplit) out = rk_combine_split(kind, b, in, dtf, rhs[k][v]);
-        else out = rk_combine(kind, b, in, dt, rhs[k][v]);
+      for (int v = 0; v < S; ++v) {
+        double out;
+        if constexpr (KIND == kRhsOnly) {
+          out = widen(rhs[k][v]);
+        } else {
+          const double b = __ldg(qbase + o + v * P.sv);
+          double in = b;
+          if constexpr (KIND != kRkEuler) in = __ldg(qin + o + v * P.sv);
+          if constexpr (kSplit) out = rk_combine_split(KIND, b, in, dtf, rhs[k][v]);
+          else out = rk_combine(KIND, b, in, dt, rhs[k][v]);
+        }
+        bad |= not_finite(out);
+        qout[o + v * P.sv] = out;
       }
-      bad |= not_finite(out);
-      qout[o + v * P.sv] = out;
-      qn[v] = out;
     }
-    if (P.monitor) {
+  };
+  switch (kind) {
+    case kRkEuler: finish(KindC<kRkEuler>{}); break;
+    case kRk2Final: finish(KindC<kRk2Final>{}); break;
+    case kRk3Mid: finish(KindC<kRk3Mid>{}); break;
+    case kRk3Final: finish(KindC<kRk3Final>{}); break;
+    default: finish(KindC<kRhsOnly>{}); break;
+  }
+  // the stability monitor (the last stage of a monitored step) reads the new
+  // state back: this thread's own stores
+  if (P.monitor) {
+    for (int k = 0; k < CPT; ++k) {
+      const int e = tid + k * NT;
+      if (e >= TX * TYE) break;
+      const int tx = e % TX, ty = e / TX;
+      const int gx = x0 + tx, gy = y0 + ty;
+      if (gx >= nx || (ND > 1 && gy >= ny)) continue;
+      const int64_t o = gy * P.sy + gx;
+      double qn[S];
+#pragma unroll
+      for (int v = 0; v < S; ++v) qn[v] = qout[o + v * P.sv];
       double inv[ND];
       inv[0] = __ldg(P.inv_d[0] + gx);
       if constexpr (ND > 1) inv[1] = __ldg(P.inv_d[1] + gy);

@@ -33,12 +33,6 @@
 
 namespace mfc {
 
-// A stage kind as a type (the sweep's last phase is compiled once per kind).
-template <int K>
-struct KindC {
-  static constexpr int value = K;
-};
-
 template <int NF, int WO, class RT, int DIR, int TA, int TB, int TC>
 struct SweepShape {
   using Q = Eqs<3, NF>;
