@@ -817,6 +817,13 @@ struct KindC {
   static constexpr int value = K;
 };
 
+// A run-time flag that is the same for a whole block, as a type (a phase is
+// compiled for both values and chosen once per block).
+template <bool B>
+struct FlagC {
+  static constexpr bool value = B;
+};
+
 __device__ __forceinline__ double rk_combine(int kind, double base, double in, double dt, double r) {
   switch (kind) {
     case kRkEuler: return base + dt * r;

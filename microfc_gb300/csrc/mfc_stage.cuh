@@ -586,29 +586,35 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         reinterpret_cast<f32x2*>(wl)[(pr * TYE + ty) * NCX + cx] = vl;
         reinterpret_cast<f32x2*>(wr)[(pr * TYE + ty) * NCX + cx] = vr;
       };
-      deal_positions<TYE * NCX, NPR, NT>(tid, [&](const int p, const int v, const bool all) {
-        const int cx = p % NCX, ty = p / NCX;
-        bool nonlin = true;
-        if constexpr (GATE) nonlin = gflag[p] != 0;
-        // the shared record of a uniform grid, else the cell's staged record
-        // (reloaded per pair: keeping it live across them costs registers)
-        auto one = [&](const int w) {
-          if (ux) {
-            const f32x2* rec = U->rec[0];
-            x_pair([&](int k) { return rec[k]; }, cx, ty, w, nonlin);
-          } else {
-            RT c[kCoefRec];
-            load_coef_record(scx + cx * kCoefRec, c);
-            x_pair([&](int k) { return f2_pack(c[k], c[k]); }, cx, ty, w, nonlin);
-          }
-        };
-        if (all) {
+      // UNI: the shared record of a uniform grid, else the cell's staged
+      // record (reloaded per pair: keeping it live across them costs
+      // registers); chosen once per block
+      auto x_positions = [&](auto uni) {
+        constexpr bool UNI = decltype(uni)::value;
+        deal_positions<TYE * NCX, NPR, NT>(tid, [&](const int p, const int v, const bool all) {
+          const int cx = p % NCX, ty = p / NCX;
+          bool nonlin = true;
+          if constexpr (GATE) nonlin = gflag[p] != 0;
+          auto one = [&](const int w) {
+            if constexpr (UNI) {
+              const f32x2* rec = U->rec[0];
+              x_pair([&](int k) { return rec[k]; }, cx, ty, w, nonlin);
+            } else {
+              RT c[kCoefRec];
+              load_coef_record(scx + cx * kCoefRec, c);
+              x_pair([&](int k) { return f2_pack(c[k], c[k]); }, cx, ty, w, nonlin);
+            }
+          };
+          if (all) {
 #pragma unroll 1
-          for (int w = 0; w < NPR; ++w) one(w);
-        } else {
-          one(v);
-        }
-      });
+            for (int w = 0; w < NPR; ++w) one(w);
+          } else {
+            one(v);
+          }
+        });
+      };
+      if (ux) x_positions(FlagC<true>{});
+      else x_positions(FlagC<false>{});
     } else if constexpr (CHAR) {
       // characteristic fields: one thread per position, all variables
       const double* cf = P.coef[0];
@@ -793,27 +799,32 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         reinterpret_cast<f32x2*>(wl)[(pr * NCY + cy) * TX + tx] = vl;
         reinterpret_cast<f32x2*>(wr)[(pr * NCY + cy) * TX + tx] = vr;
       };
-      deal_positions<NCY * TX, NPR, NT>(tid, [&](const int p, const int v, const bool all) {
-        const int tx = p % TX, cy = p / TX;
-        bool nonlin = true;
-        if constexpr (GATE) nonlin = gflag[GateShape<ND, TX, TY, NT>::NGX + p] != 0;
-        auto one = [&](const int w) {
-          if (uy) {
-            const f32x2* rec = U->rec[1];
-            y_pair([&](int k) { return rec[k]; }, tx, cy, w, nonlin);
-          } else {
-            RT c[kCoefRec];
-            load_coef_record(scy + cy * kCoefRec, c);
-            y_pair([&](int k) { return f2_pack(c[k], c[k]); }, tx, cy, w, nonlin);
-          }
-        };
-        if (all) {
+      auto y_positions = [&](auto uni) {
+        constexpr bool UNI = decltype(uni)::value;
+        deal_positions<NCY * TX, NPR, NT>(tid, [&](const int p, const int v, const bool all) {
+          const int tx = p % TX, cy = p / TX;
+          bool nonlin = true;
+          if constexpr (GATE) nonlin = gflag[GateShape<ND, TX, TY, NT>::NGX + p] != 0;
+          auto one = [&](const int w) {
+            if constexpr (UNI) {
+              const f32x2* rec = U->rec[1];
+              y_pair([&](int k) { return rec[k]; }, tx, cy, w, nonlin);
+            } else {
+              RT c[kCoefRec];
+              load_coef_record(scy + cy * kCoefRec, c);
+              y_pair([&](int k) { return f2_pack(c[k], c[k]); }, tx, cy, w, nonlin);
+            }
+          };
+          if (all) {
 #pragma unroll 1
-          for (int w = 0; w < NPR; ++w) one(w);
-        } else {
-          one(v);
-        }
-      });
+            for (int w = 0; w < NPR; ++w) one(w);
+          } else {
+            one(v);
+          }
+        });
+      };
+      if (uy) y_positions(FlagC<true>{});
+      else y_positions(FlagC<false>{});
     } else if constexpr (CHAR) {
       const double* cf = P.coef[1];
       const int cs = P.cstride[1];

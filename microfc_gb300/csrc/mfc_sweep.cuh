@@ -329,26 +329,32 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
       reinterpret_cast<f32x2*>(wl)[(pr * NP + p) * NCA + ca] = vl;
       reinterpret_cast<f32x2*>(wr)[(pr * NP + p) * NCA + ca] = vr;
     };
-    deal_positions<NP * NCA, NPR, NT>(tid, [&](const int q, const int v, const bool all) {
-      const int ca = q % NCA, p = q / NCA;
-      // the shared record of a uniform grid, else the cell's staged record
-      auto one = [&](const int w) {
-        if (ua) {
-          const f32x2* rec = U.rec[DIR];
-          pair([&](int k) { return rec[k]; }, ca, p, w);
-        } else {
-          RT c[kCoefRec];
-          load_coef_record(sc + ca * kCoefRec, c);
-          pair([&](int k) { return f2_pack(c[k], c[k]); }, ca, p, w);
-        }
-      };
-      if (all) {
+    // UNI: the shared record of a uniform grid, else the cell's staged
+    // record; chosen once per block
+    auto positions = [&](auto uni) {
+      constexpr bool UNI = decltype(uni)::value;
+      deal_positions<NP * NCA, NPR, NT>(tid, [&](const int q, const int v, const bool all) {
+        const int ca = q % NCA, p = q / NCA;
+        auto one = [&](const int w) {
+          if constexpr (UNI) {
+            const f32x2* rec = U.rec[DIR];
+            pair([&](int k) { return rec[k]; }, ca, p, w);
+          } else {
+            RT c[kCoefRec];
+            load_coef_record(sc + ca * kCoefRec, c);
+            pair([&](int k) { return f2_pack(c[k], c[k]); }, ca, p, w);
+          }
+        };
+        if (all) {
 #pragma unroll 1
-        for (int w = 0; w < NPR; ++w) one(w);
-      } else {
-        one(v);
-      }
-    });
+          for (int w = 0; w < NPR; ++w) one(w);
+        } else {
+          one(v);
+        }
+      });
+    };
+    if (ua) positions(FlagC<true>{});
+    else positions(FlagC<false>{});
   } else if constexpr (CHAR) {
     static_assert(sizeof(RT) == 8 && WO > 1, "characteristic-field WENO is compiled for FP64 WENO3/5");
     // one thread per position, all variables
