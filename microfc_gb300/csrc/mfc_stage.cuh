@@ -97,6 +97,11 @@ struct StageShape {
   // a WENO evaluation loads them with 7 vector loads
   static constexpr int NCX = TX + 2, NCY = (ND > 1) ? TY + 2 : 0;
   static constexpr int NCOEF = (sizeof(RT) == 4 && WO == 5) ? kCoefRec * (NCX + NCY) : 0;
+  // FP64 WENO5: the tile's coefficients as doubles in [k][cell] order (x
+  // cells, then y cells), staged once per tile so that the reconstructions
+  // read them from shared memory instead of issuing kNumCoef global loads
+  // each
+  static constexpr int NCOEF64 = (sizeof(RT) == 8 && WO == 5) ? kNumCoef * (NCX + NCY) : 0;
   // offsets (in RT elements) of the arrays, each rounded up to 16 bytes
   static constexpr int align16(int n) { return (n * int(sizeof(RT)) + 15) / 16 * 16 / int(sizeof(RT)); }
   static constexpr int OW = align16(NQ), OF = OW + 2 * align16(NW), OC = OF + align16(NFL);
@@ -104,7 +109,7 @@ struct StageShape {
   // records]; the records come last so that a uniform grid, which never
   // stages them, can launch without their share
   static constexpr size_t kMainBytes = sizeof(RT) * size_t(OC);
-  static constexpr size_t kCoefBytes = sizeof(RT) * size_t(NCOEF);
+  static constexpr size_t kCoefBytes = sizeof(RT) * size_t(NCOEF + NCOEF64);
   static constexpr size_t kSmemBytes = kMainBytes + kCoefBytes;
 };
 
@@ -152,12 +157,14 @@ constexpr size_t stage_coef_offset() {
   return o;
 }
 
-// Dynamic shared memory of one block: without the coefficient records when
-// the grid is uniform (every direction reads the shared record).
+// Dynamic shared memory of one block: without the split path's coefficient
+// records when the grid is uniform (every direction reads the shared
+// record); the FP64 coefficients are always staged.
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, bool VISC, bool TMA>
 constexpr size_t stage_smem_total(bool shared_coef) {
+  using Sh = StageShape<ND, NF, WO, RT, TX, TY, VISC>;
   return stage_coef_offset<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, TMA>() +
-         (shared_coef ? 0 : StageShape<ND, NF, WO, RT, TX, TY, VISC>::kCoefBytes);
+         (shared_coef && Sh::NCOEF64 == 0 ? 0 : Sh::kCoefBytes);
 }
 
 // WENO of the characteristic fields at one position (FP64): the stencil of
@@ -266,7 +273,8 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   RT* fl = sq + Sh::OF;                       // fluxes [S+1][...]
   // split: FP32 x coefficients [TX+2][kCoefRec], after the gate's share
   RT* scx = reinterpret_cast<RT*>(smem_raw + stage_coef_offset<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, TMA>());
-  RT* scy = scx + kCoefRec * Sh::NCX;         // split: FP32 y coefficients [TY+2][kCoefRec]
+  // split: FP32 y coefficients [TY+2][kCoefRec]; FP64: [kNumCoef][TY+2]
+  RT* scy = scx + (Sh::NCOEF64 > 0 ? kNumCoef : kCoefRec) * Sh::NCX;
   // element of variable v in the primitive tile and in the x / y WENO values
   constexpr bool kPair = Sh::PAIR;
   constexpr int NCX_ = TX + 2, NCY_ = TY + 2;
@@ -323,6 +331,19 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
             k < kNumCoef
                 ? d2f_bits(__ldg(P.coef[1] + k * P.cstride[1] + clamp_coef_index(y0 - 1 + cy, ny) + P.coff))
                 : 0.f;
+      }
+    }
+  }
+  if constexpr (Sh::NCOEF64 > 0 && !CHAR) {
+    // FP64 WENO5: the tile's coefficients, [k][cell], before the wait
+    for (int it = tid; it < kNumCoef * Sh::NCX; it += NT) {
+      const int cx = it % Sh::NCX, k = it / Sh::NCX;
+      scx[k * Sh::NCX + cx] = __ldg(P.coef[0] + k * P.cstride[0] + clamp_coef_index(x0 - 1 + cx, nx) + P.coff);
+    }
+    if constexpr (ND > 1) {
+      for (int it = tid; it < kNumCoef * Sh::NCY; it += NT) {
+        const int cy = it % Sh::NCY, k = it / Sh::NCY;
+        scy[k * Sh::NCY + cy] = __ldg(P.coef[1] + k * P.cstride[1] + clamp_coef_index(y0 - 1 + cy, ny) + P.coff);
       }
     }
   }
@@ -636,12 +657,18 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       // state of face x0 - 1/2), cell x0 + TX only its left-face value -- so
       // only that value is formed there (weno_cell_side, the same bits).  The
       // edge items go to the threads that have one interior item fewer.
+      // the tile's staged coefficients (WENO3: from global memory)
       const double* cf = P.coef[0];
       const int cs = P.cstride[0];
       auto coef = [&](const int cx, RT (&c)[kCoefRec]) {
-        const int gi = clamp_coef_index(x0 - 1 + cx, nx) + P.coff;
+        if constexpr (Sh::NCOEF64 > 0) {
 #pragma unroll
-        for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
+          for (int k = 0; k < kNumCoef; ++k) c[k] = scx[k * Sh::NCX + cx];
+        } else {
+          const int gi = clamp_coef_index(x0 - 1 + cx, nx) + P.coff;
+#pragma unroll
+          for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
+        }
       };
       constexpr int NI = S * TYE * TX, NE = S * TYE * 2;
       for (int it = tid; it < NI; it += NT) {
@@ -845,9 +872,14 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       const double* cf = P.coef[1];
       const int cs = P.cstride[1];
       auto coef = [&](const int cy, RT (&c)[kCoefRec]) {
-        const int gi = clamp_coef_index(y0 - 1 + cy, ny) + P.coff;
+        if constexpr (Sh::NCOEF64 > 0) {
 #pragma unroll
-        for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
+          for (int k = 0; k < kNumCoef; ++k) c[k] = scy[k * Sh::NCY + cy];
+        } else {
+          const int gi = clamp_coef_index(y0 - 1 + cy, ny) + P.coff;
+#pragma unroll
+          for (int k = 0; k < kNumCoef; ++k) c[k] = RT(__ldg(cf + k * cs + gi));
+        }
       };
       constexpr int NI = S * TY * TX, NE = S * 2 * TX;
       for (int it = tid; it < NI; it += NT) {

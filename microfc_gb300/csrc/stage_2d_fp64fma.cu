@@ -17,6 +17,7 @@ void register_stage_2d_fp64fma(std::vector<StageEntry>& r) {
   MFC_2D_FMA(2)
   MFC_2D_FMA(1)
 #undef MFC_2D_FMA
+  r.push_back(stage_entry<2, 2, 5, double, 32, 16, 640, false, 1, false, false, true>());
 }
 
 }  // namespace mfc
