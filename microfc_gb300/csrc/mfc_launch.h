@@ -129,18 +129,19 @@ StageEntry stage_entry() {
 // TA1 x TB1 x 1 tiles with x across the pencils.  TMA: tiles whose sweep
 // halo lies inside the domain arrive by one bulk tensor copy.
 // MINB2 > 0 caps the registers of the z sweep (which also does the RK
-// combination) so that MINB2 of its blocks fit on an SM.
+// combination) so that MINB2 of its blocks fit on an SM; MINB01 does the same
+// for the x and y sweeps.
 template <int NF, int WO, class RT, int TA0, int TB0, int TC0, int TA1, int TB1, int NT, bool TMA = false,
-          int MINB2 = 0, bool CHAR = false>
+          int MINB2 = 0, bool CHAR = false, int MINB01 = 0>
 struct Sweep3D {
   template <int DIR>
   using K = std::conditional_t<DIR == 0, SweepShape<NF, WO, RT, 0, TA0, TB0, TC0>,
                                SweepShape<NF, WO, RT, DIR, TA1, TB1, 1>>;
   template <int DIR>
   static constexpr auto func() {
-    if constexpr (DIR == 0) return &sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT, TMA, 0, CHAR>;
+    if constexpr (DIR == 0) return &sweep_kernel<NF, WO, RT, 0, TA0, TB0, TC0, NT, TMA, MINB01, CHAR>;
     else if constexpr (DIR == 2) return &sweep_kernel<NF, WO, RT, 2, TA1, TB1, 1, NT, TMA, MINB2, CHAR>;
-    else return &sweep_kernel<NF, WO, RT, DIR, TA1, TB1, 1, NT, TMA, 0, CHAR>;
+    else return &sweep_kernel<NF, WO, RT, DIR, TA1, TB1, 1, NT, TMA, MINB01, CHAR>;
   }
 
   template <int DIR>
