@@ -476,11 +476,16 @@ int mfc_gpu_download(mfc_gpu_ctx* c, int var, double* host_sf, int64_t ld_y, int
 // values, rows follow each other every n[0] values on the host and every
 // sy (= the padded pitch) in the register, across variables too (sv = sy *
 // rows per variable).
+// rows of n[0] values that need no padding (a pitch of n[0]): the register is
+// one contiguous block like the host array, and one linear copy moves it
 int mfc_gpu_upload_state(mfc_gpu_ctx* c, const double* host_q) {
   if (!c || !host_q) return fail(MFC_ERR_INVALID, "NULL argument");
   const size_t rows = (size_t)c->S * c->n[1] * c->n[2];
-  MFC_CUDA(cudaMemcpy2DAsync(c->reg[0], (size_t)c->sy * 8, host_q, (size_t)c->n[0] * 8, (size_t)c->n[0] * 8, rows,
-                             cudaMemcpyHostToDevice, c->stream));
+  if (c->sy == c->n[0])
+    MFC_CUDA(cudaMemcpyAsync(c->reg[0], host_q, rows * c->n[0] * 8, cudaMemcpyHostToDevice, c->stream));
+  else
+    MFC_CUDA(cudaMemcpy2DAsync(c->reg[0], (size_t)c->sy * 8, host_q, (size_t)c->n[0] * 8, (size_t)c->n[0] * 8, rows,
+                               cudaMemcpyHostToDevice, c->stream));
   MFC_CUDA(cudaStreamSynchronize(c->stream));
   return MFC_OK;
 }
@@ -507,8 +512,11 @@ int mfc_gpu_generate_ic(mfc_gpu_ctx* c, const mfc_patch* patches, int num_patche
 int mfc_gpu_download_state(mfc_gpu_ctx* c, double* host_q) {
   if (!c || !host_q) return fail(MFC_ERR_INVALID, "NULL argument");
   const size_t rows = (size_t)c->S * c->n[1] * c->n[2];
-  MFC_CUDA(cudaMemcpy2DAsync(host_q, (size_t)c->n[0] * 8, c->reg[0], (size_t)c->sy * 8, (size_t)c->n[0] * 8, rows,
-                             cudaMemcpyDeviceToHost, c->stream));
+  if (c->sy == c->n[0])
+    MFC_CUDA(cudaMemcpyAsync(host_q, c->reg[0], rows * c->n[0] * 8, cudaMemcpyDeviceToHost, c->stream));
+  else
+    MFC_CUDA(cudaMemcpy2DAsync(host_q, (size_t)c->n[0] * 8, c->reg[0], (size_t)c->sy * 8, (size_t)c->n[0] * 8, rows,
+                               cudaMemcpyDeviceToHost, c->stream));
   MFC_CUDA(cudaStreamSynchronize(c->stream));
   return MFC_OK;
 }
