@@ -34,3 +34,13 @@ def test_replica_rate_is_total_work_over_the_slowest_rank():
 def test_single_replica_needs_no_process_group():
     import bench
     assert bench.replica_rate(2.0, 1000, 1) == (500.0, 2.0)
+
+
+def test_quoted_ncu_figures_parse():
+    """The bench line quotes two figures from committed ncu summaries: the
+    headline kernel's DRAM bytes per launch and the algorithmic flop count."""
+    import bench
+    traffic = bench._profile_value("stage_kernel_fp64_droplet_1024x512.md", "dram_bytes_per_launch")
+    flops = bench._profile_value("flop_count_droplet_1024x512.md", "algorithmic_flops_per_cell_update")
+    assert traffic is not None and 1e7 < traffic < 1e9
+    assert flops is not None and 1e3 < flops < 1e4
