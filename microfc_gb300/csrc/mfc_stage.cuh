@@ -714,7 +714,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
 
   // ---- phase 3: x HLLC on faces x0-1/2 .. x0+TX-1/2 ------------------------
   {
-    constexpr int NCX = TX + 2, NFXr = TX + 1;
+    constexpr int NFXr = TX + 1;
     for (int it = tid; it < TYE * NFXr; it += NT) {
       const int f = it % NFXr, ty = it / NFXr;
       const int gface = x0 - 1 + f;  // face gface+1/2
