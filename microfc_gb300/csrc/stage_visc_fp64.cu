@@ -9,6 +9,8 @@ void register_stage_visc_fp64(std::vector<StageEntry>& r) {
   r.push_back(stage_entry<1, 2, 5, double, 128, 1, 128, false, 1, true>());
   r.push_back(stage_entry<2, 1, 5, double, 16, 16, 256, false, 1, true>());
   r.push_back(stage_entry<2, 2, 5, double, 16, 16, 256, false, 1, true>());
+  r.push_back(stage_entry<2, 2, 5, double, 32, 16, 512, false, 1, true>());
+  r.push_back(stage_entry<2, 2, 5, double, 32, 16, 640, false, 1, true>());
 }
 
 }  // namespace mfc
