@@ -56,12 +56,12 @@ cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, si
 template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool VISC, bool TMA = false,
           bool FMA = false, bool CHAR = false>
 constexpr auto stage_func() {
-  static_assert(MINB == 1 || !VISC, "register-capped variants are inviscid");
+  static_assert(MINB == 1 || !VISC || !TMA, "register-capped viscous variants load their tiles without TMA");
   static_assert(!TMA || (ND == 2 && !VISC), "TMA staging is compiled for the inviscid 2-D kernel");
   static_assert(!CHAR || (!TMA && MINB == 1), "characteristic-field WENO uses the plain stage kernel");
   if constexpr (TMA && MINB > 1) return &stage_kernel_tma_mb<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, FMA>;
   else if constexpr (TMA) return &stage_kernel_tma<ND, NF, WO, RT, TX, TY, NT, GATE, FMA>;
-  else if constexpr (MINB > 1) return &stage_kernel_mb<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, FMA>;
+  else if constexpr (MINB > 1) return &stage_kernel_mb<ND, NF, WO, RT, TX, TY, NT, GATE, MINB, FMA, VISC>;
   else return &stage_kernel<ND, NF, WO, RT, TX, TY, NT, GATE, VISC, FMA, CHAR>;
 }
 

@@ -1076,15 +1076,16 @@ __global__ void __launch_bounds__(NT) stage_kernel(const DevParams P, const __gr
 }
 
 // The same kernel with its registers capped so that MINB blocks fit on an SM.
-template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool FMA = false>
+template <int ND, int NF, int WO, class RT, int TX, int TY, int NT, bool GATE, int MINB, bool FMA = false,
+          bool VISC = false>
 __global__ void __launch_bounds__(NT, MINB) stage_kernel_mb(const DevParams P, const __grid_constant__ UniformCoef U,
                                                             const double* __restrict__ qin,
                                                             const double* __restrict__ qbase,
                                                             double* __restrict__ qout, const double dt,
                                                             const int kind) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
-                                               (ND > 1) ? blockIdx.y * TY : 0, smem_raw, &U);
+  stage_tile<ND, NF, WO, RT, TX, TY, NT, GATE, VISC>(P, qin, qbase, qout, dt, kind, blockIdx.x * TX,
+                                                     (ND > 1) ? blockIdx.y * TY : 0, smem_raw, &U);
 }
 
 // The kernel with TMA staging of interior tiles (2-D, inviscid); T maps the
