@@ -138,8 +138,9 @@ int mfc_gpu_compute_rhs(mfc_gpu_ctx* ctx, double* rhs_out, double* prim_out);
  * with the case's boundary conditions in the ghost cells (m_rhs.fpp:434-447):
  * vL / vR receive the left-face (x_{j-1/2}) and right-face (x_{j+1/2}) values
  * over the face window, the part of the reference's is1 x is2 window that the
- * Riemann solver reads.  Synchronous; both entry points allocate their
- * device buffers for the call (host arrays in and out). */
+ * Riemann solver reads.  Synchronous (host arrays in and out); both entry
+ * points work in a device scratch area that the context keeps between calls
+ * and grows to the largest request (freed by mfc_gpu_finalize). */
 int mfc_gpu_weno(mfc_gpu_ctx* ctx, int dir, double* vL, double* vR);
 
 /* Drop-in for s_hllc_riemann_solver (src/simulation/m_riemann_solvers.fpp:

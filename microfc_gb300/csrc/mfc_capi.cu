@@ -164,6 +164,10 @@ struct mfc_gpu_ctx {
   double* snap_dev[2] = {nullptr, nullptr};
   double* snap_host[2] = {nullptr, nullptr};
   cudaStream_t copy_stream = nullptr;
+  // device scratch of the standalone WENO / Riemann entry points, kept
+  // between calls and grown to the largest request
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
   cudaEvent_t snap_staged = nullptr, snap_done[2] = {nullptr, nullptr};
   bool snap_pending[2] = {false, false};
   // processor boundaries: receive buffers per side ([2*dir + side]) and their device table
@@ -201,6 +205,21 @@ bool ctx_view(mfc_gpu_ctx* c, CtxView& v) {
   v.has_proc = c->has_proc;
   v.launches = &c->launches;
   return true;
+}
+
+cudaError_t ctx_scratch(mfc_gpu_ctx* c, size_t bytes, void** out) {
+  if (bytes > c->scratch_bytes) {
+    // the entry points that use it synchronise before they return, so the
+    // old buffer is idle
+    cudaFree(c->scratch);
+    c->scratch = nullptr;
+    c->scratch_bytes = 0;
+    const cudaError_t e = cudaMalloc(&c->scratch, bytes);
+    if (e != cudaSuccess) return e;
+    c->scratch_bytes = bytes;
+  }
+  *out = c->scratch;
+  return cudaSuccess;
 }
 }  // namespace mfc
 
@@ -967,6 +986,7 @@ int mfc_gpu_finalize(mfc_gpu_ctx* c) {
   cudaFree(c->tables);
   cudaFree(c->status);
   cudaFree(c->work);
+  cudaFree(c->scratch);
   cudaFree(c->gate_w);
   cudaFree(c->gate_flags);
   cudaFree(c->monitor);

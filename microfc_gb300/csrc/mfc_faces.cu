@@ -14,6 +14,7 @@
 // Faces j + 1/2 for j = -1 .. s are stored at index j + 1 (extent s_d + 2).
 #include <cuda_runtime.h>
 
+#include <initializer_list>
 #include <string>
 
 #include "../../include/mfc_gpu.h"
@@ -163,10 +164,23 @@ cudaError_t dispatch(int nd, int nf, F&& f) {
 }
 
 // Device buffers of one call, freed on every return path.
+// Carves the context's scratch into consecutive arrays of the given byte
+// sizes, each 256-byte aligned.
 struct Buffers {
   double* p[4] = {nullptr, nullptr, nullptr, nullptr};
-  ~Buffers() {
-    for (double* b : p) cudaFree(b);
+  cudaError_t take(mfc_gpu_ctx* c, std::initializer_list<size_t> bytes) {
+    size_t total = 0;
+    for (size_t b : bytes) total += (b + 255) / 256 * 256;
+    void* base = nullptr;
+    const cudaError_t e = ctx_scratch(c, total, &base);
+    if (e != cudaSuccess) return e;
+    size_t off = 0;
+    int i = 0;
+    for (size_t b : bytes) {
+      p[i++] = reinterpret_cast<double*>(static_cast<char*>(base) + off);
+      off += (b + 255) / 256 * 256;
+    }
+    return cudaSuccess;
   }
 };
 
@@ -192,8 +206,7 @@ extern "C" int mfc_gpu_weno(mfc_gpu_ctx* ctx, int dir, double* vL, double* vR) {
   const size_t bytes = sizeof(double) * (size_t)(v.S * w.count());
   mfc::Buffers B;
   cudaError_t e;
-  if ((e = cudaMalloc(&B.p[0], bytes)) != cudaSuccess || (e = cudaMalloc(&B.p[1], bytes)) != cudaSuccess)
-    return mfc::report_error(MFC_ERR_NOMEM, cudaGetErrorString(e));
+  if ((e = B.take(ctx, {bytes, bytes})) != cudaSuccess) return mfc::report_error(MFC_ERR_NOMEM, cudaGetErrorString(e));
   e = mfc::dispatch(v.nd, v.nf, [&](auto ND, auto NF) {
     return mfc::launch_weno<decltype(ND)::value, decltype(NF)::value>(*v.dev, v.q0, v.wo, dir, w, B.p[0], B.p[1],
                                                                        v.stream);
@@ -219,8 +232,7 @@ extern "C" int mfc_gpu_riemann(mfc_gpu_ctx* ctx, int dir, const double* qL_rs, c
   const size_t src_bytes = sizeof(double) * (size_t)fw.count();
   mfc::Buffers B;
   cudaError_t e;
-  if ((e = cudaMalloc(&B.p[0], in_bytes)) != cudaSuccess || (e = cudaMalloc(&B.p[1], in_bytes)) != cudaSuccess ||
-      (e = cudaMalloc(&B.p[2], flux_bytes)) != cudaSuccess || (e = cudaMalloc(&B.p[3], src_bytes)) != cudaSuccess)
+  if ((e = B.take(ctx, {in_bytes, in_bytes, flux_bytes, src_bytes})) != cudaSuccess)
     return mfc::report_error(MFC_ERR_NOMEM, cudaGetErrorString(e));
   e = cudaMemcpyAsync(B.p[0], qL_rs, in_bytes, cudaMemcpyHostToDevice, v.stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(B.p[1], qR_rs, in_bytes, cudaMemcpyHostToDevice, v.stream);

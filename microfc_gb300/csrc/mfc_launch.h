@@ -205,6 +205,10 @@ struct CtxView {
 };
 bool ctx_view(mfc_gpu_ctx* c, CtxView& v);
 
+// The context's device scratch, at least `bytes` long (grown on demand, freed
+// with the context); for entry points that synchronise before returning.
+cudaError_t ctx_scratch(mfc_gpu_ctx* c, size_t bytes, void** out);
+
 // The default (first registered) launcher of a configuration, or nullptr.
 const StageEntry* find_stage(int nd, int nf, int wo, int prec, bool visc = false, bool chr = false);
 
