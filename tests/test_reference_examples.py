@@ -183,3 +183,22 @@ def test_reference_example_device_initial_condition_matches_the_host(name):
     with Simulation(c, *_grids(c, x, y, z), ic="device") as sim:
         got = sim.download()
     _assert_same_initial_condition(c, got, q)
+
+
+@pytest.mark.gpu
+def test_reference_example_through_the_driver_command(tmp_path, oracle_lib, capsys):
+    """The reference's Sod example as a user runs it: its case dictionary
+    into `python -m microfc_gb300.driver` (pre_process, then the p_main loop
+    with its saves every t_step_save steps and the D/ text files); the data
+    file of the last save equals the oracle's state bit for bit."""
+    from microfc_gb300 import driver, io
+    name = "1D_sodshocktube"
+    c = _case(name)
+    driver.main([os.path.join(FIXTURES, name + ".json"), "--dir", str(tmp_path)])
+    res = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert res["saved"] == list(range(c.t_step_save, c.t_step_stop + 1, c.t_step_save))
+    assert (tmp_path / "D" / f"cons.1.00.{c.t_step_stop:06d}.dat").exists()
+    _, _, _, q = io.read_data_files(str(tmp_path), c.t_step_stop, c)
+    x, y, z, q0 = preprocess.generate(c)
+    ref, _ = _oracle_run(oracle_lib, c, _grids(c, x, y, z), q0, c.t_step_stop)
+    assert np.array_equal(q.view(np.uint64), ref.view(np.uint64))
