@@ -23,7 +23,9 @@ their own t_step_stop (Sod 1000 steps, vacuum 15000, Kapila 6025, advection
 split-precision path is run on the same examples for 100 steps against the
 same FP64 oracle at the split contract's bar: relative L1 <= 1e-3 in the
 partial densities and volume fractions, and at the same bar in the energy
-and in the momentum measured as a vector.
+and in the momentum measured as a vector.  The Sod example also runs
+through the driver command (pre_process, saves, data files) as a user
+would run it.
 """
 import glob
 import json
