@@ -269,3 +269,36 @@ def test_launch_count_is_stages_times_steps():
     with Simulation(case, x_cb, q_cons=q) as sim:
         sim.run(0, 7)
         assert sim.launches == 3 * 7
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("precision", ["fp64", "split", "gated"])
+def test_full_size_periodic_box_conserves_mass_momentum_energy(precision):
+    """A size-independent property at the headline size: the droplet at
+    1024x512 in a periodic box, 100 steps on the GPU.  The partial
+    densities, momenta and energy are conserved (fluxes telescope), to FP64
+    round-off in the plain path and to the round-off of the FP32 increments
+    on the split and gated paths; the volume fractions carry a
+    non-conservative source and are not summed."""
+    from microfc_gb300 import Simulation, gate
+    import os
+    if precision == "gated" and not os.path.exists(gate.WEIGHTS_FILE):
+        pytest.skip("no trained gate parameters")
+    case = cases.shock_droplet_2d().replace(bc_x=(-1, -1), bc_y=(-1, -1), precision=precision)
+    with Simulation(case, ic="device") as sim:
+        if precision == "gated":
+            sim.set_gate(gate.load())
+        q0 = sim.download()
+        sim.run(0, 100)
+        assert sim.status() == 0
+        q1 = sim.download()
+    tol = 1e-13 if precision == "fp64" else 1e-9
+    mom = slice(case.mom_idx, case.mom_idx + case.num_dims)
+    # a momentum component that is round-off noise (rho v before the shock
+    # reaches the droplet) is measured against the momentum's own scale
+    mom_scale = np.abs(q0[mom]).sum() + np.abs(q1[mom]).sum()
+    for v in range(case.E_idx + 1):
+        s0, s1 = q0[v].sum(), q1[v].sum()
+        scale = mom_scale if case.mom_idx <= v < case.E_idx else np.abs(q0[v]).sum() + np.abs(q1[v]).sum()
+        assert abs(s1 - s0) <= tol * scale, (precision, v, s0, s1, abs(s1 - s0) / scale)
+    assert not np.array_equal(q0, q1)
