@@ -302,3 +302,25 @@ def test_full_size_periodic_box_conserves_mass_momentum_energy(precision):
         scale = mom_scale if case.mom_idx <= v < case.E_idx else np.abs(q0[v]).sum() + np.abs(q1[v]).sum()
         assert abs(s1 - s0) <= tol * scale, (precision, v, s0, s1, abs(s1 - s0) / scale)
     assert not np.array_equal(q0, q1)
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("precision,n", [("split", 256), ("fp64", 128)])
+def test_3d_periodic_box_conserves_mass_momentum_energy(precision, n):
+    """The same property on the 3-D sweeps at the config-3 size (split,
+    256^3) and at 128^3 in plain FP64, 10 steps in a periodic box."""
+    from microfc_gb300 import Simulation
+    case = cases.shock_bubble_3d(N=n, precision=precision).replace(bc_x=(-1, -1), bc_y=(-1, -1), bc_z=(-1, -1))
+    with Simulation(case, ic="device") as sim:
+        q0 = sim.download()
+        sim.run(0, 10)
+        assert sim.status() == 0
+        q1 = sim.download()
+    tol = 1e-13 if precision == "fp64" else 1e-9
+    mom = slice(case.mom_idx, case.mom_idx + case.num_dims)
+    mom_scale = np.abs(q0[mom]).sum() + np.abs(q1[mom]).sum()
+    for v in range(case.E_idx + 1):
+        s0, s1 = q0[v].sum(), q1[v].sum()
+        scale = mom_scale if case.mom_idx <= v < case.E_idx else np.abs(q0[v]).sum() + np.abs(q1[v]).sum()
+        assert abs(s1 - s0) <= tol * scale, (precision, v, s0, s1, abs(s1 - s0) / scale)
+    assert not np.array_equal(q0, q1)
