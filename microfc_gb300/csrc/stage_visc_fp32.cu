@@ -14,6 +14,7 @@ void register_stage_visc_fp32(std::vector<StageEntry>& r) {
   // with the learned WENO gate (the gate chooses the weights; the viscous
   // fluxes are those of the split path)
   r.push_back(stage_entry<2, 2, 5, float, 16, 16, 256, true, 1, true>());
+  r.push_back(stage_entry<2, 2, 5, float, 16, 16, 256, true, 4, true>());
   r.push_back(stage_entry<2, 1, 5, float, 16, 16, 256, true, 1, true>());
 }
 
