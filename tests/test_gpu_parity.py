@@ -324,3 +324,44 @@ def test_3d_periodic_box_conserves_mass_momentum_energy(precision, n):
         scale = mom_scale if case.mom_idx <= v < case.E_idx else np.abs(q0[v]).sum() + np.abs(q1[v]).sum()
         assert abs(s1 - s0) <= tol * scale, (precision, v, s0, s1, abs(s1 - s0) / scale)
     assert not np.array_equal(q0, q1)
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_state_beyond_2_31_elements_conserves(precision):
+    """A maximum-size case: the droplet at 24576x12800 (315 M cells, 2.2e9
+    values per register -- element offsets beyond 2^31 -- 17.6 GB per
+    register, ~71 GB on the device), periodic, 2 steps: the kernels' 64-bit
+    addressing keeps the partial densities, momenta and energy conserved.
+    The sums are taken one variable at a time (2.5 GB on the host)."""
+    from microfc_gb300 import Simulation
+    # dt of the 1024x512 grid scaled with the finer spacing (y); the host
+    # pre_process that would pick it is skipped: the initial condition is
+    # made on the device
+    case = cases.shock_droplet_2d(nx=24576, ny=12800, steps=2, dt=4.0e-9 * 512 / 12800).replace(
+        bc_x=(-1, -1), bc_y=(-1, -1), precision=precision)
+    assert case.sys_size * case.cells > 2 ** 31
+    nx, ny = case.m + 1, case.n + 1
+    buf = np.empty((ny, nx))
+
+    def sums():
+        out = []
+        for v in range(case.E_idx + 1):
+            sim.download_var(v, buf, nx)
+            out.append((buf.sum(), np.abs(buf).sum()))
+        # the far corner of the last variable, updated by the last tiles
+        sim.download_var(case.sys_size - 1, buf, nx)
+        return out, buf[-4:, -4:].copy()
+
+    with Simulation(case, ic="device") as sim:
+        s0, c0 = sums()
+        sim.run(0, 2)
+        assert sim.status() == 0
+        s1, c1 = sums()
+    tol = 1e-13 if precision == "fp64" else 1e-9
+    mom = range(case.mom_idx, case.E_idx)
+    mom_scale = sum(s0[v][1] + s1[v][1] for v in mom)
+    for v in range(case.E_idx + 1):
+        scale = mom_scale if v in mom else s0[v][1] + s1[v][1]
+        assert abs(s1[v][0] - s0[v][0]) <= tol * scale, (precision, v, s0[v], s1[v])
+    assert np.all(np.isfinite(c1))
