@@ -79,8 +79,10 @@ def shock_droplet_2d(nx: int = 1024, ny: int = 512, mach: float = 1.47, radius: 
 
 
 def shock_bubble_3d(N: int = 256, mach: float = 1.22, steps: int = 500, cfl: float = 0.3,
-                    precision: str = "split") -> Case:
-    """Air shock on a helium sphere in the cube [-0.5, 0.5]^3 (z-extension)."""
+                    precision: str = "split", dt: float | None = None) -> Case:
+    """Air shock on a helium sphere in the cube [-0.5, 0.5]^3 (z-extension).
+    dt: None picks it from the initial state at the given CFL number (a host
+    pre_process of the whole grid)."""
     gh, pih = stiffened(1.67)
     ga, pia = stiffened(1.4)
     rho2, u2, p2 = normal_shock(1.4, 1.0, 1.0, mach)
@@ -96,5 +98,7 @@ def shock_bubble_3d(N: int = 256, mach: float = 1.22, steps: int = 500, cfl: flo
                 weno_eps=1e-16, bc_x=(-3, -3), bc_y=(-3, -3), bc_z=(-3, -3), gammas=(gh, ga),
                 pi_infs=(pih, pia), patches=[bg, shocked, bub], precision=precision,
                 name=f"shock_bubble_3d_{N}")
-    x_cb, y_cb, z_cb, q = preprocess.generate(case)
-    return case.replace(dt=preprocess.max_wave_dt(case, q, cfl, x_cb, y_cb, z_cb))
+    if dt is None:
+        x_cb, y_cb, z_cb, q = preprocess.generate(case)
+        dt = preprocess.max_wave_dt(case, q, cfl, x_cb, y_cb, z_cb)
+    return case.replace(dt=dt)

@@ -365,3 +365,37 @@ def test_state_beyond_2_31_elements_conserves(precision):
         scale = mom_scale if v in mom else s0[v][1] + s1[v][1]
         assert abs(s1[v][0] - s0[v][0]) <= tol * scale, (precision, v, s0[v], s1[v])
     assert np.all(np.isfinite(c1))
+
+
+@pytest.mark.slow
+def test_3d_state_beyond_2_31_elements_conserves():
+    """The same on the 3-D sweeps: the bubble at 648^3 in split precision
+    (272 M cells, 2.2e9 values per register, 17.4 GB each; ~105 GB on the
+    device with the sweeps' work area, whose primitive segment reaches 4.4e9
+    values), periodic, 2 steps."""
+    from microfc_gb300 import Simulation
+    N = 648
+    # dt of the 128^3 grid at CFL 0.3, scaled with the spacing
+    case = cases.shock_bubble_3d(N=N, steps=2, precision="split", dt=6.7374e-4 * 128 / N).replace(
+        bc_x=(-1, -1), bc_y=(-1, -1), bc_z=(-1, -1))
+    assert case.sys_size * case.cells > 2 ** 31
+    buf = np.empty((N, N, N))
+
+    def sums():
+        out = []
+        for v in range(case.E_idx + 1):
+            sim.download_var(v, buf, N, N * N)
+            out.append((buf.sum(), np.abs(buf).sum()))
+        return out
+
+    with Simulation(case, ic="device") as sim:
+        s0 = sums()
+        sim.run(0, 2)
+        assert sim.status() == 0
+        s1 = sums()
+    mom = range(case.mom_idx, case.E_idx)
+    mom_scale = sum(s0[v][1] + s1[v][1] for v in mom)
+    for v in range(case.E_idx + 1):
+        scale = mom_scale if v in mom else s0[v][1] + s1[v][1]
+        assert abs(s1[v][0] - s0[v][0]) <= 1e-9 * scale, (v, s0[v], s1[v])
+    assert s1 != s0
