@@ -52,7 +52,10 @@ extern "C" {
 
 /* Bits of the device status word returned by mfc_gpu_status. */
 #define MFC_FLAG_NAN 0x1u          /* NaN or Inf written to a conserved field */
-#define MFC_FLAG_NEG_PRESSURE 0x2u /* non-positive (p + pi_inf-mix/gamma-mix) */
+#define MFC_FLAG_NEG_PRESSURE 0x2u /* non-positive squared sound speed         */
+                                   /* ((gamma_mix+1) p + pi_inf_mix <= 0), set */
+                                   /* by the stability monitor on the steps it */
+                                   /* watches (mfc_gpu_set_monitor)            */
 #define MFC_FLAG_TIMEOUT 0x4u      /* a bounded device wait gave up           */
 
 /* Precision of the reconstruction/Riemann arithmetic. */

@@ -333,10 +333,12 @@ __device__ __forceinline__ void cons_to_prim(double (&q)[Eqs<ND, NF>::S], const 
 // (m_data_output.fpp:197-242): ICFL = dt / min_d(dx_d / (|u_d| + c)) with the
 // mixture sound speed c = sqrt(((gamma + 1) p + pi_inf) / (gamma rho)),
 // from the cell's conservative state.  Non-negative, so the bit patterns of
-// the doubles order like their values (atomicMax on the bits).
+// the doubles order like their values (atomicMax on the bits).  nonphys is
+// set when the squared sound speed is not positive ((gamma + 1) p + pi_inf
+// <= 0 or NaN: a pressure below the stiffened gas's limit).
 template <int ND, int NF>
 __device__ __forceinline__ double cell_icfl(const double (&q)[Eqs<ND, NF>::S], const DevParams& P, double dt,
-                                            const double (&inv_d)[ND]) {
+                                            const double (&inv_d)[ND], bool& nonphys) {
   using Q = Eqs<ND, NF>;
   double p[Q::S];
 #pragma unroll
@@ -349,7 +351,9 @@ __device__ __forceinline__ double cell_icfl(const double (&q)[Eqs<ND, NF>::S], c
     gam = gam + p[Q::ADV + f] * P.gammas[f];
     pinf = pinf + p[Q::ADV + f] * P.pi_infs[f];
   }
-  const double c = sqrt(((gam + 1.0) * p[Q::E] + pinf) / (gam * rho));
+  const double c2 = ((gam + 1.0) * p[Q::E] + pinf) / (gam * rho);
+  nonphys = !(c2 > 0.0);
+  const double c = sqrt(c2);
   double rate = 0.0;
 #pragma unroll
   for (int d = 0; d < ND; ++d) rate = fmax(rate, (fabs(p[Q::MOM + d]) + c) * inv_d[d]);

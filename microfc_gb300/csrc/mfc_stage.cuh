@@ -1039,6 +1039,7 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
   }
   // the stability monitor (the last stage of a monitored step) reads the new
   // state back: this thread's own stores
+  bool nonphys = false;
   if (P.monitor) {
     for (int k = 0; k < CPT; ++k) {
       const int e = tid + k * NT;
@@ -1053,11 +1054,14 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
       double inv[ND];
       inv[0] = __ldg(P.inv_d[0] + gx);
       if constexpr (ND > 1) inv[1] = __ldg(P.inv_d[1] + gy);
-      const double c = cell_icfl<ND, NF>(qn, P, dt, inv);
+      bool np;
+      const double c = cell_icfl<ND, NF>(qn, P, dt, inv, np);
+      nonphys |= np;
       if (!(c <= icfl)) icfl = c;  // keeps NaN
     }
   }
-  if (bad && P.status) atomicOr(P.status, 1u);
+  if (bad && P.status) atomicOr(P.status, MFC_FLAG_NAN);
+  if (nonphys && P.status) atomicOr(P.status, MFC_FLAG_NEG_PRESSURE);
   if (P.monitor) monitor_max(P.monitor, icfl);
 }
 

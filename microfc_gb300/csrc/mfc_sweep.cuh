@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
   // ---- flux divergence, accumulation, RK on the last sweep ---------------------------
   griddep_launch_dependents();
   AT* rhs_buf = reinterpret_cast<AT*>(P.work);
-  bool bad = false;
+  bool bad = false, nonphys = false;
   double icfl = 0.0;
   const float dtf = kSplit ? __double2float_rn(dt) : 0.f;  // the split path's increments are FP32
   (void)dtf;
@@ -476,7 +476,9 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
 #pragma unroll
         for (int v = 0; v < S; ++v) qn[v] = qout[o + v * P.sv];
         const double inv[3] = {__ldg(P.inv_d[0] + x), __ldg(P.inv_d[1] + y), __ldg(P.inv_d[2] + z)};
-        const double c = cell_icfl<3, NF>(qn, P, dt, inv);
+        bool np;
+        const double c = cell_icfl<3, NF>(qn, P, dt, inv, np);
+        nonphys |= np;
         if (!(c <= icfl)) icfl = c;  // keeps NaN
       }
     }
@@ -492,7 +494,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep_kernel(const DevParams P, cons
       default: finish(KindC<kRhsOnly>{}); break;
     }
   }
-  if (bad && P.status) atomicOr(P.status, 1u);
+  if (bad && P.status) atomicOr(P.status, MFC_FLAG_NAN);
+  if (nonphys && P.status) atomicOr(P.status, MFC_FLAG_NEG_PRESSURE);
   if (DIR == 2 && P.monitor) monitor_max(P.monitor, icfl);
 }
 

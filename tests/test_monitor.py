@@ -73,3 +73,32 @@ def test_cfl_driven_steps_run_at_the_requested_cfl():
         assert t > 0 and dt > c.dt  # started at CFL 0.1
         final = sim.download()
     assert icfl_numpy(c, final, dt, (x, y)) == pytest.approx(0.3, rel=1e-9)
+
+
+@pytest.mark.parametrize("nd", [1, 2, 3])
+def test_monitor_flags_a_non_physical_pressure(nd):
+    """The stability monitor sets MFC_FLAG_NEG_PRESSURE when a cell's squared
+    sound speed is not positive: here the energy of a block of water cells
+    is zeroed, which puts their pressure below the stiffened gas's limit
+    (-gamma pi_inf; an ideal gas's pressure goes to zero or below); the same
+    case without the change leaves the status clear."""
+    from microfc_gb300._lib import MFC_FLAG_NEG_PRESSURE
+    if nd == 1:
+        c = cases.sod_1d(m=199, steps=1, dt=1e-4)
+        water = (slice(None), slice(None), slice(90, 110))
+    elif nd == 2:
+        c = cases.shock_droplet_2d(nx=96, ny=48, steps=1)
+        water = (slice(None), slice(20, 28), slice(34, 42))  # inside the droplet
+    else:
+        c = cases.shock_bubble_3d(N=28, steps=1, precision="fp64").replace(m=27, n=25, p=26)
+        water = (slice(8, 18), slice(8, 18), slice(8, 18))  # around the bubble (both gases ideal)
+    x, y, z, q = preprocess.generate(c)
+    for broken in (False, True):
+        qq = q.copy()
+        if broken:
+            qq[(c.E_idx,) + water] = 0.0
+        with Simulation(c, x, y, z, q_cons=qq) as sim:
+            sim.set_monitor(True)
+            sim.tvd_rk(0)
+            flags = sim.status(clear=True)
+        assert bool(flags & MFC_FLAG_NEG_PRESSURE) == broken, (nd, broken, flags)
