@@ -73,6 +73,10 @@ class Case:
     pi_infs: tuple = ()                 # fluid_pp(i)%pi_inf = gamma_i*pi_inf_i/(gamma_i - 1)
     re_shear: tuple = ()                # fluid_pp(i)%Re(1), shear Reynolds number (<= 0 or absent: inviscid)
     re_bulk: tuple = ()                 # fluid_pp(i)%Re(2), bulk Reynolds number
+    # weno_Re_flux: the viscous stresses from WENO-reconstructed velocity
+    # gradients (m_viscous.fpp:200-216, m_rhs.fpp:514-528) instead of the
+    # finite differences of the default; not built, refused for viscous cases
+    weno_re_flux: bool = False
     patches: list = field(default_factory=list)
     stretch_x: tuple = ()               # (a_x, x_a, x_b, loops_x) of a stretched x grid; () = uniform
     stretch_y: tuple = ()               # (a_y, y_a, y_b, loops_y)
@@ -175,6 +179,9 @@ class Case:
             bad("Unsupported value of precision mode")
         if self.char_decomp and (self.precision != "fp64" or self.viscous or self.weno_order == 1):
             bad("char_decomp needs plain FP64, an inviscid case and WENO3 or WENO5")
+        if self.weno_re_flux and self.viscous:
+            bad("weno_Re_flux = T (WENO-reconstructed velocity gradients for the viscous stresses) is not "
+                "supported; the viscous terms use the finite-difference gradients of weno_Re_flux = F")
         # grid stretching, m_start_up.fpp:238-330 (pre_process)
         for ax, st, dom, used in (("x", self.stretch_x, self.x_domain, True),
                                   ("y", self.stretch_y, self.y_domain, self.n > 0)):
@@ -288,7 +295,8 @@ class Case:
             gammas=tuple(gam), pi_infs=tuple(pinf), re_shear=tuple(res[0]), re_bulk=tuple(res[1]), patches=plist,
             stretch_x=stretch.get("x", ()), stretch_y=stretch.get("y", ()),
             precision=str(g.get("gpu_precision", "fp64")), name=str(g.get("case_name", "case")),
-            char_decomp=str(g.get("char_decomp", "F")).strip().upper() in ("T", "TRUE", ".TRUE.", "1"))
+            char_decomp=str(g.get("char_decomp", "F")).strip().upper() in ("T", "TRUE", ".TRUE.", "1"),
+            weno_re_flux=g.get("weno_Re_flux", False) in (True, 1))
 
     def to_namelist(self) -> str:
         """The &user_inputs namelist of the reference's simulation.inp."""

@@ -10,7 +10,10 @@ hot path on the reference's own physics, grids, boundary conditions and
 time steps rather than on cases written here.
 
 CPU: every fixture parses (Case.from_dict), passes the input checks
-(m_checker), carries the dictionary's values, and the Python initial
+(m_checker) -- except that the viscous example's weno_Re_flux = T (the
+viscous stresses from WENO-reconstructed velocity gradients, not built) is
+refused, and that example runs with the default finite-difference
+gradients below -- carries the dictionary's values, and the Python initial
 condition equals the oracle's C restatement of pre_process bit for bit (to
 the last bit of tanh where a patch is smoothed).
 
@@ -53,7 +56,10 @@ def _load(name):
 
 
 def _case(name) -> Case:
-    return Case.from_dict(_load(name))
+    """The example's case; the viscous example asks for weno_Re_flux = T,
+    which is refused (see the parse test), and runs here with the default
+    finite-difference velocity gradients."""
+    return Case.from_dict(_load(name)).replace(weno_re_flux=False)
 
 
 def _grids(case, x_cb, y_cb, z_cb):
@@ -83,6 +89,13 @@ def test_every_reference_example_is_present():
 def test_reference_example_parses_checks_and_keeps_its_values(name):
     d = _load(name)
     c = Case.from_dict(d)
+    if c.viscous and d.get("weno_Re_flux") == "T":
+        # WENO-reconstructed velocity gradients are not built: refused, not
+        # silently replaced by the default finite differences
+        assert c.weno_re_flux
+        with pytest.raises(ValueError, match="weno_Re_flux"):
+            c.check()
+        c = c.replace(weno_re_flux=False)
     c.check()
     nf = int(d["num_fluids"])
     assert (c.m, c.n, c.p) == (d["m"], d["n"], d.get("p", 0))
