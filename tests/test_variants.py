@@ -88,7 +88,8 @@ def test_tma_staged_variants_match_plain_loads(prec, uniform):
     from microfc_gb300 import Simulation
     from microfc_gb300._lib import MFC_FLAG_TIMEOUT, MFC_VARIANT_TMA, MfcError
     if prec.endswith("fp64") and not uniform:
-        pytest.skip("the FP64 kernels stage no coefficient records")
+        pytest.skip("the FP64 kernels have no shared record to switch off: they always stage their own "
+                    "coefficients (stretched grids: test_gpu_parity.py::test_stretched_grid_matches_oracle)")
     if prec.startswith("3d"):
         # interior tiles in every sweep: x tiles of 32 cells, y and z of 16
         c = cases.shock_bubble_3d(N=40, steps=4, precision=prec[3:])
