@@ -215,6 +215,17 @@ int mfc_gpu_status(mfc_gpu_ctx* ctx, uint32_t* flags, int clear);
  * numbers switch back to the inviscid kernels.  Call before stepping. */
 int mfc_gpu_set_viscosity(mfc_gpu_ctx* ctx, const double* re_shear, const double* re_bulk);
 
+/* weno_Re_flux (m_viscous.fpp:176-216, 381-591; m_rhs.fpp:512-528): with
+ * weno_re_flux != 0 the viscous stresses take their velocity gradients from
+ * WENO reconstructions -- the velocities reconstructed to the faces along
+ * each direction, cell gradients from them by the divergence theorem, those
+ * gradients reconstructed along the sweep direction and averaged at each
+ * face -- instead of the finite differences of weno_Re_flux = F.  Two (1-D)
+ * or four (2-D) preparation kernels run before every RK stage.  Viscous
+ * (call mfc_gpu_set_viscosity first), plain FP64, WENO5 contexts without
+ * processor boundaries; 0 switches back to the finite differences. */
+int mfc_gpu_set_viscous_gradients(mfc_gpu_ctx* ctx, int weno_re_flux);
+
 /* Variables the WENO reconstruction works on (no reference counterpart: the
  * reference reconstructs the primitive variables, m_weno.fpp:470-536).
  * MFC_RECON_CHARACTERISTIC projects each cell's stencil on the

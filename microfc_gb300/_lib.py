@@ -27,7 +27,7 @@ EXPORTS = (
     "mfc_gpu_set_monitor", "mfc_gpu_icfl", "mfc_gpu_run_cfl", "mfc_gpu_generate_ic", "mfc_gpu_ensemble_generate_ic",
     "mfc_gpu_snapshot", "mfc_gpu_snapshot_wait", "mfc_gpu_select_variant", "mfc_gpu_variant_features",
     "mfc_gpu_rk_stage", "mfc_gpu_halo_buffer", "mfc_gpu_halo_pack", "mfc_gpu_set_halo_widths",
-    "mfc_gpu_set_viscosity", "mfc_gpu_set_uniform_coefficients", "mfc_gpu_ensemble_select_variant", "mfc_gpu_ensemble_variant_features",
+    "mfc_gpu_set_viscosity", "mfc_gpu_set_viscous_gradients", "mfc_gpu_set_uniform_coefficients", "mfc_gpu_ensemble_select_variant", "mfc_gpu_ensemble_variant_features",
 )
 MFC_PREC_GATED = 2
 MFC_PREC_FP64_FMA = 3
@@ -139,6 +139,7 @@ def load(build_if_missing: bool = True):
     L.mfc_gpu_variant_features.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]
     L.mfc_gpu_rk_stage.argtypes = [vp, ctypes.c_int, ctypes.c_double]
     L.mfc_gpu_set_viscosity.argtypes = [vp, dp, dp]
+    L.mfc_gpu_set_viscous_gradients.argtypes = [vp, ctypes.c_int]
     L.mfc_gpu_set_uniform_coefficients.argtypes = [vp, ctypes.c_int, ip]
     L.mfc_gpu_ensemble_select_variant.argtypes = [vp, ctypes.c_int, ip, ip, ip]
     L.mfc_gpu_ensemble_variant_features.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]

@@ -164,6 +164,11 @@ struct mfc_gpu_ctx {
   double* snap_dev[2] = {nullptr, nullptr};
   double* snap_host[2] = {nullptr, nullptr};
   cudaStream_t copy_stream = nullptr;
+  // viscous parameters as uploaded (host copy), and weno_Re_flux = T's
+  // gradient preparation
+  mfc::ViscParams visc_host{};
+  bool wrf = false;
+  mfc::ViscGradBuffers vg;
   // device scratch of the standalone WENO / Riemann entry points, kept
   // between calls and grown to the largest request
   void* scratch = nullptr;
@@ -234,6 +239,11 @@ int launch_stage(mfc_gpu_ctx* c, const double* qin, const double* qbase, double*
                  bool last_stage = false) {
   mfc::DevParams P = c->dev;
   if (last_stage && c->monitor_on) P.monitor = c->monitor;  // ICFL of the step's new state
+  if (c->wrf && c->visc) {  // weno_Re_flux = T: the stage input's face gradients first
+    const cudaError_t g = mfc::visc_gradients_launch(c->nd, c->prm.num_fluids, c->dev, c->vg, qin, c->stream);
+    if (g != cudaSuccess) return fail(MFC_ERR_CUDA, std::string("viscous gradients: ") + cudaGetErrorString(g));
+    c->launches += c->nd == 1 ? 2 : 4;
+  }
   cudaError_t e = c->stage->launch(P, c->ucoef, qin, qbase, qout, dt, kind, c->stream);
   if (e != cudaSuccess) return fail(MFC_ERR_CUDA, std::string("stage launch: ") + cudaGetErrorString(e));
   c->launches += c->stage->kernels;
@@ -699,12 +709,101 @@ int mfc_gpu_set_viscosity(mfc_gpu_ctx* c, const double* re_shear, const double* 
   const mfc::StageEntry* e = mfc::find_stage(c->nd, nf, c->prm.weno_order, c->prm.precision, true);
   if (!e) return fail(MFC_ERR_INVALID, "no viscous kernel compiled for this fluid count / WENO order / precision");
   for (int d = 0; d < c->nd; ++d) V.dcc[d] = c->tables + c->off_dcc[d];
+  if (c->wrf) {
+    V.fg[0] = c->vg.fg[0];
+    V.fg[1] = c->vg.fg[1];
+  }
   if (!c->visc && cudaMalloc(&c->visc, sizeof(mfc::ViscParams)) != cudaSuccess)
     return fail(MFC_ERR_NOMEM, "viscous parameters");
   MFC_CUDA(cudaMemcpy(c->visc, &V, sizeof(V), cudaMemcpyHostToDevice));
   if (e->prepare() != cudaSuccess) return fail(MFC_ERR_CUDA, "viscous kernel does not fit on this device");
+  c->visc_host = V;
   c->dev.visc = c->visc;
   c->stage = e;
+  return MFC_OK;
+}
+
+namespace {
+void free_visc_gradients(mfc_gpu_ctx* c) {
+  cudaFree(c->vg.gx);
+  cudaFree(c->vg.gy);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(c->vg.fg[k]);
+    cudaFree(c->vg.w[k]);
+  }
+  c->vg = mfc::ViscGradBuffers{};
+  c->wrf = false;
+}
+}  // namespace
+
+int mfc_gpu_set_viscous_gradients(mfc_gpu_ctx* c, int weno_re_flux) {
+  if (!c) return fail(MFC_ERR_INVALID, "NULL context");
+  if (!weno_re_flux) {
+    if (c->wrf) {
+      MFC_CUDA(cudaStreamSynchronize(c->stream));
+      free_visc_gradients(c);
+      if (c->visc) {
+        c->visc_host.fg[0] = c->visc_host.fg[1] = nullptr;
+        MFC_CUDA(cudaMemcpy(c->visc, &c->visc_host, sizeof(c->visc_host), cudaMemcpyHostToDevice));
+      }
+    }
+    return MFC_OK;
+  }
+  if (!c->visc) return fail(MFC_ERR_INVALID, "weno_Re_flux needs a viscous context (mfc_gpu_set_viscosity first)");
+  if (c->prm.precision != MFC_PREC_FP64)
+    return fail(MFC_ERR_INVALID, "weno_Re_flux is built for plain FP64 (MFC_PREC_FP64) contexts");
+  if (c->prm.weno_order != 5) return fail(MFC_ERR_INVALID, "weno_Re_flux is built for WENO5");
+  if (c->has_proc) return fail(MFC_ERR_INVALID, "weno_Re_flux is built without processor boundaries");
+  if (c->wrf) return MFC_OK;
+  const int nd = c->nd, nx = c->n[0], ny = nd > 1 ? c->n[1] : 1, k = nd * nd;
+  // the WENO coefficients and cell widths of the ghost cells up to the
+  // reference's viscous buff_size (2*weno_polyn + 2 = 6): cells -3 and n+2
+  // enter the gradient reconstructions
+  const int bv = 6;
+  mfc_params q = c->prm;
+  q.x_cb = c->cb_host[0].data();
+  q.y_cb = nd > 1 ? c->cb_host[1].data() : nullptr;
+  q.z_cb = nullptr;
+  mfc::GridTables gt;
+  const std::string why = mfc::build_grid_tables(&q, nd, c->n, bv, gt);
+  if (!why.empty()) return fail(MFC_ERR_INVALID, why);
+  const int bcb[2] = {q.bc_x_beg, q.bc_y_beg}, bce[2] = {q.bc_x_end, q.bc_y_end};
+  std::vector<double> w[2];
+  for (int d = 0; d < nd; ++d) {
+    mfc::AxisHost a;
+    a.s = c->n[d] - 1;
+    a.b = bv;
+    a.cb.assign((size_t)(a.s + 2 * a.b + 2), 0.0);
+    a.d.assign((size_t)(a.s + 2 * a.b + 1), 0.0);
+    for (int i = -1; i <= a.s; ++i) a.CB(i) = c->cb_host[d][(size_t)(i + 1)];
+    mfc::grid_ghosts(a, bcb[d], bce[d]);
+    for (int cell = -mfc::kCoefPad; cell <= a.s + mfc::kCoefPad; ++cell) w[d].push_back(a.D(cell));
+  }
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](double** ptr, size_t count) {
+    if (e == cudaSuccess) e = cudaMalloc(ptr, sizeof(double) * count);
+  };
+  alloc(&c->vg.gx, (size_t)k * ny * (nx + 6));
+  alloc(&c->vg.fg[0], (size_t)k * ny * (nx + 1));
+  alloc(&c->vg.w[0], w[0].size());
+  if (nd > 1) {
+    alloc(&c->vg.gy, (size_t)k * (ny + 6) * nx);
+    alloc(&c->vg.fg[1], (size_t)k * (ny + 1) * nx);
+    alloc(&c->vg.w[1], w[1].size());
+  }
+  if (e != cudaSuccess) {
+    free_visc_gradients(c);
+    return fail(MFC_ERR_NOMEM, "weno_Re_flux buffers");
+  }
+  MFC_CUDA(cudaStreamSynchronize(c->stream));
+  MFC_CUDA(cudaMemcpy(c->tables, gt.host.data(), sizeof(double) * gt.host.size(), cudaMemcpyHostToDevice));
+  for (int d = 0; d < nd; ++d)
+    MFC_CUDA(cudaMemcpy(c->vg.w[d], w[d].data(), sizeof(double) * w[d].size(), cudaMemcpyHostToDevice));
+  if (nd == 1) c->vg.w[1] = nullptr;
+  c->visc_host.fg[0] = c->vg.fg[0];
+  c->visc_host.fg[1] = c->vg.fg[1];
+  MFC_CUDA(cudaMemcpy(c->visc, &c->visc_host, sizeof(c->visc_host), cudaMemcpyHostToDevice));
+  c->wrf = true;
   return MFC_OK;
 }
 
@@ -987,6 +1086,12 @@ int mfc_gpu_finalize(mfc_gpu_ctx* c) {
   cudaFree(c->status);
   cudaFree(c->work);
   cudaFree(c->scratch);
+  cudaFree(c->vg.gx);
+  cudaFree(c->vg.gy);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(c->vg.fg[k]);
+    cudaFree(c->vg.w[k]);
+  }
   cudaFree(c->gate_w);
   cudaFree(c->gate_flags);
   cudaFree(c->monitor);

@@ -99,6 +99,12 @@ struct ViscParams {
   int re_size[2];
   int re_idx[2][kMaxFluids];
   const double* dcc[3];
+  // weno_Re_flux = T: the face velocity gradients, prepared per stage by
+  // visc_gradients_launch (mfc_visc_grad.cu), read instead of the finite
+  // differences.  fg[0]: x faces [c*ND+d][ny][nx+1] (face i+1/2 at i+1),
+  // fg[1]: y faces [c*ND+d][ny+1][nx] (face j+1/2 at j+1); d u_c / d x_d.
+  // NULL: the finite differences of weno_Re_flux = F.
+  const double* fg[2];
 };
 
 

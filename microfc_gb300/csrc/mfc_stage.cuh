@@ -732,23 +732,37 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         RT vs[ND], dxv[2] = {RT(0), RT(0)}, dyv[2] = {RT(0), RT(0)}, vf[3];
         hllc_face<ND, NF, 0, RT, true>(qL, qR, gam_i, pi_i, F, us, vs);
         const ViscParams& V = *P.visc;
-        const int ly = (ND > 1) ? ty + H : 0, lx = f + H - 1;  // the face's left cell
-        auto U = [&](int c, int x, int y) { return sq[qi(Q::MOM + c, y, x)]; };
-        const auto Dx = divisor(narrow<RT>(__ldg(V.dcc[0] + min(x0 + f, nx))));  // x_cc(j+1) - x_cc(j)
-#pragma unroll
-        for (int c = 0; c < ND; ++c) {
-          const RT g = div_rn(U(c, lx + 1, ly) - U(c, lx, ly), Dx);
-          dxv[c] = RT(0.5) * (g + g);
-        }
-        if constexpr (ND > 1) {
-          const int gy = min(y0 + ty, ny - 1);
-          const auto D0 = divisor(narrow<RT>(__ldg(V.dcc[1] + gy))), D1 = divisor(narrow<RT>(__ldg(V.dcc[1] + gy + 1)));
+        if (V.fg[0] != nullptr) {
+          // weno_Re_flux = T: the prepared face gradients (clamped indices
+          // for the rows and faces of partial tiles, whose results are dropped)
+          const int gy = (ND > 1) ? min(y0 + ty, ny - 1) : 0;
+          const int64_t plane = (int64_t)(ND > 1 ? ny : 1) * (nx + 1);
+          const double* g = V.fg[0] + (int64_t)gy * (nx + 1) + (min(max(gface, -1), nx - 1) + 1);
 #pragma unroll
           for (int c = 0; c < ND; ++c) {
-            auto Ly = [&](int x) { return div_rn(U(c, x, ly) - U(c, x, ly - 1), D0); };
-            auto Ry = [&](int x) { return div_rn(U(c, x, ly + 1) - U(c, x, ly), D1); };
-            const RT A = RT(0.25) * (Ly(lx + 1) + Ry(lx + 1) + Ly(lx) + Ry(lx));
-            dyv[c] = RT(0.5) * (A + A);
+            dxv[c] = narrow<RT>(__ldg(g + (c * ND) * plane));
+            if constexpr (ND > 1) dyv[c] = narrow<RT>(__ldg(g + (c * ND + 1) * plane));
+          }
+        } else {
+          const int ly = (ND > 1) ? ty + H : 0, lx = f + H - 1;  // the face's left cell
+          auto U = [&](int c, int x, int y) { return sq[qi(Q::MOM + c, y, x)]; };
+          const auto Dx = divisor(narrow<RT>(__ldg(V.dcc[0] + min(x0 + f, nx))));  // x_cc(j+1) - x_cc(j)
+#pragma unroll
+          for (int c = 0; c < ND; ++c) {
+            const RT g = div_rn(U(c, lx + 1, ly) - U(c, lx, ly), Dx);
+            dxv[c] = RT(0.5) * (g + g);
+          }
+          if constexpr (ND > 1) {
+            const int gy = min(y0 + ty, ny - 1);
+            const auto D0 = divisor(narrow<RT>(__ldg(V.dcc[1] + gy))),
+                       D1 = divisor(narrow<RT>(__ldg(V.dcc[1] + gy + 1)));
+#pragma unroll
+            for (int c = 0; c < ND; ++c) {
+              auto Ly = [&](int x) { return div_rn(U(c, x, ly) - U(c, x, ly - 1), D0); };
+              auto Ry = [&](int x) { return div_rn(U(c, x, ly + 1) - U(c, x, ly), D1); };
+              const RT A = RT(0.25) * (Ly(lx + 1) + Ry(lx + 1) + Ly(lx) + Ry(lx));
+              dyv[c] = RT(0.5) * (A + A);
+            }
           }
         }
         viscous_face_flux<ND, NF, 0, RT>(qL, qR, V, vs, dxv, dyv, vf);
@@ -940,19 +954,31 @@ __device__ __forceinline__ void stage_tile(const DevParams& P, const double* __r
         RT vs[ND], dxv[2], dyv[2], vf[3];
         hllc_face<ND, NF, 1, RT, true>(qL, qR, gam_i, pi_i, F, us, vs);
         const ViscParams& V = *P.visc;
-        const int ly = f + H - 1, lx = tx + H;  // the face's lower cell
-        auto U = [&](int c, int x, int y) { return sq[qi(Q::MOM + c, y, x)]; };
-        const auto Dy = divisor(narrow<RT>(__ldg(V.dcc[1] + min(y0 + f, ny))));  // y_cc(k+1) - y_cc(k)
         const int gx = min(x0 + tx, nx - 1);
-        const auto D0 = divisor(narrow<RT>(__ldg(V.dcc[0] + gx))), D1 = divisor(narrow<RT>(__ldg(V.dcc[0] + gx + 1)));
+        if (V.fg[1] != nullptr) {
+          // weno_Re_flux = T: the prepared face gradients
+          const int64_t plane = (int64_t)(ny + 1) * nx;
+          const double* g = V.fg[1] + (int64_t)(min(max(gface, -1), ny - 1) + 1) * nx + gx;
 #pragma unroll
-        for (int c = 0; c < 2; ++c) {
-          auto Lx = [&](int y) { return div_rn(U(c, lx, y) - U(c, lx - 1, y), D0); };
-          auto Rx = [&](int y) { return div_rn(U(c, lx + 1, y) - U(c, lx, y), D1); };
-          const RT A = RT(0.25) * (Lx(ly + 1) + Rx(ly + 1) + Lx(ly) + Rx(ly));
-          dxv[c] = RT(0.5) * (A + A);
-          const RT g = div_rn(U(c, lx, ly + 1) - U(c, lx, ly), Dy);
-          dyv[c] = RT(0.5) * (g + g);
+          for (int c = 0; c < 2; ++c) {
+            dxv[c] = narrow<RT>(__ldg(g + (c * 2) * plane));
+            dyv[c] = narrow<RT>(__ldg(g + (c * 2 + 1) * plane));
+          }
+        } else {
+          const int ly = f + H - 1, lx = tx + H;  // the face's lower cell
+          auto U = [&](int c, int x, int y) { return sq[qi(Q::MOM + c, y, x)]; };
+          const auto Dy = divisor(narrow<RT>(__ldg(V.dcc[1] + min(y0 + f, ny))));  // y_cc(k+1) - y_cc(k)
+          const auto D0 = divisor(narrow<RT>(__ldg(V.dcc[0] + gx))),
+                     D1 = divisor(narrow<RT>(__ldg(V.dcc[0] + gx + 1)));
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            auto Lx = [&](int y) { return div_rn(U(c, lx, y) - U(c, lx - 1, y), D0); };
+            auto Rx = [&](int y) { return div_rn(U(c, lx + 1, y) - U(c, lx, y), D1); };
+            const RT A = RT(0.25) * (Lx(ly + 1) + Rx(ly + 1) + Lx(ly) + Rx(ly));
+            dxv[c] = RT(0.5) * (A + A);
+            const RT g = div_rn(U(c, lx, ly + 1) - U(c, lx, ly), Dy);
+            dyv[c] = RT(0.5) * (g + g);
+          }
         }
         viscous_face_flux<ND, NF, 1, RT>(qL, qR, V, vs, dxv, dyv, vf);
 #pragma unroll

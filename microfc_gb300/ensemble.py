@@ -63,6 +63,9 @@ class Ensemble:
             self._keep.append(cb)
             self.grids.append((x_cb, y_cb))
             qs.append(q)
+        if any(c.viscous and c.weno_re_flux for c in self.cases):
+            raise ValueError("the ensemble's viscous terms use the finite-difference gradients "
+                             "(weno_Re_flux = F)")
         dts = np.array([c.dt for c in self.cases], dtype=np.float64)
         h = ctypes.c_void_p()
         _lib.check(self.L.mfc_gpu_ensemble_init(params, _dp(dts), len(self.cases), ctypes.byref(h)))

@@ -91,6 +91,8 @@ class Simulation:
         self.dt = case.dt
         if case.viscous:
             self.set_viscosity(case.re_shear, case.re_bulk)
+            if case.weno_re_flux:
+                self.set_viscous_gradients(True)
         if case.char_decomp:
             self.set_reconstruction("characteristic")
         if on_device:
@@ -218,6 +220,12 @@ class Simulation:
         a[:len(re_shear)] = re_shear
         b[:len(re_bulk)] = re_bulk
         _lib.check(self.L.mfc_gpu_set_viscosity(self._h, _dp(a), _dp(b)))
+
+    def set_viscous_gradients(self, weno_re_flux: bool = True) -> None:
+        """weno_Re_flux: the viscous stresses from WENO-reconstructed velocity
+        gradients (True) or the default finite differences (False);
+        mfc_gpu_set_viscous_gradients."""
+        _lib.check(self.L.mfc_gpu_set_viscous_gradients(self._h, int(bool(weno_re_flux))))
 
     def set_reconstruction(self, variables: str = "primitive") -> None:
         """WENO of the "primitive" variables (the reference's choice) or of

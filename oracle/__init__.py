@@ -45,6 +45,7 @@ class MfoParams(ctypes.Structure):
         ("re_shear", ctypes.c_double * MAX_FLUIDS),
         ("re_bulk", ctypes.c_double * MAX_FLUIDS),
         ("char_decomp", ctypes.c_int),
+        ("weno_re_flux", ctypes.c_int),
     ]
 
 
@@ -140,6 +141,7 @@ def params_from_case(case) -> MfoParams:
     for i, r in enumerate(getattr(case, "re_bulk", ())):
         q.re_bulk[i] = r
     q.char_decomp = int(bool(getattr(case, "char_decomp", False)))
+    q.weno_re_flux = int(bool(getattr(case, "weno_re_flux", False)))
     return q
 
 

@@ -59,6 +59,7 @@ struct Params {
   double pi_infs[kMaxFluids] = {0};  // fluid_pp(i)%pi_inf = gamma_i pi_inf_i/(gamma_i - 1)
   double re[2][kMaxFluids] = {};     // fluid_pp(i)%Re(1:2), shear and bulk; <= 0: none
   bool char_decomp = false;          // characteristic-field WENO (see weno(); not in the reference)
+  bool weno_re_flux = false;         // weno_Re_flux: viscous stresses from WENO-reconstructed gradients
 
   int num_dims() const { return 1 + (n > 0) + (p > 0); }
   int weno_polyn() const { return (weno_order - 1) / 2; }
@@ -235,6 +236,10 @@ struct Solver {
   std::vector<Field<R>> flux;          // flux at face j+1/2 stored at j
   Field<R> fsrc;                       // interface velocity at face j+1/2
   Field<R> vflux[3];                   // viscous source flux at face j+1/2: x-momentum, y-momentum, energy
+  // weno_Re_flux: grad[c][d] = cell-average d u_c / d x_d by the divergence
+  // theorem from WENO face values of u_c along d; gL/gR[c][d] = its left-
+  // and right-face WENO values along the current sweep direction
+  Field<R> grad[2][2], gL[2][2], gR[2][2];
   double dt = 0;
 
   void init(const Params& p, const double* x_cb, const double* y_cb, const double* z_cb) {
@@ -276,6 +281,13 @@ struct Solver {
     fsrc.alloc(xb, xe, yb, ye, zb, ze);
     if (P.viscous())
       for (auto& f : vflux) f.alloc(xb, xe, yb, ye, zb, ze);
+    if (P.viscous() && P.weno_re_flux)
+      for (int c = 0; c < nd; ++c)
+        for (int d = 0; d < nd; ++d) {
+          grad[c][d].alloc(xb, xe, yb, ye, zb, ze);
+          gL[c][d].alloc(xb, xe, yb, ye, zb, ze);
+          gR[c][d].alloc(xb, xe, yb, ye, zb, ze);
+        }
   }
 
   // Velocity component c of a cell (primitive, after cons_to_prim).
@@ -287,6 +299,63 @@ struct Solver {
   R Ly(int c, int i, int j) { return (U(c, i, j) - U(c, i, j - 1)) / (ax[1].CC(j) - ax[1].CC(j - 1)); }
   R Ry(int c, int i, int j) { return (U(c, i, j + 1) - U(c, i, j)) / (ax[1].CC(j + 1) - ax[1].CC(j)); }
 
+  // weno_Re_flux = T, m_viscous.fpp:176-216 (s_reconstruct_cell_boundary_
+  // values_visc, s_apply_scalar_divergence_theorem :381-455): the velocity
+  // components WENO-reconstructed along each direction d over the WENO
+  // window of d (the whole extended range across it), then the cell-average
+  // gradient (1/ds) (vR - vL) on the extended range less one cell each side
+  // (cells whose face values lie outside the window keep the zeros of the
+  // allocation; no face flux reads them).
+  void visc_gradients() {
+    const int polyn = P.weno_polyn();
+    const R eps = R(P.weno_eps);
+    for (int d = 0; d < nd; ++d) {
+      Axis<R>& a = ax[d];
+      const int di = d == 0, dj = d == 1;
+      int ib_ = xb, ie_ = xe, jb_ = yb, je_ = ye;
+      if (d == 0) { ib_ = -b + polyn; ie_ = a.s + b - polyn; }
+      else { jb_ = -b + polyn; je_ = a.s + b - polyn; }
+      for (int c = 0; c < nd; ++c) {
+        const Field<R>& u = qp[P.mom_beg() - 1 + c];
+        Field<R>& uL = gL[c][d];  // scratch: the velocity's face values
+        Field<R>& uR = gR[c][d];
+        for (int j = jb_; j <= je_; ++j)
+          for (int i = ib_; i <= ie_; ++i) {
+            auto at = [&](int o) { return u(i + o * di, j + o * dj, 0); };
+            weno_stencil(at, a.C(d == 0 ? i : j), eps, uL(i, j, 0), uR(i, j, 0));
+          }
+        int gib = xb, gie = xe, gjb = yb, gje = ye;
+        if (d == 0) { gib = xb + 1; gie = xe - 1; }
+        else { gjb = yb + 1; gje = ye - 1; }
+        for (int j = gjb; j <= gje; ++j)
+          for (int i = gib; i <= gie; ++i)
+            grad[c][d](i, j, 0) = R(1) / a.D(d == 0 ? i : j) * (uR(i, j, 0) - uL(i, j, 0));
+      }
+    }
+  }
+
+  // weno_Re_flux = T, m_rhs.fpp:512-528 (s_reconstruct_cell_boundary_values_
+  // visc_deriv, m_viscous.fpp:525-591): every gradient WENO-reconstructed
+  // along the sweep direction over its WENO window.
+  void visc_gradient_weno(int dir) {
+    const int polyn = P.weno_polyn();
+    const R eps = R(P.weno_eps);
+    Axis<R>& a = ax[dir];
+    const int di = dir == 0, dj = dir == 1;
+    int ib_ = xb, ie_ = xe, jb_ = yb, je_ = ye;
+    if (dir == 0) { ib_ = -b + polyn; ie_ = a.s + b - polyn; }
+    else { jb_ = -b + polyn; je_ = a.s + b - polyn; }
+    for (int c = 0; c < nd; ++c)
+      for (int d = 0; d < nd; ++d) {
+        const Field<R>& g = grad[c][d];
+        for (int j = jb_; j <= je_; ++j)
+          for (int i = ib_; i <= ie_; ++i) {
+            auto at = [&](int o) { return g(i + o * di, j + o * dj, 0); };
+            weno_stencil(at, a.C(dir == 0 ? i : j), eps, gL[c][d](i, j, 0), gR[c][d](i, j, 0));
+          }
+      }
+  }
+
   // Viscous source flux of the face between (i,j) and its neighbour along dir,
   // s_compute_viscous_source_flux (m_riemann_solvers.fpp:683-902), with the
   // face gradients of s_get_viscous (m_viscous.fpp:159-370): the arithmetic
@@ -296,7 +365,15 @@ struct Solver {
   void viscous_flux(int dir, int i, int j, const R (&re_avg)[2], const R (&vs)[3], R (&out)[3]) {
     R dx[2] = {R(0), R(0)}, dy[2] = {R(0), R(0)};
     const int ndv = nd;
-    if (dir == 0) {
+    if (P.weno_re_flux) {
+      // the arithmetic mean of the right-face value of this cell and the
+      // left-face value of the next (m_riemann_solvers.fpp:714-900)
+      const int ni = i + (dir == 0), nj = j + (dir == 1);
+      for (int c = 0; c < ndv; ++c) {
+        dx[c] = R(0.5) * (gR[c][0](i, j, 0) + gL[c][0](ni, nj, 0));
+        if (nd > 1) dy[c] = R(0.5) * (gR[c][1](i, j, 0) + gL[c][1](ni, nj, 0));
+      }
+    } else if (dir == 0) {
       for (int c = 0; c < ndv; ++c) dx[c] = R(0.5) * (Rx(c, i, j) + Lx(c, i + 1, j));
       if (nd > 1)
         for (int c = 0; c < ndv; ++c) {
@@ -696,8 +773,11 @@ struct Solver {
     populate_buffers();
     cons_to_prim();
     if (last_step) return false;
+    const bool wrf = P.viscous() && P.weno_re_flux;
+    if (wrf) visc_gradients();
     for (int dir = 0; dir < nd; ++dir) {
       weno(dir);
+      if (wrf) visc_gradient_weno(dir);
       hllc(dir);
       flux_add(dir);
     }

@@ -32,6 +32,7 @@ struct mfo_params {
   double re_shear[kMaxFluids];  // fluid_pp(i)%Re(1); <= 0: inviscid
   double re_bulk[kMaxFluids];   // fluid_pp(i)%Re(2)
   int char_decomp;              // 1: WENO of the characteristic fields (Solver::weno)
+  int weno_re_flux;             // 1: weno_Re_flux = T (viscous stresses from WENO-reconstructed gradients)
 };
 
 static Params to_params(const mfo_params* q) {
@@ -47,12 +48,15 @@ static Params to_params(const mfo_params* q) {
   for (int i = 0; i < kMaxFluids; ++i) { P.gammas[i] = q->gammas[i]; P.pi_infs[i] = q->pi_infs[i]; }
   for (int i = 0; i < kMaxFluids; ++i) { P.re[0][i] = q->re_shear[i]; P.re[1][i] = q->re_bulk[i]; }
   P.char_decomp = q->char_decomp != 0;
+  P.weno_re_flux = q->weno_re_flux != 0;
   return P;
 }
 
 void* mfo_create(const mfo_params* q, const double* x_cb, const double* y_cb, const double* z_cb) {
   // every used direction needs its cell boundaries
   if (!q || !x_cb || (q->n > 0 && !y_cb) || (q->p > 0 && !z_cb)) return nullptr;
+  // the viscous terms, and with them weno_Re_flux, are 1-D and 2-D
+  if (q->weno_re_flux && q->p > 0) return nullptr;
   auto* s = new (std::nothrow) Solver<double>();
   if (!s) return nullptr;
   s->init(to_params(q), x_cb, y_cb, z_cb);

@@ -219,8 +219,12 @@ def _shear_wave(nx=64, ny=25, re=100.0, amp=0.01, bulk=0.0, steps=250, dt=2e-3):
     return c, x_cb, y_cb, q, xc
 
 
-def test_viscous_shear_wave_decays_at_the_kinematic_viscosity(oracle_lib):
+@pytest.mark.parametrize("weno_re_flux", [False, True], ids=["fd_gradients", "weno_gradients"])
+def test_viscous_shear_wave_decays_at_the_kinematic_viscosity(oracle_lib, weno_re_flux):
+    """Both gradient discretisations of the viscous stresses: the default
+    finite differences and weno_Re_flux's WENO-reconstructed gradients."""
     c, x_cb, y_cb, q, xc = _shear_wave()
+    c = c.replace(weno_re_flux=weno_re_flux)
     o = oracle_lib.Oracle(c, x_cb, y_cb)
     o.set_state(q)
     o.run(0, c.t_step_stop, c.dt)

@@ -10,10 +10,9 @@ hot path on the reference's own physics, grids, boundary conditions and
 time steps rather than on cases written here.
 
 CPU: every fixture parses (Case.from_dict), passes the input checks
-(m_checker) -- except that the viscous example's weno_Re_flux = T (the
-viscous stresses from WENO-reconstructed velocity gradients, not built) is
-refused, and that example runs with the default finite-difference
-gradients below -- carries the dictionary's values, and the Python initial
+(m_checker), carries the dictionary's values (the viscous example's
+weno_Re_flux = T included: its viscous stresses take WENO-reconstructed
+velocity gradients), and the Python initial
 condition equals the oracle's C restatement of pre_process bit for bit (to
 the last bit of tanh where a patch is smoothed).
 
@@ -56,10 +55,7 @@ def _load(name):
 
 
 def _case(name) -> Case:
-    """The example's case; the viscous example asks for weno_Re_flux = T,
-    which is refused (see the parse test), and runs here with the default
-    finite-difference velocity gradients."""
-    return Case.from_dict(_load(name)).replace(weno_re_flux=False)
+    return Case.from_dict(_load(name))
 
 
 def _grids(case, x_cb, y_cb, z_cb):
@@ -89,14 +85,8 @@ def test_every_reference_example_is_present():
 def test_reference_example_parses_checks_and_keeps_its_values(name):
     d = _load(name)
     c = Case.from_dict(d)
-    if c.viscous and d.get("weno_Re_flux") == "T":
-        # WENO-reconstructed velocity gradients are not built: refused, not
-        # silently replaced by the default finite differences
-        assert c.weno_re_flux
-        with pytest.raises(ValueError, match="weno_Re_flux"):
-            c.check()
-        c = c.replace(weno_re_flux=False)
     c.check()
+    assert c.weno_re_flux == (d.get("weno_Re_flux") == "T")
     nf = int(d["num_fluids"])
     assert (c.m, c.n, c.p) == (d["m"], d["n"], d.get("p", 0))
     assert c.num_fluids == nf and c.weno_order == d["weno_order"] and c.time_stepper == d["time_stepper"]
@@ -167,7 +157,9 @@ def test_reference_example_runs_bitwise_like_the_oracle(name, oracle_lib):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", [n for n in NAMES if n != "2D_shockdroplet"])
 def test_reference_example_split_precision_within_the_contract(name, oracle_lib):
-    c = _case(name).replace(precision="split")
+    # weno_Re_flux is built for plain FP64: the split path's viscous stresses
+    # take the finite-difference gradients, and so does its FP64 reference
+    c = _case(name).replace(precision="split", weno_re_flux=False)
     stop = c.t_step_start + 100
     x, y, z, q = preprocess.generate(c)
     grids = _grids(c, x, y, z)

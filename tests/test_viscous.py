@@ -34,22 +34,30 @@ def _gpu_and_oracle(oracle_lib, case, x_cb, y_cb, q, steps):
     return got, o.get_state()
 
 
-def test_shear_wave_matches_oracle_bitwise(oracle_lib):
+WRF = pytest.mark.parametrize("wrf", [False, True], ids=["fd_gradients", "weno_Re_flux"])
+
+
+@WRF
+def test_shear_wave_matches_oracle_bitwise(oracle_lib, wrf):
     c, x_cb, y_cb, q = _shear_wave(re=100.0, bulk=40.0)
+    c = c.replace(weno_re_flux=wrf)
     got, ref = _gpu_and_oracle(oracle_lib, c, x_cb, y_cb, q, c.t_step_stop)
     assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
 
 
+@WRF
 @pytest.mark.parametrize("bc", [(-3, -3), (-2, -2), (-1, -1), (-4, -4), (-2, -3)])
-def test_viscous_droplet_matches_oracle_bitwise(oracle_lib, bc):
-    c = _viscous_droplet(bc)
+def test_viscous_droplet_matches_oracle_bitwise(oracle_lib, bc, wrf):
+    c = _viscous_droplet(bc).replace(weno_re_flux=wrf)
     x_cb, y_cb, _, q = preprocess.generate(c)
     got, ref = _gpu_and_oracle(oracle_lib, c, x_cb, y_cb, q, c.t_step_stop)
     assert np.array_equal(got.view(np.uint64), ref.view(np.uint64)), rel_l1(got, ref)
 
 
-def test_viscous_sod_1d_matches_oracle_bitwise(oracle_lib):
-    c = cases.sod_1d(m=199, steps=40, dt=1e-4).replace(re_shear=(50.0, 80.0), re_bulk=(30.0, 0.0))
+@WRF
+def test_viscous_sod_1d_matches_oracle_bitwise(oracle_lib, wrf):
+    c = cases.sod_1d(m=199, steps=40, dt=1e-4).replace(re_shear=(50.0, 80.0), re_bulk=(30.0, 0.0),
+                                                        weno_re_flux=wrf)
     x_cb, _, _, q = preprocess.generate(c)
     got, ref = _gpu_and_oracle(oracle_lib, c, x_cb, None, q, c.t_step_stop)
     assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
@@ -110,3 +118,26 @@ def test_viscous_refusals():
     with Simulation(b) as sim:
         with pytest.raises(MfcError, match="1-D and 2-D"):
             sim.set_viscosity((10.0, 10.0))
+
+
+def test_weno_re_flux_changes_the_result_and_refusals(oracle_lib):
+    """The two gradient discretisations give different results; the WENO
+    gradients are refused where they are not built."""
+    from microfc_gb300 import Simulation
+    from microfc_gb300._lib import MfcError
+    c = _viscous_droplet(steps=10)
+    x_cb, y_cb, _, q = preprocess.generate(c)
+    out = []
+    for wrf in (False, True):
+        with Simulation(c.replace(weno_re_flux=wrf), x_cb, y_cb, q_cons=q) as sim:
+            sim.run(0, 10)
+            out.append(sim.download())
+            if wrf:
+                assert sim.launches == 10 * 3 * (1 + 4)  # four preparation kernels per stage
+    assert rel_l1(out[1], out[0])[c.mom_idx] > 1e-10
+    with Simulation(c.replace(precision="split"), x_cb, y_cb, q_cons=q) as sim:
+        with pytest.raises(MfcError, match="plain FP64"):
+            sim.set_viscous_gradients(True)
+    with Simulation(cases.shock_droplet_2d(nx=96, ny=48, steps=2), x_cb, y_cb, q_cons=q) as sim:
+        with pytest.raises(MfcError, match="viscous context"):
+            sim.set_viscous_gradients(True)
