@@ -210,7 +210,8 @@ int mfc_gpu_status(mfc_gpu_ctx* ctx, uint32_t* flags, int clear);
  * m_riemann_solvers.fpp:683-902 and its divergence in m_rhs.fpp:591-651):
  * re_shear[i] / re_bulk[i] are fluid_pp(i+1)%Re(1) / %Re(2) for the
  * context's fluids (NULL or values <= 0: none).  The velocity gradients are
- * the reference's one-sided face differences (weno_Re_flux = F).  1-D and
+ * the reference's one-sided face differences (weno_Re_flux = F; see
+ * mfc_gpu_set_viscous_gradients for weno_Re_flux = T).  1-D and
  * 2-D contexts, with or without processor boundaries; all-zero Reynolds
  * numbers switch back to the inviscid kernels.  Call before stepping. */
 int mfc_gpu_set_viscosity(mfc_gpu_ctx* ctx, const double* re_shear, const double* re_bulk);
