@@ -283,14 +283,15 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
     visc = {"workload": "2D shock-droplet 1024x512 with viscous terms (Re shear 10 / 500, bulk 0 / 200)",
             "unit": "cell-updates/s"}
     vcase = case.replace(re_shear=(1.0 / 1e-1, 1.0 / 2e-3), re_bulk=(0.0, 1.0 / 5e-3))
-    for precv in ("fp64", "split"):
-        with Simulation(vcase.replace(precision=precv), x_cb, y_cb, q_cons=q0) as s:
+    for precv, wrf in (("fp64", False), ("split", False), ("fp64", True)):
+        key = precv + ("_weno_Re_flux" if wrf else "")
+        with Simulation(vcase.replace(precision=precv, weno_re_flux=wrf), x_cb, y_cb, q_cons=q0) as s:
             variant, _ = s.tune(5)
             s.select_variant(variant)
             st = torch.cuda.ExternalStream(s.stream)
             t = _time_steps(s, st, flush, args.steps, args.warmup, case.dt)
-            visc[precv] = case.cells * args.steps / t
-            visc[precv + "_vs_inviscid"] = visc[precv] / (fp64_rate if precv == "fp64" else out["split"]["value"])
+            visc[key] = case.cells * args.steps / t
+            visc[key + "_vs_inviscid"] = visc[key] / (fp64_rate if precv == "fp64" else out["split"]["value"])
     out["viscous"] = visc
     # config 4's grid: the droplet at 2048 x 1024 (7 equations, 117 MB per
     # register), gated against split and plain FP64 on the same case; the
