@@ -221,8 +221,8 @@ int mfc_gpu_set_viscosity(mfc_gpu_ctx* ctx, const double* re_shear, const double
  * WENO reconstructions -- the velocities reconstructed to the faces along
  * each direction, cell gradients from them by the divergence theorem, those
  * gradients reconstructed along the sweep direction and averaged at each
- * face -- instead of the finite differences of weno_Re_flux = F.  Two (1-D)
- * or four (2-D) preparation kernels run before every RK stage.  Viscous
+ * face -- instead of the finite differences of weno_Re_flux = F.  Three
+ * (1-D) or five (2-D) preparation kernels run before every RK stage.  Viscous
  * (call mfc_gpu_set_viscosity first), plain FP64, WENO5 contexts without
  * processor boundaries; 0 switches back to the finite differences. */
 int mfc_gpu_set_viscous_gradients(mfc_gpu_ctx* ctx, int weno_re_flux);

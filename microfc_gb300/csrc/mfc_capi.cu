@@ -242,7 +242,7 @@ int launch_stage(mfc_gpu_ctx* c, const double* qin, const double* qbase, double*
   if (c->wrf && c->visc) {  // weno_Re_flux = T: the stage input's face gradients first
     const cudaError_t g = mfc::visc_gradients_launch(c->nd, c->prm.num_fluids, c->dev, c->vg, qin, c->stream);
     if (g != cudaSuccess) return fail(MFC_ERR_CUDA, std::string("viscous gradients: ") + cudaGetErrorString(g));
-    c->launches += c->nd == 1 ? 2 : 4;
+    c->launches += c->nd == 1 ? 3 : 5;
   }
   cudaError_t e = c->stage->launch(P, c->ucoef, qin, qbase, qout, dt, kind, c->stream);
   if (e != cudaSuccess) return fail(MFC_ERR_CUDA, std::string("stage launch: ") + cudaGetErrorString(e));
@@ -725,6 +725,7 @@ int mfc_gpu_set_viscosity(mfc_gpu_ctx* c, const double* re_shear, const double* 
 
 namespace {
 void free_visc_gradients(mfc_gpu_ctx* c) {
+  cudaFree(c->vg.vel);
   cudaFree(c->vg.gx);
   cudaFree(c->vg.gy);
   for (int k = 0; k < 2; ++k) {
@@ -783,6 +784,7 @@ int mfc_gpu_set_viscous_gradients(mfc_gpu_ctx* c, int weno_re_flux) {
   auto alloc = [&](double** ptr, size_t count) {
     if (e == cudaSuccess) e = cudaMalloc(ptr, sizeof(double) * count);
   };
+  alloc(&c->vg.vel, (size_t)nd * (nd > 1 ? ny + 10 : 1) * (nx + 10));
   alloc(&c->vg.gx, (size_t)k * ny * (nx + 6));
   alloc(&c->vg.fg[0], (size_t)k * ny * (nx + 1));
   alloc(&c->vg.w[0], w[0].size());
@@ -1086,6 +1088,7 @@ int mfc_gpu_finalize(mfc_gpu_ctx* c) {
   cudaFree(c->status);
   cudaFree(c->work);
   cudaFree(c->scratch);
+  cudaFree(c->vg.vel);
   cudaFree(c->vg.gx);
   cudaFree(c->vg.gy);
   for (int k = 0; k < 2; ++k) {

@@ -10,7 +10,7 @@
 //      face value is the mean of the right-face value of the cell before the
 //      face and the left-face value of the cell after it.
 //
-// Two kernels per RK stage prepare those face values from the stage input
+// Kernels per RK stage prepare those face values from the stage input
 // (plain FP64, the arithmetic and operation order of the oracle, so the
 // result is bit-identical to it); the stage kernel's viscous flux reads them
 // (ViscParams::fg).  Cells outside the domain take the boundary conditions
@@ -50,6 +50,21 @@ __device__ __forceinline__ double velocity(const DevParams& P, const double* __r
   return div_rn(m, divisor(rho));
 }
 
+// The velocities of the cells x = -5 .. nx+4 (and y = -5 .. ny+4 in 2-D)
+// once, into vel[c][row][col] (row = y + 5, col = x + 5), which every
+// stencil of the cell gradients reads.
+template <int ND, int NF>
+__global__ void __launch_bounds__(256) visc_velocities(const DevParams P, const double* __restrict__ q,
+                                                      const int ncol, const int nrow, double* __restrict__ vel) {
+  const int64_t cells = (int64_t)ncol * nrow;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < cells; t += (int64_t)gridDim.x * blockDim.x) {
+    const int col = (int)(t % ncol), row = (int)(t / ncol);
+    const int i = col - 5, j = ND > 1 ? row - 5 : 0;
+#pragma unroll
+    for (int c = 0; c < ND; ++c) vel[(int64_t)c * cells + t] = velocity<ND, NF>(P, q, c, i, j);
+  }
+}
+
 // The WENO coefficients of cell `cell` along direction d.
 __device__ __forceinline__ void coef_of(const DevParams& P, int d, int cell, double (&c)[kCoefRec]) {
   const int gi = clamp_coef_index(cell, P.n[d]) + P.coff;
@@ -59,12 +74,14 @@ __device__ __forceinline__ void coef_of(const DevParams& P, int d, int cell, dou
 
 // Step 1 on the ncol x nrow cells from (ib, jb): out[c*ND+d][row][col].
 // w[d]: the cell widths ds of direction d for cells -kCoefPad .. n-1+kCoefPad.
-template <int ND, int NF>
-__global__ void __launch_bounds__(256) visc_cell_gradients(const DevParams P, const double* __restrict__ q,
+template <int ND>
+__global__ void __launch_bounds__(256) visc_cell_gradients(const DevParams P, const double* __restrict__ vel,
+                                                          const int vcol, const int vrow,
                                                           const double* __restrict__ w0,
                                                           const double* __restrict__ w1, const int ib, const int jb,
                                                           const int ncol, const int nrow, double* __restrict__ out) {
   const int64_t cells = (int64_t)ncol * nrow;
+  const int64_t vplane = (int64_t)vcol * vrow;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < cells; t += (int64_t)gridDim.x * blockDim.x) {
     const int col = (int)(t % ncol), row = (int)(t / ncol);
     const int i = ib + col, j = jb + row;
@@ -79,8 +96,10 @@ __global__ void __launch_bounds__(256) visc_cell_gradients(const DevParams P, co
       for (int c = 0; c < ND; ++c) {
         double st[5];
 #pragma unroll
-        for (int o = 0; o < 5; ++o)
-          st[o] = velocity<ND, NF>(P, q, c, i + (d == 0 ? o - 2 : 0), j + (d == 1 ? o - 2 : 0));
+        for (int o = 0; o < 5; ++o) {
+          const int vi = i + (d == 0 ? o - 2 : 0) + 5, vj = ND > 1 ? j + (d == 1 ? o - 2 : 0) + 5 : 0;
+          st[o] = __ldg(vel + c * vplane + (int64_t)vj * vcol + vi);
+        }
         double vl, vr;
         weno_cell<5, double>(cf, st, P.weno_eps, vl, vr);
         out[((int64_t)(c * ND + d) * nrow + row) * ncol + col] = inv * (vr - vl);
@@ -133,17 +152,20 @@ template <int ND, int NF>
 cudaError_t launch_all(const DevParams& P, const ViscGradBuffers& B, const double* q, cudaStream_t st) {
   const int nx = P.n[0], ny = ND > 1 ? P.n[1] : 1;
   auto grid = [](int64_t items) { return (unsigned)std::min<int64_t>((items + 255) / 256, 152 * 16); };
-  // region X: x = -3 .. nx+2, rows 0 .. ny-1
-  visc_cell_gradients<ND, NF><<<grid((int64_t)(nx + 6) * ny), 256, 0, st>>>(P, q, B.w[0], B.w[1], -3, 0, nx + 6,
-                                                                             ny, B.gx);
+  const int vcol = nx + 10, vrow = ND > 1 ? ny + 10 : 1;
+  visc_velocities<ND, NF><<<grid((int64_t)vcol * vrow), 256, 0, st>>>(P, q, vcol, vrow, B.vel);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  // region X: x = -3 .. nx+2, rows 0 .. ny-1
+  visc_cell_gradients<ND><<<grid((int64_t)(nx + 6) * ny), 256, 0, st>>>(P, B.vel, vcol, vrow, B.w[0], B.w[1], -3, 0,
+                                                                         nx + 6, ny, B.gx);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
   visc_face_gradients<ND, 0><<<grid((int64_t)(nx + 1) * ny), 256, 0, st>>>(P, B.gx, -3, 0, nx + 6, ny, B.fg[0]);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if constexpr (ND > 1) {
     // region Y: columns 0 .. nx-1, y = -3 .. ny+2
-    visc_cell_gradients<ND, NF><<<grid((int64_t)nx * (ny + 6)), 256, 0, st>>>(P, q, B.w[0], B.w[1], 0, -3, nx,
-                                                                               ny + 6, B.gy);
+    visc_cell_gradients<ND><<<grid((int64_t)nx * (ny + 6)), 256, 0, st>>>(P, B.vel, vcol, vrow, B.w[0], B.w[1], 0,
+                                                                           -3, nx, ny + 6, B.gy);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     visc_face_gradients<ND, 1><<<grid((int64_t)nx * (ny + 1)), 256, 0, st>>>(P, B.gy, 0, -3, nx, ny + 6, B.fg[1]);
     e = cudaGetLastError();
