@@ -75,7 +75,7 @@ class Case:
     re_bulk: tuple = ()                 # fluid_pp(i)%Re(2), bulk Reynolds number
     # weno_Re_flux: the viscous stresses from WENO-reconstructed velocity
     # gradients (m_viscous.fpp:200-216, m_rhs.fpp:514-528) instead of the
-    # finite differences of the default; plain FP64, WENO5, 1-D and 2-D
+    # finite differences of the default; WENO5, 1-D and 2-D
     weno_re_flux: bool = False
     patches: list = field(default_factory=list)
     stretch_x: tuple = ()               # (a_x, x_a, x_b, loops_x) of a stretched x grid; () = uniform
@@ -179,9 +179,9 @@ class Case:
             bad("Unsupported value of precision mode")
         if self.char_decomp and (self.precision != "fp64" or self.viscous or self.weno_order == 1):
             bad("char_decomp needs plain FP64, an inviscid case and WENO3 or WENO5")
-        if self.weno_re_flux and self.viscous and (self.precision != "fp64" or self.weno_order != 5):
+        if self.weno_re_flux and self.viscous and (self.precision == "fp64_fma" or self.weno_order != 5):
             bad("weno_Re_flux = T (WENO-reconstructed velocity gradients for the viscous stresses) is built "
-                "for plain FP64 and WENO5")
+                "for WENO5 in the FP64, split and gated precisions")
         # grid stretching, m_start_up.fpp:238-330 (pre_process)
         for ax, st, dom, used in (("x", self.stretch_x, self.x_domain, True),
                                   ("y", self.stretch_y, self.y_domain, self.n > 0)):

@@ -751,8 +751,8 @@ int mfc_gpu_set_viscous_gradients(mfc_gpu_ctx* c, int weno_re_flux) {
     return MFC_OK;
   }
   if (!c->visc) return fail(MFC_ERR_INVALID, "weno_Re_flux needs a viscous context (mfc_gpu_set_viscosity first)");
-  if (c->prm.precision != MFC_PREC_FP64)
-    return fail(MFC_ERR_INVALID, "weno_Re_flux is built for plain FP64 (MFC_PREC_FP64) contexts");
+  if (c->prm.precision == MFC_PREC_FP64_FMA)
+    return fail(MFC_ERR_INVALID, "weno_Re_flux is built for the FP64, split and gated precisions");
   if (c->prm.weno_order != 5) return fail(MFC_ERR_INVALID, "weno_Re_flux is built for WENO5");
   if (c->has_proc) return fail(MFC_ERR_INVALID, "weno_Re_flux is built without processor boundaries");
   if (c->wrf) return MFC_OK;

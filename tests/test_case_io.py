@@ -51,7 +51,7 @@ def test_case_dict_round_trip_matches_builder():
     (dict(bc_x=(-1, -3)), "bc_x%beg and bc_x%end"),
     (dict(bc_y=(-3, -3)), "n and bc_y%beg"),
     (dict(gammas=(-1.0, 2.5)), "fluid_pp(i)%gamma"),
-    (dict(weno_re_flux=True, re_shear=(10.0, 10.0), precision="split"), "weno_Re_flux"),
+    (dict(weno_re_flux=True, re_shear=(10.0, 10.0), weno_order=3, m=199), "weno_Re_flux"),
 ])
 def test_check_rejects_invalid_inputs_like_the_reference(change, msg):
     c = cases.sod_1d(m=99, steps=10, dt=1e-4).replace(**change)

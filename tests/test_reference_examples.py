@@ -157,9 +157,7 @@ def test_reference_example_runs_bitwise_like_the_oracle(name, oracle_lib):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", [n for n in NAMES if n != "2D_shockdroplet"])
 def test_reference_example_split_precision_within_the_contract(name, oracle_lib):
-    # weno_Re_flux is built for plain FP64: the split path's viscous stresses
-    # take the finite-difference gradients, and so does its FP64 reference
-    c = _case(name).replace(precision="split", weno_re_flux=False)
+    c = _case(name).replace(precision="split")
     stop = c.t_step_start + 100
     x, y, z, q = preprocess.generate(c)
     grids = _grids(c, x, y, z)

@@ -80,8 +80,9 @@ def test_viscosity_changes_the_result_and_can_be_switched_off(oracle_lib):
         assert rel_l1(sim.download(), q_inv)[c.mom_idx] > 1e-8
 
 
-def test_split_precision_viscous_error_bounded(oracle_lib):
-    c = _viscous_droplet(precision="split")
+@WRF
+def test_split_precision_viscous_error_bounded(oracle_lib, wrf):
+    c = _viscous_droplet(precision="split").replace(weno_re_flux=wrf)
     x_cb, y_cb, _, q = preprocess.generate(c)
     got, ref = _gpu_and_oracle(oracle_lib, c, x_cb, y_cb, q, c.t_step_stop)
     err = rel_l1(got, ref)
@@ -122,7 +123,7 @@ def test_viscous_refusals():
 
 def test_weno_re_flux_changes_the_result_and_refusals(oracle_lib):
     """The two gradient discretisations give different results; the WENO
-    gradients are refused where they are not built."""
+    gradients need a viscous context."""
     from microfc_gb300 import Simulation
     from microfc_gb300._lib import MfcError
     c = _viscous_droplet(steps=10)
@@ -135,9 +136,6 @@ def test_weno_re_flux_changes_the_result_and_refusals(oracle_lib):
             if wrf:
                 assert sim.launches == 10 * 3 * (1 + 5)  # five preparation kernels per stage
     assert rel_l1(out[1], out[0])[c.mom_idx] > 1e-10
-    with Simulation(c.replace(precision="split"), x_cb, y_cb, q_cons=q) as sim:
-        with pytest.raises(MfcError, match="plain FP64"):
-            sim.set_viscous_gradients(True)
     with Simulation(cases.shock_droplet_2d(nx=96, ny=48, steps=2), x_cb, y_cb, q_cons=q) as sim:
         with pytest.raises(MfcError, match="viscous context"):
             sim.set_viscous_gradients(True)
