@@ -279,11 +279,12 @@ def other_modes(args, case, x_cb, y_cb, q0, flush, fp64_rate):
                                   "vs_plain_fp64": rate / fp64_rate, "tile_variant": variant}
     # the viscous terms (m_viscous.fpp) on the same workload: water and air
     # with shear and bulk Reynolds numbers (1/mu in the case's units), plain
-    # FP64 (bit-identical to the oracle) and split precision
+    # FP64 (bit-identical to the oracle) and split precision, with
+    # finite-difference and with WENO (weno_Re_flux) velocity gradients
     visc = {"workload": "2D shock-droplet 1024x512 with viscous terms (Re shear 10 / 500, bulk 0 / 200)",
             "unit": "cell-updates/s"}
     vcase = case.replace(re_shear=(1.0 / 1e-1, 1.0 / 2e-3), re_bulk=(0.0, 1.0 / 5e-3))
-    for precv, wrf in (("fp64", False), ("split", False), ("fp64", True)):
+    for precv, wrf in (("fp64", False), ("split", False), ("fp64", True), ("split", True)):
         key = precv + ("_weno_Re_flux" if wrf else "")
         with Simulation(vcase.replace(precision=precv, weno_re_flux=wrf), x_cb, y_cb, q_cons=q0) as s:
             variant, _ = s.tune(5)

@@ -242,7 +242,7 @@ int launch_stage(mfc_gpu_ctx* c, const double* qin, const double* qbase, double*
   if (c->wrf && c->visc) {  // weno_Re_flux = T: the stage input's face gradients first
     const cudaError_t g = mfc::visc_gradients_launch(c->nd, c->prm.num_fluids, c->dev, c->vg, qin, c->stream);
     if (g != cudaSuccess) return fail(MFC_ERR_CUDA, std::string("viscous gradients: ") + cudaGetErrorString(g));
-    c->launches += c->nd == 1 ? 3 : 5;
+    c->launches += c->nd == 1 ? 3 : 4;
   }
   cudaError_t e = c->stage->launch(P, c->ucoef, qin, qbase, qout, dt, kind, c->stream);
   if (e != cudaSuccess) return fail(MFC_ERR_CUDA, std::string("stage launch: ") + cudaGetErrorString(e));
@@ -726,8 +726,7 @@ int mfc_gpu_set_viscosity(mfc_gpu_ctx* c, const double* re_shear, const double* 
 namespace {
 void free_visc_gradients(mfc_gpu_ctx* c) {
   cudaFree(c->vg.vel);
-  cudaFree(c->vg.gx);
-  cudaFree(c->vg.gy);
+  cudaFree(c->vg.g);
   for (int k = 0; k < 2; ++k) {
     cudaFree(c->vg.fg[k]);
     cudaFree(c->vg.w[k]);
@@ -785,11 +784,10 @@ int mfc_gpu_set_viscous_gradients(mfc_gpu_ctx* c, int weno_re_flux) {
     if (e == cudaSuccess) e = cudaMalloc(ptr, sizeof(double) * count);
   };
   alloc(&c->vg.vel, (size_t)nd * (nd > 1 ? ny + 10 : 1) * (nx + 10));
-  alloc(&c->vg.gx, (size_t)k * ny * (nx + 6));
+  alloc(&c->vg.g, (size_t)k * (nd > 1 ? ny + 6 : 1) * (nx + 6));
   alloc(&c->vg.fg[0], (size_t)k * ny * (nx + 1));
   alloc(&c->vg.w[0], w[0].size());
   if (nd > 1) {
-    alloc(&c->vg.gy, (size_t)k * (ny + 6) * nx);
     alloc(&c->vg.fg[1], (size_t)k * (ny + 1) * nx);
     alloc(&c->vg.w[1], w[1].size());
   }
@@ -1089,8 +1087,7 @@ int mfc_gpu_finalize(mfc_gpu_ctx* c) {
   cudaFree(c->work);
   cudaFree(c->scratch);
   cudaFree(c->vg.vel);
-  cudaFree(c->vg.gx);
-  cudaFree(c->vg.gy);
+  cudaFree(c->vg.g);
   for (int k = 0; k < 2; ++k) {
     cudaFree(c->vg.fg[k]);
     cudaFree(c->vg.w[k]);

@@ -211,19 +211,17 @@ cudaError_t ctx_scratch(mfc_gpu_ctx* c, size_t bytes, void** out);
 
 // weno_Re_flux = T (mfc_visc_grad.cu): device buffers of the gradient
 // preparation -- the velocities ([ND][ny+10][nx+10] from x = y = -5; one row
-// in 1-D), the cell gradients of region X ([ND*ND][ny][nx+6], x from -3) and
-// region Y ([ND*ND][ny+6][nx], y from -3), the face gradients
-// (ViscParams::fg) and the cell widths of each direction for cells
-// -kCoefPad .. n-1+kCoefPad.
+// in 1-D), the cell gradients ([ND*ND][ny+6][nx+6] from x = y = -3; one row
+// in 1-D), the face gradients (ViscParams::fg) and the cell widths of each
+// direction for cells -kCoefPad .. n-1+kCoefPad.
 struct ViscGradBuffers {
   double* vel = nullptr;
-  double* gx = nullptr;
-  double* gy = nullptr;
+  double* g = nullptr;
   double* fg[2] = {nullptr, nullptr};
   double* w[2] = {nullptr, nullptr};
 };
 // Prepares the face gradients of the stage input q on stream st (3 launches
-// in 1-D, 5 in 2-D).
+// in 1-D, 4 in 2-D).
 cudaError_t visc_gradients_launch(int nd, int nf, const DevParams& P, const ViscGradBuffers& B, const double* q,
                                   cudaStream_t st);
 

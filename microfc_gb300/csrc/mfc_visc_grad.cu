@@ -17,11 +17,14 @@
 // by index mapping, as everywhere else.
 //
 // Regions (x0 = 0 .. nx-1, y0 = 0 .. ny-1 the interior):
-//   x faces i+1/2, i = -1 .. nx-1, rows y0: need G on x = -3 .. nx+2, rows y0
-//     ("region X"), whose WENO along x reads u on x = -5 .. nx+4 and, for G_c1,
-//     along y on rows -2 .. ny+1 (corner ghost cells);
+//   x faces i+1/2, i = -1 .. nx-1, rows y0: need G on x = -3 .. nx+2, rows y0,
+//     whose WENO along x reads u on x = -5 .. nx+4 and, for G_c1, along y on
+//     rows -2 .. ny+1 (corner ghost cells);
 //   y faces j+1/2, j = -1 .. ny-1, columns x0: need G on y = -3 .. ny+2,
-//     columns x0 ("region Y").
+//     columns x0.
+// One launch computes G on the box x, y = -3 .. n+2 that holds both (each
+// interior cell once; the 36 corner cells of the box are computed and not
+// read), from the velocities of x, y = -5 .. n+4.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -156,18 +159,15 @@ cudaError_t launch_all(const DevParams& P, const ViscGradBuffers& B, const doubl
   visc_velocities<ND, NF><<<grid((int64_t)vcol * vrow), 256, 0, st>>>(P, q, vcol, vrow, B.vel);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  // region X: x = -3 .. nx+2, rows 0 .. ny-1
-  visc_cell_gradients<ND><<<grid((int64_t)(nx + 6) * ny), 256, 0, st>>>(P, B.vel, vcol, vrow, B.w[0], B.w[1], -3, 0,
-                                                                         nx + 6, ny, B.gx);
+  // G on x = -3 .. nx+2 (and y = -3 .. ny+2)
+  const int gcol = nx + 6, grow = ND > 1 ? ny + 6 : 1, gjb = ND > 1 ? -3 : 0;
+  visc_cell_gradients<ND><<<grid((int64_t)gcol * grow), 256, 0, st>>>(P, B.vel, vcol, vrow, B.w[0], B.w[1], -3, gjb,
+                                                                       gcol, grow, B.g);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  visc_face_gradients<ND, 0><<<grid((int64_t)(nx + 1) * ny), 256, 0, st>>>(P, B.gx, -3, 0, nx + 6, ny, B.fg[0]);
+  visc_face_gradients<ND, 0><<<grid((int64_t)(nx + 1) * ny), 256, 0, st>>>(P, B.g, -3, gjb, gcol, grow, B.fg[0]);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if constexpr (ND > 1) {
-    // region Y: columns 0 .. nx-1, y = -3 .. ny+2
-    visc_cell_gradients<ND><<<grid((int64_t)nx * (ny + 6)), 256, 0, st>>>(P, B.vel, vcol, vrow, B.w[0], B.w[1], 0,
-                                                                           -3, nx, ny + 6, B.gy);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    visc_face_gradients<ND, 1><<<grid((int64_t)nx * (ny + 1)), 256, 0, st>>>(P, B.gy, 0, -3, nx, ny + 6, B.fg[1]);
+    visc_face_gradients<ND, 1><<<grid((int64_t)nx * (ny + 1)), 256, 0, st>>>(P, B.g, -3, gjb, gcol, grow, B.fg[1]);
     e = cudaGetLastError();
   }
   return e;

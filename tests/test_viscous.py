@@ -134,7 +134,7 @@ def test_weno_re_flux_changes_the_result_and_refusals(oracle_lib):
             sim.run(0, 10)
             out.append(sim.download())
             if wrf:
-                assert sim.launches == 10 * 3 * (1 + 5)  # five preparation kernels per stage
+                assert sim.launches == 10 * 3 * (1 + 4)  # four preparation kernels per stage
     assert rel_l1(out[1], out[0])[c.mom_idx] > 1e-10
     with Simulation(cases.shock_droplet_2d(nx=96, ny=48, steps=2), x_cb, y_cb, q_cons=q) as sim:
         with pytest.raises(MfcError, match="viscous context"):
