@@ -240,7 +240,8 @@ int launch_stage(mfc_gpu_ctx* c, const double* qin, const double* qbase, double*
   mfc::DevParams P = c->dev;
   if (last_stage && c->monitor_on) P.monitor = c->monitor;  // ICFL of the step's new state
   if (c->wrf && c->visc) {  // weno_Re_flux = T: the stage input's face gradients first
-    const cudaError_t g = mfc::visc_gradients_launch(c->nd, c->prm.num_fluids, c->dev, c->vg, qin, c->stream);
+    const bool fp32 = c->prm.precision == MFC_PREC_SPLIT || c->prm.precision == MFC_PREC_GATED;
+    const cudaError_t g = mfc::visc_gradients_launch(c->nd, c->prm.num_fluids, fp32, c->dev, c->vg, qin, c->stream);
     if (g != cudaSuccess) return fail(MFC_ERR_CUDA, std::string("viscous gradients: ") + cudaGetErrorString(g));
     c->launches += c->nd == 1 ? 3 : 4;
   }
@@ -730,6 +731,7 @@ void free_visc_gradients(mfc_gpu_ctx* c) {
   for (int k = 0; k < 2; ++k) {
     cudaFree(c->vg.fg[k]);
     cudaFree(c->vg.w[k]);
+    cudaFree(c->vg.cf[k]);
   }
   c->vg = mfc::ViscGradBuffers{};
   c->wrf = false;
@@ -791,15 +793,28 @@ int mfc_gpu_set_viscous_gradients(mfc_gpu_ctx* c, int weno_re_flux) {
     alloc(&c->vg.fg[1], (size_t)k * (ny + 1) * nx);
     alloc(&c->vg.w[1], w[1].size());
   }
+  // split and gated: the reconstructions' FP32 table of each direction
+  const bool fp32 = c->prm.precision == MFC_PREC_SPLIT || c->prm.precision == MFC_PREC_GATED;
+  std::vector<float> cf[2];
+  for (int d = 0; fp32 && d < nd; ++d) {
+    const size_t stride = w[d].size();  // cells -kCoefPad .. n-1+kCoefPad
+    cf[d].resize((mfc::kNumCoef + 1) * stride);
+    for (int kk = 0; kk < mfc::kNumCoef; ++kk)
+      for (size_t j = 0; j < stride; ++j)
+        cf[d][kk * stride + j] = (float)gt.host[gt.off_coef[d] + (size_t)kk * gt.cstride[d] + j];
+    for (size_t j = 0; j < stride; ++j) cf[d][mfc::kNumCoef * stride + j] = (float)(1.0 / w[d][j]);
+    if (e == cudaSuccess) e = cudaMalloc(&c->vg.cf[d], sizeof(float) * cf[d].size());
+  }
   if (e != cudaSuccess) {
     free_visc_gradients(c);
     return fail(MFC_ERR_NOMEM, "weno_Re_flux buffers");
   }
   MFC_CUDA(cudaStreamSynchronize(c->stream));
   MFC_CUDA(cudaMemcpy(c->tables, gt.host.data(), sizeof(double) * gt.host.size(), cudaMemcpyHostToDevice));
-  for (int d = 0; d < nd; ++d)
+  for (int d = 0; d < nd; ++d) {
     MFC_CUDA(cudaMemcpy(c->vg.w[d], w[d].data(), sizeof(double) * w[d].size(), cudaMemcpyHostToDevice));
-  if (nd == 1) c->vg.w[1] = nullptr;
+    if (fp32) MFC_CUDA(cudaMemcpy(c->vg.cf[d], cf[d].data(), sizeof(float) * cf[d].size(), cudaMemcpyHostToDevice));
+  }
   c->visc_host.fg[0] = c->vg.fg[0];
   c->visc_host.fg[1] = c->vg.fg[1];
   MFC_CUDA(cudaMemcpy(c->visc, &c->visc_host, sizeof(c->visc_host), cudaMemcpyHostToDevice));
@@ -1091,6 +1106,7 @@ int mfc_gpu_finalize(mfc_gpu_ctx* c) {
   for (int k = 0; k < 2; ++k) {
     cudaFree(c->vg.fg[k]);
     cudaFree(c->vg.w[k]);
+    cudaFree(c->vg.cf[k]);
   }
   cudaFree(c->gate_w);
   cudaFree(c->gate_flags);

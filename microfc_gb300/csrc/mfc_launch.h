@@ -212,18 +212,22 @@ cudaError_t ctx_scratch(mfc_gpu_ctx* c, size_t bytes, void** out);
 // weno_Re_flux = T (mfc_visc_grad.cu): device buffers of the gradient
 // preparation -- the velocities ([ND][ny+10][nx+10] from x = y = -5; one row
 // in 1-D), the cell gradients ([ND*ND][ny+6][nx+6] from x = y = -3; one row
-// in 1-D), the face gradients (ViscParams::fg) and the cell widths of each
-// direction for cells -kCoefPad .. n-1+kCoefPad.
+// in 1-D), the face gradients (ViscParams::fg), the cell widths of each
+// direction for cells -kCoefPad .. n-1+kCoefPad and, for the split and gated
+// precisions, an FP32 table per direction: the WENO coefficients of those
+// cells ([kNumCoef][n + 2 kCoefPad]) followed by their inverse widths.
 struct ViscGradBuffers {
   double* vel = nullptr;
   double* g = nullptr;
   double* fg[2] = {nullptr, nullptr};
   double* w[2] = {nullptr, nullptr};
+  float* cf[2] = {nullptr, nullptr};
 };
 // Prepares the face gradients of the stage input q on stream st (3 launches
-// in 1-D, 4 in 2-D).
-cudaError_t visc_gradients_launch(int nd, int nf, const DevParams& P, const ViscGradBuffers& B, const double* q,
-                                  cudaStream_t st);
+// in 1-D, 4 in 2-D), reconstructing in FP32 when fp32 is set (split and
+// gated contexts), else in FP64.
+cudaError_t visc_gradients_launch(int nd, int nf, bool fp32, const DevParams& P, const ViscGradBuffers& B,
+                                  const double* q, cudaStream_t st);
 
 // The default (first registered) launcher of a configuration, or nullptr.
 const StageEntry* find_stage(int nd, int nf, int wo, int prec, bool visc = false, bool chr = false);

@@ -10,11 +10,15 @@
 //      face value is the mean of the right-face value of the cell before the
 //      face and the left-face value of the cell after it.
 //
-// Kernels per RK stage prepare those face values from the stage input
-// (plain FP64, the arithmetic and operation order of the oracle, so the
-// result is bit-identical to it); the stage kernel's viscous flux reads them
-// (ViscParams::fg).  Cells outside the domain take the boundary conditions
-// by index mapping, as everywhere else.
+// Kernels per RK stage prepare those face values from the stage input; the
+// stage kernel's viscous flux reads them (ViscParams::fg).  The velocities
+// are FP64 in every precision; the two reconstructions run in RT: FP64 for
+// the plain path (the arithmetic and operation order of the oracle, so the
+// result is bit-identical to it), FP32 for the split and gated paths, whose
+// stage kernels take the gradients in FP32 anyway.  The buffers stay FP64
+// (an FP32 value widened, so the stage kernel narrows it back exactly).
+// Cells outside the domain take the boundary conditions by index mapping,
+// as everywhere else.
 //
 // Regions (x0 = 0 .. nx-1, y0 = 0 .. ny-1 the interior):
 //   x faces i+1/2, i = -1 .. nx-1, rows y0: need G on x = -3 .. nx+2, rows y0,
@@ -68,44 +72,64 @@ __global__ void __launch_bounds__(256) visc_velocities(const DevParams P, const 
   }
 }
 
-// The WENO coefficients of cell `cell` along direction d.
-__device__ __forceinline__ void coef_of(const DevParams& P, int d, int cell, double (&c)[kCoefRec]) {
-  const int gi = clamp_coef_index(cell, P.n[d]) + P.coff;
+// The WENO coefficients of cell `cell` along direction d: FP64 from the
+// context's grid tables, FP32 from the preparation's own table cft of that
+// direction ([kNumCoef][n + 2 kCoefPad], then the inverse cell widths).
+template <class RT>
+__device__ __forceinline__ void coef_of(const DevParams& P, const float* __restrict__ cft, int d, int cell,
+                                        RT (&c)[kCoefRec]) {
+  const int gi = clamp_coef_index(cell, P.n[d]) + kCoefPad;
+  if constexpr (sizeof(RT) == 4) {
+    const int stride = P.n[d] + 2 * kCoefPad;
 #pragma unroll
-  for (int k = 0; k < kNumCoef; ++k) c[k] = __ldg(P.coef[d] + k * P.cstride[d] + gi);
+    for (int k = 0; k < kNumCoef; ++k) c[k] = __ldg(cft + k * stride + gi);
+  } else {
+#pragma unroll
+    for (int k = 0; k < kNumCoef; ++k) c[k] = __ldg(P.coef[d] + k * P.cstride[d] + gi);
+  }
+}
+
+// 1/ds of cell `cell` along direction d (w: the FP64 widths of the
+// direction, cft: its FP32 table).
+template <class RT>
+__device__ __forceinline__ RT inverse_width(const DevParams& P, const double* __restrict__ w,
+                                            const float* __restrict__ cft, int d, int cell) {
+  const int gi = clamp_coef_index(cell, P.n[d]) + kCoefPad;
+  if constexpr (sizeof(RT) == 4) return __ldg(cft + kNumCoef * (P.n[d] + 2 * kCoefPad) + gi);
+  else return div_rn(1.0, divisor(__ldg(w + gi)));
 }
 
 // Step 1 on the ncol x nrow cells from (ib, jb): out[c*ND+d][row][col].
-// w[d]: the cell widths ds of direction d for cells -kCoefPad .. n-1+kCoefPad.
-template <int ND>
-__global__ void __launch_bounds__(256) visc_cell_gradients(const DevParams P, const double* __restrict__ vel,
-                                                          const int vcol, const int vrow,
-                                                          const double* __restrict__ w0,
-                                                          const double* __restrict__ w1, const int ib, const int jb,
+// B.w[d]: the cell widths ds of direction d for cells -kCoefPad ..
+// n-1+kCoefPad; B.cf[d]: the FP32 table of the direction.
+template <int ND, class RT>
+__global__ void __launch_bounds__(256) visc_cell_gradients(const DevParams P, const ViscGradBuffers B,
+                                                          const int vcol, const int vrow, const int ib, const int jb,
                                                           const int ncol, const int nrow, double* __restrict__ out) {
+  const double* __restrict__ vel = B.vel;
   const int64_t cells = (int64_t)ncol * nrow;
   const int64_t vplane = (int64_t)vcol * vrow;
+  const RT eps = narrow<RT>(P.weno_eps);
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < cells; t += (int64_t)gridDim.x * blockDim.x) {
     const int col = (int)(t % ncol), row = (int)(t / ncol);
     const int i = ib + col, j = jb + row;
 #pragma unroll
     for (int d = 0; d < ND; ++d) {
       const int cell = d == 0 ? i : j;
-      double cf[kCoefRec];
-      coef_of(P, d, cell, cf);
-      const double* w = d == 0 ? w0 : w1;
-      const double inv = div_rn(1.0, divisor(__ldg(w + clamp_coef_index(cell, P.n[d]) + kCoefPad)));
+      RT cf[kCoefRec];
+      coef_of(P, B.cf[d], d, cell, cf);
+      const RT inv = inverse_width<RT>(P, B.w[d], B.cf[d], d, cell);
 #pragma unroll
       for (int c = 0; c < ND; ++c) {
-        double st[5];
+        RT st[5];
 #pragma unroll
         for (int o = 0; o < 5; ++o) {
           const int vi = i + (d == 0 ? o - 2 : 0) + 5, vj = ND > 1 ? j + (d == 1 ? o - 2 : 0) + 5 : 0;
-          st[o] = __ldg(vel + c * vplane + (int64_t)vj * vcol + vi);
+          st[o] = narrow<RT>(__ldg(vel + c * vplane + (int64_t)vj * vcol + vi));
         }
-        double vl, vr;
-        weno_cell<5, double>(cf, st, P.weno_eps, vl, vr);
-        out[((int64_t)(c * ND + d) * nrow + row) * ncol + col] = inv * (vr - vl);
+        RT vl, vr;
+        weno_cell<5, RT>(cf, st, eps, vl, vr);
+        out[((int64_t)(c * ND + d) * nrow + row) * ncol + col] = widen(inv * (vr - vl));
       }
     }
   }
@@ -114,44 +138,46 @@ __global__ void __launch_bounds__(256) visc_cell_gradients(const DevParams P, co
 // Step 2 along dir: faces f+1/2 for f = -1 .. n_dir-1 of the interior lines
 // across, from the cell gradients G of the region ([c*ND+d][grow][gcol],
 // origin (gib, gjb)): out[c*ND+d][...] with the face index f+1 along dir.
-template <int ND, int DIR>
-__global__ void __launch_bounds__(256) visc_face_gradients(const DevParams P, const double* __restrict__ G,
+template <int ND, int DIR, class RT>
+__global__ void __launch_bounds__(256) visc_face_gradients(const DevParams P, const float* __restrict__ cft,
+                                                          const double* __restrict__ G,
                                                           const int gib, const int gjb, const int gncol,
                                                           const int gnrow, double* __restrict__ out) {
   const int nf = P.n[DIR] + 1;                 // faces along dir
   const int nl = DIR == 0 ? (ND > 1 ? P.n[1] : 1) : P.n[0];  // lines across
   const int64_t items = (int64_t)nf * nl;
   const int64_t plane_out = items;
+  const RT eps = narrow<RT>(P.weno_eps);
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
     int f, l;  // face index (0 = face -1/2) and line
     if (DIR == 0) { f = (int)(t % nf); l = (int)(t / nf); }
     else { l = (int)(t % nl); f = (int)(t / nl); }
     const int cl = f - 1, cr = f;  // the cells before and after the face, along dir
-    double cfl[kCoefRec], cfr[kCoefRec];
-    coef_of(P, DIR, cl, cfl);
-    coef_of(P, DIR, cr, cfr);
+    RT cfl[kCoefRec], cfr[kCoefRec];
+    coef_of(P, cft, DIR, cl, cfl);
+    coef_of(P, cft, DIR, cr, cfr);
     // element (a along dir, line l) of field k of the region
-    auto at = [&](int k, int a) -> double {
+    auto at = [&](int k, int a) -> RT {
       const int i = DIR == 0 ? a : l, j = DIR == 0 ? l : a;
-      return __ldg(G + ((int64_t)k * gnrow + (j - gjb)) * gncol + (i - gib));
+      return narrow<RT>(__ldg(G + ((int64_t)k * gnrow + (j - gjb)) * gncol + (i - gib)));
     };
 #pragma unroll
     for (int k = 0; k < ND * ND; ++k) {
-      double sl[5], sr[5];
+      RT sl[5], sr[5];
 #pragma unroll
       for (int o = 0; o < 5; ++o) {
         sl[o] = at(k, cl + o - 2);
         sr[o] = at(k, cr + o - 2);
       }
-      const double right = weno_cell_side<5, 1, double>(cfl, sl, P.weno_eps);  // face value of the cell before
-      const double left = weno_cell_side<5, 0, double>(cfr, sr, P.weno_eps);   // and of the cell after
+      const RT right = weno_cell_side<5, 1, RT>(cfl, sl, eps);  // face value of the cell before
+      const RT left = weno_cell_side<5, 0, RT>(cfr, sr, eps);   // and of the cell after
       const int64_t o = DIR == 0 ? (int64_t)l * nf + f : (int64_t)f * nl + l;
-      out[k * plane_out + o] = 0.5 * (right + left);
+      out[k * plane_out + o] = widen(RT(0.5) * (right + left));
     }
   }
 }
 
-template <int ND, int NF>
+template <int ND, int NF, class RT>
 cudaError_t launch_all(const DevParams& P, const ViscGradBuffers& B, const double* q, cudaStream_t st) {
   const int nx = P.n[0], ny = ND > 1 ? P.n[1] : 1;
   auto grid = [](int64_t items) { return (unsigned)std::min<int64_t>((items + 255) / 256, 152 * 16); };
@@ -161,13 +187,15 @@ cudaError_t launch_all(const DevParams& P, const ViscGradBuffers& B, const doubl
   if (e != cudaSuccess) return e;
   // G on x = -3 .. nx+2 (and y = -3 .. ny+2)
   const int gcol = nx + 6, grow = ND > 1 ? ny + 6 : 1, gjb = ND > 1 ? -3 : 0;
-  visc_cell_gradients<ND><<<grid((int64_t)gcol * grow), 256, 0, st>>>(P, B.vel, vcol, vrow, B.w[0], B.w[1], -3, gjb,
-                                                                       gcol, grow, B.g);
+  visc_cell_gradients<ND, RT><<<grid((int64_t)gcol * grow), 256, 0, st>>>(P, B, vcol, vrow, -3, gjb, gcol, grow,
+                                                                           B.g);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  visc_face_gradients<ND, 0><<<grid((int64_t)(nx + 1) * ny), 256, 0, st>>>(P, B.g, -3, gjb, gcol, grow, B.fg[0]);
+  visc_face_gradients<ND, 0, RT><<<grid((int64_t)(nx + 1) * ny), 256, 0, st>>>(P, B.cf[0], B.g, -3, gjb, gcol, grow,
+                                                                               B.fg[0]);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if constexpr (ND > 1) {
-    visc_face_gradients<ND, 1><<<grid((int64_t)nx * (ny + 1)), 256, 0, st>>>(P, B.g, -3, gjb, gcol, grow, B.fg[1]);
+    visc_face_gradients<ND, 1, RT><<<grid((int64_t)nx * (ny + 1)), 256, 0, st>>>(P, B.cf[1], B.g, -3, gjb, gcol,
+                                                                                 grow, B.fg[1]);
     e = cudaGetLastError();
   }
   return e;
@@ -175,12 +203,20 @@ cudaError_t launch_all(const DevParams& P, const ViscGradBuffers& B, const doubl
 
 }  // namespace
 
-cudaError_t visc_gradients_launch(int nd, int nf, const DevParams& P, const ViscGradBuffers& B, const double* q,
-                                  cudaStream_t st) {
-  if (nd == 1 && nf == 1) return launch_all<1, 1>(P, B, q, st);
-  if (nd == 1 && nf == 2) return launch_all<1, 2>(P, B, q, st);
-  if (nd == 2 && nf == 1) return launch_all<2, 1>(P, B, q, st);
-  if (nd == 2 && nf == 2) return launch_all<2, 2>(P, B, q, st);
+cudaError_t visc_gradients_launch(int nd, int nf, bool fp32, const DevParams& P, const ViscGradBuffers& B,
+                                  const double* q, cudaStream_t st) {
+  if (fp32) {
+    if (B.cf[0] == nullptr || (nd > 1 && B.cf[1] == nullptr)) return cudaErrorInvalidValue;
+    if (nd == 1 && nf == 1) return launch_all<1, 1, float>(P, B, q, st);
+    if (nd == 1 && nf == 2) return launch_all<1, 2, float>(P, B, q, st);
+    if (nd == 2 && nf == 1) return launch_all<2, 1, float>(P, B, q, st);
+    if (nd == 2 && nf == 2) return launch_all<2, 2, float>(P, B, q, st);
+  } else {
+    if (nd == 1 && nf == 1) return launch_all<1, 1, double>(P, B, q, st);
+    if (nd == 1 && nf == 2) return launch_all<1, 2, double>(P, B, q, st);
+    if (nd == 2 && nf == 1) return launch_all<2, 1, double>(P, B, q, st);
+    if (nd == 2 && nf == 2) return launch_all<2, 2, double>(P, B, q, st);
+  }
   return cudaErrorInvalidValue;
 }
 
