@@ -1,7 +1,7 @@
 // Instantiations of the fused stage kernel for 2-D cases, FP64 arithmetic.
 // Tile variants (TX x TY cells, NT threads) are chosen by the autotuner; the
-// first entry per configuration is the default (the autotuner's usual choice
-// on GB300).
+// first entry per configuration is the default until it runs (on GB300 the
+// autotuner takes the 640-thread TMA entry for two fluids and WENO5).
 #include "mfc_launch.h"
 
 namespace mfc {
