@@ -240,7 +240,7 @@ int launch_stage(mfc_gpu_ctx* c, const double* qin, const double* qbase, double*
   mfc::DevParams P = c->dev;
   if (last_stage && c->monitor_on) P.monitor = c->monitor;  // ICFL of the step's new state
   if (c->wrf && c->visc) {  // weno_Re_flux = T: the stage input's face gradients first
-    const bool fp32 = c->prm.precision == MFC_PREC_SPLIT || c->prm.precision == MFC_PREC_GATED;
+    const bool fp32 = c->prm.precision != MFC_PREC_FP64;  // split or gated (contracted FP64 is refused)
     const cudaError_t g = mfc::visc_gradients_launch(c->nd, c->prm.num_fluids, fp32, c->dev, c->vg, qin, c->stream);
     if (g != cudaSuccess) return fail(MFC_ERR_CUDA, std::string("viscous gradients: ") + cudaGetErrorString(g));
     c->launches += c->nd == 1 ? 3 : 4;
@@ -928,6 +928,9 @@ int mfc_gpu_tune(mfc_gpu_ctx* c, int reps, int* variant_out, double* ms_out) {
   if (reps < 1) reps = 5;
   uint32_t saved = 0;  // the timing launches must not leave flags behind
   MFC_CUDA(cudaMemcpyAsync(&saved, c->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  if (c->wrf && c->visc)  // weno_Re_flux: the face gradients that the timed launches read
+    MFC_CUDA(mfc::visc_gradients_launch(c->nd, c->prm.num_fluids, c->prm.precision != MFC_PREC_FP64, c->dev, c->vg,
+                                        c->reg[0], c->stream));
   MFC_CUDA(cudaStreamSynchronize(c->stream));
   const mfc::StageEntry* best = nullptr;
   int idx = -1, best_idx = -1;

@@ -29,6 +29,10 @@ from . import io, preprocess
 from .case import Case
 from .solver import Simulation
 
+# runs of at least this many steps autotune the tile variant first (about
+# three launches of each variant: a few steps' worth of time)
+TUNE_MIN_STEPS = 200
+
 
 def pre_process(case: Case, case_dir: str, ic: str = "host") -> str:
     """Initial condition into p_all/p0/0/ (the pre_process executable's output)."""
@@ -54,6 +58,8 @@ def simulate(case: Case, case_dir: str, text_files: bool = True, device: int = 0
             ThreadPoolExecutor(max_workers=1) as writer:
         if monitor:
             sim.set_monitor(True)
+        if case.t_step_stop - case.t_step_start >= TUNE_MIN_STEPS:
+            sim.tune(3)  # the fastest tile variant; every variant gives the same bits
         pending = [None, None]
 
         def write(t_step, slot):
