@@ -222,8 +222,9 @@ int mfc_gpu_set_viscosity(mfc_gpu_ctx* ctx, const double* re_shear, const double
  * each direction, cell gradients from them by the divergence theorem, those
  * gradients reconstructed along the sweep direction and averaged at each
  * face -- instead of the finite differences of weno_Re_flux = F.  Three
- * (1-D) or four (2-D) preparation kernels run before every RK stage (in
- * FP64, whatever the context's precision).  Viscous (call
+ * (1-D) or four (2-D) preparation kernels run before every RK stage; they
+ * reconstruct in FP64 in FP64 contexts (bit-identical to the CPU build's
+ * operation order) and in FP32 in split and gated ones.  Viscous (call
  * mfc_gpu_set_viscosity first) WENO5 contexts of the FP64, split or gated
  * precision without processor boundaries; 0 switches back to the finite
  * differences. */

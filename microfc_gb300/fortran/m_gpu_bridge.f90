@@ -23,7 +23,8 @@ module m_gpu_bridge
     use iso_c_binding
     use m_derived_types        !< scalar_field
     use m_global_parameters    !< m, n, num_fluids, weno_order, weno_eps, time_stepper,
-                               !! bc_x, bc_y, fluid_pp, x_cb, y_cb, dt, sys_size, buff_size
+                               !! bc_x, bc_y, fluid_pp, x_cb, y_cb, dt, sys_size, buff_size,
+                               !! Re_size, weno_Re_flux
     use m_mpi_proxy            !< s_mpi_abort
 
     implicit none
@@ -102,6 +103,19 @@ module m_gpu_bridge
         type(c_ptr) function mfc_gpu_last_error() bind(C, name='mfc_gpu_last_error')
             import :: c_ptr
         end function mfc_gpu_last_error
+
+        integer(c_int) function mfc_gpu_set_viscosity(c, re_shear, re_bulk) bind(C, name='mfc_gpu_set_viscosity')
+            import :: c_ptr, c_int, c_double
+            type(c_ptr), value :: c
+            real(c_double), dimension(*), intent(in) :: re_shear, re_bulk
+        end function mfc_gpu_set_viscosity
+
+        integer(c_int) function mfc_gpu_set_viscous_gradients(c, weno_re_flux) &
+            bind(C, name='mfc_gpu_set_viscous_gradients')
+            import :: c_ptr, c_int
+            type(c_ptr), value :: c
+            integer(c_int), value :: weno_re_flux
+        end function mfc_gpu_set_viscous_gradients
     end interface
 
 contains
@@ -127,10 +141,14 @@ contains
 
     !> Creates the device context from the namelist globals and uploads
     !! q_cons_ts(1): each sf(-b:m+b, -b:n+b) is passed from sf(0, 0) with the
-    !! leading dimension m + 2*buff_size + 1.
+    !! leading dimension m + 2*buff_size + 1.  Viscous cases (a positive
+    !! fluid_pp(i)%Re, Re_size > 0) pass the Reynolds numbers of every fluid,
+    !! the unset ones as the namelist default (negative: no viscosity), and
+    !! weno_Re_flux picks the WENO velocity gradients.
     subroutine s_initialize_gpu_bridge(q_cons_vf, device)
         type(scalar_field), dimension(sys_size), intent(in) :: q_cons_vf
         integer, intent(in) :: device
+        real(c_double) :: re_shear(num_fluids), re_bulk(num_fluids)
         integer :: i
 
         prm%m = m; prm%n = n; prm%p = 0
@@ -154,6 +172,15 @@ contains
         prm%device = device
 
         call s_check(mfc_gpu_init(prm, ctx), 'mfc_gpu_init')
+        if (any(Re_size > 0)) then
+            do i = 1, num_fluids
+                re_shear(i) = fluid_pp(i)%Re(1)
+                re_bulk(i) = fluid_pp(i)%Re(2)
+            end do
+            call s_check(mfc_gpu_set_viscosity(ctx, re_shear, re_bulk), 'mfc_gpu_set_viscosity')
+            if (weno_Re_flux) call s_check(mfc_gpu_set_viscous_gradients(ctx, 1_c_int), &
+                                           'mfc_gpu_set_viscous_gradients')
+        end if
         do i = 1, sys_size
             call s_check(mfc_gpu_upload(ctx, i - 1, c_loc(q_cons_vf(i)%sf(0, 0)), &
                                         int(m + 2*buff_size + 1, c_int64_t), 0_c_int64_t), 'mfc_gpu_upload')

@@ -4,9 +4,11 @@
  * (src/simulation/p_main.fpp), standing in for the Fortran bridge
  * (microfc_gb300/fortran/m_gpu_bridge.f90) where no Fortran compiler exists:
  *
- *   p_main.fpp:188-193  mfc_gpu_init, then mfc_gpu_upload of every
- *                       q_cons_ts(1)%vf(i)%sf(-b:m+b, -b:n+b), passed from
- *                       sf(0,0) with the leading dimension m + 2b + 1
+ *   p_main.fpp:188-193  mfc_gpu_init (viscous cases: mfc_gpu_set_viscosity
+ *                       with every fluid's Re(1:2), and with weno_Re_flux
+ *                       mfc_gpu_set_viscous_gradients), then mfc_gpu_upload
+ *                       of every q_cons_ts(1)%vf(i)%sf(-b:m+b, -b:n+b),
+ *                       passed from sf(0,0) with the leading dimension m + 2b + 1
  *   p_main.fpp:196-203  t_step = t_step_start; mytime; finaltime
  *   p_main.fpp:229-235  one mfc_gpu_tvd_rk per time step (last_step at t_step_stop)
  *   p_main.fpp:284-288  dt trim: if (mytime + dt >= finaltime) dt = finaltime - mytime
@@ -16,8 +18,10 @@
  *
  * Input file (native byte order):
  *   int32 m, n, num_fluids, weno_order, time_stepper, bc_x_beg, bc_x_end,
- *         bc_y_beg, bc_y_end, t_step_start, t_step_stop, t_step_save
+ *         bc_y_beg, bc_y_end, t_step_start, t_step_stop, t_step_save,
+ *         viscous, weno_re_flux
  *   double weno_eps, dt, gammas[num_fluids], pi_infs[num_fluids]
+ *   double re_shear[num_fluids], re_bulk[num_fluids] (when viscous != 0)
  *   double x_cb[m+2], y_cb[n+2] (when n > 0)
  *   double sf[S][ny_pad][nx_pad]: every variable with its ghost layers,
  *         nx_pad = m + 2b + 1, ny_pad = n + 2b + 1 (1 when n == 0)
@@ -61,10 +65,11 @@ int main(int argc, char** argv) {
   }
   FILE* in = fopen(argv[1], "rb");
   if (!in) return 2;
-  int32_t hdr[12];
+  int32_t hdr[14];
   read_exact(in, hdr, sizeof hdr);
   const int m = hdr[0], n = hdr[1], nf = hdr[2], wo = hdr[3], ts = hdr[4];
   const int t_step_start = hdr[9], t_step_stop = hdr[10], t_step_save = hdr[11];
+  const int viscous = hdr[12], weno_re_flux = hdr[13];
   if (nf < 1 || nf > MFC_MAX_FLUIDS || m < 1 || n < 0 || t_step_save < 1) return 2;
   double weno_eps, dt;
   read_exact(in, &weno_eps, sizeof weno_eps);
@@ -86,6 +91,11 @@ int main(int argc, char** argv) {
   prm.bc_z_beg = prm.bc_z_end = -3;
   read_exact(in, prm.gammas, sizeof(double) * (size_t)nf);
   read_exact(in, prm.pi_infs, sizeof(double) * (size_t)nf);
+  double re_shear[MFC_MAX_FLUIDS] = {0}, re_bulk[MFC_MAX_FLUIDS] = {0};
+  if (viscous) {
+    read_exact(in, re_shear, sizeof(double) * (size_t)nf);
+    read_exact(in, re_bulk, sizeof(double) * (size_t)nf);
+  }
   double* x_cb = malloc(sizeof(double) * (size_t)(m + 2));
   double* y_cb = n > 0 ? malloc(sizeof(double) * (size_t)(n + 2)) : NULL;
   read_exact(in, x_cb, sizeof(double) * (size_t)(m + 2));
@@ -108,6 +118,10 @@ int main(int argc, char** argv) {
 
   mfc_gpu_ctx* ctx = NULL;
   check(mfc_gpu_init(&prm, &ctx), "mfc_gpu_init");
+  if (viscous) {
+    check(mfc_gpu_set_viscosity(ctx, re_shear, re_bulk), "mfc_gpu_set_viscosity");
+    if (weno_re_flux) check(mfc_gpu_set_viscous_gradients(ctx, 1), "mfc_gpu_set_viscous_gradients");
+  }
   for (int i = 0; i < S; ++i)
     check(mfc_gpu_upload(ctx, i, sf + i * per_var + origin, nx_pad, 0), "mfc_gpu_upload");
 

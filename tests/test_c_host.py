@@ -3,7 +3,9 @@
 tests/c_host/p_main_host.c is a plain C program, compiled with gcc against
 include/mfc_gpu.h and linked to libmfc_gpu.so, that issues the call sequence
 of the reference's p_main (src/simulation/p_main.fpp:186-193, 196-318):
-mfc_gpu_init, one mfc_gpu_upload per variable from ghost-padded
+mfc_gpu_init (with mfc_gpu_set_viscosity and, for weno_Re_flux,
+mfc_gpu_set_viscous_gradients in viscous cases), one mfc_gpu_upload per
+variable from ghost-padded
 sf(-b:m+b, -b:n+b) arrays with the leading dimension m + 2b + 1, one
 mfc_gpu_tvd_rk per time step with the last-step dt trim, and at every save
 step mfc_gpu_status (the NaN scan) and one mfc_gpu_download per variable
@@ -15,6 +17,7 @@ neither read them (boundary conditions are applied on the device) nor write
 them (downloads fill the interior only).  The saved states are compared bit
 for bit with the oracle stepped through the same loop.
 """
+import json
 import os
 import shutil
 import subprocess
@@ -22,7 +25,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from microfc_gb300 import build as gbuild, cases, preprocess
+from microfc_gb300 import Case, build as gbuild, cases, preprocess
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "c_host", "p_main_host.c")
@@ -53,7 +56,8 @@ def _write_input(path, case, x_cb, y_cb, q, t_step_start, t_step_stop, t_step_sa
     b = case.buff_size
     nf = case.num_fluids
     hdr = np.array([case.m, case.n, nf, case.weno_order, case.time_stepper, case.bc_x[0], case.bc_x[1],
-                    case.bc_y[0], case.bc_y[1], t_step_start, t_step_stop, t_step_save], dtype=np.int32)
+                    case.bc_y[0], case.bc_y[1], t_step_start, t_step_stop, t_step_save, int(case.viscous),
+                    int(case.weno_re_flux)], dtype=np.int32)
     nxp = case.m + 2 * b + 1
     nyp = case.n + 2 * b + 1 if case.n > 0 else 1
     pad = np.full((case.sys_size, nyp, nxp), np.nan)
@@ -64,11 +68,20 @@ def _write_input(path, case, x_cb, y_cb, q, t_step_start, t_step_stop, t_step_sa
         f.write(np.array([case.weno_eps, case.dt], dtype=np.float64).tobytes())
         f.write(np.asarray(case.gammas[:nf], dtype=np.float64).tobytes())
         f.write(np.asarray(case.pi_infs[:nf], dtype=np.float64).tobytes())
+        if case.viscous:
+            f.write(np.asarray(case.re_shear[:nf], dtype=np.float64).tobytes())
+            f.write(np.asarray(case.re_bulk[:nf], dtype=np.float64).tobytes())
         f.write(np.ascontiguousarray(x_cb, dtype=np.float64).tobytes())
         if case.n > 0:
             f.write(np.ascontiguousarray(y_cb, dtype=np.float64).tobytes())
         f.write(pad.tobytes())
     return pad.shape, oy, b
+
+
+def _reference_example(name):
+    """One of the reference's example cases (tests/golden/reference_cases)."""
+    with open(os.path.join(ROOT, "tests", "golden", "reference_cases", name + ".json")) as f:
+        return Case.from_dict(json.load(f))
 
 
 def _oracle_saves(oracle_lib, case, x_cb, y_cb, q, t_step_start, t_step_stop, t_step_save):
@@ -98,7 +111,8 @@ def _oracle_saves(oracle_lib, case, x_cb, y_cb, q, t_step_start, t_step_stop, t_
     lambda: cases.shock_droplet_2d(nx=96, ny=48, steps=12),
     lambda: cases.shock_droplet_2d(nx=64, ny=40, steps=12).replace(bc_x=(-2, -4), bc_y=(-1, -1)),
     lambda: cases.sod_1d(m=299, steps=12, dt=1e-4),
-], ids=["droplet", "droplet-bc-mix", "sod"])
+    lambda: _reference_example("2D_viscous"),
+], ids=["droplet", "droplet-bc-mix", "sod", "viscous-example-weno_Re_flux"])
 def test_c_host_runs_p_main_sequence_bitwise_like_the_oracle(tmp_path, oracle_lib, builder):
     exe = _compile(tmp_path)
     case = builder()
