@@ -135,44 +135,83 @@ __global__ void __launch_bounds__(256) visc_cell_gradients(const DevParams P, co
   }
 }
 
-// Step 2 along dir: faces f+1/2 for f = -1 .. n_dir-1 of the interior lines
-// across, from the cell gradients G of the region ([c*ND+d][grow][gcol],
-// origin (gib, gjb)): out[c*ND+d][...] with the face index f+1 along dir.
-template <int ND, int DIR, class RT>
-__global__ void __launch_bounds__(256) visc_face_gradients(const DevParams P, const float* __restrict__ cft,
-                                                          const double* __restrict__ G,
-                                                          const int gib, const int gjb, const int gncol,
-                                                          const int gnrow, double* __restrict__ out) {
-  const int nf = P.n[DIR] + 1;                 // faces along dir
-  const int nl = DIR == 0 ? (ND > 1 ? P.n[1] : 1) : P.n[0];  // lines across
-  const int64_t items = (int64_t)nf * nl;
-  const int64_t plane_out = items;
+// Step 2: the face values, from the cell gradients G of the region
+// ([c*ND+d][grow][gcol], origin (gib, gjb)).  Each cell's gradients are
+// WENO-reconstructed once, both face values together (weno_cell: the same
+// operations as the one-sided form, so the same bits), and face F (between
+// cells F-1 and F, F = 0 .. n_dir) takes 0.5 (right value of cell F-1 + left
+// value of cell F).  out[c*ND+d][...], the face index F along dir.
+//
+// x faces: a warp covers 31 faces of one row.  Lane L reconstructs cell
+// base + L - 1 (clamped to the last cell needed, nx); lanes 1..31 write face
+// base + L - 1 with the right value of lane L-1 (shuffle) and their own left
+// value.  Every lane of a warp runs the same iterations (the loop bound is
+// per warp), so the full-mask shuffles are safe.
+template <int ND, class RT>
+__global__ void __launch_bounds__(256) visc_face_gradients_x(const DevParams P, const float* __restrict__ cft,
+                                                            const double* __restrict__ G, const int gib,
+                                                            const int gjb, const int gncol, const int gnrow,
+                                                            double* __restrict__ out) {
+  const int nx = P.n[0], nf = nx + 1;
+  const int nl = ND > 1 ? P.n[1] : 1;  // rows
+  const int chunks = (nf + 30) / 31;
+  const int64_t warps = (int64_t)chunks * nl;
+  const int64_t plane_out = (int64_t)nf * nl;
+  const int lane = threadIdx.x & 31;
   const RT eps = narrow<RT>(P.weno_eps);
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
-    int f, l;  // face index (0 = face -1/2) and line
-    if (DIR == 0) { f = (int)(t % nf); l = (int)(t / nf); }
-    else { l = (int)(t % nl); f = (int)(t / nl); }
-    const int cl = f - 1, cr = f;  // the cells before and after the face, along dir
-    RT cfl[kCoefRec], cfr[kCoefRec];
-    coef_of(P, cft, DIR, cl, cfl);
-    coef_of(P, cft, DIR, cr, cfr);
-    // element (a along dir, line l) of field k of the region
-    auto at = [&](int k, int a) -> RT {
-      const int i = DIR == 0 ? a : l, j = DIR == 0 ? l : a;
-      return narrow<RT>(__ldg(G + ((int64_t)k * gnrow + (j - gjb)) * gncol + (i - gib)));
-    };
+  const int64_t stride = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < warps; w += stride) {
+    const int l = (int)(w / chunks), base = (int)(w % chunks) * 31;
+    const int F = base + lane - 1;   // this lane's face (written by lanes 1..31 while F < nf)
+    const int cell = min(F, nx);     // and its cell, -1 .. nx
+    RT cf[kCoefRec];
+    coef_of(P, cft, 0, cell, cf);
+    const double* row = G + (int64_t)(l - gjb) * gncol + (cell - gib);
 #pragma unroll
     for (int k = 0; k < ND * ND; ++k) {
-      RT sl[5], sr[5];
+      RT st[5];
 #pragma unroll
-      for (int o = 0; o < 5; ++o) {
-        sl[o] = at(k, cl + o - 2);
-        sr[o] = at(k, cr + o - 2);
+      for (int o = 0; o < 5; ++o) st[o] = narrow<RT>(__ldg(row + (int64_t)k * gnrow * gncol + (o - 2)));
+      RT vl, vr;
+      weno_cell<5, RT>(cf, st, eps, vl, vr);
+      const RT right = __shfl_up_sync(0xffffffffu, vr, 1);  // face value of the cell before
+      if (lane >= 1 && F < nf) out[k * plane_out + (int64_t)l * nf + F] = widen(RT(0.5) * (right + vl));
+    }
+  }
+}
+
+// y faces: a thread walks one column through a run of R faces (cells
+// f0-1 .. f0+R-1), carrying each cell's right values to the next face.
+template <int ND, class RT, int R>
+__global__ void __launch_bounds__(256) visc_face_gradients_y(const DevParams P, const float* __restrict__ cft,
+                                                            const double* __restrict__ G, const int gib,
+                                                            const int gjb, const int gncol, const int gnrow,
+                                                            double* __restrict__ out) {
+  const int nx = P.n[0], ny = P.n[1], nf = ny + 1;
+  const int runs = (nf + R - 1) / R;
+  const int64_t items = (int64_t)nx * runs;
+  const int64_t plane_out = (int64_t)nf * nx;
+  const RT eps = narrow<RT>(P.weno_eps);
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
+    const int l = (int)(t % nx), f0 = (int)(t / nx) * R;
+    RT prev[ND * ND];
+#pragma unroll 1
+    for (int j = -1; j < R; ++j) {
+      const int cell = f0 + j;  // -1 .. ny
+      if (cell > ny) break;
+      RT cf[kCoefRec];
+      coef_of(P, cft, 1, cell, cf);
+      const double* col = G + (int64_t)(cell - gjb) * gncol + (l - gib);
+#pragma unroll
+      for (int k = 0; k < ND * ND; ++k) {
+        RT st[5];
+#pragma unroll
+        for (int o = 0; o < 5; ++o) st[o] = narrow<RT>(__ldg(col + ((int64_t)k * gnrow + (o - 2)) * gncol));
+        RT vl, vr;
+        weno_cell<5, RT>(cf, st, eps, vl, vr);
+        if (j >= 0) out[k * plane_out + (int64_t)cell * nx + l] = widen(RT(0.5) * (prev[k] + vl));
+        prev[k] = vr;
       }
-      const RT right = weno_cell_side<5, 1, RT>(cfl, sl, eps);  // face value of the cell before
-      const RT left = weno_cell_side<5, 0, RT>(cfr, sr, eps);   // and of the cell after
-      const int64_t o = DIR == 0 ? (int64_t)l * nf + f : (int64_t)f * nl + l;
-      out[k * plane_out + o] = widen(RT(0.5) * (right + left));
     }
   }
 }
@@ -190,12 +229,13 @@ cudaError_t launch_all(const DevParams& P, const ViscGradBuffers& B, const doubl
   visc_cell_gradients<ND, RT><<<grid((int64_t)gcol * grow), 256, 0, st>>>(P, B, vcol, vrow, -3, gjb, gcol, grow,
                                                                            B.g);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  visc_face_gradients<ND, 0, RT><<<grid((int64_t)(nx + 1) * ny), 256, 0, st>>>(P, B.cf[0], B.g, -3, gjb, gcol, grow,
-                                                                               B.fg[0]);
+  const int64_t xwarps = (int64_t)((nx + 1 + 30) / 31) * ny;
+  visc_face_gradients_x<ND, RT><<<grid(32 * xwarps), 256, 0, st>>>(P, B.cf[0], B.g, -3, gjb, gcol, grow, B.fg[0]);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if constexpr (ND > 1) {
-    visc_face_gradients<ND, 1, RT><<<grid((int64_t)nx * (ny + 1)), 256, 0, st>>>(P, B.cf[1], B.g, -3, gjb, gcol,
-                                                                                 grow, B.fg[1]);
+    constexpr int R = sizeof(RT) == 8 ? 8 : 4;  // faces per thread (FP32 wants more threads)
+    visc_face_gradients_y<ND, RT, R><<<grid((int64_t)nx * ((ny + 1 + R - 1) / R)), 256, 0, st>>>(
+        P, B.cf[1], B.g, -3, gjb, gcol, grow, B.fg[1]);
     e = cudaGetLastError();
   }
   return e;
