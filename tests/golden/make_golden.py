@@ -6,7 +6,8 @@ against regressions and across host architectures (x86-64 here, aarch64 on
 the GPU hosts; the oracle is built without FMA contraction), and the GPU
 parity tests compare the CUDA path against them directly.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [name ...]
+(no names: every fixture).
 """
 import os
 import sys
@@ -29,6 +30,9 @@ GOLDEN = {
         bc_x=(-1, -1), bc_y=(-1, -1)), 20),
     "droplet_2d_40x32_symmetry_riemann": (lambda: cases.shock_droplet_2d(nx=40, ny=32, steps=20).replace(
         bc_x=(-4, -3), bc_y=(-2, -2)), 20),
+    # viscous terms with WENO velocity gradients (weno_Re_flux = T)
+    "viscous_droplet_2d_40x32_weno_re_flux": (lambda: cases.shock_droplet_2d(nx=40, ny=32, steps=15).replace(
+        re_shear=(10.0, 500.0), re_bulk=(0.0, 200.0), weno_re_flux=True), 15),
 }
 
 
@@ -42,8 +46,8 @@ def compute(name):
     return case, x_cb, y_cb, q0, o.get_state(), steps, dt_final
 
 
-def main():
-    for name in GOLDEN:
+def main(names):
+    for name in names or GOLDEN:
         case, x_cb, y_cb, q0, q1, steps, dt_final = compute(name)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), q0=q0, q=q1, x_cb=x_cb,
                             y_cb=y_cb if y_cb is not None else np.zeros(0), steps=steps, dt=case.dt,
@@ -52,4 +56,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -95,7 +95,8 @@ def test_compute_rhs_matches_oracle(oracle_lib):
 
 
 @pytest.mark.parametrize("name", ["sod_1d_200_weno5_rk3", "sod_1d_200_weno3_rk2", "droplet_2d_48x32_weno5_rk3",
-                                  "droplet_2d_40x40_periodic", "droplet_2d_40x32_symmetry_riemann"])
+                                  "droplet_2d_40x40_periodic", "droplet_2d_40x32_symmetry_riemann",
+                                  "viscous_droplet_2d_40x32_weno_re_flux"])
 def test_matches_golden_fixture(name):
     """The CUDA path reproduces the committed oracle fixtures bit for bit."""
     import os
